@@ -1,0 +1,350 @@
+"""Benchmark: the batched Life-like ensemble on one GB300 (weak scaling over GPUs).
+
+Workload (per GPU): 4096 independent Life-like lattices (LifelikeCA), each with
+a rule drawn uniformly from the 2**18 B/S rules, width and height drawn
+uniformly from {64, 128, 256, 512, 1024}, Bernoulli(p ~ U[0.1, 0.6]) cells --
+all seeded (``xentica_gb300.batch.ensemble_workload``).  One *step* advances
+every lattice by 256 generations: one CUDA-graph launch of the resident
+kernel.  Inputs (~645 MB of cells, one byte each) exceed the 129 MB L2, so no
+flush is needed between steps.
+
+Reported (one JSON line on rank 0):
+  value   cell-updates/s over the K timed steps, device time (CUDA events on
+          the launching stream), inputs resident in HBM;
+  e2e     the same through ``xk_batch_run`` with pinned host buffers: the host
+          -> device copy of the cells, 256 generations, and the copy back;
+  plain   the same lattices with one launch per lattice per generation;
+  roofline, cpu_baseline, clocks, gpu_launches as the benchmark contract asks.
+
+``--impl reference`` times the reference's own kernels (its translator's
+LifelikeCA source compiled for the CPU, ``oracle/_ref``) on the host cores
+instead, with the same metric.
+"""
+import argparse
+import json
+import multiprocessing
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+B_ALG = 2.0      # reference-layout bytes per cell-update (read + write one uint8)
+METRIC = "cell-updates/s (batched Life-like ensemble)"
+
+
+def parse():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--instances", type=int, default=4096)
+    ap.add_argument("--generations", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=2041)
+    ap.add_argument("--plain-generations", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (one process per GPU; barrier + max only, no data path)
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            backend = "nccl" if os.environ.get("XK_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+            if backend == "nccl":
+                import torch
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, value):
+        if not self.pg:
+            return value
+        import torch
+        dev = "cuda" if self.pg.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+
+class Clocks:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(device), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k] == "Active"})
+        loaded = [v for v in sm if v > 0.5 * max(sm)] if sm else []
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_cell():
+    """DRAM bytes per cell per launch of the resident kernel from the committed
+    ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "life_resident_traffic.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            return float(json.load(fh)["dram_bytes_per_cell"])
+    return None
+
+
+def workload(args, rank):
+    from xentica_gb300.batch import ensemble_workload
+    ctx = multiprocessing.get_context("spawn")
+    with ctx.Pool(min(32, os.cpu_count() or 1)) as pool:
+        return ensemble_workload(args.instances, args.seed + 7919 * rank, pool=pool)
+
+
+def cpu_sample(widths, heights, rules, cells, offsets, seconds, threads):
+    """Time the reference's own kernels (oracle/_ref) when built, else the
+    oracle port, on one lattice of each size class; returns a dict."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_build
+    manifest = ref_build.available()
+    seen, picks = set(), []
+    for i in range(len(widths)):
+        key = (int(widths[i]), int(heights[i]))
+        if key not in seen:
+            seen.add(key)
+            picks.append(i)
+    sample_cells = int(sum(int(widths[i]) * int(heights[i]) for i in picks))
+    if manifest:
+        import ctypes
+        kind = "reference"
+        libs = {}
+        states = []
+        for i in picks:
+            w, h = int(widths[i]), int(heights[i])
+            entry = manifest["lifelike_%dx%d" % (w, h)]
+            lib = libs.get((w, h)) or ctypes.CDLL(os.path.join(ref_build.REF_DIR, entry["so"]))
+            libs[(w, h)] = lib
+            n = w * h
+            fld = np.zeros(n * 9 + 1, dtype=np.uint8)
+            fld[:n] = cells[offsets[i]:offsets[i] + n]
+            col = np.zeros(n * 3, dtype=np.int32)
+            states.append((lib, fld, col, n, int(rules[i])))
+
+        def one_generation():
+            for lib, fld, col, n, rule in states:
+                lib.xkref_emit(ctypes.c_int(threads), ctypes.c_void_p(fld.ctypes.data), ctypes.c_int(n))
+                lib.xkref_absorb(ctypes.c_int(threads), ctypes.c_void_p(fld.ctypes.data),
+                                 ctypes.c_void_p(col.ctypes.data), ctypes.c_int(rule), ctypes.c_int(n))
+    else:
+        import oracle as O
+        kind = "port"
+        states = []
+        for i in picks:
+            w, h = int(widths[i]), int(heights[i])
+            topo = O.Topology((w, h))
+            fld = topo.field(cells[offsets[i]:offsets[i] + w * h], np.uint8)
+            states.append((topo, fld, np.zeros(w * h * 3, np.int32), int(rules[i])))
+
+        def one_generation():
+            for topo, fld, col, rule in states:
+                O.life_run(topo, fld, col, 1, born=rule & 511, sustain=rule >> 9, threads=threads)
+    one_generation()
+    gens, t0 = 0, time.perf_counter()
+    while True:
+        one_generation()
+        gens += 1
+        el = time.perf_counter() - t0
+        if el >= seconds and gens >= 2:
+            break
+    rate = sample_cells * gens / el
+    return {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": kind,
+            "sample": "%d lattices (one per size class, %d cells) x %d generations, %.1f s, "
+                      "%s" % (len(picks), sample_cells, gens, el,
+                              "reference LifelikeCA kernels compiled for the CPU (OpenMP)"
+                              if kind == "reference" else "oracle port (OpenMP)")}
+
+
+def run_reference_arm(args, dist):
+    if dist.rank != 0:
+        return
+    from xentica_gb300.batch import ensemble_workload
+    widths, heights, rules, dens, cells = ensemble_workload(min(args.instances, 64), args.seed)
+    offsets = np.concatenate([[0], np.cumsum(widths.astype(np.int64) * heights)[:-1]])
+    threads = os.cpu_count()
+    per_step = max(2.0, args.cpu_seconds / max(1, args.steps))
+    for _ in range(args.warmup):
+        cpu_sample(widths, heights, rules, cells, offsets, 0.0, threads)
+    results = [cpu_sample(widths, heights, rules, cells, offsets, per_step, threads)
+               for _ in range(max(1, args.steps))]
+    value = statistics.median(r["value"] for r in results)
+    base = results[-1]
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cell-updates/s",
+            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded)",
+            "config": {"workload": "ensemble: LifelikeCA lattices, sides {64..1024}^2, "
+                                   "random B/S rules, Bernoulli(p~U[0.1,0.6])",
+                       "instances": args.instances, "generations": args.generations},
+            "cpu_baseline": dict(base, value=value),
+            "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, dist):
+    from xentica_gb300 import build as xk_build
+    from xentica_gb300 import _native as nat
+    widths, heights, rules, dens, cells = workload(args, dist.rank)   # before any GPU call
+    xk_build.build()
+    nat.set_device(dist.local)
+    from xentica_gb300.batch import Ensemble
+    ens = Ensemble(widths, heights, rules)
+    total = ens.total_cells
+    G = args.generations
+    ens.upload(cells)
+    rows_per_band = ens.tune(min(G, 64))
+    ens.upload(cells)
+    # self-check of the timed paths on this workload: batched == e2e == plain
+    ens.step(G)
+    after = ens.download()
+    pin_in, pin_out = nat.PinnedBuffer(total), nat.PinnedBuffer(total)
+    pin_in.array[:] = cells
+    ens.run(pin_in.array, pin_out.array, G)
+    if not np.array_equal(pin_out.array, after):
+        raise SystemExit("e2e path disagrees with the device path")
+    ens.upload(cells)
+    for _ in range(args.warmup):
+        ens.step(G)
+    clocks = Clocks(dist.local)
+    dist.barrier()
+    t_wall = time.perf_counter()
+    step_ms = [ens.step(G) for _ in range(args.steps)]
+    wall = time.perf_counter() - t_wall
+    dist.barrier()
+    clk = clocks.stop()
+    dev_s = dist.max(sum(step_ms) / 1000.0)
+    updates = float(total) * G * args.steps
+    value = updates * dist.world / dev_s
+    # end to end: pinned host in -> device -> 256 generations -> pinned host out
+    ens.run(pin_in.array, pin_out.array, G)
+    dist.barrier()
+    e2e_ms = [ens.run(pin_in.array, pin_out.array, G) for _ in range(args.steps)]
+    dist.barrier()
+    e2e_s = dist.max(sum(e2e_ms) / 1000.0)
+    e2e_value = updates * dist.world / e2e_s
+    # plain form: one launch per lattice per generation
+    ens.upload(cells)
+    pg = args.plain_generations
+    plain_ms = ens.step_plain(pg)
+    plain_value = float(total) * pg / (plain_ms / 1000.0)
+    launches = ens.launches(G) * args.steps
+    peak, peak_kind = measured_peak()
+    mean_ms = statistics.mean(step_ms)
+    achieved = B_ALG * total * G / (mean_ms / 1000.0) / 1e9
+    tpc = traffic_per_cell()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind,
+                "traffic": tpc * total if tpc is not None else None,
+                "kernel": "xk_k_life_resident<true> (all instance classes of one graph)",
+                "algorithmic_bytes_per_launch": B_ALG * total * G,
+                "note": "B_alg = 2 B per cell-update (the reference's uint8 state read and "
+                        "written once per generation); the kernel keeps every lattice in "
+                        "shared memory for all 256 generations, so frac > 1 is "
+                        "reference-format effective, not DRAM traffic"}
+    line = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1000 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded Bernoulli lattices, random rules)",
+            "config": {"workload": "ensemble of %d LifelikeCA lattices x %d generations per step"
+                                   % (args.instances, G),
+                       "instances": args.instances, "generations_per_step": G,
+                       "cells": total, "sides": [64, 128, 256, 512, 1024],
+                       "l2": "inputs (%.0f MB) larger than L2, no flush" % (total / 1e6),
+                       "rows_per_band": rows_per_band, "parallelism": "replicas x%d" % dist.world},
+            "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": total,
+                    "d2h_bytes_per_step": total, "ms_per_step": e2e_s * 1000 / args.steps},
+            "plain": {"value": plain_value, "unit": "cell-updates/s", "generations": pg,
+                      "batched_over_plain": value / dist.world / plain_value},
+            "gpu_launches": launches, "wall_s": wall, "roofline": roofline, "clocks": clk}
+    if dist.rank == 0:
+        line["cpu_baseline"] = cpu_sample(widths, heights, rules, cells, ens.offsets,
+                                          args.cpu_seconds, os.cpu_count())
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference_arm(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

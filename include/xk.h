@@ -1,0 +1,169 @@
+/*
+ * xk.h -- C-ABI of libxk, the GB300 (sm_103a) engine behind the xentica_gb300
+ * Python API.
+ *
+ * Plain C: pointers, sizes and status codes only.  The library owns device
+ * memory; callers own host buffers and the library copies.  Every function
+ * returns XK_OK (0) or a negative status; xk_last_error() gives the message of
+ * the last failure on the calling thread.  A handle is not thread-safe (the
+ * Python layer serialises each model with a lock, as the reference does at
+ * xentica/core/base.py:669,716,748); each handle owns one CUDA stream.
+ *
+ * Each entry point names the reference interface it replaces.  The reference
+ * is pure Python over PyCUDA; "replaces" means the PyCUDA calls its
+ * CellularAutomaton makes for the same job.
+ */
+#ifndef XK_H
+#define XK_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XK_ABI_VERSION 1
+#define XK_MAXDIM 8
+#define XK_MAXNBR 32
+
+enum {
+    XK_OK = 0,
+    XK_ERR_ARG = -1,          /* invalid argument or descriptor            */
+    XK_ERR_CUDA = -2,         /* CUDA runtime failure                      */
+    XK_ERR_OOM = -3,          /* device allocation failed / over budget    */
+    XK_ERR_UNSUPPORTED = -4,  /* no kernel for this configuration          */
+    XK_ERR_STATE = -5,        /* call out of order (e.g. step before upload) */
+    XK_ERR_TIMEOUT = -6,      /* a bounded device-side wait gave up        */
+    XK_ERR_INVARIANT = -7     /* a conserved quantity changed              */
+};
+
+enum { XK_FAMILY_LIFE = 1, XK_FAMILY_EVOLIFE = 2, XK_FAMILY_MASS = 3 };
+enum { XK_COLOR_NONE = 0, XK_COLOR_PLAIN = 1, XK_COLOR_MOVING_AVERAGE = 2 };
+
+/* Model descriptor filled by the translator (xentica_gb300/core/templates.py)
+ * from the traced model: the template family plus its rule parameters. */
+typedef struct xk_desc {
+    int32_t abi_version;               /* XK_ABI_VERSION                          */
+    int32_t family;                    /* XK_FAMILY_*                             */
+    int32_t ndim;                      /* lattice dimensions                      */
+    int32_t nbr;                       /* neighbours per cell                     */
+    int64_t size[XK_MAXDIM];           /* cells per axis, axis 0 fastest          */
+    int8_t delta[XK_MAXNBR][XK_MAXDIM];/* neighbour offsets                       */
+    int32_t torus;                     /* 1 TorusBorder, 0 StaticBorder           */
+    int32_t state_bytes;               /* reference packed cell size: 1,2,4,8     */
+    uint64_t border_value;             /* StaticBorder packed off-board value     */
+    int32_t color_kind;                /* XK_COLOR_*                              */
+    int32_t fade_in, fade_out, smooth; /* MovingAverage constants                 */
+    int32_t proj_axis0, proj_axis1;    /* RendererPlain projection axes           */
+    int32_t render_smooth;             /* render divisor (SMOOTH_FACTOR) or 0     */
+    /* XK_FAMILY_LIFE: the next state of a cell in state s (0/1) with k live
+     * neighbours is bit k of rule0 (s == 0) or rule1 (s == 1).  For the
+     * reference's Life-like absorb ``is_born | is_sustain & state``
+     * (examples/game_of_life.py:65-70, :190-197): rule0 = B, rule1 = B | S. */
+    uint32_t rule0, rule1;
+    int32_t color_lut[6];              /* rgb of state 0, rgb of state 1          */
+    int32_t color_history_free;        /* colour is a function of state alone     */
+    /* XK_FAMILY_EVOLIFE */
+    uint32_t death_speed, max_genes;
+    double mutation_prob;
+    int32_t positional;                /* 0 GenomeColor.modular, 1 .positional    */
+    /* XK_FAMILY_MASS */
+    uint32_t wall;                     /* StaticBorder value = off-board mass     */
+    int32_t reserved[8];
+} xk_desc;
+
+typedef struct xk_model xk_model;
+
+/* Replaces GPUKernels/GPUArrays construction (SourceModule + to_gpu,
+ * xentica/core/base.py:527-569, :664): allocate the device state. */
+int xk_model_create(const xk_desc *desc, xk_model **out);
+void xk_model_destroy(xk_model *m);
+
+/* Replaces gpuarray.to_gpu(init_cells) / cells.get() (base.py:558-559,
+ * tests reading gpu.arrays.cells.get()[:cells_num]): main plane in the
+ * reference layout, desc->state_bytes per cell. */
+int xk_upload(xk_model *m, const void *host_main, int64_t ncells);
+int xk_download(xk_model *m, void *host_main, int64_t ncells);
+
+/* Replaces gpu.arrays.colors (int3 per cell, base.py:558, :659). */
+int xk_upload_colors(xk_model *m, const int32_t *host_col, int64_t ncells);
+int xk_download_colors(xk_model *m, int32_t *host_col, int64_t ncells);
+
+/* Interactive rule of the Life-like family: the values the reference passes
+ * as kernel arguments at every step (base.py:717, :722). */
+int xk_life_set_rule(xk_model *m, uint32_t rule0, uint32_t rule1, const int32_t color_lut[6]);
+
+/* Colour bookkeeping of the Life-like family: with history_free = 1 the
+ * colour after a step is a function of the state alone (the MovingAverage
+ * clamp can never bind), so steps skip the colour pass and colours are
+ * computed when read; 0 updates colours every generation like the reference's
+ * absorb (color_effects.py:106-130). */
+int xk_set_color_mode(xk_model *m, int32_t history_free);
+
+/* Replaces CellularAutomaton.step (base.py:703-728): nsteps generations of
+ * emit + absorb + colour, fused. */
+int xk_step(xk_model *m, int64_t nsteps);
+
+/* Replaces CellularAutomaton.render (base.py:730-753): width*height*3 int32. */
+int xk_render(xk_model *m, int32_t *host_img, int32_t width, int32_t height,
+              int32_t zoom, int32_t dx, int32_t dy);
+
+/* Mass family: total mass after each of the last xk_step's generations
+ * (count = that nsteps); the invariant the configuration checks. */
+int xk_mass_totals(xk_model *m, uint64_t *host_totals, int64_t count);
+
+/* Wait for all work queued on the model's stream. */
+int xk_sync(xk_model *m);
+
+/* Device time of the last xk_step / batch step, in milliseconds (CUDA events
+ * on the launching stream). */
+double xk_last_step_ms(void);
+
+/* ------------------------------------------------------------------------ */
+/* Ensemble: many independent Life-like instances (LifelikeCA with an
+ * interactive rule, examples/game_of_life.py:183-203) on 2-D tori, advanced
+ * together.  The reference has no batch API: its equivalent is one
+ * CellularAutomaton per instance, each calling step() (base.py:703-728). */
+typedef struct xk_batch xk_batch;
+
+/* width/height per instance (any positive sizes), rule = golly integer
+ * (born bits 0-8, sustain bits 9-17, xentica/tools/rules.py:5-21), applied
+ * as LifelikeCA's absorb does: next = born[k] | sustain[k] & state. */
+int xk_batch_create(int32_t count, const int32_t *width, const int32_t *height,
+                    const uint32_t *rule, xk_batch **out);
+void xk_batch_destroy(xk_batch *b);
+/* One byte per cell (0/1), instances concatenated in creation order. */
+int xk_batch_upload(xk_batch *b, const uint8_t *host_cells, int64_t total_cells);
+int xk_batch_download(xk_batch *b, uint8_t *host_cells, int64_t total_cells);
+/* Batched form: every instance resident in shared memory for all
+ * generations, one graph launch. */
+int xk_batch_step(xk_batch *b, int32_t generations);
+/* Plain form: one launch per instance per generation, reference layout
+ * (one byte per cell), for comparison. */
+int xk_batch_step_plain(xk_batch *b, int32_t generations);
+/* End to end: upload host_in, run, download into host_out. */
+int xk_batch_run(xk_batch *b, const uint8_t *host_in, uint8_t *host_out,
+                 int64_t total_cells, int32_t generations);
+/* Autotune the batched kernel's block size for this batch (timed on device). */
+int xk_batch_tune(xk_batch *b, int32_t generations, int32_t *chosen_rows_per_band);
+int64_t xk_batch_total_cells(const xk_batch *b);
+/* Kernel launches one xk_batch_step makes (one per instance class, plus
+ * per-generation launches for instances too large for a CTA). */
+int64_t xk_batch_launches(const xk_batch *b, int32_t generations);
+
+/* Select the CUDA device for handles created afterwards on this thread. */
+int xk_set_device(int32_t device);
+/* Page-lock (pin) caller-owned host memory for fast copies, and release it. */
+int xk_host_register(void *ptr, int64_t bytes);
+int xk_host_unregister(void *ptr);
+
+/* Last error message of the calling thread ("" if none). */
+const char *xk_last_error(void);
+/* Name and SM count of the current device, for logs. */
+int xk_device_info(char *buf, int32_t len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XK_H */

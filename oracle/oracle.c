@@ -126,11 +126,12 @@ static void xo_color_write(int32_t *col, int64_t i, int r, int g, int b, const x
  * neighbour buffers into an ``unsigned int`` and applies
  *   state = ((B >> k) & 1) | ((S >> k) & 1) & state
  * which is GameOfLife's (B=8, S=12, game_of_life.py:55-70) and LifelikeCA's
- * (B = rule, S = rule >> 9, game_of_life.py:190-197) absorb.  Colour is
- * state * 255 on every channel (game_of_life.py:72-90). */
+ * (B = rule, S = rule >> 9, game_of_life.py:190-197) absorb.  The colour
+ * of a cell is a per-state table (lut6: rgb of state 0, then of state 1),
+ * e.g. state * 255 on every channel for GameOfLife (game_of_life.py:72-90). */
 void xo_life_step(const xo_topo *t, void *fld, int esz, int bits,
                   uint32_t born, uint32_t sustain, int32_t *col,
-                  const xo_color *cc, int threads)
+                  const xo_color *cc, const int32_t *lut6, int threads)
 {
     const int64_t n = xo_cells(t);
     const uint64_t mask = bits >= 64 ? ~0ull : ((1ull << bits) - 1);
@@ -154,8 +155,8 @@ void xo_life_step(const xo_topo *t, void *fld, int esz, int bits,
         }
         uint64_t s = xo_load(fld, esz, i) & mask;
         uint64_t ns = (uint64_t)(((born >> alive) & 1u) | (((sustain >> alive) & 1u) & (uint32_t)s));
-        int c = (int)(ns * 255);
-        xo_color_write(col, i, c, c, c, cc);
+        const int32_t *rgb = lut6 + 3 * (ns & 1u);
+        xo_color_write(col, i, rgb[0], rgb[1], rgb[2], cc);
         xo_store(fld, esz, i, ns & mask);
     }
 }

@@ -120,14 +120,17 @@ def _ptr(a):
 
 
 def life_run(topo, fld, col, steps, born=8, sustain=12, bits=1, color=None,
-             threads=None, rule_schedule=None):
+             threads=None, rule_schedule=None, lut=(0, 0, 0, 255, 255, 255)):
     """Advance a Life-like model ``steps`` generations in place.
 
-    ``rule_schedule`` optionally maps a timestep to a new ``(born, sustain)``
-    applied before that step (an interactive rule parameter).
+    next = ((born >> k) & 1) | ((sustain >> k) & 1 & state); ``lut`` is the
+    rgb of state 0 then state 1 before the colour effect.  ``rule_schedule``
+    optionally maps a timestep to a new ``(born, sustain)`` applied before
+    that step (an interactive rule parameter).
     """
     threads = threads or os.cpu_count()
     cc = color or _color()
+    lut6 = np.ascontiguousarray(lut, dtype=np.int32)
     fn = lib().xo_life_step
     fn.restype = None
     for t in range(steps):
@@ -135,7 +138,7 @@ def life_run(topo, fld, col, steps, born=8, sustain=12, bits=1, color=None,
             born, sustain = rule_schedule[t]
         fn(ctypes.byref(topo._c), _ptr(fld), ctypes.c_int(fld.itemsize), ctypes.c_int(bits),
            ctypes.c_uint32(born), ctypes.c_uint32(sustain), _ptr(col),
-           ctypes.byref(cc), ctypes.c_int(threads))
+           ctypes.byref(cc), _ptr(lut6), ctypes.c_int(threads))
 
 
 def mass_run(topo, fld, col, steps, wall=2 ** 32 - 1, threads=None, totals=None):

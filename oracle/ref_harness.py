@@ -130,20 +130,25 @@ def _kernel_wrappers(model):
     return "\n".join(out) + "\n"
 
 
-def compile_model(model, workdir):
+def compile_cpp(cpp, so):
+    """g++ recipe for one dumped reference kernel source."""
+    cmd = ["g++", "-O2", "-ffp-contract=off", "-fno-fast-math", "-w",
+           "-fopenmp", "-shared", "-fPIC",
+           "-include", os.path.join(HERE, "ref_shim.h"), cpp, "-o", so]
+    subprocess.run(cmd, check=True)
+
+
+def compile_model(model, workdir, name=None):
     """Compile the model's generated source; return the loaded CDLL."""
     src = model.cuda_source + "\n" + _kernel_wrappers(model)
-    key = hashlib.sha1(src.encode()).hexdigest()[:16]
+    key = name or hashlib.sha1(src.encode()).hexdigest()[:16]
     os.makedirs(workdir, exist_ok=True)
     cpp = os.path.join(workdir, "ref_%s.cpp" % key)
     so = os.path.join(workdir, "ref_%s.so" % key)
-    if not os.path.exists(so):
+    if not os.path.exists(so) or name:
         with open(cpp, "w") as fh:
             fh.write(src)
-        cmd = ["g++", "-O2", "-ffp-contract=off", "-fno-fast-math", "-w",
-               "-fopenmp", "-shared", "-fPIC",
-               "-include", os.path.join(HERE, "ref_shim.h"), cpp, "-o", so]
-        subprocess.run(cmd, check=True)
+        compile_cpp(cpp, so)
     return ctypes.CDLL(so), cpp
 
 
@@ -180,7 +185,7 @@ def run_job(job):
         exp_cls = type("XkJobExperiment", (exp_cls,), overrides)
     model = model_cls(exp_cls, **job.get("model_kwargs", {}))
     threads = int(job.get("threads", 1))
-    lib, cpp = compile_model(model, job.get("workdir") or tempfile.mkdtemp())
+    lib, cpp = compile_model(model, job.get("workdir") or tempfile.mkdtemp(), job.get("name"))
     bind_kernels(model, lib, threads)
     n = model.cells_num
     res = {"cells_num": np.int64(n), "size": np.array(model.size),

@@ -1,0 +1,106 @@
+"""Generate ``tests/golden/golden.json`` from the reference implementation.
+
+Run in a checkout where the reference source is available::
+
+    python tests/golden/make_golden.py /path/to/xentica-reference
+
+Every case runs the reference's own ``CellularAutomaton.step()`` /
+``render()`` with its translator-generated kernels compiled for the CPU
+(``oracle/ref_harness.py``) and records CRC32 checksums: the initial main
+plane (pins the seed streams), the main plane and colours at checkpoints, and
+rendered images.  The fixtures are what the GPU tests compare against; they do
+not need the reference at test time.
+"""
+import binascii
+import json
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from ref_harness import run_reference  # noqa: E402
+
+GOL = "examples.game_of_life"
+REF_MODELS = os.path.join(HERE, "ref_models.py")
+
+# name -> job (see ref_harness.py for the keys)
+CASES = {
+    "gol_640x360": dict(model=GOL + ":GameOfLife", experiment=GOL + ":GOLExperiment",
+                        exp_overrides={"zoom": 1}, checkpoints=[1, 10, 1000],
+                        render={"viewport": [640, 360]}),
+    "gol_zoom3_pos": dict(model=GOL + ":GameOfLife", experiment=GOL + ":GOLExperiment",
+                          exp_overrides={"zoom": 3, "pos": [-7, 13]}, checkpoints=[40],
+                          render={"viewport": [700, 300]}),
+    "gol_static_640x360": dict(model=GOL + ":GameOfLifeStatic", experiment=GOL + ":GOLExperiment",
+                               checkpoints=[1000]),
+    "lifelike_diamoeba": dict(model=GOL + ":LifelikeCA", experiment=GOL + ":DiamoebaExperiment",
+                              checkpoints=[1, 23, 24, 1000]),
+    "gol6d_64x36": dict(model=GOL + ":GameOfLife6D", experiment=GOL + ":GOLExperiment2",
+                        exp_overrides={"size": [64, 36, 3, 3, 3, 3], "zoom": 2},
+                        checkpoints=[1, 1000], render={"viewport": [100, 50]}),
+    "gol_int16": dict(model=REF_MODELS + ":GameOfLifeInt", experiment=GOL + ":GOLExperiment",
+                      checkpoints=[1000]),
+    "gol_color_fade": dict(model=REF_MODELS + ":GameOfLifeFade", experiment=REF_MODELS + ":FadeExperiment",
+                           checkpoints=[1, 5, 60], render={"viewport": [50, 30]}),
+    "gol_plain_color": dict(model=REF_MODELS + ":GameOfLifePlainColor",
+                            experiment=GOL + ":GOLExperiment2",
+                            exp_overrides={"size": [45, 29], "zoom": 1}, checkpoints=[3, 30],
+                            render={"viewport": [45, 29]}),
+    "gol3d_moore_static": dict(model=REF_MODELS + ":GameOfLife3DStatic",
+                               experiment=GOL + ":GOLExperiment2",
+                               exp_overrides={"size": [12, 10, 7]}, checkpoints=[1, 25],
+                               render={"viewport": [12, 10]}),
+}
+
+# odd sizes, both borders: pins word-boundary and wrap handling
+for w, h in [(1, 1), (1, 17), (17, 1), (2, 2), (31, 5), (32, 7), (33, 9), (63, 64), (64, 63),
+             (65, 3), (100, 100), (1023, 5), (1024, 3), (1025, 4), (2000, 11), (3, 1200)]:
+    for model in ("GameOfLife", "GameOfLifeStatic"):
+        name = "%s_%dx%d" % ("gol" if model == "GameOfLife" else "static", w, h)
+        CASES[name] = dict(model=GOL + ":" + model, experiment=GOL + ":GOLExperiment2",
+                           exp_overrides={"size": [w, h], "word": "ODD %d %d" % (w, h)},
+                           checkpoints=[1, 2, 7, 50])
+
+for name, rule in [("highlife", "B36/S23"), ("seeds", "B2/S"), ("life_without_death", "B3/S012345678"),
+                   ("b0_rule", "B0123/S45"), ("b8_rule", "B8/S8")]:
+    CASES["rule_" + name] = dict(model=REF_MODELS + ":LifelikeFixed", experiment=GOL + ":GOLExperiment2",
+                                 exp_overrides={"size": [77, 51], "word": name, "rule": rule},
+                                 checkpoints=[1, 3, 20])
+
+
+def crc(a):
+    return binascii.crc32(a) & 0xFFFFFFFF
+
+
+def main(ref_root):
+    out = {}
+    for name, job in CASES.items():
+        job = dict(job)
+        job.setdefault("threads", os.cpu_count())
+        job["workdir"] = os.path.join(ROOT, "oracle", "_ref")
+        job["sys_path"] = [HERE]
+        overrides = dict(job.get("exp_overrides", {}))
+        if "rule" in overrides:
+            sys.path.insert(0, os.path.join(ROOT))
+            from xentica_gb300.tools.rules import LifeLike
+            overrides["rule"] = LifeLike.golly2int(overrides["rule"])
+            job["exp_overrides"] = overrides
+        res = run_reference(job, ref_root)
+        case = {"job": {k: v for k, v in job.items() if k not in ("workdir", "threads", "sys_path")},
+                "cells_num": int(res["cells_num"]),
+                "init": crc(res["init_cells"]), "steps": {}}
+        for cp in job["checkpoints"]:
+            entry = {"cells": crc(res["cells_%d" % cp]), "colors": crc(res["colors_%d" % cp])}
+            if "img_%d" % cp in res:
+                entry["img"] = crc(res["img_%d" % cp])
+            case["steps"][str(cp)] = entry
+        out[name] = case
+        print(name, case["init"], json.dumps(case["steps"]), flush=True)
+    with open(os.path.join(HERE, "golden.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,89 @@
+"""GPU parity of the ensemble (``xk_batch_*``): every lattice, bit-exact.
+
+Mixed sizes exercise every kernel path: resident in shared memory with one or
+many row groups per warp, partial last words, the in-place 1024-wide case, and
+lattices too wide for a CTA (plain per-generation launches).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from xentica_gb300.batch import Ensemble, ensemble_workload
+from xentica_gb300.core.exceptions import XenticaException
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(1, 1), (1, 9), (9, 1), (37, 23), (64, 64), (33, 200), (1024, 1024), (1000, 3),
+         (2000, 10), (128, 1024), (1024, 64), (95, 95)]
+
+
+def _ensemble(seed=7):
+    rng = np.random.RandomState(seed)
+    widths = [w for w, _ in SIZES]
+    heights = [h for _, h in SIZES]
+    rules = [int(r) for r in rng.randint(0, 2 ** 18, len(SIZES))]
+    rules[4] = 6152     # B3/S23
+    ens = Ensemble(widths, heights, rules)
+    cells = (rng.random_sample(ens.total_cells) < 0.4).astype(np.uint8)
+    return ens, cells
+
+
+def _oracle(ens, cells, generations):
+    out = cells.copy()
+    for i in range(ens.count):
+        w, h, rule = int(ens.widths[i]), int(ens.heights[i]), int(ens.rules[i])
+        topo = O.Topology((w, h))
+        fld = topo.field(ens.lattice(cells, i).ravel(), np.uint8)
+        col = np.zeros(topo.cells * 3, dtype=np.int32)
+        O.life_run(topo, fld, col, generations, born=rule & 511, sustain=rule >> 9)
+        ens.lattice(out, i)[...] = fld[:topo.cells].reshape(h, w)
+    return out
+
+
+@pytest.mark.parametrize("generations", [1, 2, 17])
+def test_batched_matches_oracle(generations):
+    ens, cells = _ensemble()
+    ens.upload(cells)
+    ens.step(generations)
+    got = ens.download()
+    want = _oracle(ens, cells, generations)
+    for i in range(ens.count):
+        assert np.array_equal(ens.lattice(got, i), ens.lattice(want, i)), "lattice %d %s" % (i, SIZES[i])
+
+
+def test_plain_run_and_tune_agree():
+    ens, cells = _ensemble(3)
+    ens.upload(cells)
+    ens.step_plain(9)
+    plain = ens.download()
+    ens.upload(cells)
+    ens.step(4)
+    ens.step(5)
+    assert np.array_equal(ens.download(), plain)
+    out = np.zeros_like(cells)
+    ens.run(cells, out, 9)
+    assert np.array_equal(out, plain)
+    ens.upload(cells)
+    ens.tune(3)
+    assert np.array_equal(ens.download(), cells)   # tuning leaves the state alone
+    ens.step(9)
+    assert np.array_equal(ens.download(), plain)
+
+
+def test_rejects_non_binary_cells():
+    ens, cells = _ensemble()
+    cells[5] = 3
+    ens.upload(cells)
+    with pytest.raises(XenticaException, match="0 or 1"):
+        ens.step(1)
+
+
+def test_workload_generator_subsample():
+    widths, heights, rules, dens, cells = ensemble_workload(count=24, base_seed=11,
+                                                            sides=(64, 128))
+    ens = Ensemble(widths, heights, rules)
+    ens.upload(cells)
+    ens.step(5)
+    got = ens.download()
+    want = _oracle(ens, cells, 5)
+    assert np.array_equal(got, want)

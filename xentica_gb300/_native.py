@@ -1,0 +1,148 @@
+"""ctypes binding of ``libxk.so`` (the C-ABI declared in ``include/xk.h``).
+
+The library is built in-tree by :mod:`xentica_gb300.build`.  Nothing here
+falls back to another implementation: if the library or a CUDA device is
+missing, every GPU entry point raises :class:`XenticaException`.
+"""
+import ctypes
+import os
+import threading
+
+from xentica_gb300.core.exceptions import XenticaException
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "libxk.so")
+
+XK_ABI_VERSION = 1
+XK_MAXDIM = 8
+XK_MAXNBR = 32
+XK_FAMILY_LIFE, XK_FAMILY_EVOLIFE, XK_FAMILY_MASS = 1, 2, 3
+XK_COLOR_NONE, XK_COLOR_PLAIN, XK_COLOR_MOVING_AVERAGE = 0, 1, 2
+
+_I32, _U32, _I64, _U64 = ctypes.c_int32, ctypes.c_uint32, ctypes.c_int64, ctypes.c_uint64
+_P = ctypes.c_void_p
+
+
+class XkDesc(ctypes.Structure):
+    """Mirror of ``xk_desc``."""
+
+    _fields_ = [
+        ("abi_version", _I32), ("family", _I32), ("ndim", _I32), ("nbr", _I32),
+        ("size", _I64 * XK_MAXDIM),
+        ("delta", (ctypes.c_int8 * XK_MAXDIM) * XK_MAXNBR),
+        ("torus", _I32), ("state_bytes", _I32),
+        ("border_value", _U64),
+        ("color_kind", _I32), ("fade_in", _I32), ("fade_out", _I32), ("smooth", _I32),
+        ("proj_axis0", _I32), ("proj_axis1", _I32), ("render_smooth", _I32),
+        ("rule0", _U32), ("rule1", _U32),
+        ("color_lut", _I32 * 6),
+        ("color_history_free", _I32),
+        ("death_speed", _U32), ("max_genes", _U32),
+        ("mutation_prob", ctypes.c_double),
+        ("positional", _I32),
+        ("wall", _U32),
+        ("reserved", _I32 * 8),
+    ]
+
+
+# name -> (restype, argtypes); every symbol declared in include/xk.h
+SIGNATURES = {
+    "xk_model_create": (_I32, [ctypes.POINTER(XkDesc), ctypes.POINTER(_P)]),
+    "xk_model_destroy": (None, [_P]),
+    "xk_upload": (_I32, [_P, _P, _I64]),
+    "xk_download": (_I32, [_P, _P, _I64]),
+    "xk_upload_colors": (_I32, [_P, _P, _I64]),
+    "xk_download_colors": (_I32, [_P, _P, _I64]),
+    "xk_life_set_rule": (_I32, [_P, _U32, _U32, _P]),
+    "xk_set_color_mode": (_I32, [_P, _I32]),
+    "xk_step": (_I32, [_P, _I64]),
+    "xk_render": (_I32, [_P, _P, _I32, _I32, _I32, _I32, _I32]),
+    "xk_mass_totals": (_I32, [_P, _P, _I64]),
+    "xk_sync": (_I32, [_P]),
+    "xk_last_step_ms": (ctypes.c_double, []),
+    "xk_batch_create": (_I32, [_I32, _P, _P, _P, ctypes.POINTER(_P)]),
+    "xk_batch_destroy": (None, [_P]),
+    "xk_batch_upload": (_I32, [_P, _P, _I64]),
+    "xk_batch_download": (_I32, [_P, _P, _I64]),
+    "xk_batch_step": (_I32, [_P, _I32]),
+    "xk_batch_step_plain": (_I32, [_P, _I32]),
+    "xk_batch_run": (_I32, [_P, _P, _P, _I64, _I32]),
+    "xk_batch_tune": (_I32, [_P, _I32, ctypes.POINTER(_I32)]),
+    "xk_batch_total_cells": (_I64, [_P]),
+    "xk_batch_launches": (_I64, [_P, _I32]),
+    "xk_set_device": (_I32, [_I32]),
+    "xk_host_register": (_I32, [_P, _I64]),
+    "xk_host_unregister": (_I32, [_P]),
+    "xk_last_error": (ctypes.c_char_p, []),
+    "xk_device_info": (_I32, [ctypes.c_char_p, _I32]),
+}
+
+_LIB = None
+_LOCK = threading.Lock()
+
+
+def load(path=LIBPATH):
+    """Load the library (no CUDA call is made); raises if it is missing."""
+    global _LIB
+    with _LOCK:
+        if _LIB is not None:
+            return _LIB
+        if not os.path.exists(path):
+            raise XenticaException(
+                "libxk.so is not built (%s); run `python -m xentica_gb300.build`" % path)
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = lib
+        return lib
+
+
+def last_error():
+    msg = load().xk_last_error()
+    return msg.decode(errors="replace") if msg else ""
+
+
+def check(rc, what):
+    """Raise :class:`XenticaException` for a non-zero status."""
+    if rc != 0:
+        raise XenticaException("%s failed (status %d): %s" % (what, rc, last_error()))
+
+
+def device_info():
+    buf = ctypes.create_string_buffer(256)
+    check(load().xk_device_info(buf, 256), "xk_device_info")
+    return buf.value.decode()
+
+
+def set_device(device):
+    """Make ``device`` current for libxk handles created on this thread."""
+    check(load().xk_set_device(int(device)), "xk_set_device")
+
+
+class PinnedBuffer:
+    """A page-locked host array (NumPy) for fast host<->device copies."""
+
+    def __init__(self, nbytes, dtype="uint8"):
+        import numpy as np
+        self.array = np.empty(nbytes, dtype=dtype)
+        check(load().xk_host_register(ptr(self.array), self.array.nbytes), "xk_host_register")
+
+    def release(self):
+        if self.array is not None:
+            load().xk_host_unregister(ptr(self.array))
+            self.array = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+def ptr(array):
+    """Raw pointer of a contiguous NumPy array."""
+    if not array.flags["C_CONTIGUOUS"]:
+        raise XenticaException("array must be C-contiguous")
+    return ctypes.c_void_p(array.ctypes.data)

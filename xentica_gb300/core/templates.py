@@ -1,0 +1,261 @@
+"""Template matcher: traced model -> hand-written GB300 kernel + parameters.
+
+This replaces the reference's code generation (``xentica/core/base.py:440-541``,
+PyCUDA ``SourceModule``).  A model's traced programs (``model.programs``) are
+analysed and, when they implement a family one of the libxk kernels computes,
+turned into an ``xk_desc``: the family and its rule parameters.  Anything else
+raises :class:`XenticaException` -- there is no fallback.
+
+Life-like family (``XK_FAMILY_LIFE``)
+    one integer property whose values stay in {0, 1}; ``emit`` copies it to
+    every buffer; ``absorb`` sets it from its own value and the *sum* of the
+    neighbours' buffers; the colour is a function of the new state.  The rule
+    is read off by executing the traced absorb (with C semantics) on every
+    combination of a cell's state and its neighbours' buffers -- 2**(N+1)
+    lanes at once -- and checking that the result depends on the neighbours
+    only through their sum.  Interactive parameters are re-bound and the rule
+    re-extracted whenever their values change (LifelikeCA,
+    ``examples/game_of_life.py:183-203``).
+"""
+import numpy as np
+
+from xentica_gb300 import _native as nat
+from xentica_gb300.core import ir
+from xentica_gb300.core.exceptions import XenticaException
+from xentica_gb300.core.properties import IntegerProperty
+from xentica_gb300.core.topology.border import TorusBorder, StaticBorder
+from xentica_gb300.core.topology.lattice import OrthogonalLattice
+from xentica_gb300.core.topology.neighborhood import OrthogonalNeighborhood
+from xentica_gb300.core.renderers import RendererPlain
+
+__all__ = ['match', 'LifeTemplate', 'NoTemplate']
+
+MAX_EXHAUSTIVE_NBR = 16
+
+
+class NoTemplate(Exception):
+    """Raised internally when a family does not match (with the reason)."""
+
+
+def _topology(model):
+    topo = model.topology
+    if not isinstance(topo.lattice, OrthogonalLattice):
+        raise NoTemplate("lattice %s" % type(topo.lattice).__name__)
+    if not isinstance(topo.neighborhood, OrthogonalNeighborhood):
+        raise NoTemplate("neighbourhood %s" % type(topo.neighborhood).__name__)
+    deltas = topo.neighborhood.deltas
+    if len(deltas) > nat.XK_MAXNBR - 1:
+        raise NoTemplate("%d neighbours (max %d)" % (len(deltas), nat.XK_MAXNBR - 1))
+    if topo.dimensions > nat.XK_MAXDIM:
+        raise NoTemplate("%d dimensions (max %d)" % (topo.dimensions, nat.XK_MAXDIM))
+    if isinstance(topo.border, TorusBorder):
+        torus, border = True, 0
+    elif isinstance(topo.border, StaticBorder):
+        torus, border = False, int(topo.border.value)
+    else:
+        raise NoTemplate("border %s" % type(topo.border).__name__)
+    return deltas, torus, border
+
+
+def _base_desc(model, family):
+    deltas, torus, border = _topology(model)
+    d = nat.XkDesc()
+    d.abi_version = nat.XK_ABI_VERSION
+    d.family = family
+    d.ndim = model.topology.dimensions
+    d.nbr = len(deltas)
+    for i, s in enumerate(model.size[:d.ndim]):
+        d.size[i] = int(s)
+    for k, delta in enumerate(deltas):
+        for i, v in enumerate(delta):
+            d.delta[k][i] = int(v)
+    d.torus = int(torus)
+    d.state_bytes = np.dtype(model.main.dtype).itemsize
+    d.border_value = border & 0xFFFFFFFFFFFFFFFF
+    renderer = model.renderer
+    axes = tuple(getattr(renderer, "projection_axes", (0, 1)))
+    d.proj_axis0, d.proj_axis1 = (int(axes[0]), int(axes[1])) if d.ndim > 1 else (0, 0)
+    d.render_smooth = 0
+    if model.is_constant("SMOOTH_FACTOR"):
+        d.render_smooth = int(model.constants["SMOOTH_FACTOR"].value)
+    return d
+
+
+def _color_stmt(program):
+    stmts = [st for st in program.stmts if st.op == "color"]
+    if len(stmts) > 1:
+        raise NoTemplate("colour written more than once")
+    return stmts[0] if stmts else None
+
+
+def _store_keys(program):
+    return {st.extra for st in program.stmts if st.op == "store"}
+
+
+class LifeTemplate:
+    """Binary outer-totalistic rule; see the module docstring."""
+
+    family = nat.XK_FAMILY_LIFE
+
+    def __init__(self, model):
+        props = list(model.main.properties.values())
+        if len(props) != 1 or not isinstance(props[0], IntegerProperty):
+            raise NoTemplate("needs exactly one IntegerProperty")
+        self.model = model
+        self.prop = props[0]
+        self.mask = (1 << self.prop.bit_width) - 1
+        deltas, torus, border = _topology(model)
+        self.nbr = len(deltas)
+        self.border_state = border & self.mask
+        if not torus and self.border_state not in (0, 1):
+            raise NoTemplate("static border state %d is not 0/1" % self.border_state)
+        self._check_emit(model.programs["emit"])
+        absorb = model.programs["absorb"]
+        loads = absorb.loads()
+        allowed = {("main", -1)} | {("nbuf", k) for k in range(self.nbr)}
+        if not loads <= allowed:
+            raise NoTemplate("absorb reads %s" % sorted(loads - allowed))
+        if _store_keys(absorb) != {("main", 0)}:
+            raise NoTemplate("absorb must write only the cell's own main state")
+        self.absorb = absorb
+        self.color = _color_stmt(absorb)
+        if self.color is not None and self.color.extra["kind"] not in ("plain", "moving_average"):
+            raise NoTemplate("custom colour effect")
+        self.param_names = sorted(absorb.params())
+        self._cache = {}
+        self.rule0, self.rule1, self.lut = self.rule_for(self.current_params())
+
+    # -- analysis ----------------------------------------------------------
+    def _check_emit(self, emit):
+        loads = emit.loads()
+        if not loads <= {("main", -1)}:
+            raise NoTemplate("emit reads %s" % sorted(loads))
+        if emit.params():
+            raise NoTemplate("emit depends on parameters")
+        keys = _store_keys(emit)
+        planes = {("buf", p) for p in range(1, self.nbr + 1)}
+        if keys != planes:
+            raise NoTemplate("emit must write every buffer")
+        lanes = np.array([0, 1], dtype=np.uint64)
+        ev = ir.evaluate(emit, {("main", -1): lanes}, lanes=2)
+        for key in planes:
+            out = ev.stores[key].astype(np.uint64) & np.uint64(self.mask)
+            if not np.array_equal(out, lanes):
+                raise NoTemplate("emit does not copy the state to every buffer")
+
+    def current_params(self):
+        return {name: self.model.meta.__dict__[name].value for name in self.param_names}
+
+    def _inputs(self):
+        n = self.nbr
+        if n <= MAX_EXHAUSTIVE_NBR:
+            combos = np.arange(2 ** (n + 1), dtype=np.uint64)
+        else:
+            rng = np.random.RandomState(12345)
+            combos = rng.randint(0, 2 ** 62, size=1 << 17, dtype=np.int64).astype(np.uint64)
+            # make sure every (state, count) pair is present
+            extra = []
+            for s in (0, 1):
+                for k in range(n + 1):
+                    extra.append((((1 << k) - 1) << 1) | s)
+            combos = np.concatenate([combos & np.uint64((1 << (n + 1)) - 1),
+                                     np.array(extra, dtype=np.uint64)])
+        state = combos & np.uint64(1)
+        inputs = {("main", -1): state}
+        count = np.zeros(len(combos), dtype=np.int64)
+        for k in range(n):
+            bit = (combos >> np.uint64(k + 1)) & np.uint64(1)
+            inputs[("nbuf", k)] = bit
+            count += bit.astype(np.int64)
+        return inputs, state.astype(np.int64), count
+
+    def rule_for(self, params):
+        """``(rule0, rule1, lut6)`` for the given interactive parameter values."""
+        key = tuple(sorted(params.items()))
+        if key in self._cache:
+            return self._cache[key]
+        inputs, state, count = self._inputs()
+        ev = ir.evaluate(self.absorb, inputs, params=params, lanes=len(state))
+        new = ev.stores[("main", 0)].astype(np.uint64) & np.uint64(self.mask)
+        if np.any(new > 1):
+            raise XenticaException("Life-like absorb produced a state other than 0/1")
+        new = new.astype(np.int64)
+        rules = [0, 0]
+        for s in (0, 1):
+            for k in range(self.nbr + 1):
+                sel = (state == s) & (count == k)
+                vals = np.unique(new[sel])
+                if len(vals) > 1:
+                    raise XenticaException(
+                        "absorb depends on more than the number of live neighbours")
+                if len(vals) and vals[0]:
+                    rules[s] |= 1 << k
+        lut = [0] * 6
+        if ev.color is not None:
+            rgb = ev.color[0]
+            for s in (0, 1):
+                sel = new == s
+                for c in range(3):
+                    vals = np.unique(rgb[c][sel])
+                    if len(vals) > 1:
+                        raise XenticaException("colour depends on more than the new state")
+                    if len(vals):
+                        lut[3 * s + c] = int(vals[0])
+        result = (rules[0], rules[1], lut)
+        self._cache[key] = result
+        return result
+
+    # -- colour bookkeeping ------------------------------------------------
+    def color_kind(self):
+        if self.color is None:
+            return nat.XK_COLOR_NONE
+        if self.color.extra["kind"] == "moving_average":
+            return nat.XK_COLOR_MOVING_AVERAGE
+        return nat.XK_COLOR_PLAIN
+
+    def _fades(self):
+        info = self.color.extra
+        return info.get("fade_in", 0), info.get("fade_out", 0), info.get("smooth", 1)
+
+    def history_free(self, lut, old_colors):
+        """Whether one step makes every colour equal its state's table value,
+        given the colours ``old_colors`` hold (min, max) before it."""
+        kind = self.color_kind()
+        if kind != nat.XK_COLOR_MOVING_AVERAGE:
+            return True
+        fade_in, fade_out, smooth = self._fades()
+        vals = [v * smooth for v in lut]
+        vmin, vmax = min(vals), max(vals)
+        omin, omax = old_colors
+        first = (omax - fade_out <= vmin) and (vmax <= omin + fade_in)
+        steady = (vmax - vmin <= fade_in) and (vmax - vmin <= fade_out)
+        return first and steady
+
+    def descriptor(self):
+        d = _base_desc(self.model, self.family)
+        d.border_value = self.border_state
+        d.rule0, d.rule1 = self.rule0, self.rule1
+        for i, v in enumerate(self.lut):
+            d.color_lut[i] = int(v)
+        d.color_kind = self.color_kind()
+        if self.color is not None:
+            d.fade_in, d.fade_out, d.smooth = self._fades()
+        else:
+            d.smooth = 1
+        d.color_history_free = int(self.history_free(self.lut, (0, 0)))
+        return d
+
+
+FAMILIES = (LifeTemplate, )
+
+
+def match(model):
+    """Template instance for ``model``; raises :class:`XenticaException`."""
+    reasons = []
+    for family in FAMILIES:
+        try:
+            return family(model)
+        except NoTemplate as exc:
+            reasons.append("%s: %s" % (family.__name__, exc))
+    raise XenticaException("No GB300 kernel template implements model %s (%s)."
+                           % (type(model).__name__, "; ".join(reasons)))

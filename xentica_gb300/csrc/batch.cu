@@ -1,0 +1,424 @@
+// Ensembles of independent Life-like lattices (include/xk.h, xk_batch_*).
+//
+// Every instance keeps the reference's one-byte-per-cell layout in HBM,
+// concatenated in creation order.  The batched form advances all of them with
+// the resident kernel: one CTA per instance loads it (packing to 32 cells per
+// word), runs every generation of the call out of shared memory and stores it
+// back, so HBM sees two bytes per cell per call however many generations run.
+// Instances are grouped into classes with the same CTA shape (threads,
+// shared memory); each class is one launch, classes run concurrently on their
+// own streams, and the whole fork/join is captured once per generation count
+// as a CUDA graph.  Instances too wide or too large for one CTA take the plain
+// path below.
+//
+// The plain form is the reference's execution model on the same GPU: one
+// launch per instance per generation over the byte layout.
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <new>
+#include <vector>
+
+#include "xk_internal.cuh"
+
+namespace {
+
+struct Class {
+    int threads = 0, smem = 0;
+    int first = 0, count = 0;      // range in the sorted instance table
+    cudaStream_t stream = nullptr;
+};
+
+}  // namespace
+
+struct xk_batch {
+    int n = 0;
+    std::vector<int32_t> W, H;
+    std::vector<uint32_t> rule;
+    std::vector<int64_t> off;      // byte offset of each instance
+    int64_t total = 0;
+    uint8_t *cells = nullptr;      // current state, bytes
+    uint8_t *scratch = nullptr;    // plain-form ping-pong partner
+    unsigned int *bad = nullptr;   // value-check flag of the resident kernel
+    LifeInst *d_inst = nullptr;
+    std::vector<LifeInst> h_inst;  // sorted by class, largest first
+    std::vector<Class> classes;
+    std::vector<int> big;          // instances run with the plain kernel
+    int rows_per_band = 8;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, fork = nullptr;
+    std::vector<cudaEvent_t> joins;
+    std::map<int, cudaGraphExec_t> graphs;
+};
+
+static void destroy_graphs(xk_batch *b)
+{
+    for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    b->graphs.clear();
+}
+
+static void free_batch(xk_batch *b)
+{
+    if (!b) return;
+    destroy_graphs(b);
+    for (auto &c : b->classes)
+        if (c.stream) cudaStreamDestroy(c.stream);
+    for (auto e : b->joins) cudaEventDestroy(e);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->cells) cudaFree(b->cells);
+    if (b->scratch) cudaFree(b->scratch);
+    if (b->bad) cudaFree(b->bad);
+    if (b->d_inst) cudaFree(b->d_inst);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+static inline uint32_t rule0_of(uint32_t golly) { return golly & 511u; }
+static inline uint32_t rule1_of(uint32_t golly) { return (golly & 511u) | ((golly >> 9) & 511u); }
+
+// (re)build the class table for the current rows_per_band
+static int plan_classes(xk_batch *b)
+{
+    destroy_graphs(b);
+    for (auto &c : b->classes)
+        if (c.stream) cudaStreamDestroy(c.stream);
+    for (auto e : b->joins) cudaEventDestroy(e);
+    b->classes.clear();
+    b->joins.clear();
+    b->big.clear();
+    struct Item {
+        int idx, threads, smem;
+        int64_t cells;
+    };
+    std::vector<Item> items;
+    for (int i = 0; i < b->n; ++i) {
+        int threads = 0, smem = 0;
+        if (xk_life_resident_config(b->W[i], b->H[i], b->rows_per_band, &threads, &smem))
+            items.push_back({i, threads, smem, (int64_t)b->W[i] * b->H[i]});
+        else
+            b->big.push_back(i);
+    }
+    // classes: same block size, shared memory rounded up to 8 KB buckets
+    std::sort(items.begin(), items.end(), [](const Item &a, const Item &c) {
+        if (a.threads != c.threads) return a.threads > c.threads;
+        if (a.smem != c.smem) return a.smem > c.smem;
+        return a.cells > c.cells;
+    });
+    b->h_inst.clear();
+    for (size_t k = 0; k < items.size(); ++k) {
+        const Item &it = items[k];
+        const int bucket = (it.smem + 8191) / 8192 * 8192;
+        if (b->classes.empty() || b->classes.back().threads != it.threads ||
+            (b->classes.back().smem + 8191) / 8192 * 8192 != bucket) {
+            Class c;
+            c.threads = it.threads;
+            c.smem = it.smem;   // the first (largest) member sets the allocation
+            c.first = (int)k;
+            b->classes.push_back(c);
+        }
+        Class &c = b->classes.back();
+        c.smem = std::max(c.smem, it.smem);
+        c.count++;
+        LifeInst in;
+        memset(&in, 0, sizeof(in));
+        in.off = b->off[it.idx];
+        in.W = b->W[it.idx];
+        in.H = b->H[it.idx];
+        in.wpr = (in.W + 31) / 32;
+        in.rlast = in.W - 32 * (in.wpr - 1);
+        in.lastmask = in.rlast == 32 ? 0xFFFFFFFFu : ((1u << in.rlast) - 1u);
+        in.rule0 = rule0_of(b->rule[it.idx]);
+        in.rule1 = rule1_of(b->rule[it.idx]);
+        in.smem_words = it.smem / 4;
+        b->h_inst.push_back(in);
+    }
+    for (auto &c : b->classes) {
+        XK_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+        cudaEvent_t e;
+        XK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        b->joins.push_back(e);
+    }
+    if (b->d_inst) cudaFree(b->d_inst);
+    b->d_inst = nullptr;
+    if (!b->h_inst.empty()) {
+        XK_CUDA(cudaMalloc(&b->d_inst, b->h_inst.size() * sizeof(LifeInst)));
+        XK_CUDA(cudaMemcpy(b->d_inst, b->h_inst.data(), b->h_inst.size() * sizeof(LifeInst),
+                           cudaMemcpyHostToDevice));
+    }
+    return XK_OK;
+}
+
+extern "C" int xk_batch_create(int32_t count, const int32_t *width, const int32_t *height,
+                               const uint32_t *rule, xk_batch **out)
+{
+    XK_REQUIRE(out && width && height && rule, XK_ERR_ARG, "xk_batch_create: null argument");
+    *out = nullptr;
+    XK_REQUIRE(count > 0, XK_ERR_ARG, "xk_batch_create: count %d", count);
+    xk_batch *b = new (std::nothrow) xk_batch();
+    XK_REQUIRE(b, XK_ERR_OOM, "host allocation failed");
+    b->n = count;
+    b->W.assign(width, width + count);
+    b->H.assign(height, height + count);
+    b->rule.assign(rule, rule + count);
+    b->off.resize(count);
+    for (int i = 0; i < count; ++i) {
+        if (b->W[i] < 1 || b->H[i] < 1 || (int64_t)b->W[i] * b->H[i] > (1LL << 31)) {
+            xk_set_error("instance %d has size %dx%d", i, b->W[i], b->H[i]);
+            free_batch(b);
+            return XK_ERR_ARG;
+        }
+        if (b->rule[i] >> 18) {
+            xk_set_error("instance %d rule %u has bits above 17", i, b->rule[i]);
+            free_batch(b);
+            return XK_ERR_ARG;
+        }
+        b->off[i] = b->total;
+        b->total += (int64_t)b->W[i] * b->H[i];
+    }
+    int rc = XK_OK;
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreate(&b->ev0)) != cudaSuccess || (e = cudaEventCreate(&b->ev1)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaMalloc(&b->cells, (size_t)b->total + 16)) != cudaSuccess ||
+        (e = cudaMalloc(&b->bad, sizeof(unsigned int))) != cudaSuccess ||
+        (e = cudaMemset(b->cells, 0, (size_t)b->total + 16)) != cudaSuccess ||
+        (e = cudaMemset(b->bad, 0, sizeof(unsigned int))) != cudaSuccess) {
+        rc = xk_cuda_status(e, "xk_batch_create");
+        free_batch(b);
+        return rc;
+    }
+    rc = plan_classes(b);
+    if (rc != XK_OK) {
+        free_batch(b);
+        return rc;
+    }
+    *out = b;
+    return XK_OK;
+}
+
+extern "C" void xk_batch_destroy(xk_batch *b)
+{
+    if (b && b->stream) cudaStreamSynchronize(b->stream);
+    free_batch(b);
+}
+
+extern "C" int64_t xk_batch_total_cells(const xk_batch *b) { return b ? b->total : -1; }
+
+extern "C" int xk_batch_upload(xk_batch *b, const uint8_t *host_cells, int64_t total_cells)
+{
+    XK_REQUIRE(b && host_cells, XK_ERR_ARG, "xk_batch_upload: null argument");
+    XK_REQUIRE(total_cells == b->total, XK_ERR_ARG, "xk_batch_upload: %lld cells, batch has %lld",
+               (long long)total_cells, (long long)b->total);
+    XK_CUDA(cudaMemcpyAsync(b->cells, host_cells, (size_t)b->total, cudaMemcpyHostToDevice, b->stream));
+    XK_CUDA(cudaStreamSynchronize(b->stream));
+    return XK_OK;
+}
+
+extern "C" int xk_batch_download(xk_batch *b, uint8_t *host_cells, int64_t total_cells)
+{
+    XK_REQUIRE(b && host_cells, XK_ERR_ARG, "xk_batch_download: null argument");
+    XK_REQUIRE(total_cells == b->total, XK_ERR_ARG, "xk_batch_download: %lld cells, batch has %lld",
+               (long long)total_cells, (long long)b->total);
+    XK_CUDA(cudaMemcpyAsync(host_cells, b->cells, (size_t)b->total, cudaMemcpyDeviceToHost, b->stream));
+    XK_CUDA(cudaStreamSynchronize(b->stream));
+    return XK_OK;
+}
+
+// plain per-generation launches for one instance (also used for instances
+// the resident kernel cannot hold)
+static int plain_instance(xk_batch *b, int i, int generations, cudaStream_t s)
+{
+    if (!b->scratch) XK_CUDA(cudaMalloc(&b->scratch, (size_t)b->total + 16));
+    uint8_t *a = b->cells + b->off[i], *c = b->scratch + b->off[i];
+    const uint32_t r0 = rule0_of(b->rule[i]), r1 = rule1_of(b->rule[i]);
+    for (int g = 0; g < generations; ++g) {
+        XK_CUDA(xk_life_step_bytes2d(a, c, b->W[i], b->H[i], r0, r1, s));
+        std::swap(a, c);
+    }
+    if (generations & 1)
+        XK_CUDA(cudaMemcpyAsync(b->cells + b->off[i], a, (size_t)b->W[i] * b->H[i],
+                                cudaMemcpyDeviceToDevice, s));
+    return XK_OK;
+}
+
+// record the batched step (fork, one launch per class, join) on b->stream
+static int enqueue_batched(xk_batch *b, int generations)
+{
+    XK_CUDA(cudaEventRecord(b->fork, b->stream));
+    for (size_t k = 0; k < b->classes.size(); ++k) {
+        const Class &c = b->classes[k];
+        XK_CUDA(cudaStreamWaitEvent(c.stream, b->fork, 0));
+        XK_CUDA(xk_life_step_resident(b->d_inst + c.first, c.count, b->cells, 1, generations, 1, 0u,
+                                      b->bad, c.threads, c.smem, c.stream));
+        XK_CUDA(cudaEventRecord(b->joins[k], c.stream));
+    }
+    for (int i : b->big) {
+        int rc = plain_instance(b, i, generations, b->stream);
+        if (rc != XK_OK) return rc;
+    }
+    for (size_t k = 0; k < b->classes.size(); ++k) XK_CUDA(cudaStreamWaitEvent(b->stream, b->joins[k], 0));
+    return XK_OK;
+}
+
+static int graph_for(xk_batch *b, int generations, cudaGraphExec_t *exec)
+{
+    auto it = b->graphs.find(generations);
+    if (it != b->graphs.end()) {
+        *exec = it->second;
+        return XK_OK;
+    }
+    if (!b->big.empty() && !b->scratch) XK_CUDA(cudaMalloc(&b->scratch, (size_t)b->total + 16));
+    // kernel attributes are set outside capture
+    for (const Class &c : b->classes)
+        XK_CUDA(xk_life_step_resident(b->d_inst + c.first, 0, b->cells, 1, 0, 1, 0u, b->bad,
+                                      c.threads, c.smem, b->stream));
+    XK_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_batched(b, generations);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+    if (rc != XK_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    XK_CUDA(e);
+    cudaGraphExec_t g = nullptr;
+    e = cudaGraphInstantiate(&g, graph, 0);
+    cudaGraphDestroy(graph);
+    XK_CUDA(e);
+    b->graphs[generations] = g;
+    *exec = g;
+    return XK_OK;
+}
+
+static int check_bad(xk_batch *b)
+{
+    unsigned int hbad = 0;
+    XK_CUDA(cudaMemcpyAsync(&hbad, b->bad, sizeof(hbad), cudaMemcpyDeviceToHost, b->stream));
+    XK_CUDA(cudaStreamSynchronize(b->stream));
+    if (hbad) {
+        XK_CUDA(cudaMemsetAsync(b->bad, 0, sizeof(unsigned int), b->stream));
+        XK_CUDA(cudaStreamSynchronize(b->stream));
+        xk_set_error("ensemble cells must hold 0 or 1; the uploaded state has other values");
+        return XK_ERR_ARG;
+    }
+    return XK_OK;
+}
+
+extern "C" int xk_batch_step(xk_batch *b, int32_t generations)
+{
+    XK_REQUIRE(b, XK_ERR_ARG, "xk_batch_step: null batch");
+    XK_REQUIRE(generations >= 0, XK_ERR_ARG, "xk_batch_step: negative generations");
+    if (generations == 0) return XK_OK;
+    cudaGraphExec_t g;
+    int rc = graph_for(b, generations, &g);
+    if (rc != XK_OK) return rc;
+    XK_CUDA(cudaEventRecord(b->ev0, b->stream));
+    XK_CUDA(cudaGraphLaunch(g, b->stream));
+    XK_CUDA(cudaEventRecord(b->ev1, b->stream));
+    XK_CUDA(cudaEventSynchronize(b->ev1));
+    float ms = 0.f;
+    XK_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    xk_set_last_step_ms(ms);
+    return check_bad(b);
+}
+
+extern "C" int xk_batch_step_plain(xk_batch *b, int32_t generations)
+{
+    XK_REQUIRE(b, XK_ERR_ARG, "xk_batch_step_plain: null batch");
+    XK_REQUIRE(generations >= 0, XK_ERR_ARG, "xk_batch_step_plain: negative generations");
+    XK_CUDA(cudaEventRecord(b->ev0, b->stream));
+    // generation-major order, like a host loop calling step() on every model
+    if (!b->scratch) XK_CUDA(cudaMalloc(&b->scratch, (size_t)b->total + 16));
+    for (int g = 0; g < generations; ++g) {
+        uint8_t *src = (g & 1) ? b->scratch : b->cells;
+        uint8_t *dst = (g & 1) ? b->cells : b->scratch;
+        for (int i = 0; i < b->n; ++i)
+            XK_CUDA(xk_life_step_bytes2d(src + b->off[i], dst + b->off[i], b->W[i], b->H[i],
+                                         rule0_of(b->rule[i]), rule1_of(b->rule[i]), b->stream));
+    }
+    if (generations & 1)
+        XK_CUDA(cudaMemcpyAsync(b->cells, b->scratch, (size_t)b->total, cudaMemcpyDeviceToDevice,
+                                b->stream));
+    XK_CUDA(cudaEventRecord(b->ev1, b->stream));
+    XK_CUDA(cudaEventSynchronize(b->ev1));
+    float ms = 0.f;
+    XK_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    xk_set_last_step_ms(ms);
+    return XK_OK;
+}
+
+extern "C" int xk_batch_run(xk_batch *b, const uint8_t *host_in, uint8_t *host_out,
+                            int64_t total_cells, int32_t generations)
+{
+    XK_REQUIRE(b && host_in && host_out, XK_ERR_ARG, "xk_batch_run: null argument");
+    XK_REQUIRE(total_cells == b->total, XK_ERR_ARG, "xk_batch_run: %lld cells, batch has %lld",
+               (long long)total_cells, (long long)b->total);
+    XK_REQUIRE(generations >= 0, XK_ERR_ARG, "xk_batch_run: negative generations");
+    cudaGraphExec_t g = nullptr;
+    if (generations > 0) {
+        int rc = graph_for(b, generations, &g);
+        if (rc != XK_OK) return rc;
+    }
+    XK_CUDA(cudaEventRecord(b->ev0, b->stream));
+    XK_CUDA(cudaMemcpyAsync(b->cells, host_in, (size_t)b->total, cudaMemcpyHostToDevice, b->stream));
+    if (g) XK_CUDA(cudaGraphLaunch(g, b->stream));
+    XK_CUDA(cudaMemcpyAsync(host_out, b->cells, (size_t)b->total, cudaMemcpyDeviceToHost, b->stream));
+    XK_CUDA(cudaEventRecord(b->ev1, b->stream));
+    XK_CUDA(cudaEventSynchronize(b->ev1));
+    float ms = 0.f;
+    XK_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    xk_set_last_step_ms(ms);
+    return check_bad(b);
+}
+
+extern "C" int xk_batch_tune(xk_batch *b, int32_t generations, int32_t *chosen)
+{
+    XK_REQUIRE(b && chosen, XK_ERR_ARG, "xk_batch_tune: null argument");
+    XK_REQUIRE(generations > 0, XK_ERR_ARG, "xk_batch_tune: generations must be positive");
+    // candidates for the band length; each is timed on a copy of the state so
+    // tuning never changes the batch's cells
+    static const int cand[] = {2, 4, 8, 16, 32};
+    uint8_t *keep = nullptr;
+    XK_CUDA(cudaMalloc(&keep, (size_t)b->total + 16));
+    XK_CUDA(cudaMemcpyAsync(keep, b->cells, (size_t)b->total, cudaMemcpyDeviceToDevice, b->stream));
+    float best = 1e30f;
+    int best_rpb = b->rows_per_band;
+    int rc = XK_OK;
+    for (int r : cand) {
+        b->rows_per_band = r;
+        if ((rc = plan_classes(b)) != XK_OK) break;
+        cudaGraphExec_t g;
+        if ((rc = graph_for(b, generations, &g)) != XK_OK) break;
+        float ms = 0.f;
+        for (int rep = 0; rep < 2; ++rep) {
+            cudaEventRecord(b->ev0, b->stream);
+            cudaGraphLaunch(g, b->stream);
+            cudaEventRecord(b->ev1, b->stream);
+            cudaEventSynchronize(b->ev1);
+            cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+        }
+        if (ms < best) {
+            best = ms;
+            best_rpb = r;
+        }
+    }
+    cudaMemcpyAsync(b->cells, keep, (size_t)b->total, cudaMemcpyDeviceToDevice, b->stream);
+    cudaStreamSynchronize(b->stream);
+    cudaFree(keep);
+    if (rc != XK_OK) return rc;
+    b->rows_per_band = best_rpb;
+    rc = plan_classes(b);
+    *chosen = best_rpb;
+    return rc;
+}
+
+extern "C" int64_t xk_batch_launches(const xk_batch *b, int32_t generations)
+{
+    if (!b) return -1;
+    return (int64_t)b->classes.size() + (int64_t)b->big.size() * generations +
+           (int64_t)b->big.size() * (generations & 1);
+}

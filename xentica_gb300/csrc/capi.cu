@@ -1,0 +1,510 @@
+// C-ABI of single models (include/xk.h): device state, layout conversion and
+// generation stepping for the kernel families.
+#include <stdarg.h>
+#include <string.h>
+
+#include <mutex>
+#include <new>
+
+#include "xk_internal.cuh"
+
+// ---------------------------------------------------------------------------
+// errors
+
+static thread_local char g_err[1024] = "";
+static std::mutex g_ms_mu;
+static double g_last_ms = 0.0;
+
+void xk_set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int xk_cuda_status(cudaError_t err, const char *what)
+{
+    xk_set_error("CUDA error in %s: %s", what, cudaGetErrorString(err));
+    return err == cudaErrorMemoryAllocation ? XK_ERR_OOM : XK_ERR_CUDA;
+}
+
+void xk_set_last_step_ms(double ms)
+{
+    std::lock_guard<std::mutex> lk(g_ms_mu);
+    g_last_ms = ms;
+}
+
+extern "C" double xk_last_step_ms(void)
+{
+    std::lock_guard<std::mutex> lk(g_ms_mu);
+    return g_last_ms;
+}
+
+extern "C" const char *xk_last_error(void) { return g_err; }
+
+int xk_sm_count()
+{
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    return sms;
+}
+
+int xk_max_smem_optin()
+{
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
+    return v;
+}
+
+extern "C" int xk_device_info(char *buf, int32_t len)
+{
+    int dev = 0;
+    XK_CUDA(cudaGetDevice(&dev));
+    cudaDeviceProp p;
+    XK_CUDA(cudaGetDeviceProperties(&p, dev));
+    snprintf(buf, len, "%s sm_%d%d SMs=%d smem_optin=%zu", p.name, p.major, p.minor,
+             p.multiProcessorCount, (size_t)p.sharedMemPerBlockOptin);
+    return XK_OK;
+}
+
+// ---------------------------------------------------------------------------
+// model object
+
+enum { LAYOUT_BITS2D = 1, LAYOUT_BYTES = 2 };
+
+struct xk_model {
+    xk_desc d;
+    int64_t n = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int layout = 0;
+    LifeGeo lg;
+    NdGeo ng;
+    uint32_t *bits[2] = {nullptr, nullptr};
+    uint8_t *bytes[2] = {nullptr, nullptr};
+    int cur = 0;
+    void *stage = nullptr;       // reference-layout staging + validity flag
+    int32_t *col = nullptr;      // colours (3 int32 per cell) when materialised
+    int32_t *img = nullptr;
+    int64_t img_cap = 0;
+    LifeInst *d_inst = nullptr;  // the lattice as a one-instance resident batch
+    int resident = 0, res_threads = 0, res_smem = 0;
+    uint32_t rule0 = 0, rule1 = 0;
+    int32_t lut[6] = {0, 0, 0, 0, 0, 0};
+    int hf = 0;                  // colour is a function of the state alone
+    int derived = 0;             // colours currently implied by the state
+    int uploaded = 0;
+};
+
+static int64_t cells_of(const xk_desc &d)
+{
+    int64_t n = 1;
+    for (int i = 0; i < d.ndim; ++i) n *= d.size[i];
+    return n;
+}
+
+static bool is_moore2d(const xk_desc &d)
+{
+    if (d.ndim != 2 || d.nbr != 8) return false;
+    // Moore 2-D neighbour order of the reference: product([-1,0,1], repeat=2)
+    // without (0,0); any order works for a totalistic count, but every offset
+    // must appear once
+    int seen = 0;
+    for (int k = 0; k < 8; ++k) {
+        int dx = d.delta[k][0], dy = d.delta[k][1];
+        if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || (dx == 0 && dy == 0)) return false;
+        seen |= 1 << ((dy + 1) * 3 + (dx + 1));
+    }
+    return seen == (0x1FF & ~(1 << 4));
+}
+
+int xk_life_resident_config(int W, int H, int rows_per_band, int *threads, int *smem_bytes)
+{
+    const int wpr = (W + 31) / 32;
+    if (wpr > 32) return 0;
+    int P = 1;
+    while (P < wpr) P <<= 1;
+    const int gpw = 32 / P;
+    const int groups = (H + rows_per_band - 1) / rows_per_band;
+    int warps = (groups + gpw - 1) / gpw;
+    if (warps > 32) warps = 32;
+    if (warps < 1) warps = 1;
+    const int64_t words = xk_life_resident_words(W, H, warps * 32);
+    const int64_t bytes = words * 4;
+    if (words < 0 || bytes > xk_max_smem_optin()) return 0;
+    *threads = warps * 32;
+    *smem_bytes = (int)bytes;
+    return 1;
+}
+
+static int resident_plan_for(xk_model *m)
+{
+    return xk_life_resident_config(m->lg.W, m->lg.H, 8, &m->res_threads, &m->res_smem);
+}
+
+static void free_model(xk_model *m)
+{
+    if (!m) return;
+    for (int i = 0; i < 2; ++i) {
+        if (m->bits[i]) cudaFree(m->bits[i]);
+        if (m->bytes[i]) cudaFree(m->bytes[i]);
+    }
+    if (m->stage) cudaFree(m->stage);
+    if (m->col) cudaFree(m->col);
+    if (m->img) cudaFree(m->img);
+    if (m->d_inst) cudaFree(m->d_inst);
+    if (m->ev0) cudaEventDestroy(m->ev0);
+    if (m->ev1) cudaEventDestroy(m->ev1);
+    if (m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+}
+
+static int upload_inst(xk_model *m)
+{
+    LifeInst in;
+    memset(&in, 0, sizeof(in));
+    in.off = 0;
+    in.W = m->lg.W;
+    in.H = m->lg.H;
+    in.wpr = m->lg.wpr;
+    in.rlast = m->lg.rlast;
+    in.lastmask = m->lg.lastmask;
+    in.rule0 = m->rule0;
+    in.rule1 = m->rule1;
+    in.smem_words = m->res_smem / 4;
+    XK_CUDA(cudaMemcpyAsync(m->d_inst, &in, sizeof(in), cudaMemcpyHostToDevice, m->stream));
+    return XK_OK;
+}
+
+extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
+{
+    XK_REQUIRE(desc && out, XK_ERR_ARG, "xk_model_create: null argument");
+    *out = nullptr;
+    const xk_desc &d = *desc;
+    XK_REQUIRE(d.abi_version == XK_ABI_VERSION, XK_ERR_ARG, "ABI version %d, library has %d",
+               d.abi_version, XK_ABI_VERSION);
+    XK_REQUIRE(d.ndim >= 1 && d.ndim <= XK_MAXDIM, XK_ERR_ARG, "ndim %d outside 1..%d", d.ndim,
+               XK_MAXDIM);
+    XK_REQUIRE(d.nbr >= 1 && d.nbr <= XK_MAXNBR - 1, XK_ERR_ARG, "%d neighbours outside 1..%d",
+               d.nbr, XK_MAXNBR - 1);
+    for (int i = 0; i < d.ndim; ++i)
+        XK_REQUIRE(d.size[i] >= 1 && d.size[i] <= (1LL << 31) - 1, XK_ERR_ARG,
+                   "size[%d] = %lld out of range", i, (long long)d.size[i]);
+    XK_REQUIRE(d.state_bytes == 1 || d.state_bytes == 2 || d.state_bytes == 4 || d.state_bytes == 8,
+               XK_ERR_ARG, "state_bytes %d", d.state_bytes);
+    const int64_t n = cells_of(d);
+    XK_REQUIRE(n <= (1LL << 40), XK_ERR_ARG, "lattice of %lld cells too large", (long long)n);
+    XK_REQUIRE(d.family == XK_FAMILY_LIFE, XK_ERR_UNSUPPORTED,
+               "model family %d is not available in this build", d.family);
+    XK_REQUIRE(d.rule0 >> (d.nbr + 1) == 0 && d.rule1 >> (d.nbr + 1) == 0, XK_ERR_ARG,
+               "rule tables have bits above %d neighbours", d.nbr);
+
+    xk_model *m = new (std::nothrow) xk_model();
+    XK_REQUIRE(m, XK_ERR_OOM, "host allocation failed");
+    m->d = d;
+    m->n = n;
+    m->rule0 = d.rule0;
+    m->rule1 = d.rule1;
+    memcpy(m->lut, d.color_lut, sizeof(m->lut));
+    m->hf = d.color_history_free;
+    int rc = XK_OK;
+#define XK_TRY(call)                                                          \
+    do {                                                                      \
+        cudaError_t e_ = (call);                                              \
+        if (e_ != cudaSuccess) { rc = xk_cuda_status(e_, #call); goto fail; } \
+    } while (0)
+    XK_TRY(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+    XK_TRY(cudaEventCreate(&m->ev0));
+    XK_TRY(cudaEventCreate(&m->ev1));
+    {
+        const int border_state = (int)(d.border_value & 1u);
+        if (is_moore2d(d)) {
+            m->layout = LAYOUT_BITS2D;
+            m->lg = xk_life_geo(d.size[0], d.size[1], d.torus, border_state);
+            const size_t words = (size_t)m->lg.H * m->lg.wpr;
+            XK_TRY(cudaMalloc(&m->bits[0], (words + 4) * 4));
+            XK_TRY(cudaMalloc(&m->bits[1], (words + 4) * 4));
+            XK_TRY(cudaMemsetAsync(m->bits[0], 0, (words + 4) * 4, m->stream));
+            XK_TRY(cudaMalloc(&m->d_inst, sizeof(LifeInst)));
+            m->resident = resident_plan_for(m);
+        } else {
+            m->layout = LAYOUT_BYTES;
+            memset(&m->ng, 0, sizeof(m->ng));
+            m->ng.ndim = d.ndim;
+            m->ng.nbr = d.nbr;
+            m->ng.torus = d.torus;
+            m->ng.border_state = (uint32_t)border_state;
+            for (int i = 0; i < d.ndim; ++i) m->ng.size[i] = d.size[i];
+            memcpy(m->ng.delta, d.delta, sizeof(m->ng.delta));
+            const size_t bytes = ((size_t)n + 15) / 16 * 16 + 16;
+            XK_TRY(cudaMalloc(&m->bytes[0], bytes));
+            XK_TRY(cudaMalloc(&m->bytes[1], bytes));
+            XK_TRY(cudaMemsetAsync(m->bytes[0], 0, bytes, m->stream));
+        }
+        XK_TRY(cudaMalloc(&m->stage, (size_t)n * d.state_bytes + 16));
+        XK_TRY(cudaMalloc(&m->col, (size_t)n * 3 * sizeof(int32_t)));
+        XK_TRY(cudaMemsetAsync(m->col, 0, (size_t)n * 3 * sizeof(int32_t), m->stream));
+    }
+    if (m->layout == LAYOUT_BITS2D) {
+        rc = upload_inst(m);
+        if (rc != XK_OK) goto fail;
+    }
+    XK_TRY(cudaStreamSynchronize(m->stream));
+#undef XK_TRY
+    *out = m;
+    return XK_OK;
+fail:
+    free_model(m);
+    return rc;
+}
+
+extern "C" void xk_model_destroy(xk_model *m)
+{
+    if (m && m->stream) cudaStreamSynchronize(m->stream);
+    free_model(m);
+}
+
+extern "C" int xk_upload(xk_model *m, const void *host_main, int64_t ncells)
+{
+    XK_REQUIRE(m && host_main, XK_ERR_ARG, "xk_upload: null argument");
+    XK_REQUIRE(ncells == m->n, XK_ERR_ARG, "xk_upload: %lld cells given, model has %lld",
+               (long long)ncells, (long long)m->n);
+    const int esz = m->d.state_bytes;
+    XK_CUDA(cudaMemcpyAsync(m->stage, host_main, (size_t)m->n * esz, cudaMemcpyHostToDevice,
+                            m->stream));
+    unsigned int *bad;
+    if (m->layout == LAYOUT_BITS2D) {
+        XK_CUDA(xk_life_pack(m->stage, esz, m->bits[m->cur], m->lg, m->stream));
+        bad = (unsigned int *)(m->bits[m->cur] + (int64_t)m->lg.H * m->lg.wpr);
+    } else {
+        XK_CUDA(xk_nd_pack(m->stage, esz, m->bytes[m->cur], m->n, m->stream));
+        bad = (unsigned int *)(m->bytes[m->cur] + ((m->n + 15) / 16) * 16);
+    }
+    unsigned int hbad = 0;
+    XK_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(hbad), cudaMemcpyDeviceToHost, m->stream));
+    XK_CUDA(cudaStreamSynchronize(m->stream));
+    XK_REQUIRE(hbad == 0, XK_ERR_ARG,
+               "Life-like kernel needs every cell state to be 0 or 1; the upload has other values");
+    m->uploaded = 1;
+    return XK_OK;
+}
+
+extern "C" int xk_download(xk_model *m, void *host_main, int64_t ncells)
+{
+    XK_REQUIRE(m && host_main, XK_ERR_ARG, "xk_download: null argument");
+    XK_REQUIRE(ncells == m->n, XK_ERR_ARG, "xk_download: %lld cells given, model has %lld",
+               (long long)ncells, (long long)m->n);
+    const int esz = m->d.state_bytes;
+    if (m->layout == LAYOUT_BITS2D)
+        XK_CUDA(xk_life_unpack(m->bits[m->cur], m->stage, esz, m->lg, m->stream));
+    else
+        XK_CUDA(xk_nd_unpack(m->bytes[m->cur], m->stage, esz, m->n, m->stream));
+    XK_CUDA(cudaMemcpyAsync(host_main, m->stage, (size_t)m->n * esz, cudaMemcpyDeviceToHost,
+                            m->stream));
+    XK_CUDA(cudaStreamSynchronize(m->stream));
+    return XK_OK;
+}
+
+// write the colours implied by the state into m->col
+static int materialize_colors(xk_model *m)
+{
+    if (!m->derived) return XK_OK;
+    const int smooth = m->d.color_kind == XK_COLOR_MOVING_AVERAGE ? m->d.smooth : 1;
+    if (m->layout == LAYOUT_BITS2D)
+        XK_CUDA(xk_life_colors(m->bits[m->cur], m->col, m->lg, m->lut, smooth, m->stream));
+    else
+        XK_CUDA(xk_nd_colors(m->bytes[m->cur], m->col, m->n, m->lut, smooth, m->stream));
+    m->derived = 0;
+    return XK_OK;
+}
+
+extern "C" int xk_upload_colors(xk_model *m, const int32_t *host_col, int64_t ncells)
+{
+    XK_REQUIRE(m && host_col, XK_ERR_ARG, "xk_upload_colors: null argument");
+    XK_REQUIRE(ncells == m->n, XK_ERR_ARG, "xk_upload_colors: cell count mismatch");
+    XK_CUDA(cudaMemcpyAsync(m->col, host_col, (size_t)m->n * 3 * sizeof(int32_t),
+                            cudaMemcpyHostToDevice, m->stream));
+    XK_CUDA(cudaStreamSynchronize(m->stream));
+    m->derived = 0;
+    return XK_OK;
+}
+
+extern "C" int xk_download_colors(xk_model *m, int32_t *host_col, int64_t ncells)
+{
+    XK_REQUIRE(m && host_col, XK_ERR_ARG, "xk_download_colors: null argument");
+    XK_REQUIRE(ncells == m->n, XK_ERR_ARG, "xk_download_colors: cell count mismatch");
+    int rc = materialize_colors(m);
+    if (rc != XK_OK) return rc;
+    XK_CUDA(cudaMemcpyAsync(host_col, m->col, (size_t)m->n * 3 * sizeof(int32_t),
+                            cudaMemcpyDeviceToHost, m->stream));
+    XK_CUDA(cudaStreamSynchronize(m->stream));
+    return XK_OK;
+}
+
+extern "C" int xk_life_set_rule(xk_model *m, uint32_t rule0, uint32_t rule1,
+                                const int32_t color_lut[6])
+{
+    XK_REQUIRE(m, XK_ERR_ARG, "xk_life_set_rule: null model");
+    XK_REQUIRE(m->d.family == XK_FAMILY_LIFE, XK_ERR_STATE, "not a Life-like model");
+    XK_REQUIRE(rule0 >> (m->d.nbr + 1) == 0 && rule1 >> (m->d.nbr + 1) == 0, XK_ERR_ARG,
+               "rule tables have bits above %d neighbours", m->d.nbr);
+    if (color_lut && memcmp(color_lut, m->lut, sizeof(m->lut)) != 0) {
+        // colours shown until the next step follow the table they were made with
+        int rc = materialize_colors(m);
+        if (rc != XK_OK) return rc;
+        memcpy(m->lut, color_lut, sizeof(m->lut));
+    }
+    if (rule0 != m->rule0 || rule1 != m->rule1) {
+        m->rule0 = rule0;
+        m->rule1 = rule1;
+        if (m->layout == LAYOUT_BITS2D) return upload_inst(m);
+    }
+    return XK_OK;
+}
+
+extern "C" int xk_set_color_mode(xk_model *m, int32_t history_free)
+{
+    XK_REQUIRE(m, XK_ERR_ARG, "xk_set_color_mode: null model");
+    if (!history_free) {
+        int rc = materialize_colors(m);
+        if (rc != XK_OK) return rc;
+    }
+    m->hf = history_free ? 1 : 0;
+    return XK_OK;
+}
+
+static int life_color_step(xk_model *m)
+{
+    if (m->d.color_kind == XK_COLOR_NONE) return XK_OK;
+    const int plain = m->d.color_kind == XK_COLOR_PLAIN;
+    if (m->layout == LAYOUT_BITS2D)
+        XK_CUDA(xk_life_color_step(m->bits[m->cur], m->col, m->lg, m->lut, m->d.fade_in,
+                                   m->d.fade_out, m->d.smooth, plain, m->stream));
+    else
+        XK_CUDA(xk_nd_color_step(m->bytes[m->cur], m->col, m->n, m->lut, m->d.fade_in,
+                                 m->d.fade_out, m->d.smooth, plain, m->stream));
+    return XK_OK;
+}
+
+extern "C" int xk_step(xk_model *m, int64_t nsteps)
+{
+    XK_REQUIRE(m, XK_ERR_ARG, "xk_step: null model");
+    XK_REQUIRE(nsteps >= 0, XK_ERR_ARG, "xk_step: negative step count");
+    XK_REQUIRE(m->uploaded, XK_ERR_STATE, "xk_step before xk_upload");
+    if (nsteps == 0) return XK_OK;
+    const bool colors_free = m->hf || m->d.color_kind == XK_COLOR_NONE;
+    if (!colors_free) {
+        int rc = materialize_colors(m);
+        if (rc != XK_OK) return rc;
+    }
+    XK_CUDA(cudaEventRecord(m->ev0, m->stream));
+    if (m->layout == LAYOUT_BITS2D && m->resident && colors_free) {
+        // whole lattice in shared memory; long runs are cut into launches of
+        // at most 4096 generations
+        int64_t left = nsteps;
+        while (left > 0) {
+            const int g = (int)(left > 4096 ? 4096 : left);
+            XK_CUDA(xk_life_step_resident(m->d_inst, 1, m->bits[m->cur], 0, g, m->lg.torus,
+                                          m->lg.bfill, nullptr, m->res_threads, m->res_smem,
+                                          m->stream));
+            left -= g;
+        }
+    } else {
+        const LifeTable t = xk_life_table(m->rule0, m->rule1);
+        for (int64_t s = 0; s < nsteps; ++s) {
+            if (m->layout == LAYOUT_BITS2D) {
+                if (m->resident)
+                    XK_CUDA(xk_life_step_resident(m->d_inst, 1, m->bits[m->cur], 0, 1, m->lg.torus,
+                                                  m->lg.bfill, nullptr, m->res_threads,
+                                                  m->res_smem, m->stream));
+                else {
+                    XK_CUDA(xk_life_step_global(m->bits[m->cur], m->bits[1 - m->cur], m->lg, t,
+                                                m->stream));
+                    m->cur = 1 - m->cur;
+                }
+            } else {
+                XK_CUDA(xk_life_step_nd(m->bytes[m->cur], m->bytes[1 - m->cur], m->ng, m->rule0,
+                                        m->rule1, m->stream));
+                m->cur = 1 - m->cur;
+            }
+            if (!colors_free) {
+                int rc = life_color_step(m);
+                if (rc != XK_OK) return rc;
+            }
+        }
+    }
+    XK_CUDA(cudaEventRecord(m->ev1, m->stream));
+    XK_CUDA(cudaEventSynchronize(m->ev1));
+    float ms = 0.f;
+    XK_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+    xk_set_last_step_ms(ms);
+    if (colors_free && m->d.color_kind != XK_COLOR_NONE) m->derived = 1;
+    return XK_OK;
+}
+
+extern "C" int xk_render(xk_model *m, int32_t *host_img, int32_t width, int32_t height,
+                         int32_t zoom, int32_t dx, int32_t dy)
+{
+    XK_REQUIRE(m && host_img, XK_ERR_ARG, "xk_render: null argument");
+    XK_REQUIRE(width > 0 && height > 0 && zoom > 0, XK_ERR_ARG, "xk_render: bad viewport %dx%d zoom %d",
+               width, height, zoom);
+    const int64_t npx = (int64_t)width * height;
+    if (npx * 3 > m->img_cap) {
+        if (m->img) cudaFree(m->img);
+        m->img = nullptr;
+        XK_CUDA(cudaMalloc(&m->img, (size_t)npx * 3 * sizeof(int32_t)));
+        m->img_cap = npx * 3;
+    }
+    int rc = materialize_colors(m);
+    if (rc != XK_OK) return rc;
+    RenderGeo g;
+    memset(&g, 0, sizeof(g));
+    g.ndim = m->d.ndim;
+    g.a0 = m->d.proj_axis0;
+    g.a1 = m->d.proj_axis1;
+    for (int i = 0; i < m->d.ndim; ++i) g.size[i] = m->d.size[i];
+    g.smooth = m->d.render_smooth;
+    XK_CUDA(xk_render_colors(m->col, m->img, g, width, height, zoom, dx, dy, m->stream));
+    XK_CUDA(cudaMemcpyAsync(host_img, m->img, (size_t)npx * 3 * sizeof(int32_t),
+                            cudaMemcpyDeviceToHost, m->stream));
+    XK_CUDA(cudaStreamSynchronize(m->stream));
+    return XK_OK;
+}
+
+extern "C" int xk_mass_totals(xk_model *m, uint64_t *host_totals, int64_t count)
+{
+    XK_REQUIRE(m && host_totals, XK_ERR_ARG, "xk_mass_totals: null argument");
+    XK_REQUIRE(m->d.family == XK_FAMILY_MASS, XK_ERR_STATE, "not a mass-transfer model");
+    (void)count;
+    return XK_ERR_UNSUPPORTED;
+}
+
+extern "C" int xk_sync(xk_model *m)
+{
+    XK_REQUIRE(m, XK_ERR_ARG, "xk_sync: null model");
+    XK_CUDA(cudaStreamSynchronize(m->stream));
+    return XK_OK;
+}
+
+extern "C" int xk_set_device(int32_t device)
+{
+    XK_CUDA(cudaSetDevice(device));
+    return XK_OK;
+}
+
+extern "C" int xk_host_register(void *ptr, int64_t bytes)
+{
+    XK_REQUIRE(ptr && bytes > 0, XK_ERR_ARG, "xk_host_register: bad buffer");
+    XK_CUDA(cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault));
+    return XK_OK;
+}
+
+extern "C" int xk_host_unregister(void *ptr)
+{
+    XK_REQUIRE(ptr, XK_ERR_ARG, "xk_host_unregister: null pointer");
+    XK_CUDA(cudaHostUnregister(ptr));
+    return XK_OK;
+}

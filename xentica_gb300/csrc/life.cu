@@ -1,0 +1,625 @@
+// Life-like (outer-totalistic, binary state) generation kernels for sm_103a.
+//
+// Reference semantics: GameOfLife / LifelikeCA emit copies the state to every
+// buffer and absorb applies  next = ((B >> k) & 1) | ((S >> k) & 1 & state)
+// with k = sum of the neighbours' buffers (examples/game_of_life.py:42-70,
+// :183-203; buffers and planes per xentica/core/base.py:226-236).  Emit and
+// absorb are fused: a cell's buffer towards each neighbour equals its state,
+// so absorb can read the neighbours' states directly and the N buffer planes
+// never exist.  The rule arrives as a truth table (rule0 for dead cells,
+// rule1 for live ones) extracted from the traced model.
+//
+// Layout: 32 cells per 32-bit word, LSB = lowest x; a generation is pure
+// bitwise logic -- a carry-save adder network counts the 8 neighbours of 32
+// cells at once and a LOP3 multiplexer tree applies the runtime rule.
+#include "xk_internal.cuh"
+
+LifeTable xk_life_table(uint32_t rule0, uint32_t rule1)
+{
+    LifeTable t;
+    for (int s = 0; s < 2; ++s) {
+        uint32_t r = s ? rule1 : rule0;
+        for (int k = 0; k < 8; ++k) t.tab[s * 8 + k] = ((r >> k) & 1u) ? 0xFFFFFFFFu : 0u;
+        t.t8[s] = ((r >> 8) & 1u) ? 0xFFFFFFFFu : 0u;
+    }
+    return t;
+}
+
+LifeGeo xk_life_geo(int64_t W, int64_t H, int torus, int border_state)
+{
+    LifeGeo g;
+    g.W = (int32_t)W;
+    g.H = (int32_t)H;
+    g.wpr = (int32_t)((W + 31) / 32);
+    g.rlast = (int32_t)(W - 32 * (int64_t)(g.wpr - 1));
+    g.lastmask = g.rlast == 32 ? 0xFFFFFFFFu : ((1u << g.rlast) - 1u);
+    g.torus = torus;
+    g.bfill = border_state ? 0xFFFFFFFFu : 0u;
+    return g;
+}
+
+// ---------------------------------------------------------------------------
+// word-level logic
+
+__device__ __forceinline__ uint32_t xk_mux(uint32_t sel, uint32_t a, uint32_t b)
+{
+    return (a & ~sel) | (b & sel);
+}
+
+__device__ __forceinline__ uint32_t xk_maj(uint32_t a, uint32_t b, uint32_t c)
+{
+    return (a & b) | (c & (a ^ b));
+}
+
+// Next state of 32 cells.  (Lu, Cu, Ru) are the row above shifted so that bit
+// b holds the up-left, up and up-right neighbour of cell b; (Lm, Rm) the left
+// and right neighbours; (Ld, Cd, Rd) the row below; Cm the cells themselves.
+template <class Tab>
+__device__ __forceinline__ uint32_t xk_life_word(uint32_t Lu, uint32_t Cu, uint32_t Ru,
+                                                 uint32_t Lm, uint32_t Cm, uint32_t Rm,
+                                                 uint32_t Ld, uint32_t Cd, uint32_t Rd,
+                                                 const Tab &t)
+{
+    // neighbour count k = b0 + 2 b1 + 4 b2 + 8 b3 (k <= 8, so b3 implies k == 8)
+    const uint32_t su = Lu ^ Cu ^ Ru, cu = xk_maj(Lu, Cu, Ru);
+    const uint32_t sd = Ld ^ Cd ^ Rd, cd = xk_maj(Ld, Cd, Rd);
+    const uint32_t sm = Lm ^ Rm, cm = Lm & Rm;
+    const uint32_t b0 = su ^ sd ^ sm, k1 = xk_maj(su, sd, sm);
+    const uint32_t tw = cu ^ cd ^ cm, k2 = xk_maj(cu, cd, cm);
+    const uint32_t b1 = tw ^ k1, k3 = tw & k1;
+    const uint32_t b2 = k2 ^ k3, b3 = k2 & k3;
+    // rule lookup: multiplexer tree over (state, b2, b1, b0), then b3
+    uint32_t m[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) m[q] = xk_mux(b0, t.tab[2 * q], t.tab[2 * q + 1]);
+    uint32_t n[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) n[q] = xk_mux(b1, m[2 * q], m[2 * q + 1]);
+    const uint32_t dead = xk_mux(b2, n[0], n[1]);
+    const uint32_t live = xk_mux(b2, n[2], n[3]);
+    const uint32_t low = xk_mux(Cm, dead, live);
+    const uint32_t eight = xk_mux(Cm, t.t8[0], t.t8[1]);
+    return xk_mux(b3, low, eight);
+}
+
+// Neighbour vectors of word j of a row, given the row's word and the words
+// left and right of it (already wrapped).  lshift: bit of `left` that is
+// the cell left of bit 0; top: bit of R that receives the cell right of the
+// word's last cell.
+struct RowVec {
+    uint32_t L, C, R;
+};
+
+__device__ __forceinline__ RowVec xk_row_vec(uint32_t c, uint32_t left, uint32_t right,
+                                             int lshift, int top, uint32_t ledge, uint32_t redge,
+                                             int use_ledge, int use_redge)
+{
+    RowVec v;
+    uint32_t lb = use_ledge ? ledge : ((left >> lshift) & 1u);
+    uint32_t rb = use_redge ? redge : (right & 1u);
+    v.C = c;
+    v.L = (c << 1) | lb;
+    v.R = (c >> 1) | (rb << top);
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// one generation straight from global memory (lattices too large for a CTA)
+
+__global__ void __launch_bounds__(256)
+xk_k_life_global(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, LifeGeo g,
+                 LifeTable t)
+{
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)g.H * g.wpr;
+    if (idx >= total) return;
+    const int y = (int)(idx / g.wpr);
+    const int j = (int)(idx - (int64_t)y * g.wpr);
+    const int last = g.wpr - 1;
+    const int jl = j > 0 ? j - 1 : last, jr = j < last ? j + 1 : 0;
+    const int lshift = j > 0 ? 31 : g.rlast - 1;
+    const int top = j == last ? g.rlast - 1 : 31;
+    const int use_le = (!g.torus) && j == 0, use_re = (!g.torus) && j == last;
+    const uint32_t edge = g.bfill & 1u;
+    RowVec v[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        int yy = y + r - 1;
+        bool off = yy < 0 || yy >= g.H;
+        if (off && !g.torus) {
+            v[r].L = v[r].C = v[r].R = g.bfill;
+            continue;
+        }
+        if (yy < 0) yy += g.H;
+        if (yy >= g.H) yy -= g.H;
+        const uint32_t *row = src + (int64_t)yy * g.wpr;
+        v[r] = xk_row_vec(__ldg(row + j), __ldg(row + jl), __ldg(row + jr), lshift, top, edge,
+                          edge, use_le, use_re);
+    }
+    uint32_t out = xk_life_word(v[0].L, v[0].C, v[0].R, v[1].L, v[1].C, v[1].R, v[2].L, v[2].C,
+                                v[2].R, t);
+    if (j == last) out &= g.lastmask;
+    dst[idx] = out;
+}
+
+cudaError_t xk_life_step_global(const uint32_t *src, uint32_t *dst, const LifeGeo &g,
+                                const LifeTable &t, cudaStream_t s)
+{
+    const int64_t total = (int64_t)g.H * g.wpr;
+    const int threads = 256;
+    const int64_t blocks = (total + threads - 1) / threads;
+    xk_k_life_global<<<(unsigned)blocks, threads, 0, s>>>(src, dst, g, t);
+    return cudaGetLastError();
+}
+
+__device__ __forceinline__ LifeTable xk_life_table_dev(uint32_t rule0, uint32_t rule1)
+{
+    LifeTable t;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        t.tab[k] = 0u - ((rule0 >> k) & 1u);
+        t.tab[8 + k] = 0u - ((rule1 >> k) & 1u);
+    }
+    t.t8[0] = 0u - ((rule0 >> 8) & 1u);
+    t.t8[1] = 0u - ((rule1 >> 8) & 1u);
+    return t;
+}
+
+// ---------------------------------------------------------------------------
+// resident lattices: a whole lattice (W <= 1024) lives in shared memory for
+// all generations of a launch; one CTA per lattice.
+//
+// Lanes are grouped: a group of P = next_pow2(wpr) lanes covers one row, lane
+// j of the group owning column word j.  The lattice's rows are cut into one
+// band of consecutive rows per group; a group walks down its band keeping the
+// neighbour vectors of three rows in registers, so every generation costs one
+// shared load, two shuffles and one shared store per 32 cells.  Updates are
+// in place: a lane only ever touches its own column word of its own band, and
+// the first and last row of every band are copied to a halo area before the
+// generation starts, so neighbouring bands read the previous generation.
+//
+// Shared layout interleaves the bands' rows (local row i of band b at
+// (i * G + b) * wpr) so that the groups of a warp hit consecutive words.
+
+struct ResidentPlan {
+    int P, gpw, G, L, nb;  // lanes per group, groups per warp, groups, band length, live bands
+};
+
+__host__ __device__ inline ResidentPlan xk_resident_plan(int wpr, int H, int threads)
+{
+    ResidentPlan p;
+    int P = 1;
+    while (P < wpr) P <<= 1;
+    p.P = P;
+    p.gpw = 32 / P;
+    int groups = (threads / 32) * p.gpw;
+    if (groups > H) groups = H;
+    p.G = groups;
+    p.L = (H + groups - 1) / groups;
+    p.nb = (H + p.L - 1) / p.L;
+    return p;
+}
+
+int64_t xk_life_resident_words(int W, int H, int threads)
+{
+    const int wpr = (W + 31) / 32;
+    if (wpr > 32) return -1;
+    ResidentPlan p = xk_resident_plan(wpr, H, threads);
+    return (int64_t)p.L * p.G * wpr + 2LL * p.G * wpr;
+}
+
+// BYTES = false: the lattice is stored bit-packed (LifeInst.off in words);
+// BYTES = true: one byte per cell, 0/1, row-major (LifeInst.off in bytes) --
+// the reference's own layout, converted to bit-slices while loading and back
+// while storing, so no separate pack/unpack pass touches HBM.
+template <bool BYTES>
+__global__ void __launch_bounds__(1024)
+xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
+                   int generations, int torus, uint32_t bfill, unsigned int *__restrict__ bad)
+{
+    extern __shared__ uint32_t sm[];
+    const LifeInst I = insts[blockIdx.x];
+    const int wpr = I.wpr, H = I.H, W = I.W;
+    const ResidentPlan p = xk_resident_plan(wpr, H, blockDim.x);
+    uint32_t *lat = sm;
+    uint32_t *halo = sm + (int64_t)p.L * p.G * wpr;   // [band][2][wpr]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+
+    // load: global row-major -> band-interleaved shared layout
+    if (BYTES) {
+        const uint8_t *src = (const uint8_t *)state + I.off;
+        unsigned int flag = 0;
+        for (int y = warp; y < H; y += nwarps) {
+            const int b = y / p.L, i = y - b * p.L;
+            for (int jj = 0; jj < wpr; ++jj) {
+                const int x = jj * 32 + lane;
+                const uint32_t v = x < W ? src[(int64_t)y * W + x] : 0u;
+                flag |= v > 1u;
+                const uint32_t w = __ballot_sync(0xFFFFFFFFu, v != 0u);
+                if (lane == 0) lat[(i * p.G + b) * wpr + jj] = w;
+            }
+        }
+        if (flag) atomicOr(bad, 1u);
+    } else {
+        const uint32_t *src = (const uint32_t *)state + I.off;
+        for (int w = threadIdx.x; w < H * wpr; w += blockDim.x) {
+            const int y = w / wpr, jj = w - y * wpr;
+            const int b = y / p.L, i = y - b * p.L;
+            lat[(i * p.G + b) * wpr + jj] = src[w];
+        }
+    }
+
+    const int q = lane / p.P, j = lane - q * p.P;
+    const int band = warp * p.gpw + q;
+    const bool active = band < p.nb && j < wpr;
+    const int y0 = band * p.L;
+    const int y1 = min(H, y0 + p.L);
+    const int last = wpr - 1;
+    const int gbase = q * p.P;
+    const int src_l = gbase + (j > 0 ? j - 1 : last);
+    const int src_r = gbase + (j < last ? j + 1 : 0);
+    const int lshift = j > 0 ? 31 : I.rlast - 1;
+    const int top = j == last ? I.rlast - 1 : 31;
+    const int use_le = (!torus) && j == 0, use_re = (!torus) && j == last;
+    const uint32_t edge = bfill & 1u;
+    const uint32_t outmask = j == last ? I.lastmask : 0xFFFFFFFFu;
+    const LifeTable t = xk_life_table_dev(I.rule0, I.rule1);
+
+    __syncthreads();
+    for (int gen = 0; gen < generations; ++gen) {
+        if (active) {
+            halo[(band * 2 + 0) * wpr + j] = lat[(0 * p.G + band) * wpr + j];
+            halo[(band * 2 + 1) * wpr + j] = lat[((y1 - 1 - y0) * p.G + band) * wpr + j];
+        }
+        __syncthreads();
+        // the row above the band, the band's first row, then rows below
+        uint32_t wu, wm;
+        bool off_u = false;
+        if (band > 0) wu = active ? halo[((band - 1) * 2 + 1) * wpr + j] : 0u;
+        else if (torus) wu = active ? halo[((p.nb - 1) * 2 + 1) * wpr + j] : 0u;
+        else { wu = bfill; off_u = true; }
+        wm = active ? lat[band * wpr + j] : 0u;
+        RowVec vu, vm, vd;
+        {
+            uint32_t l = __shfl_sync(0xFFFFFFFFu, wu, src_l), r = __shfl_sync(0xFFFFFFFFu, wu, src_r);
+            vu = xk_row_vec(wu, l, r, lshift, top, edge, edge, use_le, use_re);
+            if (off_u) vu.L = vu.C = vu.R = bfill;
+            l = __shfl_sync(0xFFFFFFFFu, wm, src_l);
+            r = __shfl_sync(0xFFFFFFFFu, wm, src_r);
+            vm = xk_row_vec(wm, l, r, lshift, top, edge, edge, use_le, use_re);
+        }
+        // every lane runs all L iterations so the shuffles always see the
+        // full warp; rows past the band's end are computed and discarded
+        for (int i = 0; i < p.L; ++i) {
+            const int y = y0 + i;
+            const bool row_ok = active && y < y1;
+            uint32_t wd = 0u;
+            bool off_d = false;
+            if (y + 1 < y1) wd = row_ok ? lat[((i + 1) * p.G + band) * wpr + j] : 0u;
+            else if (y + 1 < H) wd = row_ok ? halo[((band + 1) * 2 + 0) * wpr + j] : 0u;
+            else if (torus) wd = row_ok ? halo[(0 * 2 + 0) * wpr + j] : 0u;
+            else { wd = bfill; off_d = true; }
+            const uint32_t l = __shfl_sync(0xFFFFFFFFu, wd, src_l);
+            const uint32_t r = __shfl_sync(0xFFFFFFFFu, wd, src_r);
+            vd = xk_row_vec(wd, l, r, lshift, top, edge, edge, use_le, use_re);
+            if (off_d) vd.L = vd.C = vd.R = bfill;
+            const uint32_t out = xk_life_word(vu.L, vu.C, vu.R, vm.L, vm.C, vm.R, vd.L, vd.C, vd.R, t);
+            if (row_ok) lat[(i * p.G + band) * wpr + j] = out & outmask;
+            vu = vm;
+            vm = vd;
+        }
+        __syncthreads();
+    }
+    if (BYTES) {
+        uint8_t *dst = (uint8_t *)state + I.off;
+        for (int y = warp; y < H; y += nwarps) {
+            const int b = y / p.L, i = y - b * p.L;
+            const uint32_t *row = lat + (i * p.G + b) * wpr;
+            for (int x = lane; x < W; x += 32) dst[(int64_t)y * W + x] = (uint8_t)((row[x >> 5] >> (x & 31)) & 1u);
+        }
+    } else {
+        uint32_t *dst = (uint32_t *)state + I.off;
+        for (int w = threadIdx.x; w < H * wpr; w += blockDim.x) {
+            const int y = w / wpr, jj = w - y * wpr;
+            const int b = y / p.L, i = y - b * p.L;
+            dst[w] = lat[(i * p.G + b) * wpr + jj];
+        }
+    }
+}
+
+// ninst == 0 only sets the kernel's shared-memory attribute (done before a
+// graph capture, where attribute changes are not recorded)
+cudaError_t xk_life_step_resident(const LifeInst *inst, int ninst, void *state, int bytes_io,
+                                  int generations, int torus, uint32_t bfill, unsigned int *bad,
+                                  int threads, int smem_bytes, cudaStream_t s)
+{
+    cudaError_t e;
+    if (bytes_io) {
+        e = cudaFuncSetAttribute(xk_k_life_resident<true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+        if (e != cudaSuccess || ninst <= 0) return e;
+        xk_k_life_resident<true><<<ninst, threads, smem_bytes, s>>>(inst, state, generations, torus,
+                                                                   bfill, bad);
+    } else {
+        e = cudaFuncSetAttribute(xk_k_life_resident<false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+        if (e != cudaSuccess || ninst <= 0) return e;
+        xk_k_life_resident<false><<<ninst, threads, smem_bytes, s>>>(inst, state, generations, torus,
+                                                                    bfill, bad);
+    }
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// layout conversion: reference main plane (esz bytes per cell, values 0/1)
+// <-> bit-packed rows.  One warp builds one word with a ballot.
+
+__device__ __forceinline__ uint64_t xk_load_cell(const void *src, int esz, int64_t i)
+{
+    switch (esz) {
+    case 1: return ((const uint8_t *)src)[i];
+    case 2: return ((const uint16_t *)src)[i];
+    case 4: return ((const uint32_t *)src)[i];
+    default: return ((const uint64_t *)src)[i];
+    }
+}
+
+__device__ __forceinline__ void xk_store_cell(void *dst, int esz, int64_t i, uint64_t v)
+{
+    switch (esz) {
+    case 1: ((uint8_t *)dst)[i] = (uint8_t)v; break;
+    case 2: ((uint16_t *)dst)[i] = (uint16_t)v; break;
+    case 4: ((uint32_t *)dst)[i] = (uint32_t)v; break;
+    default: ((uint64_t *)dst)[i] = v; break;
+    }
+}
+
+__global__ void xk_k_life_pack(const void *__restrict__ src, int esz, uint32_t *__restrict__ dst,
+                               LifeGeo g, unsigned int *__restrict__ bad)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t word = t >> 5;
+    if (word >= (int64_t)g.H * g.wpr) return;   // whole warps exit together
+    const int lane = threadIdx.x & 31;
+    const int y = (int)(word / g.wpr);
+    const int j = (int)(word - (int64_t)y * g.wpr);
+    const int x = j * 32 + lane;
+    uint64_t v = 0;
+    if (x < g.W) v = xk_load_cell(src, esz, (int64_t)y * g.W + x);
+    if (v > 1u) atomicOr(bad, 1u);
+    const uint32_t bits = __ballot_sync(0xFFFFFFFFu, v != 0);
+    if (lane == 0) dst[word] = bits;
+}
+
+cudaError_t xk_life_pack(const void *src, int esz, uint32_t *dst, const LifeGeo &g, cudaStream_t s)
+{
+    // `bad` lives right after the packed words (the caller sizes the buffer)
+    unsigned int *bad = (unsigned int *)(dst + (int64_t)g.H * g.wpr);
+    cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return e;
+    const int64_t threads_total = (int64_t)g.H * g.wpr * 32;
+    const int threads = 256;
+    xk_k_life_pack<<<(unsigned)((threads_total + threads - 1) / threads), threads, 0, s>>>(
+        src, esz, dst, g, bad);
+    return cudaGetLastError();
+}
+
+__global__ void xk_k_life_unpack(const uint32_t *__restrict__ src, void *__restrict__ dst, int esz,
+                                 LifeGeo g)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)g.W * g.H) return;
+    const int y = (int)(i / g.W), x = (int)(i - (int64_t)y * g.W);
+    const uint32_t w = src[(int64_t)y * g.wpr + (x >> 5)];
+    xk_store_cell(dst, esz, i, (w >> (x & 31)) & 1u);
+}
+
+cudaError_t xk_life_unpack(const uint32_t *src, void *dst, int esz, const LifeGeo &g, cudaStream_t s)
+{
+    const int64_t n = (int64_t)g.W * g.H;
+    const int threads = 256;
+    xk_k_life_unpack<<<(unsigned)((n + threads - 1) / threads), threads, 0, s>>>(src, dst, esz, g);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// colours of Life-like models: the traced colour is a function of the new
+// state; lut6 = rgb of state 0 then of state 1 (before the effect).
+
+__device__ __forceinline__ int xk_clamp_ma(int v, int old, int fade_in, int fade_out)
+{
+    // max(min(v, old + FADE_IN), old - FADE_OUT)  (color_effects.py:118-129)
+    int m = v < old + fade_in ? v : old + fade_in;
+    return m > old - fade_out ? m : old - fade_out;
+}
+
+struct Lut6 {
+    int32_t v[6];
+};
+
+__global__ void xk_k_life_colors(const uint32_t *__restrict__ bits, int32_t *__restrict__ col,
+                                 LifeGeo g, Lut6 lut, int smooth)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)g.W * g.H) return;
+    const int y = (int)(i / g.W), x = (int)(i - (int64_t)y * g.W);
+    const int s = (bits[(int64_t)y * g.wpr + (x >> 5)] >> (x & 31)) & 1;
+    for (int c = 0; c < 3; ++c) col[3 * i + c] = lut.v[3 * s + c] * smooth;
+}
+
+cudaError_t xk_life_colors(const uint32_t *bits, int32_t *col, const LifeGeo &g,
+                           const int32_t *lut6, int smooth, cudaStream_t s)
+{
+    Lut6 l;
+    for (int c = 0; c < 6; ++c) l.v[c] = lut6[c];
+    const int64_t n = (int64_t)g.W * g.H;
+    xk_k_life_colors<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(bits, col, g, l, smooth);
+    return cudaGetLastError();
+}
+
+__global__ void xk_k_life_color_step(const uint32_t *__restrict__ bits, int32_t *__restrict__ col,
+                                     LifeGeo g, Lut6 lut, int fade_in, int fade_out, int smooth,
+                                     int plain)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)g.W * g.H) return;
+    const int y = (int)(i / g.W), x = (int)(i - (int64_t)y * g.W);
+    const int s = (bits[(int64_t)y * g.wpr + (x >> 5)] >> (x & 31)) & 1;
+    for (int c = 0; c < 3; ++c) {
+        const int v = lut.v[3 * s + c];
+        col[3 * i + c] = plain ? v : xk_clamp_ma(v * smooth, col[3 * i + c], fade_in, fade_out);
+    }
+}
+
+cudaError_t xk_life_color_step(const uint32_t *bits, int32_t *col, const LifeGeo &g,
+                               const int32_t *lut6, int fade_in, int fade_out, int smooth,
+                               int plain, cudaStream_t s)
+{
+    Lut6 l;
+    for (int c = 0; c < 6; ++c) l.v[c] = lut6[c];
+    const int64_t n = (int64_t)g.W * g.H;
+    xk_k_life_color_step<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(bits, col, g, l, fade_in,
+                                                                        fade_out, smooth, plain);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// byte-per-cell lattices: any dimensionality and neighbourhood
+
+__global__ void xk_k_nd_pack(const void *__restrict__ src, int esz, uint8_t *__restrict__ dst,
+                             int64_t n, unsigned int *__restrict__ bad)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t v = xk_load_cell(src, esz, i);
+    if (v > 1u) atomicOr(bad, 1u);
+    dst[i] = (uint8_t)(v != 0);
+}
+
+cudaError_t xk_nd_pack(const void *src, int esz, uint8_t *dst, int64_t n, cudaStream_t s)
+{
+    unsigned int *bad = (unsigned int *)(dst + ((n + 15) / 16) * 16);
+    cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return e;
+    xk_k_nd_pack<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, esz, dst, n, bad);
+    return cudaGetLastError();
+}
+
+__global__ void xk_k_nd_unpack(const uint8_t *__restrict__ src, void *__restrict__ dst, int esz,
+                               int64_t n)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) xk_store_cell(dst, esz, i, src[i]);
+}
+
+cudaError_t xk_nd_unpack(const uint8_t *src, void *dst, int esz, int64_t n, cudaStream_t s)
+{
+    xk_k_nd_unpack<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, dst, esz, n);
+    return cudaGetLastError();
+}
+
+// index -> coords with axis 0 fastest (lattice.py:146-170); neighbour k at
+// coords + delta_k, wrapped (border.py:104-117) or off-board (static value).
+__global__ void xk_k_life_nd(const uint8_t *__restrict__ src, uint8_t *__restrict__ dst, NdGeo g,
+                             uint32_t rule0, uint32_t rule1, int64_t n)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int64_t x[XK_MAXDIM];
+    int64_t rem = i;
+    for (int d = 0; d < g.ndim; ++d) {
+        if (d < g.ndim - 1) { x[d] = rem % g.size[d]; rem /= g.size[d]; }
+        else x[d] = rem;
+    }
+    uint32_t alive = 0;
+    for (int k = 0; k < g.nbr; ++k) {
+        int64_t idx = 0, stride = 1;
+        bool off = false;
+        for (int d = 0; d < g.ndim; ++d) {
+            int64_t c = x[d] + g.delta[k][d];
+            if (c < 0 || c >= g.size[d]) {
+                off = true;
+                c = (c + g.size[d]) % g.size[d];
+            }
+            idx += c * stride;
+            stride *= g.size[d];
+        }
+        alive += (off && !g.torus) ? g.border_state : src[idx];
+    }
+    const uint32_t rule = src[i] ? rule1 : rule0;
+    dst[i] = (uint8_t)((rule >> alive) & 1u);
+}
+
+cudaError_t xk_life_step_nd(const uint8_t *src, uint8_t *dst, const NdGeo &g, uint32_t rule0,
+                            uint32_t rule1, cudaStream_t s)
+{
+    int64_t n = 1;
+    for (int d = 0; d < g.ndim; ++d) n *= g.size[d];
+    xk_k_life_nd<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, dst, g, rule0, rule1, n);
+    return cudaGetLastError();
+}
+
+// plain 2-D Moore torus on bytes: the reference's one-byte-per-cell layout,
+// one launch per lattice per generation (the "plain form" of the ensemble)
+__global__ void xk_k_life_bytes2d(const uint8_t *__restrict__ src, uint8_t *__restrict__ dst, int W,
+                                  int H, uint32_t rule0, uint32_t rule1)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)W * H) return;
+    const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
+    const int xl = x > 0 ? x - 1 : W - 1, xr = x < W - 1 ? x + 1 : 0;
+    const int yu = y > 0 ? y - 1 : H - 1, yd = y < H - 1 ? y + 1 : 0;
+    const uint8_t *ru = src + (int64_t)yu * W, *rm = src + (int64_t)y * W, *rd = src + (int64_t)yd * W;
+    const uint32_t k = ru[xl] + ru[x] + ru[xr] + rm[xl] + rm[xr] + rd[xl] + rd[x] + rd[xr];
+    const uint32_t rule = rm[x] ? rule1 : rule0;
+    dst[i] = (uint8_t)((rule >> k) & 1u);
+}
+
+cudaError_t xk_life_step_bytes2d(const uint8_t *src, uint8_t *dst, int W, int H, uint32_t rule0,
+                                 uint32_t rule1, cudaStream_t s)
+{
+    const int64_t n = (int64_t)W * H;
+    xk_k_life_bytes2d<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, dst, W, H, rule0, rule1);
+    return cudaGetLastError();
+}
+
+__global__ void xk_k_nd_colors(const uint8_t *__restrict__ st, int32_t *__restrict__ col, int64_t n,
+                               Lut6 lut, int smooth)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int s = st[i];
+    for (int c = 0; c < 3; ++c) col[3 * i + c] = lut.v[3 * s + c] * smooth;
+}
+
+cudaError_t xk_nd_colors(const uint8_t *st, int32_t *col, int64_t n, const int32_t *lut6,
+                         int smooth, cudaStream_t s)
+{
+    Lut6 l;
+    for (int c = 0; c < 6; ++c) l.v[c] = lut6[c];
+    xk_k_nd_colors<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(st, col, n, l, smooth);
+    return cudaGetLastError();
+}
+
+__global__ void xk_k_nd_color_step(const uint8_t *__restrict__ st, int32_t *__restrict__ col,
+                                   int64_t n, Lut6 lut, int fade_in, int fade_out, int smooth,
+                                   int plain)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int s = st[i];
+    for (int c = 0; c < 3; ++c) {
+        const int v = lut.v[3 * s + c];
+        col[3 * i + c] = plain ? v : xk_clamp_ma(v * smooth, col[3 * i + c], fade_in, fade_out);
+    }
+}
+
+cudaError_t xk_nd_color_step(const uint8_t *st, int32_t *col, int64_t n, const int32_t *lut6,
+                             int fade_in, int fade_out, int smooth, int plain, cudaStream_t s)
+{
+    Lut6 l;
+    for (int c = 0; c < 6; ++c) l.v[c] = lut6[c];
+    xk_k_nd_color_step<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(st, col, n, l, fade_in,
+                                                                     fade_out, smooth, plain);
+    return cudaGetLastError();
+}

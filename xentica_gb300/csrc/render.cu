@@ -1,0 +1,65 @@
+// RendererPlain for sm_103a (reference xentica/core/renderers.py:220-270).
+//
+// Pixel i of a width x height viewport looks at lattice coordinates
+//   xa = (int)((float)(i % width) / (float)zoom) + dx
+//   xb = (int)((float)(i / width) / (float)zoom) + dy
+// on the projection axes (a0, a1), wrapped onto the board with the reference's
+// two-step rule, then sums the colours of every cell along the other axes in
+// float (outer loop = lowest axis), and stores r / num (/ SMOOTH_FACTOR) as an
+// int.  Same operations, same order, same float rounding.
+#include "xk_internal.cuh"
+
+__global__ void xk_k_render(const int32_t *__restrict__ col, int32_t *__restrict__ img,
+                            RenderGeo g, int width, int height, int zoom, int dx, int dy)
+{
+    const int64_t ip = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ip >= (int64_t)width * height) return;
+    const unsigned i = (unsigned)ip;
+    const int w0 = (int)g.size[g.a0], w1 = (int)g.size[g.a1];
+    int xa = (int)(__fdiv_rn((float)(i % (unsigned)width), (float)zoom)) + dx;
+    int xb = (int)(__fdiv_rn((float)(i / (unsigned)width), (float)zoom)) + dy;
+    if (xa < 0) xa = w0 - (-xa % w0);
+    if (xa >= w0) xa = xa % w0;
+    if (xb < 0) xb = w1 - (-xb % w1);
+    if (xb >= w1) xb = xb % w1;
+    int rest[XK_MAXDIM];
+    int nrest = 0;
+    int64_t projected = 1;
+    for (int d = 0; d < g.ndim; ++d)
+        if (d != g.a0 && d != g.a1) { rest[nrest++] = d; projected *= g.size[d]; }
+    int64_t stride[XK_MAXDIM];
+    int64_t s = 1;
+    for (int d = 0; d < g.ndim; ++d) { stride[d] = s; s *= g.size[d]; }
+    const int64_t base = xa * stride[g.a0] + xb * stride[g.a1];
+    float r = 0.f, gg = 0.f, b = 0.f;
+    for (int64_t q = 0; q < projected; ++q) {
+        int64_t rem = q, idx = base;
+        for (int m = nrest - 1; m >= 0; --m) {
+            const int d = rest[m];
+            idx += (rem % g.size[d]) * stride[d];
+            rem /= g.size[d];
+        }
+        r = __fadd_rn(r, (float)col[3 * idx]);
+        gg = __fadd_rn(gg, (float)col[3 * idx + 1]);
+        b = __fadd_rn(b, (float)col[3 * idx + 2]);
+    }
+    const float num = (float)(int)projected;
+    float vr = __fdiv_rn(r, num), vg = __fdiv_rn(gg, num), vb = __fdiv_rn(b, num);
+    if (g.smooth > 0) {
+        const float sf = (float)g.smooth;
+        vr = __fdiv_rn(vr, sf);
+        vg = __fdiv_rn(vg, sf);
+        vb = __fdiv_rn(vb, sf);
+    }
+    img[3 * ip] = (int)vr;
+    img[3 * ip + 1] = (int)vg;
+    img[3 * ip + 2] = (int)vb;
+}
+
+cudaError_t xk_render_colors(const int32_t *col, int32_t *img, const RenderGeo &g, int width,
+                             int height, int zoom, int dx, int dy, cudaStream_t s)
+{
+    const int64_t n = (int64_t)width * height;
+    xk_k_render<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(col, img, g, width, height, zoom, dx, dy);
+    return cudaGetLastError();
+}

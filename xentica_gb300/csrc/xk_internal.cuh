@@ -1,0 +1,113 @@
+// Internal declarations shared by the libxk translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string>
+
+#include "../../include/xk.h"
+
+// ---------------------------------------------------------------------------
+// error handling: every C-ABI function returns a status and records a message
+void xk_set_error(const char *fmt, ...);
+int xk_cuda_status(cudaError_t err, const char *what);
+
+#define XK_CUDA(call)                                                         \
+    do {                                                                      \
+        cudaError_t xk_e_ = (call);                                           \
+        if (xk_e_ != cudaSuccess) return xk_cuda_status(xk_e_, #call);        \
+    } while (0)
+
+#define XK_REQUIRE(cond, code, ...)                                           \
+    do {                                                                      \
+        if (!(cond)) { xk_set_error(__VA_ARGS__); return (code); }            \
+    } while (0)
+
+void xk_set_last_step_ms(double ms);
+
+// ---------------------------------------------------------------------------
+// Life-like bit-packed lattices: cell x of row y is bit (x & 31) of word
+// y * wpr + (x >> 5); padding bits past the row's last cell are always 0.
+
+// Rule truth table as warp-uniform masks: tab[s * 8 + k] is all-ones when a
+// cell in state s with k live neighbours lives next generation (k < 8);
+// t8[s] the same for k == 8.
+struct LifeTable {
+    uint32_t tab[16];
+    uint32_t t8[2];
+};
+
+LifeTable xk_life_table(uint32_t rule0, uint32_t rule1);
+
+struct LifeGeo {
+    int32_t W, H, wpr, rlast;  // width, height, words per row, bits in last word
+    uint32_t lastmask;         // valid bits of a row's last word
+    int32_t torus;             // 1: wrap; 0: off-board cells read as bfill
+    uint32_t bfill;            // 0 or ~0: static border state replicated
+};
+
+LifeGeo xk_life_geo(int64_t W, int64_t H, int torus, int border_state);
+
+// one lattice (or ensemble instance) for the resident kernel
+struct LifeInst {
+    int64_t off;               // first word in the state array
+    int32_t W, H, wpr, rlast;
+    uint32_t lastmask;
+    uint32_t rule0, rule1;
+    int32_t smem_words;        // shared memory the instance needs
+};
+
+// shared-memory words a resident lattice needs with `threads` threads
+int64_t xk_life_resident_words(int W, int H, int threads);
+// largest dynamic shared memory a CTA may use on this device
+int xk_max_smem_optin();
+
+// launchers (stream-ordered, no synchronisation)
+cudaError_t xk_life_pack(const void *src, int esz, uint32_t *dst, const LifeGeo &g, cudaStream_t s);
+cudaError_t xk_life_unpack(const uint32_t *src, void *dst, int esz, const LifeGeo &g, cudaStream_t s);
+cudaError_t xk_life_step_global(const uint32_t *src, uint32_t *dst, const LifeGeo &g,
+                                const LifeTable &t, cudaStream_t s);
+// bytes_io: state is one byte per cell (LifeInst.off in bytes) instead of
+// bit-packed words; `bad` (bytes_io only) is or-ed with 1 if a cell held a
+// value other than 0/1
+cudaError_t xk_life_step_resident(const LifeInst *inst, int ninst, void *state, int bytes_io,
+                                  int generations, int torus, uint32_t bfill, unsigned int *bad,
+                                  int threads, int smem_bytes, cudaStream_t s);
+// threads and dynamic shared memory of the resident kernel for one lattice;
+// rows_per_band: target band length (controls the number of warps)
+int xk_life_resident_config(int W, int H, int rows_per_band, int *threads, int *smem_bytes);
+cudaError_t xk_life_colors(const uint32_t *bits, int32_t *col, const LifeGeo &g,
+                           const int32_t *lut6, int smooth, cudaStream_t s);
+cudaError_t xk_life_color_step(const uint32_t *bits, int32_t *col, const LifeGeo &g,
+                               const int32_t *lut6, int fade_in, int fade_out, int smooth,
+                               int plain, cudaStream_t s);
+
+// byte-per-cell lattices (N-D, any neighbourhood; and the plain 2-D form)
+struct NdGeo {
+    int32_t ndim, nbr, torus;
+    int64_t size[XK_MAXDIM];
+    int8_t delta[XK_MAXNBR][XK_MAXDIM];
+    uint32_t border_state;      // 0/1 state of off-board cells
+};
+cudaError_t xk_nd_pack(const void *src, int esz, uint8_t *dst, int64_t n, cudaStream_t s);
+cudaError_t xk_nd_unpack(const uint8_t *src, void *dst, int esz, int64_t n, cudaStream_t s);
+cudaError_t xk_life_step_nd(const uint8_t *src, uint8_t *dst, const NdGeo &g, uint32_t rule0,
+                            uint32_t rule1, cudaStream_t s);
+cudaError_t xk_life_step_bytes2d(const uint8_t *src, uint8_t *dst, int W, int H,
+                                 uint32_t rule0, uint32_t rule1, cudaStream_t s);
+cudaError_t xk_nd_colors(const uint8_t *st, int32_t *col, int64_t n, const int32_t *lut6,
+                         int smooth, cudaStream_t s);
+cudaError_t xk_nd_color_step(const uint8_t *st, int32_t *col, int64_t n, const int32_t *lut6,
+                             int fade_in, int fade_out, int smooth, int plain, cudaStream_t s);
+
+// RendererPlain over an int3 colour array of an N-D lattice
+struct RenderGeo {
+    int32_t ndim, a0, a1;
+    int64_t size[XK_MAXDIM];
+    int32_t smooth;             // 0: no SMOOTH_FACTOR division
+};
+cudaError_t xk_render_colors(const int32_t *col, int32_t *img, const RenderGeo &g, int width,
+                             int height, int zoom, int dx, int dy, cudaStream_t s);
+
+int xk_sm_count();
