@@ -227,17 +227,34 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
 
     // load: global row-major -> band-interleaved shared layout
     if (BYTES) {
+        // one thread per word: 32 bytes in two 16-byte loads when the row
+        // segment is whole and aligned, byte by byte otherwise
         const uint8_t *src = (const uint8_t *)state + I.off;
         unsigned int flag = 0;
-        for (int y = warp; y < H; y += nwarps) {
+        for (int w = threadIdx.x; w < H * wpr; w += blockDim.x) {
+            const int y = w / wpr, jj = w - y * wpr;
             const int b = y / p.L, i = y - b * p.L;
-            for (int jj = 0; jj < wpr; ++jj) {
-                const int x = jj * 32 + lane;
-                const uint32_t v = x < W ? src[(int64_t)y * W + x] : 0u;
-                flag |= v > 1u;
-                const uint32_t w = __ballot_sync(0xFFFFFFFFu, v != 0u);
-                if (lane == 0) lat[(i * p.G + b) * wpr + jj] = w;
+            const int x0 = jj * 32;
+            const uint8_t *seg = src + (int64_t)y * W + x0;
+            uint32_t word = 0;
+            if (x0 + 32 <= W && ((uintptr_t)seg & 15u) == 0) {
+                const uint4 lo = *(const uint4 *)seg, hi = *(const uint4 *)(seg + 16);
+                const uint64_t q[4] = {((uint64_t)lo.y << 32) | lo.x, ((uint64_t)lo.w << 32) | lo.z,
+                                       ((uint64_t)hi.y << 32) | hi.x, ((uint64_t)hi.w << 32) | hi.z};
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    flag |= (q[k] & 0xFEFEFEFEFEFEFEFEull) != 0;
+                    word |= (uint32_t)((q[k] * 0x0102040810204080ull) >> 56) << (8 * k);
+                }
+            } else {
+                const int nb = min(32, W - x0);
+                for (int k = 0; k < nb; ++k) {
+                    const uint32_t v = seg[k];
+                    flag |= v > 1u;
+                    word |= (v != 0u) << k;
+                }
             }
+            lat[(i * p.G + b) * wpr + jj] = word;
         }
         if (flag) atomicOr(bad, 1u);
     } else {
@@ -289,16 +306,26 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
             vm = xk_row_vec(wm, l, r, lshift, top, edge, edge, use_le, use_re);
         }
         // every lane runs all L iterations so the shuffles always see the
-        // full warp; rows past the band's end are computed and discarded
+        // full warp; rows past the band's end are computed and discarded.
+        // The shared word of the row below is fetched one iteration ahead.
+        auto fetch = [&](int i, bool &off) -> uint32_t {
+            const int y = y0 + i;
+            const bool row_ok = active && y < y1;
+            off = false;
+            if (y + 1 < y1) return row_ok ? lat[((i + 1) * p.G + band) * wpr + j] : 0u;
+            if (y + 1 < H) return row_ok ? halo[((band + 1) * 2 + 0) * wpr + j] : 0u;
+            if (torus) return row_ok ? halo[(0 * 2 + 0) * wpr + j] : 0u;
+            off = true;
+            return bfill;
+        };
+        bool off_next;
+        uint32_t wnext = fetch(0, off_next);
         for (int i = 0; i < p.L; ++i) {
             const int y = y0 + i;
             const bool row_ok = active && y < y1;
-            uint32_t wd = 0u;
-            bool off_d = false;
-            if (y + 1 < y1) wd = row_ok ? lat[((i + 1) * p.G + band) * wpr + j] : 0u;
-            else if (y + 1 < H) wd = row_ok ? halo[((band + 1) * 2 + 0) * wpr + j] : 0u;
-            else if (torus) wd = row_ok ? halo[(0 * 2 + 0) * wpr + j] : 0u;
-            else { wd = bfill; off_d = true; }
+            const uint32_t wd = wnext;
+            const bool off_d = off_next;
+            if (i + 1 < p.L) wnext = fetch(i + 1, off_next);
             const uint32_t l = __shfl_sync(0xFFFFFFFFu, wd, src_l);
             const uint32_t r = __shfl_sync(0xFFFFFFFFu, wd, src_r);
             vd = xk_row_vec(wd, l, r, lshift, top, edge, edge, use_le, use_re);
@@ -312,10 +339,28 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
     }
     if (BYTES) {
         uint8_t *dst = (uint8_t *)state + I.off;
-        for (int y = warp; y < H; y += nwarps) {
+        for (int w = threadIdx.x; w < H * wpr; w += blockDim.x) {
+            const int y = w / wpr, jj = w - y * wpr;
             const int b = y / p.L, i = y - b * p.L;
-            const uint32_t *row = lat + (i * p.G + b) * wpr;
-            for (int x = lane; x < W; x += 32) dst[(int64_t)y * W + x] = (uint8_t)((row[x >> 5] >> (x & 31)) & 1u);
+            const uint32_t word = lat[(i * p.G + b) * wpr + jj];
+            const int x0 = jj * 32;
+            uint8_t *seg = dst + (int64_t)y * W + x0;
+            if (x0 + 32 <= W && ((uintptr_t)seg & 15u) == 0) {
+                uint64_t q[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    uint64_t u = ((uint64_t)((word >> (8 * k)) & 0xFFu) * 0x0101010101010101ull) &
+                                 0x8040201008040201ull;
+                    q[k] = ((u + 0x7F7F7F7F7F7F7F7Full) >> 7) & 0x0101010101010101ull;
+                }
+                *(uint4 *)seg = make_uint4((uint32_t)q[0], (uint32_t)(q[0] >> 32), (uint32_t)q[1],
+                                           (uint32_t)(q[1] >> 32));
+                *(uint4 *)(seg + 16) = make_uint4((uint32_t)q[2], (uint32_t)(q[2] >> 32),
+                                                  (uint32_t)q[3], (uint32_t)(q[3] >> 32));
+            } else {
+                const int nb = min(32, W - x0);
+                for (int k = 0; k < nb; ++k) seg[k] = (uint8_t)((word >> k) & 1u);
+            }
         }
     } else {
         uint32_t *dst = (uint32_t *)state + I.off;
@@ -327,8 +372,6 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
     }
 }
 
-// ninst == 0 only sets the kernel's shared-memory attribute (done before a
-// graph capture, where attribute changes are not recorded)
 cudaError_t xk_life_step_resident(const LifeInst *inst, int ninst, void *state, int bytes_io,
                                   int generations, int torus, uint32_t bfill, unsigned int *bad,
                                   int threads, int smem_bytes, cudaStream_t s)
