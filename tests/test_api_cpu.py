@@ -281,7 +281,10 @@ def test_random_known_answers():
 
 
 def test_primordial_soup_checksum():
-    bsca = GameOfLife(type("E", (GOLExperiment, ), {"size": (100, 100)}))
+    # a fresh seed pattern: patterns clamp their area to the field in place,
+    # so resizing an experiment that shares one would change it for others
+    bsca = GameOfLife(type("E", (GOLExperiment, ), {"size": (100, 100), "seed": PrimordialSoup(
+        vals={'state': RandInt(0, 1)})}))
     seed = PrimordialSoup(vals={'state': RandInt(0, 1)})
     cells = np.zeros((10000, ), dtype=np.int32)
     seed.random = LocalRandom("test")
