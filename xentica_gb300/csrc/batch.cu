@@ -13,6 +13,7 @@
 //
 // The plain form is the reference's execution model on the same GPU: one
 // launch per instance per generation over the byte layout.
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -264,6 +265,26 @@ static int enqueue_batched(xk_batch *b, int generations)
     return XK_OK;
 }
 
+// XK_GRAPHS=0 in the environment launches the class kernels directly on their
+// streams instead of through a captured graph (same kernels, same order) --
+// for tools that cannot follow graph launches
+static bool graphs_enabled()
+{
+    const char *v = getenv("XK_GRAPHS");
+    return !(v && v[0] == '0');
+}
+
+static int set_class_attributes(xk_batch *b)
+{
+    for (const Class &c : b->classes)
+        XK_CUDA(xk_life_step_resident(b->d_inst + c.first, 0, b->cells, 1, 0, 1, 0u, b->bad,
+                                      c.threads, c.smem, b->stream));
+    return XK_OK;
+}
+
+// enqueue one batched step of `generations` on b->stream (graph or direct)
+static int launch_batched(xk_batch *b, int generations);
+
 static int graph_for(xk_batch *b, int generations, cudaGraphExec_t *exec)
 {
     auto it = b->graphs.find(generations);
@@ -273,9 +294,8 @@ static int graph_for(xk_batch *b, int generations, cudaGraphExec_t *exec)
     }
     if (!b->big.empty() && !b->scratch) XK_CUDA(cudaMalloc(&b->scratch, (size_t)b->total + 16));
     // kernel attributes are set outside capture
-    for (const Class &c : b->classes)
-        XK_CUDA(xk_life_step_resident(b->d_inst + c.first, 0, b->cells, 1, 0, 1, 0u, b->bad,
-                                      c.threads, c.smem, b->stream));
+    int arc = set_class_attributes(b);
+    if (arc != XK_OK) return arc;
     XK_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     int rc = enqueue_batched(b, generations);
     cudaGraph_t graph = nullptr;
@@ -291,6 +311,22 @@ static int graph_for(xk_batch *b, int generations, cudaGraphExec_t *exec)
     XK_CUDA(e);
     b->graphs[generations] = g;
     *exec = g;
+    return XK_OK;
+}
+
+static int launch_batched(xk_batch *b, int generations)
+{
+    if (generations <= 0) return XK_OK;
+    if (!graphs_enabled()) {
+        if (!b->big.empty() && !b->scratch) XK_CUDA(cudaMalloc(&b->scratch, (size_t)b->total + 16));
+        int rc = set_class_attributes(b);
+        if (rc != XK_OK) return rc;
+        return enqueue_batched(b, generations);
+    }
+    cudaGraphExec_t g;
+    int rc = graph_for(b, generations, &g);
+    if (rc != XK_OK) return rc;
+    XK_CUDA(cudaGraphLaunch(g, b->stream));
     return XK_OK;
 }
 
@@ -313,11 +349,14 @@ extern "C" int xk_batch_step(xk_batch *b, int32_t generations)
     XK_REQUIRE(b, XK_ERR_ARG, "xk_batch_step: null batch");
     XK_REQUIRE(generations >= 0, XK_ERR_ARG, "xk_batch_step: negative generations");
     if (generations == 0) return XK_OK;
-    cudaGraphExec_t g;
-    int rc = graph_for(b, generations, &g);
-    if (rc != XK_OK) return rc;
+    if (graphs_enabled()) {
+        cudaGraphExec_t g;
+        int rc = graph_for(b, generations, &g);   // instantiate outside the timed region
+        if (rc != XK_OK) return rc;
+    }
     XK_CUDA(cudaEventRecord(b->ev0, b->stream));
-    XK_CUDA(cudaGraphLaunch(g, b->stream));
+    int rc = launch_batched(b, generations);
+    if (rc != XK_OK) return rc;
     XK_CUDA(cudaEventRecord(b->ev1, b->stream));
     XK_CUDA(cudaEventSynchronize(b->ev1));
     float ms = 0.f;
@@ -358,14 +397,15 @@ extern "C" int xk_batch_run(xk_batch *b, const uint8_t *host_in, uint8_t *host_o
     XK_REQUIRE(total_cells == b->total, XK_ERR_ARG, "xk_batch_run: %lld cells, batch has %lld",
                (long long)total_cells, (long long)b->total);
     XK_REQUIRE(generations >= 0, XK_ERR_ARG, "xk_batch_run: negative generations");
-    cudaGraphExec_t g = nullptr;
-    if (generations > 0) {
+    if (generations > 0 && graphs_enabled()) {
+        cudaGraphExec_t g;
         int rc = graph_for(b, generations, &g);
         if (rc != XK_OK) return rc;
     }
     XK_CUDA(cudaEventRecord(b->ev0, b->stream));
     XK_CUDA(cudaMemcpyAsync(b->cells, host_in, (size_t)b->total, cudaMemcpyHostToDevice, b->stream));
-    if (g) XK_CUDA(cudaGraphLaunch(g, b->stream));
+    int rc = launch_batched(b, generations);
+    if (rc != XK_OK) return rc;
     XK_CUDA(cudaMemcpyAsync(host_out, b->cells, (size_t)b->total, cudaMemcpyDeviceToHost, b->stream));
     XK_CUDA(cudaEventRecord(b->ev1, b->stream));
     XK_CUDA(cudaEventSynchronize(b->ev1));
@@ -391,16 +431,16 @@ extern "C" int xk_batch_tune(xk_batch *b, int32_t generations, int32_t *chosen)
     for (int r : cand) {
         b->rows_per_band = r;
         if ((rc = plan_classes(b)) != XK_OK) break;
-        cudaGraphExec_t g;
-        if ((rc = graph_for(b, generations, &g)) != XK_OK) break;
         float ms = 0.f;
         for (int rep = 0; rep < 2; ++rep) {
+            if ((rc = launch_batched(b, generations)) != XK_OK) break;   // builds the graph
             cudaEventRecord(b->ev0, b->stream);
-            cudaGraphLaunch(g, b->stream);
+            if ((rc = launch_batched(b, generations)) != XK_OK) break;
             cudaEventRecord(b->ev1, b->stream);
             cudaEventSynchronize(b->ev1);
             cudaEventElapsedTime(&ms, b->ev0, b->ev1);
         }
+        if (rc != XK_OK) break;
         if (ms < best) {
             best = ms;
             best_rpb = r;
