@@ -152,19 +152,6 @@ cudaError_t xk_life_step_global(const uint32_t *src, uint32_t *dst, const LifeGe
     return cudaGetLastError();
 }
 
-__device__ __forceinline__ LifeTable xk_life_table_dev(uint32_t rule0, uint32_t rule1)
-{
-    LifeTable t;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        t.tab[k] = 0u - ((rule0 >> k) & 1u);
-        t.tab[8 + k] = 0u - ((rule1 >> k) & 1u);
-    }
-    t.t8[0] = 0u - ((rule0 >> 8) & 1u);
-    t.t8[1] = 0u - ((rule1 >> 8) & 1u);
-    return t;
-}
-
 // ---------------------------------------------------------------------------
 // resident lattices: a whole lattice (W <= 1024) lives in shared memory for
 // all generations of a launch; one CTA per lattice.
@@ -179,7 +166,11 @@ __device__ __forceinline__ LifeTable xk_life_table_dev(uint32_t rule0, uint32_t 
 // generation starts, so neighbouring bands read the previous generation.
 //
 // Shared layout interleaves the bands' rows (local row i of band b at
-// (i * G + b) * wpr) so that the groups of a warp hit consecutive words.
+// (i * G + b) * wpr) so that the groups of a warp hit consecutive words; the
+// rule table sits after the halo and is read into registers once (a value
+// loaded from shared memory is never recomputed per use).
+
+#define XK_TAB_WORDS 32
 
 struct ResidentPlan {
     int P, gpw, G, L, nb;  // lanes per group, groups per warp, groups, band length, live bands
@@ -205,17 +196,27 @@ int64_t xk_life_resident_words(int W, int H, int threads)
     const int wpr = (W + 31) / 32;
     if (wpr > 32) return -1;
     ResidentPlan p = xk_resident_plan(wpr, H, threads);
-    return (int64_t)p.L * p.G * wpr + 2LL * p.G * wpr;
+    return (int64_t)p.L * p.G * wpr + 2LL * p.G * wpr + XK_TAB_WORDS;
 }
 
-// BYTES = false: the lattice is stored bit-packed (LifeInst.off in words);
-// BYTES = true: one byte per cell, 0/1, row-major (LifeInst.off in bytes) --
-// the reference's own layout, converted to bit-slices while loading and back
-// while storing, so no separate pack/unpack pass touches HBM.
-template <bool BYTES>
+// neighbour vectors of a torus row: left bit taken from `left` (already the
+// wrapped neighbour word), right bit from `right`; lpre moves the left
+// neighbour's bit to position 31, top / topbit place the right neighbour
+// after the row's last cell
+__device__ __forceinline__ RowVec xk_torus_vec(uint32_t c, uint32_t left, uint32_t right, int lpre,
+                                               int top, uint32_t topbit)
+{
+    RowVec v;
+    v.C = c;
+    v.L = __funnelshift_l(left << lpre, c, 1);
+    v.R = (c >> 1) | ((right << top) & topbit);
+    return v;
+}
+
+template <bool BYTES, bool TORUS>
 __global__ void __launch_bounds__(1024)
 xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
-                   int generations, int torus, uint32_t bfill, unsigned int *__restrict__ bad)
+                   int generations, uint32_t bfill, unsigned int *__restrict__ bad)
 {
     extern __shared__ uint32_t sm[];
     const LifeInst I = insts[blockIdx.x];
@@ -223,7 +224,8 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
     const ResidentPlan p = xk_resident_plan(wpr, H, blockDim.x);
     uint32_t *lat = sm;
     uint32_t *halo = sm + (int64_t)p.L * p.G * wpr;   // [band][2][wpr]
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    uint32_t *tabs = halo + 2 * p.G * wpr;            // rule table
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
     // load: global row-major -> band-interleaved shared layout
     if (BYTES) {
@@ -265,75 +267,108 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
             lat[(i * p.G + b) * wpr + jj] = src[w];
         }
     }
+    if (threadIdx.x < 18) {
+        const uint32_t r = threadIdx.x < 8 ? I.rule0 : threadIdx.x < 16 ? I.rule1
+                                                     : (threadIdx.x == 16 ? I.rule0 : I.rule1);
+        const int k = threadIdx.x < 16 ? (threadIdx.x & 7) : 8;
+        tabs[threadIdx.x] = 0u - ((r >> k) & 1u);
+    }
 
     const int q = lane / p.P, j = lane - q * p.P;
     const int band = warp * p.gpw + q;
     const bool active = band < p.nb && j < wpr;
-    const int y0 = band * p.L;
+    // clamped indices: idle lanes read valid (ignored) words, so no load
+    // needs a predicate
+    const int bc = band < p.nb ? band : p.nb - 1;
+    const int jc = j < wpr ? j : wpr - 1;
+    const int y0 = bc * p.L;
     const int y1 = min(H, y0 + p.L);
     const int last = wpr - 1;
     const int gbase = q * p.P;
-    const int src_l = gbase + (j > 0 ? j - 1 : last);
-    const int src_r = gbase + (j < last ? j + 1 : 0);
-    const int lshift = j > 0 ? 31 : I.rlast - 1;
-    const int top = j == last ? I.rlast - 1 : 31;
-    const int use_le = (!torus) && j == 0, use_re = (!torus) && j == last;
+    const int src_l = gbase + (jc > 0 ? jc - 1 : last);
+    const int src_r = gbase + (jc < last ? jc + 1 : 0);
+    const int lshift = jc > 0 ? 31 : I.rlast - 1;
+    const int lpre = 31 - lshift;
+    const int top = jc == last ? I.rlast - 1 : 31;
+    const uint32_t topbit = 1u << top;
+    const uint32_t outmask = jc == last ? I.lastmask : 0xFFFFFFFFu;
     const uint32_t edge = bfill & 1u;
-    const uint32_t outmask = j == last ? I.lastmask : 0xFFFFFFFFu;
-    const LifeTable t = xk_life_table_dev(I.rule0, I.rule1);
-
+    const int use_le = (!TORUS) && jc == 0, use_re = (!TORUS) && jc == last;
+    const int hup = bc > 0 ? bc - 1 : p.nb - 1;        // band holding the row above
+    const int hdn = bc + 1 < p.nb ? bc + 1 : 0;         // band holding the row below
+    const bool full = (H % p.L) == 0;                   // every band has L rows
     __syncthreads();
+    LifeTable t;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) t.tab[k] = tabs[k];
+    t.t8[0] = tabs[16];
+    t.t8[1] = tabs[17];
+
     for (int gen = 0; gen < generations; ++gen) {
         if (active) {
             halo[(band * 2 + 0) * wpr + j] = lat[(0 * p.G + band) * wpr + j];
             halo[(band * 2 + 1) * wpr + j] = lat[((y1 - 1 - y0) * p.G + band) * wpr + j];
         }
         __syncthreads();
-        // the row above the band, the band's first row, then rows below
-        uint32_t wu, wm;
-        bool off_u = false;
-        if (band > 0) wu = active ? halo[((band - 1) * 2 + 1) * wpr + j] : 0u;
-        else if (torus) wu = active ? halo[((p.nb - 1) * 2 + 1) * wpr + j] : 0u;
-        else { wu = bfill; off_u = true; }
-        wm = active ? lat[band * wpr + j] : 0u;
         RowVec vu, vm, vd;
-        {
+        const uint32_t wu = (!TORUS && bc == 0) ? bfill : halo[(hup * 2 + 1) * wpr + jc];
+        const uint32_t wm = lat[bc * wpr + jc];
+        if (TORUS) {
+            uint32_t l = __shfl_sync(0xFFFFFFFFu, wu, src_l), r = __shfl_sync(0xFFFFFFFFu, wu, src_r);
+            vu = xk_torus_vec(wu, l, r, lpre, top, topbit);
+            l = __shfl_sync(0xFFFFFFFFu, wm, src_l);
+            r = __shfl_sync(0xFFFFFFFFu, wm, src_r);
+            vm = xk_torus_vec(wm, l, r, lpre, top, topbit);
+        } else {
             uint32_t l = __shfl_sync(0xFFFFFFFFu, wu, src_l), r = __shfl_sync(0xFFFFFFFFu, wu, src_r);
             vu = xk_row_vec(wu, l, r, lshift, top, edge, edge, use_le, use_re);
-            if (off_u) vu.L = vu.C = vu.R = bfill;
+            if (bc == 0) vu.L = vu.C = vu.R = bfill;
             l = __shfl_sync(0xFFFFFFFFu, wm, src_l);
             r = __shfl_sync(0xFFFFFFFFu, wm, src_r);
             vm = xk_row_vec(wm, l, r, lshift, top, edge, edge, use_le, use_re);
         }
-        // every lane runs all L iterations so the shuffles always see the
-        // full warp; rows past the band's end are computed and discarded.
-        // The shared word of the row below is fetched one iteration ahead.
-        auto fetch = [&](int i, bool &off) -> uint32_t {
-            const int y = y0 + i;
-            const bool row_ok = active && y < y1;
-            off = false;
-            if (y + 1 < y1) return row_ok ? lat[((i + 1) * p.G + band) * wpr + j] : 0u;
-            if (y + 1 < H) return row_ok ? halo[((band + 1) * 2 + 0) * wpr + j] : 0u;
-            if (torus) return row_ok ? halo[(0 * 2 + 0) * wpr + j] : 0u;
-            off = true;
-            return bfill;
-        };
-        bool off_next;
-        uint32_t wnext = fetch(0, off_next);
-        for (int i = 0; i < p.L; ++i) {
-            const int y = y0 + i;
-            const bool row_ok = active && y < y1;
-            const uint32_t wd = wnext;
-            const bool off_d = off_next;
-            if (i + 1 < p.L) wnext = fetch(i + 1, off_next);
-            const uint32_t l = __shfl_sync(0xFFFFFFFFu, wd, src_l);
-            const uint32_t r = __shfl_sync(0xFFFFFFFFu, wd, src_r);
-            vd = xk_row_vec(wd, l, r, lshift, top, edge, edge, use_le, use_re);
-            if (off_d) vd.L = vd.C = vd.R = bfill;
-            const uint32_t out = xk_life_word(vu.L, vu.C, vu.R, vm.L, vm.C, vm.R, vd.L, vd.C, vd.R, t);
-            if (row_ok) lat[(i * p.G + band) * wpr + j] = out & outmask;
-            vu = vm;
-            vm = vd;
+        if (TORUS && full) {
+            // fast path: every band has exactly L rows; the word of the row
+            // below comes from the band itself except for the last row
+            uint32_t wd = p.L > 1 ? lat[(1 * p.G + bc) * wpr + jc] : halo[(hdn * 2 + 0) * wpr + jc];
+            for (int i = 0; i < p.L; ++i) {
+                uint32_t wnext = 0u;
+                if (i + 2 < p.L) wnext = lat[((i + 2) * p.G + bc) * wpr + jc];
+                else if (i + 2 == p.L) wnext = halo[(hdn * 2 + 0) * wpr + jc];
+                const uint32_t l = __shfl_sync(0xFFFFFFFFu, wd, src_l);
+                const uint32_t r = __shfl_sync(0xFFFFFFFFu, wd, src_r);
+                vd = xk_torus_vec(wd, l, r, lpre, top, topbit);
+                const uint32_t out = xk_life_word(vu.L, vu.C, vu.R, vm.L, vm.C, vm.R, vd.L, vd.C, vd.R, t);
+                if (active) lat[(i * p.G + bc) * wpr + jc] = out & outmask;
+                vu = vm;
+                vm = vd;
+                wd = wnext;
+            }
+        } else {
+            // general path: bands may be shorter than L; every lane still
+            // runs L iterations so the shuffles always see the full warp
+            for (int i = 0; i < p.L; ++i) {
+                const int y = y0 + i;
+                const bool row_ok = active && y < y1;
+                uint32_t wd;
+                bool off_d = false;
+                if (y + 1 < y1) wd = lat[((i + 1) * p.G + bc) * wpr + jc];
+                else if (y + 1 < H) wd = halo[((bc + 1) * 2 + 0) * wpr + jc];
+                else if (TORUS) wd = halo[(0 * 2 + 0) * wpr + jc];
+                else { wd = bfill; off_d = true; }
+                const uint32_t l = __shfl_sync(0xFFFFFFFFu, wd, src_l);
+                const uint32_t r = __shfl_sync(0xFFFFFFFFu, wd, src_r);
+                if (TORUS) {
+                    vd = xk_torus_vec(wd, l, r, lpre, top, topbit);
+                } else {
+                    vd = xk_row_vec(wd, l, r, lshift, top, edge, edge, use_le, use_re);
+                    if (off_d) vd.L = vd.C = vd.R = bfill;
+                }
+                const uint32_t out = xk_life_word(vu.L, vu.C, vu.R, vm.L, vm.C, vm.R, vd.L, vd.C, vd.R, t);
+                if (row_ok) lat[(i * p.G + bc) * wpr + jc] = out & outmask;
+                vu = vm;
+                vm = vd;
+            }
         }
         __syncthreads();
     }
@@ -346,17 +381,17 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
             const int x0 = jj * 32;
             uint8_t *seg = dst + (int64_t)y * W + x0;
             if (x0 + 32 <= W && ((uintptr_t)seg & 15u) == 0) {
-                uint64_t q[4];
+                uint64_t qq[4];
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     uint64_t u = ((uint64_t)((word >> (8 * k)) & 0xFFu) * 0x0101010101010101ull) &
                                  0x8040201008040201ull;
-                    q[k] = ((u + 0x7F7F7F7F7F7F7F7Full) >> 7) & 0x0101010101010101ull;
+                    qq[k] = ((u + 0x7F7F7F7F7F7F7F7Full) >> 7) & 0x0101010101010101ull;
                 }
-                *(uint4 *)seg = make_uint4((uint32_t)q[0], (uint32_t)(q[0] >> 32), (uint32_t)q[1],
-                                           (uint32_t)(q[1] >> 32));
-                *(uint4 *)(seg + 16) = make_uint4((uint32_t)q[2], (uint32_t)(q[2] >> 32),
-                                                  (uint32_t)q[3], (uint32_t)(q[3] >> 32));
+                *(uint4 *)seg = make_uint4((uint32_t)qq[0], (uint32_t)(qq[0] >> 32), (uint32_t)qq[1],
+                                           (uint32_t)(qq[1] >> 32));
+                *(uint4 *)(seg + 16) = make_uint4((uint32_t)qq[2], (uint32_t)(qq[2] >> 32),
+                                                  (uint32_t)qq[3], (uint32_t)(qq[3] >> 32));
             } else {
                 const int nb = min(32, W - x0);
                 for (int k = 0; k < nb; ++k) seg[k] = (uint8_t)((word >> k) & 1u);
@@ -372,25 +407,34 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
     }
 }
 
+template <bool BYTES, bool TORUS>
+static cudaError_t xk_launch_resident(const LifeInst *inst, int ninst, void *state, int generations,
+                                      uint32_t bfill, unsigned int *bad, int threads, int smem_bytes,
+                                      cudaStream_t s)
+{
+    cudaError_t e = cudaFuncSetAttribute(xk_k_life_resident<BYTES, TORUS>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    if (e != cudaSuccess || ninst <= 0) return e;
+    xk_k_life_resident<BYTES, TORUS><<<ninst, threads, smem_bytes, s>>>(inst, state, generations,
+                                                                        bfill, bad);
+    return cudaGetLastError();
+}
+
+// ninst == 0 only sets the kernel's shared-memory attribute (done before a
+// graph capture, where attribute changes are not recorded)
 cudaError_t xk_life_step_resident(const LifeInst *inst, int ninst, void *state, int bytes_io,
                                   int generations, int torus, uint32_t bfill, unsigned int *bad,
                                   int threads, int smem_bytes, cudaStream_t s)
 {
-    cudaError_t e;
-    if (bytes_io) {
-        e = cudaFuncSetAttribute(xk_k_life_resident<true>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
-        if (e != cudaSuccess || ninst <= 0) return e;
-        xk_k_life_resident<true><<<ninst, threads, smem_bytes, s>>>(inst, state, generations, torus,
-                                                                   bfill, bad);
-    } else {
-        e = cudaFuncSetAttribute(xk_k_life_resident<false>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
-        if (e != cudaSuccess || ninst <= 0) return e;
-        xk_k_life_resident<false><<<ninst, threads, smem_bytes, s>>>(inst, state, generations, torus,
-                                                                    bfill, bad);
-    }
-    return cudaGetLastError();
+    if (bytes_io)
+        return torus ? xk_launch_resident<true, true>(inst, ninst, state, generations, bfill, bad,
+                                                      threads, smem_bytes, s)
+                     : xk_launch_resident<true, false>(inst, ninst, state, generations, bfill, bad,
+                                                       threads, smem_bytes, s);
+    return torus ? xk_launch_resident<false, true>(inst, ninst, state, generations, bfill, bad,
+                                                   threads, smem_bytes, s)
+                 : xk_launch_resident<false, false>(inst, ninst, state, generations, bfill, bad,
+                                                    threads, smem_bytes, s);
 }
 
 // ---------------------------------------------------------------------------
