@@ -82,6 +82,33 @@ __device__ __forceinline__ uint32_t xk_life_word(uint32_t Lu, uint32_t Cu, uint3
     return xk_mux(b3, low, eight);
 }
 
+// Same as xk_life_word, with the rows above and below already reduced to
+// their column sums: (su, cu) = FA(Lu, Cu, Ru) and (sd, cd) = FA(Ld, Cd, Rd).
+// A row's sums are computed once and reused while it is the row below and,
+// two rows later, the row above.
+template <class Tab>
+__device__ __forceinline__ uint32_t xk_life_word_fa(uint32_t su, uint32_t cu, uint32_t Lm,
+                                                    uint32_t Cm, uint32_t Rm, uint32_t sd,
+                                                    uint32_t cd, const Tab &t)
+{
+    const uint32_t sm = Lm ^ Rm, cm = Lm & Rm;
+    const uint32_t b0 = su ^ sd ^ sm, k1 = xk_maj(su, sd, sm);
+    const uint32_t tw = cu ^ cd ^ cm, k2 = xk_maj(cu, cd, cm);
+    const uint32_t b1 = tw ^ k1, k3 = tw & k1;
+    const uint32_t b2 = k2 ^ k3, b3 = k2 & k3;
+    uint32_t m[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) m[q] = xk_mux(b0, t.tab[2 * q], t.tab[2 * q + 1]);
+    uint32_t n[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) n[q] = xk_mux(b1, m[2 * q], m[2 * q + 1]);
+    const uint32_t dead = xk_mux(b2, n[0], n[1]);
+    const uint32_t live = xk_mux(b2, n[2], n[3]);
+    const uint32_t low = xk_mux(Cm, dead, live);
+    const uint32_t eight = xk_mux(Cm, t.t8[0], t.t8[1]);
+    return xk_mux(b3, low, eight);
+}
+
 // Neighbour vectors of word j of a row, given the row's word and the words
 // left and right of it (already wrapped).  lshift: bit of `left` that is
 // the cell left of bit 0; top: bit of R that receives the cell right of the
@@ -329,20 +356,51 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
         }
         if (TORUS && full) {
             // fast path: every band has exactly L rows; the word of the row
-            // below comes from the band itself except for the last row
-            uint32_t wd = p.L > 1 ? lat[(1 * p.G + bc) * wpr + jc] : halo[(hdn * 2 + 0) * wpr + jc];
-            for (int i = 0; i < p.L; ++i) {
-                uint32_t wnext = 0u;
-                if (i + 2 < p.L) wnext = lat[((i + 2) * p.G + bc) * wpr + jc];
-                else if (i + 2 == p.L) wnext = halo[(hdn * 2 + 0) * wpr + jc];
+            // below comes from the band itself except for the band's last
+            // row (halo).  Rows whose width is a multiple of 32 need no
+            // partial-word handling: both neighbour vectors are one funnel
+            // shift and no output mask applies.
+            const bool fullw = I.rlast == 32;
+            uint32_t su = vu.L ^ vu.C ^ vu.R, cu = xk_maj(vu.L, vu.C, vu.R);
+            uint32_t sm_ = vm.L ^ vm.C ^ vm.R, cm_ = xk_maj(vm.L, vm.C, vm.R);
+            uint32_t Lm = vm.L, Cm = vm.C, Rm = vm.R;
+            auto row = [&](uint32_t wd, int i) {
                 const uint32_t l = __shfl_sync(0xFFFFFFFFu, wd, src_l);
                 const uint32_t r = __shfl_sync(0xFFFFFFFFu, wd, src_r);
-                vd = xk_torus_vec(wd, l, r, lpre, top, topbit);
-                const uint32_t out = xk_life_word(vu.L, vu.C, vu.R, vm.L, vm.C, vm.R, vd.L, vd.C, vd.R, t);
-                if (active) lat[(i * p.G + bc) * wpr + jc] = out & outmask;
-                vu = vm;
-                vm = vd;
-                wd = wnext;
+                uint32_t Ld, Rd;
+                if (fullw) {
+                    Ld = __funnelshift_l(l, wd, 1);
+                    Rd = __funnelshift_r(wd, r, 1);
+                } else {
+                    const RowVec d = xk_torus_vec(wd, l, r, lpre, top, topbit);
+                    Ld = d.L;
+                    Rd = d.R;
+                }
+                const uint32_t sd = Ld ^ wd ^ Rd, cd = xk_maj(Ld, wd, Rd);
+                uint32_t out = xk_life_word_fa(su, cu, Lm, Cm, Rm, sd, cd, t);
+                if (!fullw) out &= outmask;
+                if (active) lat[(i * p.G + bc) * wpr + jc] = out;
+                su = sm_;
+                cu = cm_;
+                sm_ = sd;
+                cm_ = cd;
+                Lm = Ld;
+                Cm = wd;
+                Rm = Rd;
+            };
+            const uint32_t whalo = halo[(hdn * 2 + 0) * wpr + jc];
+            if (p.L == 1) {
+                row(whalo, 0);
+            } else {
+                uint32_t wd = lat[(1 * p.G + bc) * wpr + jc];
+                int i = 0;
+                for (; i + 2 < p.L; ++i) {
+                    const uint32_t wnext = lat[((i + 2) * p.G + bc) * wpr + jc];
+                    row(wd, i);
+                    wd = wnext;
+                }
+                row(wd, i);          // i == L - 2: row below is the band's last row
+                row(whalo, i + 1);   // i == L - 1: row below is the next band's first row
             }
         } else {
             // general path: bands may be shorter than L; every lane still
