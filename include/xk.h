@@ -152,6 +152,24 @@ int64_t xk_batch_total_cells(const xk_batch *b);
  * per-generation launches for instances too large for a CTA). */
 int64_t xk_batch_launches(const xk_batch *b, int32_t generations);
 
+/* Ensemble step that allocates nothing.  No counterpart in the reference.
+ * For callers that cannot call cudaMalloc (a host framework owns every
+ * device allocation, or nothing may be allocated after start-up): d_cells is
+ * the caller's device buffer of concatenated lattices (one byte per cell,
+ * 0/1), advanced in place by `generations` on `stream` (a cudaStream_t, NULL
+ * for the default stream); the call returns when the work is done.  The only
+ * other device memory used is a file-scope array sized for
+ * XK_NOALLOC_MAX_LATTICES lattice descriptors (~128 KB), held by every device
+ * that loads the library until exit.  Every call shares it, so calls whose
+ * GPU work overlaps race; the first call on a device looks the array up
+ * (cudaGetSymbolAddress) and should come before any stream capture.  More
+ * lattices, or lattices wider than 1024 cells or too large for one CTA, are
+ * rejected with an error. */
+#define XK_NOALLOC_MAX_LATTICES 4096
+int xk_batch_step_noalloc(uint8_t *d_cells, int32_t count, const int32_t *width,
+                          const int32_t *height, const uint32_t *rule, int32_t generations,
+                          void *stream);
+
 /* Select the CUDA device for handles created afterwards on this thread. */
 int xk_set_device(int32_t device);
 /* Page-lock (pin) caller-owned host memory for fast copies, and release it. */

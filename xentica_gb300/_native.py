@@ -70,6 +70,7 @@ SIGNATURES = {
     "xk_batch_tune": (_I32, [_P, _I32, ctypes.POINTER(_I32)]),
     "xk_batch_total_cells": (_I64, [_P]),
     "xk_batch_launches": (_I64, [_P, _I32]),
+    "xk_batch_step_noalloc": (_I32, [_P, _I32, _P, _P, _P, _I32, _P]),
     "xk_set_device": (_I32, [_I32]),
     "xk_host_register": (_I32, [_P, _I64]),
     "xk_host_unregister": (_I32, [_P]),
