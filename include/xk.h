@@ -68,6 +68,7 @@ typedef struct xk_desc {
     uint32_t death_speed, max_genes;
     double mutation_prob;
     int32_t positional;                /* 0 GenomeColor.modular, 1 .positional    */
+    double palette[54];                /* positional: rgb weight of each of 18 genes */
     /* XK_FAMILY_MASS */
     uint32_t wall;                     /* StaticBorder value = off-board mass     */
     int32_t reserved[8];

@@ -54,6 +54,25 @@ CASES = {
                                render={"viewport": [12, 10]}),
 }
 
+EVO = "examples.evolife"
+CASES.update({
+    # reference tests/core/test_base.py:197-216 (colours compared as stored)
+    "evolife_cross1_positional": dict(model=EVO + ":EvoLife", experiment=EVO + ":CrossbreedingExperiment",
+                                      model_kwargs={"legacy_coloring": False}, checkpoints=[1, 100]),
+    "evolife_cross2": dict(model=EVO + ":EvoLife", experiment=EVO + ":CrossbreedingExperiment2",
+                           checkpoints=[1, 100], render={"viewport": [480, 270]},
+                           exp_overrides={"zoom": 4, "pos": [100, 50]}),
+    "evolife_bigbang_160x120": dict(model=EVO + ":EvoLife", experiment=EVO + ":BigBangExperiment",
+                                    exp_overrides={"size": [160, 120], "zoom": 1},
+                                    checkpoints=[1, 2, 10, 60], render={"viewport": [160, 120]}),
+    "evolife_bigbang_mut_131x101": dict(model=EVO + ":EvoLife", experiment=EVO + ":BigBangExperiment",
+                                        exp_overrides={"size": [131, 101], "mutation_prob": 0.05,
+                                                       "death_speed": 7, "max_genes": 5,
+                                                       "fade_in": 40, "fade_out": 11},
+                                        model_kwargs={"legacy_coloring": False},
+                                        checkpoints=[1, 5, 40]),
+})
+
 # odd sizes, both borders: pins word-boundary and wrap handling
 for w, h in [(1, 1), (1, 17), (17, 1), (2, 2), (31, 5), (32, 7), (33, 9), (63, 64), (64, 63),
              (65, 3), (100, 100), (1023, 5), (1024, 3), (1025, 4), (2000, 11), (3, 1200)]:
@@ -75,8 +94,15 @@ def crc(a):
 
 
 def main(ref_root):
+    only = set(sys.argv[2:])
     out = {}
+    path = os.path.join(HERE, "golden.json")
+    if only and os.path.exists(path):
+        with open(path) as fh:
+            out = json.load(fh)
     for name, job in CASES.items():
+        if only and name not in only:
+            continue
         job = dict(job)
         job.setdefault("threads", os.cpu_count())
         job["workdir"] = os.path.join(ROOT, "oracle", "_ref")
@@ -98,9 +124,10 @@ def main(ref_root):
             case["steps"][str(cp)] = entry
         out[name] = case
         print(name, case["init"], json.dumps(case["steps"]), flush=True)
-    with open(os.path.join(HERE, "golden.json"), "w") as fh:
+    with open(path, "w") as fh:
         json.dump(out, fh, indent=1, sort_keys=True)
 
 
 if __name__ == "__main__":
+    # usage: make_golden.py [reference checkout] [case ...]
     main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

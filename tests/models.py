@@ -210,7 +210,8 @@ EXPERIMENTS = {
 
 
 def from_job(job):
-    """Our model and experiment for a golden-fixture job (see make_golden.py)."""
+    """Our model and experiment for a golden-fixture job (see make_golden.py);
+    model keyword arguments are in ``job["model_kwargs"]``."""
     model = MODELS[job["model"].rsplit(":", 1)[1]]
     exp = EXPERIMENTS[job["experiment"].rsplit(":", 1)[1]]
     overrides = dict(job.get("exp_overrides", {}))
@@ -221,3 +222,159 @@ def from_job(job):
     if overrides:
         exp = type("GoldenExperiment", (exp,), overrides)
     return model, exp
+
+
+def build_from_job(job):
+    """Construct the model of a fixture job as a fresh reference process
+    would: meta-parameters are class-level and keep the last experiment's
+    values, so they start from their declared defaults here."""
+    model_cls, exp = from_job(job)
+    for param in model_cls.meta.__dict__.values():
+        if hasattr(param, "default"):
+            param.__set__(None, param.default)
+    return model_cls(exp, **job.get("model_kwargs", {}))
+
+
+class RegularCA(core.CellularAutomaton):
+    """2-D Moore torus template without logic (examples/base.py:11-37)."""
+
+    class Topology:
+        dimensions = 2
+        lattice = core.OrthogonalLattice()
+        neighborhood = core.MooreNeighborhood()
+        border = core.TorusBorder()
+
+
+class RegularExperiment(core.Experiment):
+    word = "I AM MUNDANE"
+    size = (640, 360, )
+    zoom = 3
+    pos = [0, 0]
+
+
+class EvoLife(RegularCA):
+    """Life-like CA whose every cell carries its own rule, energy and RNG."""
+
+    energy = core.IntegerProperty(max_val=255 * 2)
+    rule = core.TotalisticRuleProperty(outer=True)
+    rng = core.RandomProperty()
+    death_speed = core.Parameter(default=15)
+    max_genes = core.Parameter(default=9)
+    mutation_prob = core.Parameter(default=.0)
+
+    def __init__(self, *args, legacy_coloring=True):
+        self._legacy_coloring = legacy_coloring
+        super().__init__(*args)
+
+    def emit(self):
+        for buf in self.buffers:
+            buf.energy = self.main.energy
+            buf.rule = self.main.rule
+
+    def absorb(self):
+        num_neighbors = core.IntegerVariable()
+        for i in range(len(self.buffers)):
+            nbr_energy = self.neighbors[i].buffer.energy
+            nbr_rule = self.neighbors[i].buffer.rule
+            num_neighbors += xmath.min(1, (nbr_energy + nbr_rule))
+        is_sustained = core.IntegerVariable()
+        is_sustained += self.main.rule.is_sustained(num_neighbors)
+        fitnesses = []
+        for i in range(len(self.buffers)):
+            fitnesses.append(core.IntegerVariable(name="fit%d" % i))
+        num_parents = core.IntegerVariable()
+        for gene in range(len(self.buffers)):
+            num_parents *= 0
+            for i in range(len(self.buffers)):
+                nbr_energy = self.neighbors[i].buffer.energy
+                nbr_rule = self.neighbors[i].buffer.rule
+                is_alive = xmath.min(1, (nbr_energy + nbr_rule))
+                is_fit = self.neighbors[i].buffer.rule.is_born(gene + 1)
+                num_parents += is_alive * is_fit
+            fitnesses[gene] += num_parents * (num_parents == (gene + 1))
+        num_fit = core.IntegerVariable()
+        num_fit += xmath.max(*fitnesses)
+        genomes = []
+        for i in range(len(self.buffers)):
+            genomes.append(core.IntegerVariable(name="genome%d" % i))
+        for i in range(len(self.buffers)):
+            is_fit = self.neighbors[i].buffer.rule.is_born(num_fit)
+            genomes[i] += self.neighbors[i].buffer.rule * is_fit
+        num_genes = self.main.rule.bit_width
+        old_rule = core.IntegerVariable()
+        old_rule += self.main.rule
+        old_energy = core.IntegerVariable()
+        old_energy += self.main.energy
+        new_genome = genome_crossover(
+            self.main, num_genes, *genomes,
+            max_genes=self.meta.max_genes,
+            mutation_prob=self.meta.mutation_prob
+        )
+        self.main.rule = new_genome + self.main.rule * (new_genome == 0)
+        self.main.energy *= 0
+        is_live = core.IntegerVariable()
+        old_live = (old_energy + old_rule) == 0
+        is_live += (old_energy < 0xff) & (old_live | is_sustained)
+        old_dead = (old_energy + old_rule) != 0
+        new_energy = old_energy + self.meta.death_speed * old_dead
+        self.main.energy = new_energy * (self.main.rule == old_rule) + \
+            self.main.energy * (self.main.rule != old_rule)
+        self.main.rule = old_rule * (self.main.rule == old_rule) + \
+            self.main.rule * (self.main.rule != old_rule)
+        self.main.energy *= is_live
+        self.main.rule *= is_live
+
+    @color_effects.MovingAverage
+    def color(self):
+        if self._legacy_coloring:
+            red, green, blue = GenomeColor.modular(self.main.rule >> 1, 360)
+        else:
+            red, green, blue = GenomeColor.positional(self.main.rule,
+                                                      self.main.rule.bit_width)
+        is_live = (self.main.rule > 0) * (self.main.energy < 255)
+        energy = (255 - self.main.energy) * is_live
+        red = xmath.int(red * energy)
+        green = xmath.int(green * energy)
+        blue = xmath.int(blue * energy)
+        return (red, green, blue, )
+
+
+class CrossbreedingExperiment(RegularExperiment):
+    word = "FUTURE BREEDING MACHINE 2041"
+    size = (1920, 1080)
+    zoom = 1
+    fade_in = 18
+    fade_out = 3
+    seed_diamoeba = seeds.patterns.BigBang(
+        pos=(380, 280), size=(440, 340),
+        vals={"energy": 0, "rule": LifeLike.golly2int("B35678/S5678") * RandInt(0, 1),
+              "rng": RandInt(0, 2 ** 16 - 1)})
+    seed_conway = seeds.patterns.BigBang(
+        pos=(0, 0), size=(1280, 720),
+        vals={"energy": 0, "rule": +RandInt(0, 1) * LifeLike.golly2int("B3/S23"),
+              "rng": 0 + RandInt(0, 2 ** 16 - 1)})
+    seed_rng = seeds.patterns.PrimordialSoup(vals={"rng": RandInt(0, 2 ** 16 - 1)})
+    seed = seed_rng + seed_conway + seed_diamoeba
+
+
+class CrossbreedingExperiment2(CrossbreedingExperiment):
+    death_speed = 25
+    max_genes = 9
+    mutation_prob = 0.0001
+
+
+class BigBangExperiment(RegularExperiment):
+    death_speed = 0
+    max_genes = 9
+    seed_bang = seeds.patterns.BigBang(
+        pos=(0, 0), size=(100, 100),
+        vals={"energy": RandInt(0, 255), "rule": RandInt(0, 2 ** 18 - 1) & 0b111111110111111110,
+              "rng": RandInt(0, 2 ** 16 - 1)})
+    seed_rng = seeds.patterns.PrimordialSoup(vals={"rng": RandInt(0, 2 ** 16 - 1)})
+    seed = seed_rng + seed_bang
+
+
+MODELS["EvoLife"] = EvoLife
+EXPERIMENTS.update({"CrossbreedingExperiment": CrossbreedingExperiment,
+                    "CrossbreedingExperiment2": CrossbreedingExperiment2,
+                    "BigBangExperiment": BigBangExperiment})

@@ -14,7 +14,7 @@ import pytest
 
 import oracle as O
 from tests.models import (GameOfLife, GOLExperiment, LifelikeFixed, GOLExperiment2,
-                          GameOfLifeStatic, from_job)
+                          GameOfLifeStatic, build_from_job)
 from tests.test_oracle import crc
 
 pytestmark = pytest.mark.gpu
@@ -23,8 +23,7 @@ pytestmark = pytest.mark.gpu
 def _run_case(golden, case):
     entry = golden[case]
     job = entry["job"]
-    model_cls, exp = from_job(job)
-    model = model_cls(exp)
+    model = build_from_job(job)
     viewport = job.get("render", {}).get("viewport")
     if viewport:
         model.set_viewport(tuple(viewport))

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from tests.models import from_job
+from tests.models import build_from_job
 from xentica_gb300.core.topology.border import StaticBorder
 from xentica_gb300.core.topology.neighborhood import VonNeumannNeighborhood
 from xentica_gb300.tools.rules import LifeLike
@@ -23,8 +23,7 @@ def crc(a):
 
 def oracle_setup(job):
     """(topology, fld, col, model) for a fixture job, seeded by our API."""
-    model_cls, exp = from_job(job)
-    model = model_cls(exp)
+    model = build_from_job(job)
     border = model.topology.border
     kind = "vonneumann" if isinstance(model.topology.neighborhood, VonNeumannNeighborhood) else "moore"
     topo = O.Topology(model.size, kind, border.value if isinstance(border, StaticBorder) else None)
@@ -85,7 +84,8 @@ def _fixture_cases(golden_json):
     import os
     with open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")) as fh:
         data = json.load(fh)
-    return sorted(k for k, v in data.items() if v["cells_num"] <= 200000 and "lifelike" not in k)
+    return sorted(k for k, v in data.items()
+                  if v["cells_num"] <= 200000 and "lifelike" not in k and "evolife" not in k)
 
 
 @pytest.mark.parametrize("case", _fixture_cases(None))
@@ -113,3 +113,33 @@ def test_oracle_fixtures(golden, case):
             img = O.render(topo, col, w, h, zoom=zoom, dx=pos[0], dy=pos[1], axes=axes,
                            smooth=smooth).astype(np.uint8)
             assert crc(img) == exp["img"], "image at step %d" % cp
+
+
+def evolife_run(model, topo, fld, col, steps):
+    tpl = model.gpu.template
+    info = tpl.color.extra
+    O.evolife_run(topo, fld, col, steps, death_speed=tpl.params["death_speed"],
+                  max_genes=tpl.params["max_genes"], mutation_prob=tpl.params["mutation_prob"],
+                  positional=not tpl.legacy, fade_in=info["fade_in"], fade_out=info["fade_out"],
+                  smooth=info["smooth"])
+
+
+@pytest.mark.parametrize("case", ["evolife_bigbang_160x120", "evolife_bigbang_mut_131x101"])
+def test_oracle_evolife_fixtures(golden, case):
+    entry = golden[case]
+    topo, fld, col, model = oracle_setup(entry["job"])
+    assert crc(fld[:topo.cells]) == entry["init"]
+    done = 0
+    for cp in sorted(int(c) for c in entry["steps"]):
+        evolife_run(model, topo, fld, col, cp - done)
+        done = cp
+        assert crc(fld[:topo.cells]) == entry["steps"][str(cp)]["cells"], "cells at %d" % cp
+        assert crc(col) == entry["steps"][str(cp)]["colors"], "colours at %d" % cp
+
+
+def test_oracle_evolife_reference_golden(golden):
+    # reference tests/core/test_base.py:208-216 (CrossbreedingExperiment2, 100 steps)
+    topo, fld, col, model = oracle_setup(golden["evolife_cross2"]["job"])
+    evolife_run(model, topo, fld, col, 100)
+    assert crc(fld[:topo.cells]) == 3381214984
+    assert crc(col) == 2253830262

@@ -40,6 +40,7 @@ class XkDesc(ctypes.Structure):
         ("death_speed", _U32), ("max_genes", _U32),
         ("mutation_prob", ctypes.c_double),
         ("positional", _I32),
+        ("palette", ctypes.c_double * 54),
         ("wall", _U32),
         ("reserved", _I32 * 8),
     ]

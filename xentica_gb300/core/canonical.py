@@ -1,0 +1,126 @@
+"""Reference programs of the kernel families matched by fingerprint.
+
+A family whose kernel restates one specific model (rather than a rule table
+read off by evaluation) is defined here by that model, written in the DSL.
+A user model matches when its traced programs are identical to the
+reference program traced with the user's parameter values (variables may be
+named differently).  The EvoLife kernel (``csrc/evolife.cu``) implements
+exactly the program below -- the EvoLife example of the reference
+(``examples/evolife.py:20-128``), whose operation order fixes the random
+stream and the float rounding, so it is kept statement for statement.
+"""
+import threading
+
+from xentica_gb300 import core
+from xentica_gb300.core import color_effects
+from xentica_gb300.core.base import Translator
+from xentica_gb300.tools import xmath
+from xentica_gb300.tools.color import GenomeColor
+from xentica_gb300.tools.genetics import genome_crossover
+
+_LOCK = threading.Lock()
+
+
+class EvoLifeProgram(core.CellularAutomaton):
+    """EvoLife: per-cell outer-totalistic genome, energy and random stream."""
+
+    energy = core.IntegerProperty(max_val=255 * 2)
+    rule = core.TotalisticRuleProperty(outer=True)
+    rng = core.RandomProperty()
+    death_speed = core.Parameter(default=15)
+    max_genes = core.Parameter(default=9)
+    mutation_prob = core.Parameter(default=.0)
+
+    class Topology:
+        dimensions = 2
+        lattice = core.OrthogonalLattice()
+        neighborhood = core.MooreNeighborhood()
+        border = core.TorusBorder()
+
+    def emit(self):
+        for buf in self.buffers:
+            buf.energy = self.main.energy
+            buf.rule = self.main.rule
+
+    def absorb(self):
+        num_neighbors = core.IntegerVariable()
+        for i in range(len(self.buffers)):
+            nbr_energy = self.neighbors[i].buffer.energy
+            nbr_rule = self.neighbors[i].buffer.rule
+            num_neighbors += xmath.min(1, (nbr_energy + nbr_rule))
+        is_sustained = core.IntegerVariable()
+        is_sustained += self.main.rule.is_sustained(num_neighbors)
+        fitnesses = []
+        for i in range(len(self.buffers)):
+            fitnesses.append(core.IntegerVariable(name="fit%d" % i))
+        num_parents = core.IntegerVariable()
+        for gene in range(len(self.buffers)):
+            num_parents *= 0
+            for i in range(len(self.buffers)):
+                nbr_energy = self.neighbors[i].buffer.energy
+                nbr_rule = self.neighbors[i].buffer.rule
+                is_alive = xmath.min(1, (nbr_energy + nbr_rule))
+                is_fit = self.neighbors[i].buffer.rule.is_born(gene + 1)
+                num_parents += is_alive * is_fit
+            fitnesses[gene] += num_parents * (num_parents == (gene + 1))
+        num_fit = core.IntegerVariable()
+        num_fit += xmath.max(*fitnesses)
+        genomes = []
+        for i in range(len(self.buffers)):
+            genomes.append(core.IntegerVariable(name="genome%d" % i))
+        for i in range(len(self.buffers)):
+            is_fit = self.neighbors[i].buffer.rule.is_born(num_fit)
+            genomes[i] += self.neighbors[i].buffer.rule * is_fit
+        num_genes = self.main.rule.bit_width
+        old_rule = core.IntegerVariable()
+        old_rule += self.main.rule
+        old_energy = core.IntegerVariable()
+        old_energy += self.main.energy
+        new_genome = genome_crossover(self.main, num_genes, *genomes,
+                                      max_genes=self.meta.max_genes,
+                                      mutation_prob=self.meta.mutation_prob)
+        self.main.rule = new_genome + self.main.rule * (new_genome == 0)
+        self.main.energy *= 0
+        is_live = core.IntegerVariable()
+        old_live = (old_energy + old_rule) == 0
+        is_live += (old_energy < 0xff) & (old_live | is_sustained)
+        old_dead = (old_energy + old_rule) != 0
+        new_energy = old_energy + self.meta.death_speed * old_dead
+        self.main.energy = new_energy * (self.main.rule == old_rule) + \
+            self.main.energy * (self.main.rule != old_rule)
+        self.main.rule = old_rule * (self.main.rule == old_rule) + \
+            self.main.rule * (self.main.rule != old_rule)
+        self.main.energy *= is_live
+        self.main.rule *= is_live
+
+    @color_effects.MovingAverage
+    def color(self):
+        if self._legacy_coloring:
+            red, green, blue = GenomeColor.modular(self.main.rule >> 1, 360)
+        else:
+            red, green, blue = GenomeColor.positional(self.main.rule, self.main.rule.bit_width)
+        is_live = (self.main.rule > 0) * (self.main.energy < 255)
+        energy = (255 - self.main.energy) * is_live
+        red = xmath.int(red * energy)
+        green = xmath.int(green * energy)
+        blue = xmath.int(blue * energy)
+        return (red, green, blue, )
+
+
+def trace(program_cls, size, params, attrs):
+    """Traced ``{"emit", "absorb"}`` programs of ``program_cls`` with the given
+    meta-parameter values and model attributes."""
+    with _LOCK:
+        inst = program_cls.__new__(program_cls)
+        Translator.__init__(inst)
+        inst.size = tuple(size)
+        for name, value in attrs.items():
+            setattr(inst, name, value)
+        for name, value in params.items():
+            inst.meta.__dict__[name].__set__(inst, value)
+        inst.cells_num = 1
+        for s in inst.size:
+            inst.cells_num *= s
+        inst.build_emit()
+        inst.build_absorb()
+        return inst.programs

@@ -529,3 +529,50 @@ def evaluate(program, inputs, params=None, lanes=None):
         return Evaluator(program, inputs, params, lanes).run()
     except _Unsupported as exc:
         raise XenticaException("Model cannot be analysed: %s." % exc)
+
+
+def fingerprint(program):
+    """Structure of a program with variables renamed by first appearance.
+
+    Two programs with equal fingerprints execute the same statements on the
+    same types and constants, whatever their variables are called.
+    """
+    names = {}
+
+    def nm(name):
+        return names.setdefault(name, "v%d" % len(names))
+
+    def fp(n):
+        if n is None:
+            return None
+        if isinstance(n, Lit):
+            return ("L", n.ctype.name, repr(n.value))
+        if isinstance(n, VarRef):
+            return ("V", nm(n.name), n.ctype.name)
+        if isinstance(n, ParamRef):
+            return ("P", n.name, n.ctype.name)
+        if isinstance(n, Load):
+            return ("M", n.kind, n.k, n.plane, n.ctype.name)
+        if isinstance(n, Bin):
+            return ("B", n.op, fp(n.a), fp(n.b))
+        if isinstance(n, Un):
+            return ("U", n.op, fp(n.a))
+        if isinstance(n, Cast):
+            return ("C", n.ctype.name, fp(n.a))
+        if isinstance(n, BitCast):
+            return ("X", n.ctype.name, fp(n.a))
+        if isinstance(n, Cond):
+            return ("Q", fp(n.c), fp(n.a), fp(n.b))
+        if isinstance(n, Call):
+            return ("F", n.fn, tuple(fp(a) for a in n.args))
+        return ("R", n.text())
+
+    out = []
+    for st in program.stmts:
+        if st.op == "color":
+            out.append(("color", st.extra["kind"], tuple(fp(x) for x in st.extra["rgb"])))
+        else:
+            out.append((st.op, nm(st.var) if st.var else None,
+                        st.ctype.name if st.ctype is not None else None, fp(st.expr), st.aug,
+                        st.extra))
+    return tuple(out)

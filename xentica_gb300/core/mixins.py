@@ -17,10 +17,14 @@ __all__ = ['BscaDetectorMixin', 'DimensionsMixin', ]
 ACTIVE = []
 
 _CORE_DIR = os.path.dirname(os.path.abspath(__file__))
+# modules whose frames are DSL machinery, never the code that names a variable
+_MACHINERY = {os.path.join(_CORE_DIR, name + ".py") for name in (
+    "base", "expressions", "variables", "properties", "parameters", "mixins",
+    "color_effects", "renderers", "ir")}
 
 
 def _is_core_frame(frame):
-    return os.path.dirname(os.path.abspath(frame.f_code.co_filename)) == _CORE_DIR
+    return os.path.abspath(frame.f_code.co_filename) in _MACHINERY
 
 
 class BscaDetectorMixin:

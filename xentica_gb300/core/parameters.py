@@ -30,6 +30,7 @@ class Parameter(BscaDetectorMixin):
 
     def __init__(self, default=0, interactive=False):
         self._value = default
+        self._default = default
         self._interactive = interactive
         self._declared = False
         self._name = "param" + str(id(self))
@@ -38,6 +39,11 @@ class Parameter(BscaDetectorMixin):
     def value(self):
         """Current value."""
         return self._value
+
+    @property
+    def default(self):
+        """Value the parameter was declared with."""
+        return self._default
 
     @property
     def interactive(self):

@@ -246,7 +246,60 @@ class LifeTemplate:
         return d
 
 
-FAMILIES = (LifeTemplate, )
+class EvoLifeTemplate:
+    """EvoLife (``canonical.EvoLifeProgram``): matched by program fingerprint.
+
+    Parameters come from the model's meta-parameters ``death_speed``,
+    ``max_genes``, ``mutation_prob``, its ``_legacy_coloring`` flag and the
+    MovingAverage settings; the model's traced programs must equal the
+    reference program traced with those values.
+    """
+
+    family = nat.XK_FAMILY_EVOLIFE
+    PARAMS = ("death_speed", "max_genes", "mutation_prob")
+
+    def __init__(self, model):
+        from xentica_gb300.core import canonical
+        names = [type(p).__name__ for p in model.main.properties.values()]
+        if names != ["IntegerProperty", "TotalisticRuleProperty", "RandomProperty"]:
+            raise NoTemplate("not the EvoLife property layout")
+        meta = model.meta.__dict__
+        if not all(name in meta for name in self.PARAMS):
+            raise NoTemplate("missing EvoLife meta-parameters")
+        deltas, torus, border = _topology(model)
+        if model.topology.dimensions != 2 or len(deltas) != 8 or not torus:
+            raise NoTemplate("EvoLife kernel is 2-D Moore on a torus")
+        self.model = model
+        self.params = {name: meta[name].value for name in self.PARAMS}
+        self.legacy = bool(getattr(model, "_legacy_coloring", True))
+        attrs = {"_legacy_coloring": self.legacy}
+        for name in ("fade_in", "fade_out", "smooth_factor"):
+            if name in model.__dict__:
+                attrs[name] = model.__dict__[name]
+        programs = canonical.trace(canonical.EvoLifeProgram, model.size, self.params, attrs)
+        for key in ("emit", "absorb"):
+            if ir.fingerprint(programs[key]) != ir.fingerprint(model.programs[key]):
+                raise NoTemplate("%s differs from the EvoLife program" % key)
+        self.color = _color_stmt(model.programs["absorb"])
+
+    def descriptor(self):
+        from xentica_gb300.tools.color import hsv2rgb
+        d = _base_desc(self.model, self.family)
+        d.death_speed = int(self.params["death_speed"]) & 0xFFFFFFFF
+        d.max_genes = int(self.params["max_genes"]) & 0xFFFFFFFF
+        d.mutation_prob = float(self.params["mutation_prob"])
+        d.positional = int(not self.legacy)
+        for i in range(18):
+            rgb = hsv2rgb(i / 18, 1, 1 / 18)
+            for c in range(3):
+                d.palette[3 * i + c] = float(rgb[c])
+        info = self.color.extra
+        d.color_kind = nat.XK_COLOR_MOVING_AVERAGE
+        d.fade_in, d.fade_out, d.smooth = info["fade_in"], info["fade_out"], info["smooth"]
+        return d
+
+
+FAMILIES = (LifeTemplate, EvoLifeTemplate)
 
 
 def match(model):

@@ -1,5 +1,6 @@
 // C-ABI of single models (include/xk.h): device state, layout conversion and
 // generation stepping for the kernel families.
+#include <math.h>
 #include <stdarg.h>
 #include <string.h>
 
@@ -73,7 +74,15 @@ extern "C" int xk_device_info(char *buf, int32_t len)
 // ---------------------------------------------------------------------------
 // model object
 
-enum { LAYOUT_BITS2D = 1, LAYOUT_BYTES = 2 };
+enum { LAYOUT_BITS2D = 1, LAYOUT_BYTES = 2, LAYOUT_CELLS64 = 3 };
+
+// largest float t with (double)u < p  <=>  u <= t for every float u
+static float below_threshold(double p)
+{
+    float t = (float)p;
+    if ((double)t >= p) t = nextafterf(t, -INFINITY);
+    return t;
+}
 
 struct xk_model {
     xk_desc d;
@@ -85,6 +94,8 @@ struct xk_model {
     NdGeo ng;
     uint32_t *bits[2] = {nullptr, nullptr};
     uint8_t *bytes[2] = {nullptr, nullptr};
+    uint64_t *cells64[2] = {nullptr, nullptr};  // EvoLife: reference layout, ping-pong
+    float mut_thresh = 0.f;
     int cur = 0;
     void *stage = nullptr;       // reference-layout staging + validity flag
     int32_t *col = nullptr;      // colours (3 int32 per cell) when materialised
@@ -151,6 +162,7 @@ static void free_model(xk_model *m)
     for (int i = 0; i < 2; ++i) {
         if (m->bits[i]) cudaFree(m->bits[i]);
         if (m->bytes[i]) cudaFree(m->bytes[i]);
+        if (m->cells64[i]) cudaFree(m->cells64[i]);
     }
     if (m->stage) cudaFree(m->stage);
     if (m->col) cudaFree(m->col);
@@ -197,10 +209,14 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
                XK_ERR_ARG, "state_bytes %d", d.state_bytes);
     const int64_t n = cells_of(d);
     XK_REQUIRE(n <= (1LL << 40), XK_ERR_ARG, "lattice of %lld cells too large", (long long)n);
-    XK_REQUIRE(d.family == XK_FAMILY_LIFE, XK_ERR_UNSUPPORTED,
+    XK_REQUIRE(d.family == XK_FAMILY_LIFE || d.family == XK_FAMILY_EVOLIFE, XK_ERR_UNSUPPORTED,
                "model family %d is not available in this build", d.family);
-    XK_REQUIRE(d.rule0 >> (d.nbr + 1) == 0 && d.rule1 >> (d.nbr + 1) == 0, XK_ERR_ARG,
-               "rule tables have bits above %d neighbours", d.nbr);
+    if (d.family == XK_FAMILY_LIFE)
+        XK_REQUIRE(d.rule0 >> (d.nbr + 1) == 0 && d.rule1 >> (d.nbr + 1) == 0, XK_ERR_ARG,
+                   "rule tables have bits above %d neighbours", d.nbr);
+    if (d.family == XK_FAMILY_EVOLIFE)
+        XK_REQUIRE(is_moore2d(d) && d.torus && d.state_bytes == 8, XK_ERR_ARG,
+                   "EvoLife needs a 2-D Moore torus of 64-bit cells");
 
     xk_model *m = new (std::nothrow) xk_model();
     XK_REQUIRE(m, XK_ERR_OOM, "host allocation failed");
@@ -221,7 +237,14 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
     XK_TRY(cudaEventCreate(&m->ev1));
     {
         const int border_state = (int)(d.border_value & 1u);
-        if (is_moore2d(d)) {
+        if (d.family == XK_FAMILY_EVOLIFE) {
+            m->layout = LAYOUT_CELLS64;
+            XK_TRY(cudaMalloc(&m->cells64[0], (size_t)n * 8));
+            XK_TRY(cudaMalloc(&m->cells64[1], (size_t)n * 8));
+            XK_TRY(cudaMemsetAsync(m->cells64[0], 0, (size_t)n * 8, m->stream));
+            XK_TRY(xk_evolife_set_positional(d.palette));
+            m->mut_thresh = below_threshold(d.mutation_prob);
+        } else if (is_moore2d(d)) {
             m->layout = LAYOUT_BITS2D;
             m->lg = xk_life_geo(d.size[0], d.size[1], d.torus, border_state);
             const size_t words = (size_t)m->lg.H * m->lg.wpr;
@@ -244,7 +267,8 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
             XK_TRY(cudaMalloc(&m->bytes[1], bytes));
             XK_TRY(cudaMemsetAsync(m->bytes[0], 0, bytes, m->stream));
         }
-        XK_TRY(cudaMalloc(&m->stage, (size_t)n * d.state_bytes + 16));
+        if (m->layout != LAYOUT_CELLS64)
+            XK_TRY(cudaMalloc(&m->stage, (size_t)n * d.state_bytes + 16));
         XK_TRY(cudaMalloc(&m->col, (size_t)n * 3 * sizeof(int32_t)));
         XK_TRY(cudaMemsetAsync(m->col, 0, (size_t)n * 3 * sizeof(int32_t), m->stream));
     }
@@ -273,6 +297,13 @@ extern "C" int xk_upload(xk_model *m, const void *host_main, int64_t ncells)
     XK_REQUIRE(ncells == m->n, XK_ERR_ARG, "xk_upload: %lld cells given, model has %lld",
                (long long)ncells, (long long)m->n);
     const int esz = m->d.state_bytes;
+    if (m->layout == LAYOUT_CELLS64) {
+        XK_CUDA(cudaMemcpyAsync(m->cells64[m->cur], host_main, (size_t)m->n * 8,
+                                cudaMemcpyHostToDevice, m->stream));
+        XK_CUDA(cudaStreamSynchronize(m->stream));
+        m->uploaded = 1;
+        return XK_OK;
+    }
     XK_CUDA(cudaMemcpyAsync(m->stage, host_main, (size_t)m->n * esz, cudaMemcpyHostToDevice,
                             m->stream));
     unsigned int *bad;
@@ -298,6 +329,12 @@ extern "C" int xk_download(xk_model *m, void *host_main, int64_t ncells)
     XK_REQUIRE(ncells == m->n, XK_ERR_ARG, "xk_download: %lld cells given, model has %lld",
                (long long)ncells, (long long)m->n);
     const int esz = m->d.state_bytes;
+    if (m->layout == LAYOUT_CELLS64) {
+        XK_CUDA(cudaMemcpyAsync(host_main, m->cells64[m->cur], (size_t)m->n * 8,
+                                cudaMemcpyDeviceToHost, m->stream));
+        XK_CUDA(cudaStreamSynchronize(m->stream));
+        return XK_OK;
+    }
     if (m->layout == LAYOUT_BITS2D)
         XK_CUDA(xk_life_unpack(m->bits[m->cur], m->stage, esz, m->lg, m->stream));
     else
@@ -395,6 +432,20 @@ extern "C" int xk_step(xk_model *m, int64_t nsteps)
     XK_REQUIRE(nsteps >= 0, XK_ERR_ARG, "xk_step: negative step count");
     XK_REQUIRE(m->uploaded, XK_ERR_STATE, "xk_step before xk_upload");
     if (nsteps == 0) return XK_OK;
+    if (m->layout == LAYOUT_CELLS64) {
+        XK_CUDA(cudaEventRecord(m->ev0, m->stream));
+        for (int64_t g = 0; g < nsteps; ++g) {
+            XK_CUDA(xk_evolife_step(m->cells64[m->cur], m->cells64[1 - m->cur], m->col, m->d,
+                                    m->mut_thresh, m->stream));
+            m->cur = 1 - m->cur;
+        }
+        XK_CUDA(cudaEventRecord(m->ev1, m->stream));
+        XK_CUDA(cudaEventSynchronize(m->ev1));
+        float ms = 0.f;
+        XK_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+        xk_set_last_step_ms(ms);
+        return XK_OK;
+    }
     const bool colors_free = m->hf || m->d.color_kind == XK_COLOR_NONE;
     if (!colors_free) {
         int rc = materialize_colors(m);

@@ -1,0 +1,240 @@
+// EvoLife generation kernel for sm_103a.
+//
+// Restates, per cell and in the same operation order, the absorb + colour
+// program the reference generates for EvoLife (examples/evolife.py:20-128,
+// tools/genetics.py:7-56, tools/color.py:8-125):
+//   cell = energy (9 bits) | rule (18 bits) << 9 | rng (16 bits) << 27, uint64
+//   (properties.py:496-541); 2-D Moore torus, neighbour k at the reference's
+//   delta order (-1,-1) (-1,0) (-1,1) (0,-1) (0,1) (1,-1) (1,0) (1,1).
+// Emit copies energy and rule to every buffer, so a neighbour's buffer is its
+// main state: emit is fused away and the kernel reads neighbours directly
+// (ping-pong state buffers).  Every read of the cell's RandomProperty advances
+// x = (x * 58321 + 11113) % 65535 (properties.py:638-660): once for the start
+// gene, then once per gene (twice with mutation).  Floats follow IEEE
+// round-to-nearest with no contraction (__fdiv_rn, __fmul_rn, __fadd_rn).
+#include <string.h>
+
+#include "xk_internal.cuh"
+
+// GenomeColor.positional weights (double) per gene and channel
+__constant__ double c_evo_pos[18 * 3];
+
+__device__ __forceinline__ uint32_t xk_lcg(uint32_t x) { return (x * 58321u + 11113u) % 65535u; }
+
+// the uniform draw (float)x / 65535 of RandomProperty.uniform
+__device__ __forceinline__ float xk_uniform(uint32_t x) { return __fdiv_rn((float)x, 65535.0f); }
+
+// float -> unsigned int as the GPU converts: truncation, NaN -> 0
+__device__ __forceinline__ uint32_t xk_f2u(float v) { return __float2uint_rz(v); }
+
+// 8 bits -> 8 nibbles (bit g to bit 4g)
+__device__ __forceinline__ uint32_t xk_spread_nibbles(uint32_t b)
+{
+    b = (b | (b << 12)) & 0x000F000Fu;
+    b = (b | (b << 6)) & 0x03030303u;
+    b = (b | (b << 3)) & 0x11111111u;
+    return b;
+}
+
+__device__ __forceinline__ int xk_ma_clamp(int v, int old, int fade_in, int fade_out)
+{
+    int m = v < old + fade_in ? v : old + fade_in;
+    return m > old - fade_out ? m : old - fade_out;
+}
+
+// hsv2rgb(hue, 1, 1) with deferred hue (tools/color.py:8-60) and the energy
+// weighting of EvoLife.color (evolife.py:431-444), modular genome colour
+__device__ __forceinline__ void xk_evo_color_modular(uint32_t rule, uint32_t energy, int *rgb)
+{
+    float hue_f = 0.0f;
+    hue_f = __fadd_rn(hue_f, __fmul_rn(__fdiv_rn((float)((rule >> 1) % 360u), 360.0f), 6.0f));
+    uint32_t hue_i = 0;
+    hue_i += xk_f2u(hue_f);
+    hue_f = __fsub_rn(hue_f, (float)hue_i);
+    float sat = 0.0f;
+    sat = __fadd_rn(sat, 1.0f);
+    float val = 0.0f;
+    val = __fadd_rn(val, 1.0f);
+    float grad_p = 0.0f, grad_q = 0.0f, grad_t = 0.0f;
+    grad_p = __fadd_rn(grad_p, __fmul_rn(val, __fsub_rn(1.0f, sat)));
+    grad_q = __fadd_rn(grad_q, __fmul_rn(val, __fsub_rn(1.0f, __fmul_rn(sat, hue_f))));
+    grad_t = __fadd_rn(grad_t, __fmul_rn(val, __fsub_rn(1.0f, __fmul_rn(sat, __fsub_rn(1.0f, hue_f)))));
+    float r = __fmul_rn((float)((hue_i == 0) | (hue_i >= 5)), val);
+    r = __fadd_rn(r, __fmul_rn((float)(hue_i == 1), grad_q));
+    r = __fadd_rn(r, __fmul_rn((float)((hue_i == 2) | (hue_i == 3)), grad_p));
+    r = __fadd_rn(r, __fmul_rn((float)(hue_i == 4), grad_t));
+    float g = __fmul_rn((float)((hue_i == 0) | (hue_i >= 6)), grad_t);
+    g = __fadd_rn(g, __fmul_rn((float)((hue_i == 1) | (hue_i == 2)), val));
+    g = __fadd_rn(g, __fmul_rn((float)(hue_i == 3), grad_q));
+    g = __fadd_rn(g, __fmul_rn((float)((hue_i == 4) | (hue_i == 5)), grad_p));
+    float b = __fmul_rn((float)(((hue_i == 0) | (hue_i == 1)) | (hue_i >= 6)), grad_p);
+    b = __fadd_rn(b, __fmul_rn((float)(hue_i == 2), grad_t));
+    b = __fadd_rn(b, __fmul_rn((float)((hue_i == 3) | (hue_i == 4)), val));
+    b = __fadd_rn(b, __fmul_rn((float)(hue_i == 5), grad_q));
+    const int e = (255 - (int)energy) * ((int)(rule > 0) * (int)(energy < 255));
+    rgb[0] = (int)xk_f2u(__fmul_rn(r, (float)e));
+    rgb[1] = (int)xk_f2u(__fmul_rn(g, (float)e));
+    rgb[2] = (int)xk_f2u(__fmul_rn(b, (float)e));
+}
+
+// GenomeColor.positional (tools/color.py:63-104): double weights added into
+// float variables, then normalised by the float maximum
+__device__ __forceinline__ void xk_evo_color_positional(uint32_t rule, uint32_t energy, int *rgb)
+{
+    float red = 0.0f, green = 0.0f, blue = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 18; ++i) {
+        if ((rule >> i) & 1u) {
+            red = __double2float_rn(__dadd_rn((double)red, c_evo_pos[3 * i]));
+            green = __double2float_rn(__dadd_rn((double)green, c_evo_pos[3 * i + 1]));
+            blue = __double2float_rn(__dadd_rn((double)blue, c_evo_pos[3 * i + 2]));
+        }
+    }
+    float maxval = 0.0f;
+    const float m01 = red > green ? red : green;
+    maxval = __fadd_rn(maxval, m01 > blue ? m01 : blue);
+    red = __fdiv_rn(red, maxval);
+    green = __fdiv_rn(green, maxval);
+    blue = __fdiv_rn(blue, maxval);
+    const int e = (255 - (int)energy) * ((int)(rule > 0) * (int)(energy < 255));
+    rgb[0] = (int)xk_f2u(__fmul_rn(red, (float)e));
+    rgb[1] = (int)xk_f2u(__fmul_rn(green, (float)e));
+    rgb[2] = (int)xk_f2u(__fmul_rn(blue, (float)e));
+}
+
+struct EvoParams {
+    int32_t W, H;
+    uint32_t death_speed, max_genes;
+    float mut_thresh;          // mutated iff uniform <= mut_thresh ((double)u < p exactly)
+    int32_t mutation;          // mutation_prob > 0
+    int32_t positional;
+    int32_t color_kind;        // XK_COLOR_*
+    int32_t fade_in, fade_out, smooth;
+};
+
+#define XK_EVO_BX 32
+#define XK_EVO_BY 8
+
+__global__ void __launch_bounds__(XK_EVO_BX * XK_EVO_BY)
+xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32_t *__restrict__ col,
+             EvoParams p)
+{
+    __shared__ uint32_t gsm[8][XK_EVO_BX * XK_EVO_BY];   // compacted parent genomes
+    const int x = blockIdx.x * XK_EVO_BX + threadIdx.x;
+    const int y = blockIdx.y * XK_EVO_BY + threadIdx.y;
+    const int tid = threadIdx.y * XK_EVO_BX + threadIdx.x;
+    if (x >= p.W || y >= p.H) return;   // no block-wide synchronisation below
+    const int xl = x > 0 ? x - 1 : p.W - 1, xr = x < p.W - 1 ? x + 1 : 0;
+    const int yu = y > 0 ? y - 1 : p.H - 1, yd = y < p.H - 1 ? y + 1 : 0;
+    const int nxs[8] = {xl, xl, xl, x, x, xr, xr, xr};
+    const int nys[8] = {yu, y, yd, yu, yd, yu, y, yd};
+    uint32_t nr[8], alive[8];
+    uint32_t num_neighbors = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint64_t v = __ldg(src + (int64_t)nys[k] * p.W + nxs[k]);
+        const uint32_t ne = (uint32_t)(v & 511u);
+        nr[k] = (uint32_t)((v >> 9) & 262143u);
+        alive[k] = (ne + nr[k]) != 0u;              // xmath.min(1, e + r)
+        num_neighbors += alive[k];
+    }
+    const int64_t i = (int64_t)y * p.W + x;
+    const uint64_t c = src[i];
+    uint32_t energy = (uint32_t)(c & 511u);
+    uint32_t rule = (uint32_t)((c >> 9) & 262143u);
+    uint32_t rng = (uint32_t)((c >> 27) & 65535u);
+    const uint32_t is_sustained = ((rule & 261120u) >> (num_neighbors + 9)) & 1u;
+    // num_parents for every birth count 1..8 at once: nibble g counts the
+    // live neighbours whose rule has bit g + 1
+    uint32_t acc = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc += xk_spread_nibbles(alive[k] ? ((nr[k] >> 1) & 255u) : 0u);
+    uint32_t num_fit = 0;
+#pragma unroll
+    for (int g = 0; g < 8; ++g) {
+        const uint32_t np = (acc >> (4 * g)) & 15u;
+        const uint32_t fit = np * (uint32_t)(np == (uint32_t)(g + 1));
+        num_fit = num_fit > fit ? num_fit : fit;
+    }
+    // parents: rules with the winning birth count, compacted in neighbour order
+    uint32_t n = 0, any = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint32_t genome = nr[k] * (((nr[k] & 510u) >> num_fit) & 1u);
+        if (genome > 0) {
+            gsm[n][tid] = genome;
+            ++n;
+            any |= genome;
+        }
+    }
+    const uint32_t old_rule = rule, old_energy = energy;
+    // genome_crossover(main, 18, *genomes, max_genes, mutation_prob)
+    rng = xk_lcg(rng);
+    const uint32_t start_gene = xk_f2u(__fmul_rn(xk_uniform(rng), 18.0f)) % 8u;
+    const float nf = (float)n;
+    uint32_t new_genome = 0, num_active = 0;
+    uint32_t gene = start_gene;
+    for (int step = 0; step < 18; ++step) {
+        rng = xk_lcg(rng);
+        const uint32_t winner = xk_f2u(__fmul_rn(xk_uniform(rng), nf));
+        uint32_t new_gene = (winner < n) ? ((gsm[winner][tid] >> gene) & 1u) : 0u;
+        num_active += new_gene;
+        new_gene *= (uint32_t)(num_active <= p.max_genes);
+        uint32_t mutated = 0;
+        if (p.mutation) {
+            rng = xk_lcg(rng);
+            mutated = (uint32_t)(xk_uniform(rng) <= p.mut_thresh) & ((any >> gene) & 1u);
+        }
+        new_genome += (new_gene ^ mutated) << gene;
+        gene = gene == 17 ? 0 : gene + 1;
+    }
+    rule = new_genome + rule * (uint32_t)(new_genome == 0);
+    const uint32_t is_live = (uint32_t)(old_energy < 255u) &
+                             ((uint32_t)((old_energy + old_rule) == 0u) | is_sustained);
+    const uint32_t new_energy = old_energy + p.death_speed * (uint32_t)((old_energy + old_rule) != 0u);
+    energy = (uint16_t)(new_energy * (uint32_t)(rule == old_rule));
+    rule = old_rule * (uint32_t)(rule == old_rule) + rule * (uint32_t)(rule != old_rule);
+    energy = (uint16_t)(energy * is_live);
+    rule *= is_live;
+    if (p.color_kind != XK_COLOR_NONE) {
+        int rgb[3];
+        if (p.positional) xk_evo_color_positional(rule, energy, rgb);
+        else xk_evo_color_modular(rule, energy, rgb);
+        if (p.color_kind == XK_COLOR_MOVING_AVERAGE) {
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch)
+                rgb[ch] = xk_ma_clamp(rgb[ch] * p.smooth, col[3 * i + ch], p.fade_in, p.fade_out);
+        }
+        col[3 * i] = rgb[0];
+        col[3 * i + 1] = rgb[1];
+        col[3 * i + 2] = rgb[2];
+    }
+    dst[i] = ((uint64_t)energy & 511u) + (((uint64_t)rule & 262143u) << 9) +
+             (((uint64_t)rng & 65535u) << 27);
+}
+
+cudaError_t xk_evolife_set_positional(const double *lut54)
+{
+    return cudaMemcpyToSymbol(c_evo_pos, lut54, 54 * sizeof(double));
+}
+
+cudaError_t xk_evolife_step(const uint64_t *src, uint64_t *dst, int32_t *col, const xk_desc &d,
+                            float mut_thresh, cudaStream_t s)
+{
+    EvoParams p;
+    p.W = (int32_t)d.size[0];
+    p.H = (int32_t)d.size[1];
+    p.death_speed = d.death_speed;
+    p.max_genes = d.max_genes;
+    p.mut_thresh = mut_thresh;
+    p.mutation = d.mutation_prob > 0.0;
+    p.positional = d.positional;
+    p.color_kind = d.color_kind;
+    p.fade_in = d.fade_in;
+    p.fade_out = d.fade_out;
+    p.smooth = d.smooth;
+    dim3 block(XK_EVO_BX, XK_EVO_BY);
+    dim3 grid((p.W + XK_EVO_BX - 1) / XK_EVO_BX, (p.H + XK_EVO_BY - 1) / XK_EVO_BY);
+    xk_k_evolife<<<grid, block, 0, s>>>(src, dst, col, p);
+    return cudaGetLastError();
+}

@@ -12,6 +12,8 @@
 // Layout: 32 cells per 32-bit word, LSB = lowest x; a generation is pure
 // bitwise logic -- a carry-save adder network counts the 8 neighbours of 32
 // cells at once and a LOP3 multiplexer tree applies the runtime rule.
+#include <type_traits>
+
 #include "xk_internal.cuh"
 
 LifeTable xk_life_table(uint32_t rule0, uint32_t rule1)
@@ -41,14 +43,37 @@ LifeGeo xk_life_geo(int64_t W, int64_t H, int torus, int border_state)
 // ---------------------------------------------------------------------------
 // word-level logic
 
+// Three-input boolean functions as single lop3 instructions (PTX lop3.b32:
+// the immediate is the function evaluated on a = 0xF0, b = 0xCC, c = 0xAA).
+__device__ __forceinline__ uint32_t xk_lop3_mux(uint32_t sel, uint32_t a, uint32_t b)
+{
+    uint32_t d;   // sel ? b : a, bitwise
+    asm("lop3.b32 %0, %1, %2, %3, 0xAC;" : "=r"(d) : "r"(sel), "r"(a), "r"(b));
+    return d;
+}
+
+__device__ __forceinline__ uint32_t xk_lop3_maj(uint32_t a, uint32_t b, uint32_t c)
+{
+    uint32_t d;   // majority: carry of a full adder
+    asm("lop3.b32 %0, %1, %2, %3, 0xE8;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
+__device__ __forceinline__ uint32_t xk_lop3_xor3(uint32_t a, uint32_t b, uint32_t c)
+{
+    uint32_t d;   // sum of a full adder
+    asm("lop3.b32 %0, %1, %2, %3, 0x96;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
 __device__ __forceinline__ uint32_t xk_mux(uint32_t sel, uint32_t a, uint32_t b)
 {
-    return (a & ~sel) | (b & sel);
+    return xk_lop3_mux(sel, a, b);
 }
 
 __device__ __forceinline__ uint32_t xk_maj(uint32_t a, uint32_t b, uint32_t c)
 {
-    return (a & b) | (c & (a ^ b));
+    return xk_lop3_maj(a, b, c);
 }
 
 // Next state of 32 cells.  (Lu, Cu, Ru) are the row above shifted so that bit
@@ -61,11 +86,11 @@ __device__ __forceinline__ uint32_t xk_life_word(uint32_t Lu, uint32_t Cu, uint3
                                                  const Tab &t)
 {
     // neighbour count k = b0 + 2 b1 + 4 b2 + 8 b3 (k <= 8, so b3 implies k == 8)
-    const uint32_t su = Lu ^ Cu ^ Ru, cu = xk_maj(Lu, Cu, Ru);
-    const uint32_t sd = Ld ^ Cd ^ Rd, cd = xk_maj(Ld, Cd, Rd);
+    const uint32_t su = xk_lop3_xor3(Lu, Cu, Ru), cu = xk_maj(Lu, Cu, Ru);
+    const uint32_t sd = xk_lop3_xor3(Ld, Cd, Rd), cd = xk_maj(Ld, Cd, Rd);
     const uint32_t sm = Lm ^ Rm, cm = Lm & Rm;
-    const uint32_t b0 = su ^ sd ^ sm, k1 = xk_maj(su, sd, sm);
-    const uint32_t tw = cu ^ cd ^ cm, k2 = xk_maj(cu, cd, cm);
+    const uint32_t b0 = xk_lop3_xor3(su, sd, sm), k1 = xk_maj(su, sd, sm);
+    const uint32_t tw = xk_lop3_xor3(cu, cd, cm), k2 = xk_maj(cu, cd, cm);
     const uint32_t b1 = tw ^ k1, k3 = tw & k1;
     const uint32_t b2 = k2 ^ k3, b3 = k2 & k3;
     // rule lookup: multiplexer tree over (state, b2, b1, b0), then b3
@@ -92,8 +117,8 @@ __device__ __forceinline__ uint32_t xk_life_word_fa(uint32_t su, uint32_t cu, ui
                                                     uint32_t cd, const Tab &t)
 {
     const uint32_t sm = Lm ^ Rm, cm = Lm & Rm;
-    const uint32_t b0 = su ^ sd ^ sm, k1 = xk_maj(su, sd, sm);
-    const uint32_t tw = cu ^ cd ^ cm, k2 = xk_maj(cu, cd, cm);
+    const uint32_t b0 = xk_lop3_xor3(su, sd, sm), k1 = xk_maj(su, sd, sm);
+    const uint32_t tw = xk_lop3_xor3(cu, cd, cm), k2 = xk_maj(cu, cd, cm);
     const uint32_t b1 = tw ^ k1, k3 = tw & k1;
     const uint32_t b2 = k2 ^ k3, b3 = k2 & k3;
     uint32_t m[8];
@@ -359,49 +384,59 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
             // below comes from the band itself except for the band's last
             // row (halo).  Rows whose width is a multiple of 32 need no
             // partial-word handling: both neighbour vectors are one funnel
-            // shift and no output mask applies.
-            const bool fullw = I.rlast == 32;
-            uint32_t su = vu.L ^ vu.C ^ vu.R, cu = xk_maj(vu.L, vu.C, vu.R);
-            uint32_t sm_ = vm.L ^ vm.C ^ vm.R, cm_ = xk_maj(vm.L, vm.C, vm.R);
+            // shift and no output mask applies.  The width test is uniform
+            // per CTA and taken outside the row loop.
+            uint32_t su = xk_lop3_xor3(vu.L, vu.C, vu.R), cu = xk_maj(vu.L, vu.C, vu.R);
+            uint32_t sm_ = xk_lop3_xor3(vm.L, vm.C, vm.R), cm_ = xk_maj(vm.L, vm.C, vm.R);
             uint32_t Lm = vm.L, Cm = vm.C, Rm = vm.R;
-            auto row = [&](uint32_t wd, int i) {
-                const uint32_t l = __shfl_sync(0xFFFFFFFFu, wd, src_l);
-                const uint32_t r = __shfl_sync(0xFFFFFFFFu, wd, src_r);
-                uint32_t Ld, Rd;
-                if (fullw) {
-                    Ld = __funnelshift_l(l, wd, 1);
-                    Rd = __funnelshift_r(wd, r, 1);
-                } else {
-                    const RowVec d = xk_torus_vec(wd, l, r, lpre, top, topbit);
-                    Ld = d.L;
-                    Rd = d.R;
-                }
-                const uint32_t sd = Ld ^ wd ^ Rd, cd = xk_maj(Ld, wd, Rd);
-                uint32_t out = xk_life_word_fa(su, cu, Lm, Cm, Rm, sd, cd, t);
-                if (!fullw) out &= outmask;
-                if (active) lat[(i * p.G + bc) * wpr + jc] = out;
-                su = sm_;
-                cu = cm_;
-                sm_ = sd;
-                cm_ = cd;
-                Lm = Ld;
-                Cm = wd;
-                Rm = Rd;
-            };
+            const int stride = p.G * wpr;                       // words between band rows
+            uint32_t *wp = lat + bc * wpr + jc;                 // this lane's word of row i
             const uint32_t whalo = halo[(hdn * 2 + 0) * wpr + jc];
-            if (p.L == 1) {
-                row(whalo, 0);
-            } else {
-                uint32_t wd = lat[(1 * p.G + bc) * wpr + jc];
-                int i = 0;
-                for (; i + 2 < p.L; ++i) {
-                    const uint32_t wnext = lat[((i + 2) * p.G + bc) * wpr + jc];
-                    row(wd, i);
+            auto band_rows = [&](auto fullw_tag) {
+                constexpr bool FULLW = decltype(fullw_tag)::value;
+                auto row = [&](uint32_t wd, uint32_t *dst) {
+                    const uint32_t l = __shfl_sync(0xFFFFFFFFu, wd, src_l);
+                    const uint32_t r = __shfl_sync(0xFFFFFFFFu, wd, src_r);
+                    uint32_t Ld, Rd;
+                    if (FULLW) {
+                        Ld = __funnelshift_l(l, wd, 1);
+                        Rd = __funnelshift_r(wd, r, 1);
+                    } else {
+                        const RowVec d = xk_torus_vec(wd, l, r, lpre, top, topbit);
+                        Ld = d.L;
+                        Rd = d.R;
+                    }
+                    const uint32_t sd = xk_lop3_xor3(Ld, wd, Rd), cd = xk_maj(Ld, wd, Rd);
+                    uint32_t out = xk_life_word_fa(su, cu, Lm, Cm, Rm, sd, cd, t);
+                    if (!FULLW) out &= outmask;
+                    if (active) *dst = out;
+                    su = sm_;
+                    cu = cm_;
+                    sm_ = sd;
+                    cm_ = cd;
+                    Lm = Ld;
+                    Cm = wd;
+                    Rm = Rd;
+                };
+                if (p.L == 1) {
+                    row(whalo, wp);
+                    return;
+                }
+                uint32_t wd = wp[stride];
+                uint32_t *dst = wp;
+                const uint32_t *src = wp + 2 * stride;
+                const uint32_t *src_end = wp + p.L * stride;
+#pragma unroll 2
+                for (; src < src_end; src += stride, dst += stride) {
+                    const uint32_t wnext = *src;
+                    row(wd, dst);
                     wd = wnext;
                 }
-                row(wd, i);          // i == L - 2: row below is the band's last row
-                row(whalo, i + 1);   // i == L - 1: row below is the next band's first row
-            }
+                row(wd, dst);              // row L-2: row below is the band's last row
+                row(whalo, dst + stride);  // row L-1: row below is the next band's first
+            };
+            if (I.rlast == 32) band_rows(std::true_type());
+            else band_rows(std::false_type());
         } else {
             // general path: bands may be shorter than L; every lane still
             // runs L iterations so the shuffles always see the full warp

@@ -111,3 +111,8 @@ cudaError_t xk_render_colors(const int32_t *col, int32_t *img, const RenderGeo &
                              int height, int zoom, int dx, int dy, cudaStream_t s);
 
 int xk_sm_count();
+
+// EvoLife family (evolife.cu)
+cudaError_t xk_evolife_set_positional(const double *lut54);
+cudaError_t xk_evolife_step(const uint64_t *src, uint64_t *dst, int32_t *col, const xk_desc &d,
+                            float mut_thresh, cudaStream_t s);
