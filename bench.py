@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=2041)
     ap.add_argument("--plain-generations", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--workload", choices=("ensemble", "evolife"), default="ensemble",
+                    help="ensemble: the batched Life-like ensemble (default); evolife: EvoLife "
+                         "1920x1080 with a render every generation")
     return ap.parse_args()
 
 
@@ -335,12 +338,104 @@ def run_ours(args, dist):
         print(json.dumps(line), flush=True)
 
 
+def evolife_experiment():
+    """CrossbreedingExperiment2 of the reference (examples/evolife.py:447-488)."""
+    from xentica_gb300 import core, seeds
+    from xentica_gb300.seeds.random import RandInt
+    from xentica_gb300.tools.rules import LifeLike
+
+    class Crossbreeding(core.Experiment):
+        word = "FUTURE BREEDING MACHINE 2041"
+        size = (1920, 1080)
+        zoom = 1
+        pos = [0, 0]
+        fade_in = 18
+        fade_out = 3
+        death_speed = 25
+        max_genes = 9
+        mutation_prob = 0.0001
+        seed = (seeds.patterns.PrimordialSoup(vals={"rng": RandInt(0, 2 ** 16 - 1)})
+                + seeds.patterns.BigBang(pos=(0, 0), size=(1280, 720), vals={
+                    "energy": 0, "rule": +RandInt(0, 1) * LifeLike.golly2int("B3/S23"),
+                    "rng": 0 + RandInt(0, 2 ** 16 - 1)})
+                + seeds.patterns.BigBang(pos=(380, 280), size=(440, 340), vals={
+                    "energy": 0, "rule": LifeLike.golly2int("B35678/S5678") * RandInt(0, 1),
+                    "rng": RandInt(0, 2 ** 16 - 1)}))
+    return Crossbreeding
+
+
+def run_evolife(args, dist):
+    """EvoLife 1920x1080: K steps of 100 generations, each generation
+    followed by a full-frame render (image copied to the host)."""
+    from xentica_gb300 import build as xk_build
+    from xentica_gb300 import _native as nat
+    from xentica_gb300.core.canonical import EvoLifeProgram
+    xk_build.build()
+    nat.set_device(dist.local)
+    lib = nat.load()
+    model = EvoLifeProgram(evolife_experiment())
+    model.set_viewport(model.size)
+    n = model.cells_num
+    gens = 100
+    model.gpu.step(1)
+    for _ in range(args.warmup):
+        model.gpu.step(gens)
+    clocks = Clocks(dist.local)
+    time.sleep(0.6)
+    dist.barrier()
+    step_ms = []
+    for _ in range(args.steps):
+        model.gpu.step(gens)
+        step_ms.append(lib.xk_last_step_ms())
+    dist.barrier()
+    clk = clocks.stop()
+    t0 = time.perf_counter()
+    for _ in range(5):
+        model.render()
+    render_ms = (time.perf_counter() - t0) / 5 * 1000
+    dev_s = dist.max(sum(step_ms) / 1000.0)
+    value = float(n) * gens * args.steps * dist.world / dev_s
+    bytes_per_update = 8 * 2 + 12 * 2      # uint64 state read+write, int3 colour read+write
+    peak, peak_kind = measured_peak()
+    achieved = bytes_per_update * n * gens / (statistics.mean(step_ms) / 1000.0) / 1e9
+    line = {"metric": "cell-updates/s (EvoLife)", "value": value, "unit": "cell-updates/s",
+            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dev_s * 1000 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (seeded CrossbreedingExperiment2 layout)",
+            "config": {"workload": "EvoLife 1920x1080 torus, 100 generations per step, "
+                                   "modular colour, MovingAverage(18, 3)",
+                       "l2": "state + colours (41 MB) fit in L2"},
+            "render_ms_per_frame": render_ms,
+            "roofline": {"bound": "alu", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "note": "40 B per cell-update of state and colour traffic; the "
+                                 "kernel is integer-ALU bound (genome crossover)"},
+            "clocks": clk}
+    if dist.rank == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        topo = O.Topology(model.size)
+        fld = topo.field(model.gpu.arrays.cells.get()[:n], np.uint64)
+        col = model.gpu.arrays.colors.get()
+        t0 = time.perf_counter()
+        O.evolife_run(topo, fld, col, 2, death_speed=25, max_genes=9, mutation_prob=0.0001,
+                      fade_in=18, fade_out=3)
+        el = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n * 2 / el, "unit": "cell-updates/s",
+                                "cores": os.cpu_count(), "kind": "port",
+                                "sample": "2 generations of the full lattice, oracle (OpenMP)"}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
         if args.impl == "reference":
             run_reference_arm(args, dist)
+        elif args.workload == "evolife":
+            run_evolife(args, dist)
         else:
             run_ours(args, dist)
     finally:

@@ -27,6 +27,7 @@ class EvoLifeProgram(core.CellularAutomaton):
     energy = core.IntegerProperty(max_val=255 * 2)
     rule = core.TotalisticRuleProperty(outer=True)
     rng = core.RandomProperty()
+    _legacy_coloring = True          # GenomeColor.modular; False: .positional
     death_speed = core.Parameter(default=15)
     max_genes = core.Parameter(default=9)
     mutation_prob = core.Parameter(default=.0)
