@@ -34,7 +34,7 @@ def _oracle_step(model, fld, col, steps):
 
 @pytest.mark.parametrize("legacy,mutation", [(True, 0.0), (False, 0.2), (True, 0.0001)])
 def test_random_states_vs_oracle(legacy, mutation):
-    w, h = 97, 61
+    w, h = 131, 103          # at least the BigBang seed area (100 x 100)
     model = _model((w, h), legacy, mutation_prob=mutation, death_speed=9, max_genes=7,
                    fade_in=30, fade_out=7)
     rng = np.random.RandomState(int(mutation * 1e4) + legacy)
