@@ -50,9 +50,10 @@ def parse():
     ap.add_argument("--seed", type=int, default=2041)
     ap.add_argument("--plain-generations", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--workload", choices=("ensemble", "evolife"), default="ensemble",
+    ap.add_argument("--workload", choices=("ensemble", "evolife", "mass"), default="ensemble",
                     help="ensemble: the batched Life-like ensemble (default); evolife: EvoLife "
-                         "1920x1080 with a render every generation")
+                         "1920x1080 with a render every generation; mass: 3-D sand transfer "
+                         "256^3 with the total checked every generation")
     return ap.parse_args()
 
 
@@ -428,6 +429,81 @@ def run_evolife(args, dist):
         print(json.dumps(line), flush=True)
 
 
+def run_mass(args, dist):
+    """Mass transfer 256^3, Poisson(4) masses: K steps of 100 generations; the
+    total mass of every generation (reduced inside the kernel) is checked
+    against the initial total after each step; z-projection render timed."""
+    from xentica_gb300 import build as xk_build
+    from xentica_gb300 import _native as nat
+    from xentica_gb300 import core, seeds
+    from xentica_gb300.core.canonical import MassTransferProgram
+    xk_build.build()
+    nat.set_device(dist.local)
+    lib = nat.load()
+
+    class SandPiles(core.Experiment):
+        word = "SAND PILES 3D"
+        size = (256, 256, 256)
+        zoom = 1
+        pos = [0, 0]
+        seed = seeds.patterns.PrimordialSoup(vals={"mass": seeds.random.RandPoisson(4)})
+
+    model = MassTransferProgram(SandPiles)
+    model.set_viewport((256, 256))
+    n = model.cells_num
+    total0 = int(model.gpu.arrays.cells.get()[:n].astype(np.uint64).sum())
+    gens = 100
+    for _ in range(args.warmup):
+        model.gpu.step(gens)
+    clocks = Clocks(dist.local)
+    time.sleep(0.6)
+    dist.barrier()
+    step_ms = []
+    conserved = True
+    for _ in range(args.steps):
+        model.gpu.step(gens)
+        step_ms.append(lib.xk_last_step_ms())
+        totals = model.gpu.mass_totals(gens)
+        conserved &= bool((totals == total0).all())
+    dist.barrier()
+    clk = clocks.stop()
+    t0 = time.perf_counter()
+    for _ in range(5):
+        model.render()
+    render_ms = (time.perf_counter() - t0) / 5 * 1000
+    dev_s = dist.max(sum(step_ms) / 1000.0)
+    value = float(n) * gens * args.steps * dist.world / dev_s
+    bytes_per_update = 4 * 2           # uint32 mass read + write
+    peak, peak_kind = measured_peak()
+    achieved = bytes_per_update * n * gens / (statistics.mean(step_ms) / 1000.0) / 1e9
+    line = {"metric": "cell-updates/s (mass transfer 3-D)", "value": value,
+            "unit": "cell-updates/s", "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_s * 1000 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded Poisson(4) masses)",
+            "config": {"workload": "mass transfer 256^3 von Neumann, StaticBorder wall, "
+                                   "100 generations per step, total checked every generation",
+                       "l2": "state (2 x 64 MB) close to L2 size; no flush"},
+            "mass_conserved": conserved, "render_ms_per_frame": render_ms,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "note": "8 B per cell-update (uint32 read + write)"},
+            "clocks": clk}
+    if dist.rank == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        topo = O.Topology(model.size, "von_neumann", border=2 ** 32 - 1)
+        fld = topo.field(model.gpu.arrays.cells.get()[:n], np.uint32)
+        col = model.gpu.arrays.colors.get()
+        t0 = time.perf_counter()
+        O.mass_run(topo, fld, col, 3)
+        el = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n * 3 / el, "unit": "cell-updates/s",
+                                "cores": os.cpu_count(), "kind": "port",
+                                "sample": "3 generations of the full lattice, oracle (OpenMP)"}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -436,6 +512,8 @@ def main():
             run_reference_arm(args, dist)
         elif args.workload == "evolife":
             run_evolife(args, dist)
+        elif args.workload == "mass":
+            run_mass(args, dist)
         else:
             run_ours(args, dist)
     finally:

@@ -73,6 +73,17 @@ CASES.update({
                                         checkpoints=[1, 5, 40]),
 })
 
+CASES.update({
+    "mass_24x20x12": dict(model=REF_MODELS + ":MassTransfer", experiment=REF_MODELS + ":MassExperiment",
+                          checkpoints=[1, 2, 10, 50], render={"viewport": [24, 20]}),
+    "mass_37x5x64": dict(model=REF_MODELS + ":MassTransfer", experiment=REF_MODELS + ":MassExperiment",
+                         exp_overrides={"size": [37, 5, 64], "word": "tall"}, checkpoints=[1, 7, 40],
+                         render={"viewport": [40, 9]}),
+    "mass_64cube": dict(model=REF_MODELS + ":MassTransfer", experiment=REF_MODELS + ":MassExperiment",
+                        exp_overrides={"size": [64, 64, 64], "word": "cube", "zoom": 2, "pos": [3, -5]},
+                        checkpoints=[1, 30], render={"viewport": [100, 90]}),
+})
+
 # odd sizes, both borders: pins word-boundary and wrap handling
 for w, h in [(1, 1), (1, 17), (17, 1), (2, 2), (31, 5), (32, 7), (33, 9), (63, 64), (64, 63),
              (65, 3), (100, 100), (1023, 5), (1024, 3), (1025, 4), (2000, 11), (3, 1200)]:

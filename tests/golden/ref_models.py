@@ -67,3 +67,70 @@ class LifelikeFixed(GameOfLife):
         is_born = (self.rule >> neighbors_alive) & 1
         is_sustain = (self.rule >> 9 >> neighbors_alive) & 1
         self.main.state = is_born | is_sustain & self.main.state
+
+
+import functools as _functools
+import operator as _operator
+
+from xentica import seeds as _seeds
+from xentica.core.expressions import PatternExpression
+from xentica.tools import xmath
+
+
+class RandPoisson(PatternExpression):
+    """Poisson(lam) per cell from the pattern's NumPy stream (the seed
+    expression xentica_gb300.seeds.random.RandPoisson adds)."""
+
+    def __init__(self, lam):
+        super().__init__()
+        self.lam = lam
+
+    def __get__(self, instance, owner):
+        n = _functools.reduce(_operator.mul, instance.size)
+        return instance.random.numpy.poisson(self.lam, n).astype("int64")
+
+
+WALL = 2 ** 32 - 1
+
+
+class MassTransfer(core.CellularAutomaton):
+    """Mass-conserving sand transfer on a 3-D von Neumann lattice whose
+    border is a wall: every cell sends mass // 7 to each neighbour that is
+    not a wall and absorbs what its neighbours send."""
+
+    mass = core.IntegerProperty(max_val=2 ** 32 - 2)
+
+    class Topology:
+        dimensions = 3
+        lattice = core.OrthogonalLattice()
+        neighborhood = core.VonNeumannNeighborhood()
+        border = core.StaticBorder(WALL)
+
+    def emit(self):
+        share = core.IntegerVariable()
+        share += self.main.mass / 7
+        for i in range(len(self.buffers)):
+            self.buffers[i].mass = share * (self.neighbors[i].main.mass != WALL)
+
+    def absorb(self):
+        total = core.IntegerVariable()
+        total += self.main.mass
+        for i in range(len(self.buffers)):
+            total -= self.buffers[i].mass
+        for i in range(len(self.buffers)):
+            incoming = self.neighbors[i].buffer.mass
+            total += incoming * (incoming != WALL)
+        self.main.mass = total
+
+    @color_effects.ColorEffect
+    def color(self):
+        v = xmath.min(self.main.mass * 32, 255)
+        return (v, v, v)
+
+
+class MassExperiment(core.Experiment):
+    word = "SAND PILES 3D"
+    size = (24, 20, 12)
+    zoom = 1
+    pos = [0, 0]
+    seed = _seeds.patterns.PrimordialSoup(vals={"mass": RandPoisson(4)})

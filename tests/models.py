@@ -378,3 +378,51 @@ MODELS["EvoLife"] = EvoLife
 EXPERIMENTS.update({"CrossbreedingExperiment": CrossbreedingExperiment,
                     "CrossbreedingExperiment2": CrossbreedingExperiment2,
                     "BigBangExperiment": BigBangExperiment})
+
+
+WALL = 2 ** 32 - 1
+
+
+class MassTransfer(core.CellularAutomaton):
+    """Mass-conserving sand transfer, 3-D von Neumann, wall border."""
+
+    mass = core.IntegerProperty(max_val=2 ** 32 - 2)
+
+    class Topology:
+        dimensions = 3
+        lattice = core.OrthogonalLattice()
+        neighborhood = core.VonNeumannNeighborhood()
+        border = core.StaticBorder(WALL)
+
+    def emit(self):
+        share = core.IntegerVariable()
+        share += self.main.mass / 7
+        for i in range(len(self.buffers)):
+            self.buffers[i].mass = share * (self.neighbors[i].main.mass != WALL)
+
+    def absorb(self):
+        total = core.IntegerVariable()
+        total += self.main.mass
+        for i in range(len(self.buffers)):
+            total -= self.buffers[i].mass
+        for i in range(len(self.buffers)):
+            incoming = self.neighbors[i].buffer.mass
+            total += incoming * (incoming != WALL)
+        self.main.mass = total
+
+    @color_effects.ColorEffect
+    def color(self):
+        v = xmath.min(self.main.mass * 32, 255)
+        return (v, v, v)
+
+
+class MassExperiment(core.Experiment):
+    word = "SAND PILES 3D"
+    size = (24, 20, 12)
+    zoom = 1
+    pos = [0, 0]
+    seed = seeds.patterns.PrimordialSoup(vals={"mass": seeds.random.RandPoisson(4)})
+
+
+MODELS["MassTransfer"] = MassTransfer
+EXPERIMENTS["MassExperiment"] = MassExperiment

@@ -394,3 +394,18 @@ def test_bridge_actions():
     assert model.paused != paused
     Bridge.toggle_sysinfo(model, gui)
     assert gui.sysinfo.toggled
+
+
+def test_template_match_repeated_instances():
+    # the translator's container state carries over between models of one
+    # class (a buffer read by one kernel is declared with a load in the next
+    # model's kernels); every instance must still match its kernel family
+    from xentica_gb300.core import canonical
+    from tests.models import MassTransfer, MassExperiment, EvoLife, BigBangExperiment
+    small = type("E", (MassExperiment, ), {"size": (12, 10, 8)})
+    for cls in (MassTransfer, canonical.MassTransferProgram, MassTransfer):
+        for _ in range(2):
+            assert type(cls(small).gpu.template).__name__ == "MassTemplate"
+    evo = type("E", (BigBangExperiment, ), {"size": (128, 128)})
+    for _ in range(2):
+        assert type(EvoLife(evo).gpu.template).__name__ == "EvoLifeTemplate"

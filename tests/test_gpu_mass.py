@@ -1,0 +1,69 @@
+"""GPU parity of the mass-transfer kernel (3-D von Neumann, wall border).
+
+Fixture cases (reference checksums) replay through ``test_gpu_life``'s
+fixture test; here: random states with large masses (unsigned wrap-around of
+the reference's arithmetic, cells equal to the wall value) compared with the
+oracle cell by cell, image parity, and conservation of the total mass over a
+long run read from the kernel's own per-generation totals.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from tests.models import MassTransfer, MassExperiment, WALL
+
+pytestmark = pytest.mark.gpu
+
+
+def _model(size):
+    exp = type("E", (MassExperiment, ), {"size": size})
+    return MassTransfer(exp)
+
+
+def _topo(size):
+    return O.Topology(size, "von_neumann", border=WALL)
+
+
+@pytest.mark.parametrize("size,high", [((33, 17, 9), 2 ** 32 - 1), ((64, 8, 31), 2 ** 20),
+                                       ((7, 129, 5), 100)])
+def test_random_states_vs_oracle(size, high):
+    model = _model(size)
+    n = model.cells_num
+    rng = np.random.RandomState(size[0])
+    cells = rng.randint(0, high, n, dtype=np.uint64).astype(np.uint32)
+    if high > 2 ** 31:
+        cells[rng.randint(0, n, 20)] = WALL
+    colors = np.zeros(3 * n, dtype=np.int32)
+    model.gpu.load(cells, colors)
+    topo = _topo(size)
+    fld = topo.field(cells, np.uint32)
+    col = colors.copy()
+    for step in range(5):
+        model.step()
+        O.mass_run(topo, fld, col, 1)
+        assert np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n]), "step %d" % step
+        assert np.array_equal(model.gpu.arrays.colors.get(), col), "colours step %d" % step
+    w, h = size[0] + 5, size[1] + 3
+    img = O.render(topo, col, w, h, zoom=1, dx=-2, dy=3, smooth=0).astype(np.uint8)
+    model.set_viewport((w, h))
+    model.pos = [-2, 3]
+    assert np.array_equal(model.render(), img)
+
+
+def test_mass_conserved_long_run():
+    model = _model((96, 80, 40))
+    before = int(model.gpu.arrays.cells.get()[:model.cells_num].astype(np.uint64).sum())
+    model.gpu.step(500)
+    totals = model.gpu.mass_totals(500)
+    assert totals.tolist() == [before] * 500
+    after = int(model.gpu.arrays.cells.get()[:model.cells_num].astype(np.uint64).sum())
+    assert after == before
+
+
+def test_multi_generation_call_equals_single_steps():
+    a, b = _model((40, 24, 16)), _model((40, 24, 16))
+    a.gpu.step(7)
+    for _ in range(7):
+        b.step()
+    assert np.array_equal(a.gpu.arrays.cells.get(), b.gpu.arrays.cells.get())
+    assert np.array_equal(a.gpu.arrays.colors.get(), b.gpu.arrays.colors.get())

@@ -94,14 +94,17 @@ def test_oracle_fixtures(golden, case):
     job = entry["job"]
     topo, fld, col, model = oracle_setup(job)
     assert crc(fld[:topo.cells]) == entry["init"]
-    tpl, color = life_params(model)
+    tpl, color = life_params(model) if type(model).__name__ != "MassTransfer" else (None, None)
     done = 0
     axes = model.renderer.projection_axes
     smooth = model.constants["SMOOTH_FACTOR"].value if model.is_constant("SMOOTH_FACTOR") else 0
     for cp in sorted(int(c) for c in entry["steps"]):
-        O.life_run(topo, fld, col, cp - done, born=tpl.rule0, sustain=tpl.rule1, color=color,
-                   bits=model.main.properties["state"].bit_width,
-                   lut=LUTS.get(type(model).__name__, (0, 0, 0, 255, 255, 255)))
+        if type(model).__name__ == "MassTransfer":
+            O.mass_run(topo, fld, col, cp - done)
+        else:
+            O.life_run(topo, fld, col, cp - done, born=tpl.rule0, sustain=tpl.rule1, color=color,
+                       bits=model.main.properties["state"].bit_width,
+                       lut=LUTS.get(type(model).__name__, (0, 0, 0, 255, 255, 255)))
         done = cp
         exp = entry["steps"][str(cp)]
         assert crc(fld[:topo.cells]) == exp["cells"], "cells at step %d" % cp
@@ -143,3 +146,11 @@ def test_oracle_evolife_reference_golden(golden):
     evolife_run(model, topo, fld, col, 100)
     assert crc(fld[:topo.cells]) == 3381214984
     assert crc(col) == 2253830262
+
+
+def test_oracle_mass_conserved(golden):
+    topo, fld, col, model = oracle_setup(golden["mass_64cube"]["job"])
+    totals = []
+    before = int(fld[:topo.cells].astype(np.uint64).sum())
+    O.mass_run(topo, fld, col, 30, totals=totals)
+    assert totals == [before] * 30

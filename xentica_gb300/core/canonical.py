@@ -125,3 +125,41 @@ def trace(program_cls, size, params, attrs):
         inst.build_emit()
         inst.build_absorb()
         return inst.programs
+
+
+#: off-board (and wall) mass of the mass-transfer family
+MASS_WALL = 2 ** 32 - 1
+
+
+class MassTransferProgram(core.CellularAutomaton):
+    """Mass-conserving sand transfer: each cell sends mass / 7 to every
+    neighbour that is not the wall and absorbs what it is sent."""
+
+    mass = core.IntegerProperty(max_val=2 ** 32 - 2)
+
+    class Topology:
+        dimensions = 3
+        lattice = core.OrthogonalLattice()
+        neighborhood = core.VonNeumannNeighborhood()
+        border = core.StaticBorder(MASS_WALL)
+
+    def emit(self):
+        share = core.IntegerVariable()
+        share += self.main.mass / 7
+        for i in range(len(self.buffers)):
+            self.buffers[i].mass = share * (self.neighbors[i].main.mass != MASS_WALL)
+
+    def absorb(self):
+        total = core.IntegerVariable()
+        total += self.main.mass
+        for i in range(len(self.buffers)):
+            total -= self.buffers[i].mass
+        for i in range(len(self.buffers)):
+            incoming = self.neighbors[i].buffer.mass
+            total += incoming * (incoming != MASS_WALL)
+        self.main.mass = total
+
+    @color_effects.ColorEffect
+    def color(self):
+        v = xmath.min(self.main.mass * 32, 255)
+        return (v, v, v)

@@ -134,6 +134,15 @@ class GPU:
                   "xk_render")
         return img
 
+    def mass_totals(self, count):
+        """Total mass after each generation of the last ``step(count)`` (mass
+        transfer models): the conserved quantity."""
+        self._ensure()
+        out = np.zeros(int(count), dtype=np.uint64)
+        nat.check(self._lib.xk_mass_totals(self._handle, nat.ptr(out), int(count)),
+                  "xk_mass_totals")
+        return out
+
     def main_plane(self):
         """Main state in the reference dtype (``cells_num`` values)."""
         if self._handle is None:

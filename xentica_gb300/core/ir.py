@@ -531,13 +531,59 @@ def evaluate(program, inputs, params=None, lanes=None):
         raise XenticaException("Model cannot be analysed: %s." % exc)
 
 
+def _reads(n, out):
+    """Add the variable names ``n`` reads to ``out``; False if ``n`` holds
+    opaque text (which may read anything)."""
+    if n is None:
+        return True
+    if isinstance(n, Raw):
+        return False
+    if isinstance(n, VarRef):
+        out.add(n.name)
+        return True
+    if isinstance(n, Call):
+        return all(_reads(a, out) for a in n.args)
+    return all(_reads(getattr(n, attr, None), out) for attr in ("a", "b", "c"))
+
+
+def dead_initializers(program):
+    """Indices of ``decl`` statements whose initial value is overwritten by a
+    plain assignment before anything reads the variable.
+
+    The translator declares a packed container with a load of its memory cell
+    once any earlier kernel of the same model class has read that container,
+    so a second model of a class declares the buffer cells it only writes
+    with a load that the first model omits; the loaded value is dead.
+    """
+    stmts = program.stmts
+    dead = set()
+    for i, st in enumerate(stmts):
+        if st.op != "decl" or st.expr is None:
+            continue
+        for later in stmts[i + 1:]:
+            reads = set()
+            nodes = [later.expr]
+            if later.op == "color":
+                nodes = list(later.extra["rgb"])
+            if not all(_reads(x, reads) for x in nodes) or st.var in reads:
+                break
+            if later.op == "aug" and later.var == st.var:
+                break
+            if later.op == "assign" and later.var == st.var:
+                dead.add(i)
+                break
+    return dead
+
+
 def fingerprint(program):
     """Structure of a program with variables renamed by first appearance.
 
     Two programs with equal fingerprints execute the same statements on the
-    same types and constants, whatever their variables are called.
+    same types and constants, whatever their variables are called; dead
+    initial values of declarations (``dead_initializers``) are left out.
     """
     names = {}
+    dead = dead_initializers(program)
 
     def nm(name):
         return names.setdefault(name, "v%d" % len(names))
@@ -568,11 +614,11 @@ def fingerprint(program):
         return ("R", n.text())
 
     out = []
-    for st in program.stmts:
+    for i, st in enumerate(program.stmts):
         if st.op == "color":
             out.append(("color", st.extra["kind"], tuple(fp(x) for x in st.extra["rgb"])))
         else:
             out.append((st.op, nm(st.var) if st.var else None,
-                        st.ctype.name if st.ctype is not None else None, fp(st.expr), st.aug,
-                        st.extra))
+                        st.ctype.name if st.ctype is not None else None,
+                        None if i in dead else fp(st.expr), st.aug, st.extra))
     return tuple(out)

@@ -299,7 +299,37 @@ class EvoLifeTemplate:
         return d
 
 
-FAMILIES = (LifeTemplate, EvoLifeTemplate)
+class MassTemplate:
+    """Mass transfer (``canonical.MassTransferProgram``): 3-D von Neumann,
+    StaticBorder(2**32 - 1), matched by program fingerprint."""
+
+    family = nat.XK_FAMILY_MASS
+
+    def __init__(self, model):
+        from xentica_gb300.core import canonical
+        names = [type(p).__name__ for p in model.main.properties.values()]
+        if names != ["IntegerProperty"] or model.main.bit_width != 32:
+            raise NoTemplate("not one 32-bit integer property")
+        deltas, torus, border = _topology(model)
+        if model.topology.dimensions != 3 or len(deltas) != 6 or torus \
+                or border != canonical.MASS_WALL:
+            raise NoTemplate("mass kernel is 3-D von Neumann with a 2**32-1 wall")
+        programs = canonical.trace(canonical.MassTransferProgram, model.size, {}, {})
+        for key in ("emit", "absorb"):
+            if ir.fingerprint(programs[key]) != ir.fingerprint(model.programs[key]):
+                raise NoTemplate("%s differs from the mass-transfer program" % key)
+        self.model = model
+        self.wall = canonical.MASS_WALL
+
+    def descriptor(self):
+        d = _base_desc(self.model, self.family)
+        d.wall = self.wall
+        d.color_kind = nat.XK_COLOR_PLAIN
+        d.smooth = 1
+        return d
+
+
+FAMILIES = (LifeTemplate, EvoLifeTemplate, MassTemplate)
 
 
 def match(model):

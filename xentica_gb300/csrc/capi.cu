@@ -74,7 +74,7 @@ extern "C" int xk_device_info(char *buf, int32_t len)
 // ---------------------------------------------------------------------------
 // model object
 
-enum { LAYOUT_BITS2D = 1, LAYOUT_BYTES = 2, LAYOUT_CELLS64 = 3 };
+enum { LAYOUT_BITS2D = 1, LAYOUT_BYTES = 2, LAYOUT_CELLS64 = 3, LAYOUT_MASS = 4 };
 
 // largest float t with (double)u < p  <=>  u <= t for every float u
 static float below_threshold(double p)
@@ -96,6 +96,11 @@ struct xk_model {
     uint8_t *bytes[2] = {nullptr, nullptr};
     uint64_t *cells64[2] = {nullptr, nullptr};  // EvoLife: reference layout, ping-pong
     float mut_thresh = 0.f;
+    uint32_t *cells32[2] = {nullptr, nullptr};  // mass transfer: reference layout, ping-pong
+    uint32_t *proj = nullptr;                   // mass: colour sum of every (x, y) column
+    int proj_valid = 0;
+    unsigned long long *totals = nullptr;       // mass: total after each generation
+    int64_t totals_cap = 0, totals_count = 0;
     int cur = 0;
     void *stage = nullptr;       // reference-layout staging + validity flag
     int32_t *col = nullptr;      // colours (3 int32 per cell) when materialised
@@ -163,7 +168,10 @@ static void free_model(xk_model *m)
         if (m->bits[i]) cudaFree(m->bits[i]);
         if (m->bytes[i]) cudaFree(m->bytes[i]);
         if (m->cells64[i]) cudaFree(m->cells64[i]);
+        if (m->cells32[i]) cudaFree(m->cells32[i]);
     }
+    if (m->proj) cudaFree(m->proj);
+    if (m->totals) cudaFree(m->totals);
     if (m->stage) cudaFree(m->stage);
     if (m->col) cudaFree(m->col);
     if (m->img) cudaFree(m->img);
@@ -209,8 +217,12 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
                XK_ERR_ARG, "state_bytes %d", d.state_bytes);
     const int64_t n = cells_of(d);
     XK_REQUIRE(n <= (1LL << 40), XK_ERR_ARG, "lattice of %lld cells too large", (long long)n);
-    XK_REQUIRE(d.family == XK_FAMILY_LIFE || d.family == XK_FAMILY_EVOLIFE, XK_ERR_UNSUPPORTED,
-               "model family %d is not available in this build", d.family);
+    XK_REQUIRE(d.family == XK_FAMILY_LIFE || d.family == XK_FAMILY_EVOLIFE ||
+                   d.family == XK_FAMILY_MASS,
+               XK_ERR_UNSUPPORTED, "model family %d is not available in this build", d.family);
+    if (d.family == XK_FAMILY_MASS)
+        XK_REQUIRE(d.ndim == 3 && d.nbr == 6 && !d.torus && d.state_bytes == 4, XK_ERR_ARG,
+                   "mass transfer needs a 3-D von Neumann lattice of 32-bit cells with a wall");
     if (d.family == XK_FAMILY_LIFE)
         XK_REQUIRE(d.rule0 >> (d.nbr + 1) == 0 && d.rule1 >> (d.nbr + 1) == 0, XK_ERR_ARG,
                    "rule tables have bits above %d neighbours", d.nbr);
@@ -237,7 +249,13 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
     XK_TRY(cudaEventCreate(&m->ev1));
     {
         const int border_state = (int)(d.border_value & 1u);
-        if (d.family == XK_FAMILY_EVOLIFE) {
+        if (d.family == XK_FAMILY_MASS) {
+            m->layout = LAYOUT_MASS;
+            XK_TRY(cudaMalloc(&m->cells32[0], (size_t)n * 4));
+            XK_TRY(cudaMalloc(&m->cells32[1], (size_t)n * 4));
+            XK_TRY(cudaMemsetAsync(m->cells32[0], 0, (size_t)n * 4, m->stream));
+            XK_TRY(cudaMalloc(&m->proj, (size_t)d.size[0] * d.size[1] * 4));
+        } else if (d.family == XK_FAMILY_EVOLIFE) {
             m->layout = LAYOUT_CELLS64;
             XK_TRY(cudaMalloc(&m->cells64[0], (size_t)n * 8));
             XK_TRY(cudaMalloc(&m->cells64[1], (size_t)n * 8));
@@ -267,7 +285,7 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
             XK_TRY(cudaMalloc(&m->bytes[1], bytes));
             XK_TRY(cudaMemsetAsync(m->bytes[0], 0, bytes, m->stream));
         }
-        if (m->layout != LAYOUT_CELLS64)
+        if (m->layout != LAYOUT_CELLS64 && m->layout != LAYOUT_MASS)
             XK_TRY(cudaMalloc(&m->stage, (size_t)n * d.state_bytes + 16));
         XK_TRY(cudaMalloc(&m->col, (size_t)n * 3 * sizeof(int32_t)));
         XK_TRY(cudaMemsetAsync(m->col, 0, (size_t)n * 3 * sizeof(int32_t), m->stream));
@@ -297,10 +315,12 @@ extern "C" int xk_upload(xk_model *m, const void *host_main, int64_t ncells)
     XK_REQUIRE(ncells == m->n, XK_ERR_ARG, "xk_upload: %lld cells given, model has %lld",
                (long long)ncells, (long long)m->n);
     const int esz = m->d.state_bytes;
-    if (m->layout == LAYOUT_CELLS64) {
-        XK_CUDA(cudaMemcpyAsync(m->cells64[m->cur], host_main, (size_t)m->n * 8,
-                                cudaMemcpyHostToDevice, m->stream));
+    if (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_MASS) {
+        void *dst = m->layout == LAYOUT_MASS ? (void *)m->cells32[m->cur] : (void *)m->cells64[m->cur];
+        XK_CUDA(cudaMemcpyAsync(dst, host_main, (size_t)m->n * esz, cudaMemcpyHostToDevice,
+                                m->stream));
         XK_CUDA(cudaStreamSynchronize(m->stream));
+        m->proj_valid = 0;
         m->uploaded = 1;
         return XK_OK;
     }
@@ -329,9 +349,11 @@ extern "C" int xk_download(xk_model *m, void *host_main, int64_t ncells)
     XK_REQUIRE(ncells == m->n, XK_ERR_ARG, "xk_download: %lld cells given, model has %lld",
                (long long)ncells, (long long)m->n);
     const int esz = m->d.state_bytes;
-    if (m->layout == LAYOUT_CELLS64) {
-        XK_CUDA(cudaMemcpyAsync(host_main, m->cells64[m->cur], (size_t)m->n * 8,
-                                cudaMemcpyDeviceToHost, m->stream));
+    if (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_MASS) {
+        const void *src = m->layout == LAYOUT_MASS ? (const void *)m->cells32[m->cur]
+                                                   : (const void *)m->cells64[m->cur];
+        XK_CUDA(cudaMemcpyAsync(host_main, src, (size_t)m->n * esz, cudaMemcpyDeviceToHost,
+                                m->stream));
         XK_CUDA(cudaStreamSynchronize(m->stream));
         return XK_OK;
     }
@@ -348,6 +370,10 @@ extern "C" int xk_download(xk_model *m, void *host_main, int64_t ncells)
 // write the colours implied by the state into m->col
 static int materialize_colors(xk_model *m)
 {
+    if (m->layout == LAYOUT_MASS) {
+        XK_CUDA(xk_mass_colors(m->cells32[m->cur], m->col, m->n, m->stream));
+        return XK_OK;
+    }
     if (!m->derived) return XK_OK;
     const int smooth = m->d.color_kind == XK_COLOR_MOVING_AVERAGE ? m->d.smooth : 1;
     if (m->layout == LAYOUT_BITS2D)
@@ -432,6 +458,30 @@ extern "C" int xk_step(xk_model *m, int64_t nsteps)
     XK_REQUIRE(nsteps >= 0, XK_ERR_ARG, "xk_step: negative step count");
     XK_REQUIRE(m->uploaded, XK_ERR_STATE, "xk_step before xk_upload");
     if (nsteps == 0) return XK_OK;
+    if (m->layout == LAYOUT_MASS) {
+        if (nsteps > m->totals_cap) {
+            if (m->totals) cudaFree(m->totals);
+            m->totals = nullptr;
+            m->totals_cap = 0;
+            XK_CUDA(cudaMalloc(&m->totals, (size_t)nsteps * sizeof(unsigned long long)));
+            m->totals_cap = nsteps;
+        }
+        XK_CUDA(cudaMemsetAsync(m->totals, 0, (size_t)nsteps * sizeof(unsigned long long), m->stream));
+        XK_CUDA(cudaEventRecord(m->ev0, m->stream));
+        for (int64_t g = 0; g < nsteps; ++g) {
+            XK_CUDA(xk_mass_step(m->cells32[m->cur], m->cells32[1 - m->cur], m->proj, m->totals + g,
+                                 m->d, m->stream));
+            m->cur = 1 - m->cur;
+        }
+        XK_CUDA(cudaEventRecord(m->ev1, m->stream));
+        XK_CUDA(cudaEventSynchronize(m->ev1));
+        float ms = 0.f;
+        XK_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+        xk_set_last_step_ms(ms);
+        m->totals_count = nsteps;
+        m->proj_valid = 1;
+        return XK_OK;
+    }
     if (m->layout == LAYOUT_CELLS64) {
         XK_CUDA(cudaEventRecord(m->ev0, m->stream));
         for (int64_t g = 0; g < nsteps; ++g) {
@@ -509,6 +559,18 @@ extern "C" int xk_render(xk_model *m, int32_t *host_img, int32_t width, int32_t 
         XK_CUDA(cudaMalloc(&m->img, (size_t)npx * 3 * sizeof(int32_t)));
         m->img_cap = npx * 3;
     }
+    if (m->layout == LAYOUT_MASS && m->d.proj_axis0 == 0 && m->d.proj_axis1 == 1 &&
+        m->d.render_smooth == 0) {
+        if (!m->proj_valid) {
+            XK_CUDA(xk_mass_project(m->cells32[m->cur], m->proj, m->d, m->stream));
+            m->proj_valid = 1;
+        }
+        XK_CUDA(xk_mass_render(m->proj, m->img, m->d, width, height, zoom, dx, dy, m->stream));
+        XK_CUDA(cudaMemcpyAsync(host_img, m->img, (size_t)npx * 3 * sizeof(int32_t),
+                                cudaMemcpyDeviceToHost, m->stream));
+        XK_CUDA(cudaStreamSynchronize(m->stream));
+        return XK_OK;
+    }
     int rc = materialize_colors(m);
     if (rc != XK_OK) return rc;
     RenderGeo g;
@@ -529,8 +591,14 @@ extern "C" int xk_mass_totals(xk_model *m, uint64_t *host_totals, int64_t count)
 {
     XK_REQUIRE(m && host_totals, XK_ERR_ARG, "xk_mass_totals: null argument");
     XK_REQUIRE(m->d.family == XK_FAMILY_MASS, XK_ERR_STATE, "not a mass-transfer model");
-    (void)count;
-    return XK_ERR_UNSUPPORTED;
+    XK_REQUIRE(count == m->totals_count, XK_ERR_ARG,
+               "xk_mass_totals: %lld totals asked, the last step recorded %lld", (long long)count,
+               (long long)m->totals_count);
+    if (count == 0) return XK_OK;
+    XK_CUDA(cudaMemcpyAsync(host_totals, m->totals, (size_t)count * sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, m->stream));
+    XK_CUDA(cudaStreamSynchronize(m->stream));
+    return XK_OK;
 }
 
 extern "C" int xk_sync(xk_model *m)
