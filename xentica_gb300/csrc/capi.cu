@@ -469,8 +469,8 @@ extern "C" int xk_step(xk_model *m, int64_t nsteps)
         XK_CUDA(cudaMemsetAsync(m->totals, 0, (size_t)nsteps * sizeof(unsigned long long), m->stream));
         XK_CUDA(cudaEventRecord(m->ev0, m->stream));
         for (int64_t g = 0; g < nsteps; ++g) {
-            XK_CUDA(xk_mass_step(m->cells32[m->cur], m->cells32[1 - m->cur], m->proj, m->totals + g,
-                                 m->d, m->stream));
+            XK_CUDA(xk_mass_step(m->cells32[m->cur], m->cells32[1 - m->cur], m->totals + g, m->d,
+                                 m->stream));
             m->cur = 1 - m->cur;
         }
         XK_CUDA(cudaEventRecord(m->ev1, m->stream));
@@ -479,7 +479,7 @@ extern "C" int xk_step(xk_model *m, int64_t nsteps)
         XK_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
         xk_set_last_step_ms(ms);
         m->totals_count = nsteps;
-        m->proj_valid = 1;
+        m->proj_valid = 0;
         return XK_OK;
     }
     if (m->layout == LAYOUT_CELLS64) {

@@ -11,14 +11,24 @@
 //   m'         = m - sum_k sent_k + sum_k incoming_k
 // Colour (plain ColorEffect): min(m' * 32, 255) on every channel.
 //
-// One thread per (x, y) column walks z with a three-deep register queue; the
-// x/y neighbours of plane z come from a shared tile with a one-cell halo.  The
-// same pass writes the column's colour sum (RendererPlain's projection over
-// z, exact in float because it is a sum of integers below 2^24) and adds the
-// column's mass to the generation's total (the conserved quantity).
+// Work split: a CTA owns a 32*V-wide, 8-row tile of a run of zc planes; a
+// thread owns V consecutive cells of one row (one 128-bit load and store per
+// plane when V = 4) and walks its z run with a three-plane register queue.
+// x neighbours come from the neighbouring lanes (shuffles; lanes 0 and 31
+// load the one cell beyond the warp), y neighbours are 128-bit loads of the
+// rows above and below (the neighbouring warps' own rows, so mostly L1
+// hits), z neighbours are the queue.  No shared-memory tile and no barrier
+// inside the loop.  Each cell carries (m, m / 7); an off-board cell reads as
+// (WALL, 0), which makes the sent and incoming sums need no bounds test:
+//   m' = m - (m / 7) * #{k : m_k != WALL} + (m != WALL) * sum_k q_k
+// (q_k = m_k / 7 < WALL, so the reference's "incoming != WALL" test always
+// holds).  Each CTA adds its cells' new mass to the generation's total with
+// one 64-bit atomic.  Colours and the RendererPlain projection are derived
+// from the state when they are read, not every generation.
+#include <cstdlib>
+
 #include "xk_internal.cuh"
 
-#define XK_MASS_BX 32
 #define XK_MASS_BY 8
 
 struct MassParams {
@@ -32,69 +42,266 @@ __device__ __forceinline__ uint32_t xk_mass_color(uint32_t m)
     return v < 255u ? v : 255u;
 }
 
-__global__ void __launch_bounds__(XK_MASS_BX * XK_MASS_BY)
-xk_k_mass(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, uint32_t *__restrict__ proj,
-          unsigned long long *__restrict__ total, MassParams p)
+template <int V>
+struct MassRow {
+    uint32_t m[V];
+    uint32_t q[V];
+};
+
+// V cells from element index idx of src when ok, else V off-board cells
+template <int V>
+__device__ __forceinline__ void xk_mass_load(const uint32_t *__restrict__ src, int64_t idx, bool ok,
+                                             uint32_t wall, MassRow<V> &r)
 {
-    __shared__ uint32_t tile[XK_MASS_BY + 2][XK_MASS_BX + 2];
-    __shared__ unsigned long long warp_sums[XK_MASS_BX * XK_MASS_BY / 32];
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int x = blockIdx.x * XK_MASS_BX + tx, y = blockIdx.y * XK_MASS_BY + ty;
-    const bool in = x < p.W && y < p.H;
-    const int64_t plane = (int64_t)p.W * p.H;
-    const int64_t col = (int64_t)y * p.W + x;
-    // in-board flags of the x/y neighbours (z neighbours are checked per plane)
-    const bool has_xp = x + 1 < p.W, has_xm = x > 0, has_yp = y + 1 < p.H, has_ym = y > 0;
-    uint32_t m_prev = p.wall;
-    uint32_t m_cur = in ? src[col] : p.wall;
-    uint32_t proj_sum = 0;
-    unsigned long long mass_sum = 0;
-    for (int z = 0; z < p.D; ++z) {
-        const uint32_t m_next = (in && z + 1 < p.D) ? src[(int64_t)(z + 1) * plane + col] : p.wall;
-        tile[ty + 1][tx + 1] = m_cur;
-        const int64_t zb = (int64_t)z * plane;
-        if (tx == 0)
-            tile[ty + 1][0] = (y < p.H && x > 0 && x - 1 < p.W) ? src[zb + col - 1] : p.wall;
-        if (tx == XK_MASS_BX - 1)
-            tile[ty + 1][XK_MASS_BX + 1] = (y < p.H && x + 1 < p.W) ? src[zb + col + 1] : p.wall;
-        if (ty == 0)
-            tile[0][tx + 1] = (x < p.W && y > 0 && y - 1 < p.H) ? src[zb + col - p.W] : p.wall;
-        if (ty == XK_MASS_BY - 1)
-            tile[XK_MASS_BY + 1][tx + 1] = (x < p.W && y + 1 < p.H) ? src[zb + col + p.W] : p.wall;
-        __syncthreads();
-        if (in) {
-            const uint32_t m = m_cur;
-            // von Neumann order: +x, -x, +y, -y, +z, -z
-            const uint32_t mk[6] = {tile[ty + 1][tx + 2], tile[ty + 1][tx], tile[ty + 2][tx + 1],
-                                    tile[ty][tx + 1], m_next, m_prev};
-            const bool on[6] = {has_xp, has_xm, has_yp, has_ym, z + 1 < p.D, z > 0};
-            const uint32_t share = m / 7u;
-            const uint32_t keep = (uint32_t)(m != p.wall);
-            uint32_t v = m;
+    if (V == 4) {
+        uint4 u = make_uint4(wall, wall, wall, wall);
+        if (ok) u = __ldg(reinterpret_cast<const uint4 *>(src + idx));
+        r.m[0] = u.x;
+        r.m[1] = u.y;
+        r.m[2] = u.z;
+        r.m[3] = u.w;
+    } else {
 #pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                const uint32_t mkk = on[k] ? mk[k] : p.wall;
-                v -= share * (uint32_t)(mkk != p.wall);
-                const uint32_t nb = (mkk / 7u) * keep;
-                v += on[k] ? nb * (uint32_t)(nb != p.wall) : 0u;
-            }
-            dst[zb + col] = v;
-            proj_sum += xk_mass_color(v);
-            mass_sum += v;
-        }
-        __syncthreads();
-        m_prev = m_cur;
-        m_cur = m_next;
+        for (int i = 0; i < V; ++i) r.m[i] = ok ? __ldg(src + idx + i) : wall;
     }
-    if (in && proj) proj[col] = proj_sum;
-    // block total -> one atomic per CTA
+#pragma unroll
+    for (int i = 0; i < V; ++i) r.q[i] = ok ? r.m[i] / 7u : 0u;
+}
+
+template <int V>
+__global__ void __launch_bounds__(32 * XK_MASS_BY)
+xk_k_mass(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
+          unsigned long long *__restrict__ total, MassParams p, int zc)
+{
+    __shared__ unsigned long long warp_sums[XK_MASS_BY];
+    const int lane = threadIdx.x;
+    const int x0 = (blockIdx.x * 32 + lane) * V;
+    const int y = blockIdx.y * XK_MASS_BY + threadIdx.y;
+    const int z0 = blockIdx.z * zc;
+    const int z1 = min(z0 + zc, p.D);
+    const bool in = x0 < p.W && y < p.H;
+    const int64_t plane = (int64_t)p.W * p.H;
+    const int64_t col = in ? (int64_t)y * p.W + x0 : 0;
+    const bool has_ym = in && y > 0, has_yp = in && y + 1 < p.H;
+    const bool has_xl = in && x0 > 0, has_xr = in && x0 + V < p.W;
+    const uint32_t wall = p.wall;
+    MassRow<V> prv, cur, nxt, ym, yp;
+    xk_mass_load<V>(src, (int64_t)(z0 - 1) * plane + col, in && z0 > 0, wall, prv);
+    xk_mass_load<V>(src, (int64_t)z0 * plane + col, in && z0 < p.D, wall, cur);
+    unsigned long long mass_sum = 0;
+    for (int z = z0; z < z1; ++z) {
+        const int64_t zb = (int64_t)z * plane;
+        xk_mass_load<V>(src, zb + plane + col, in && z + 1 < p.D, wall, nxt);
+        xk_mass_load<V>(src, zb + col - p.W, has_ym, wall, ym);
+        xk_mass_load<V>(src, zb + col + p.W, has_yp, wall, yp);
+        uint32_t lm = __shfl_up_sync(0xFFFFFFFFu, cur.m[V - 1], 1);
+        uint32_t lq = __shfl_up_sync(0xFFFFFFFFu, cur.q[V - 1], 1);
+        uint32_t rm = __shfl_down_sync(0xFFFFFFFFu, cur.m[0], 1);
+        uint32_t rq = __shfl_down_sync(0xFFFFFFFFu, cur.q[0], 1);
+        if (lane == 0) {
+            lm = has_xl ? __ldg(src + zb + col - 1) : wall;
+            lq = has_xl ? lm / 7u : 0u;
+        }
+        if (lane == 31) {
+            rm = has_xr ? __ldg(src + zb + col + V) : wall;
+            rq = has_xr ? rm / 7u : 0u;
+        }
+        uint32_t out[V];
+#pragma unroll
+        for (int i = 0; i < V; ++i) {
+            const uint32_t m = cur.m[i];
+            // von Neumann: +x, -x, +y, -y, +z, -z (order does not change the sums)
+            const uint32_t mx_p = i + 1 < V ? cur.m[i + 1 < V ? i + 1 : 0] : rm;
+            const uint32_t qx_p = i + 1 < V ? cur.q[i + 1 < V ? i + 1 : 0] : rq;
+            const uint32_t mx_m = i > 0 ? cur.m[i > 0 ? i - 1 : 0] : lm;
+            const uint32_t qx_m = i > 0 ? cur.q[i > 0 ? i - 1 : 0] : lq;
+            const uint32_t cnt = (uint32_t)(mx_p != wall) + (uint32_t)(mx_m != wall) +
+                                 (uint32_t)(yp.m[i] != wall) + (uint32_t)(ym.m[i] != wall) +
+                                 (uint32_t)(nxt.m[i] != wall) + (uint32_t)(prv.m[i] != wall);
+            const uint32_t sq = qx_p + qx_m + yp.q[i] + ym.q[i] + nxt.q[i] + prv.q[i];
+            out[i] = m - cur.q[i] * cnt + (m != wall ? sq : 0u);
+            mass_sum += out[i];
+        }
+        if (in) {
+            if (V == 4)
+                *reinterpret_cast<uint4 *>(dst + zb + col) = make_uint4(out[0], out[V > 1 ? 1 : 0],
+                                                                        out[V > 2 ? 2 : 0],
+                                                                        out[V > 3 ? 3 : 0]);
+            else
+#pragma unroll
+                for (int i = 0; i < V; ++i) dst[zb + col + i] = out[i];
+        }
+        prv = cur;
+        cur = nxt;
+    }
+    if (!in) mass_sum = 0;
     for (int off = 16; off > 0; off >>= 1) mass_sum += __shfl_down_sync(0xFFFFFFFFu, mass_sum, off);
-    const int tid = ty * XK_MASS_BX + tx;
-    if ((tid & 31) == 0) warp_sums[tid >> 5] = mass_sum;
+    if (lane == 0) warp_sums[threadIdx.y] = mass_sum;
     __syncthreads();
-    if (tid == 0) {
+    if (threadIdx.y == 0 && lane == 0) {
         unsigned long long s = 0;
-        for (int w = 0; w < XK_MASS_BX * XK_MASS_BY / 32; ++w) s += warp_sums[w];
+        for (int w = 0; w < XK_MASS_BY; ++w) s += warp_sums[w];
+        atomicAdd(total, s);
+    }
+}
+
+// Tiled form for W % 4 == 0 (the usual case): the (m, m / 7) pairs of the
+// CTA's eight rows of plane z go through a double-buffered shared tile, so
+// every m / 7 is computed once, by the thread that loaded the cell; rows
+// y - 1 and y + 8 (the tile's halo) are loaded by warps 0 and 7 and the x
+// halo cells by lanes 0 and 31.  A thread's own column is a four-deep
+// register queue (planes z - 1 .. z + 2, the last one in flight).  Every
+// loaded cell is tested for the wall value once; while no CTA thread has met
+// one (a sticky flag OR-ed at the one barrier per plane) every on-board
+// neighbour counts in the "sent" sum, so
+//   m' = m - (m / 7) * (#on-board neighbours) + sum_k q_k,
+// else the exact per-neighbour form of the generic kernel is used.
+#define XK_MT_ROW 128
+
+struct MassTile {
+    uint32_t m[2][XK_MASS_BY + 2][XK_MT_ROW];
+    uint32_t q[2][XK_MASS_BY + 2][XK_MT_ROW];
+};
+
+__device__ __forceinline__ uint4 xk_mass_ld4(const uint32_t *__restrict__ src, int64_t idx, bool ok,
+                                              uint32_t wall)
+{
+    uint4 u = make_uint4(wall, wall, wall, wall);
+    if (ok) u = __ldg(reinterpret_cast<const uint4 *>(src + idx));
+    return u;
+}
+
+// q of four loaded cells (0 when off-board); marks a loaded wall value
+__device__ __forceinline__ uint4 xk_mass_q4(const uint4 m, bool ok, uint32_t wall, bool &seen)
+{
+    seen |= ok && (m.x == wall || m.y == wall || m.z == wall || m.w == wall);
+    return ok ? make_uint4(m.x / 7u, m.y / 7u, m.z / 7u, m.w / 7u) : make_uint4(0u, 0u, 0u, 0u);
+}
+
+__device__ __forceinline__ uint32_t xk_get(const uint4 &u, int i)
+{
+    return i == 0 ? u.x : i == 1 ? u.y : i == 2 ? u.z : u.w;
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(32 * XK_MASS_BY, MINB)
+xk_k_mass_tiled(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
+                unsigned long long *__restrict__ total, MassParams p, int zc)
+{
+    __shared__ __align__(16) MassTile t;
+    __shared__ unsigned long long warp_sums[XK_MASS_BY];
+    const int lane = threadIdx.x, ty = threadIdx.y;
+    const int x0 = (blockIdx.x * 32 + lane) * 4;
+    const int y = blockIdx.y * XK_MASS_BY + ty;
+    const int z0 = blockIdx.z * zc;
+    const int z1 = min(z0 + zc, p.D);
+    const bool in = x0 < p.W && y < p.H;
+    const int64_t plane = (int64_t)p.W * p.H;
+    const int64_t col = in ? (int64_t)y * p.W + x0 : 0;
+    const uint32_t wall = p.wall;
+    // x halo: lane 0 owns the cell left of the warp's row, lane 31 the one right of it
+    const bool hx_ok = in && ((lane == 0 && x0 > 0) || (lane == 31 && x0 + 4 < p.W));
+    const int64_t hx_col = lane == 0 ? col - 1 : col + 4;
+    // y halo rows: warp 0 loads row y - 1, warp 7 row y + 1 (of the tile's edge rows)
+    const bool hy_warp = ty == 0 || ty == XK_MASS_BY - 1;
+    const bool hy_ok = in && ((ty == 0 && y > 0) || (ty == XK_MASS_BY - 1 && y + 1 < p.H));
+    const int64_t hy_col = ty == 0 ? col - p.W : col + p.W;
+    const int hy_row = ty == 0 ? 0 : XK_MASS_BY + 1;
+    // on-board x/y neighbours of each of the four cells
+    int cxy[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        cxy[i] = (x0 + i > 0) + (x0 + i + 1 < p.W) + (y > 0) + (y + 1 < p.H);
+
+    bool seen = false;
+    uint4 prv_m = xk_mass_ld4(src, (int64_t)(z0 - 1) * plane + col, in && z0 > 0, wall);
+    uint4 prv_q = xk_mass_q4(prv_m, in && z0 > 0, wall, seen);
+    uint4 cur_m = xk_mass_ld4(src, (int64_t)z0 * plane + col, in, wall);
+    uint4 cur_q = xk_mass_q4(cur_m, in, wall, seen);
+    uint4 nxt_m = xk_mass_ld4(src, (int64_t)(z0 + 1) * plane + col, in && z0 + 1 < p.D, wall);
+    uint32_t hx_m = hx_ok ? __ldg(src + (int64_t)z0 * plane + hx_col) : wall;
+    uint4 hy_m = hy_warp ? xk_mass_ld4(src, (int64_t)z0 * plane + hy_col, hy_ok, wall)
+                         : make_uint4(wall, wall, wall, wall);
+    unsigned long long mass_sum = 0;
+    for (int z = z0; z < z1; ++z) {
+        const int b = z & 1;
+        const int64_t zb = (int64_t)z * plane;
+        // in flight for later planes: own column z + 2, halos of z + 1
+        const uint4 nn_m = xk_mass_ld4(src, zb + 2 * plane + col, in && z + 2 < p.D, wall);
+        const uint4 nxt_q = xk_mass_q4(nxt_m, in && z + 1 < p.D, wall, seen);
+        const uint32_t hx_q = hx_ok ? hx_m / 7u : 0u;
+        seen |= hx_ok && hx_m == wall;
+        *reinterpret_cast<uint4 *>(&t.m[b][ty + 1][lane * 4]) = cur_m;
+        *reinterpret_cast<uint4 *>(&t.q[b][ty + 1][lane * 4]) = cur_q;
+        if (hy_warp) {
+            const uint4 hy_q = xk_mass_q4(hy_m, hy_ok, wall, seen);
+            *reinterpret_cast<uint4 *>(&t.m[b][hy_row][lane * 4]) = hy_m;
+            *reinterpret_cast<uint4 *>(&t.q[b][hy_row][lane * 4]) = hy_q;
+        }
+        const bool more = z + 1 < z1;
+        const uint32_t hx_next = hx_ok && more ? __ldg(src + zb + plane + hx_col) : wall;
+        const uint4 hy_next = hy_warp ? xk_mass_ld4(src, zb + plane + hy_col, hy_ok && more, wall)
+                                      : make_uint4(wall, wall, wall, wall);
+        const bool walls = __syncthreads_or(seen);
+        const uint4 ym_q = *reinterpret_cast<const uint4 *>(&t.q[b][ty][lane * 4]);
+        const uint4 yp_q = *reinterpret_cast<const uint4 *>(&t.q[b][ty + 2][lane * 4]);
+        uint32_t xl_q = __shfl_up_sync(0xFFFFFFFFu, cur_q.w, 1);
+        uint32_t xr_q = __shfl_down_sync(0xFFFFFFFFu, cur_q.x, 1);
+        if (lane == 0) xl_q = hx_q;
+        if (lane == 31) xr_q = hx_q;
+        uint32_t out[4];
+        if (!walls) {
+            const int cz = (z > 0) + (z + 1 < p.D);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const uint32_t ql = i == 0 ? xl_q : xk_get(cur_q, i > 0 ? i - 1 : 0);
+                const uint32_t qr = i == 3 ? xr_q : xk_get(cur_q, i < 3 ? i + 1 : 3);
+                const uint32_t sq = ql + qr + xk_get(ym_q, i) + xk_get(yp_q, i) +
+                                    xk_get(prv_q, i) + xk_get(nxt_q, i);
+                out[i] = xk_get(cur_m, i) - xk_get(cur_q, i) * (uint32_t)(cxy[i] + cz) + sq;
+            }
+        } else {
+            const uint4 ym_m = *reinterpret_cast<const uint4 *>(&t.m[b][ty][lane * 4]);
+            const uint4 yp_m = *reinterpret_cast<const uint4 *>(&t.m[b][ty + 2][lane * 4]);
+            uint32_t xl_m = __shfl_up_sync(0xFFFFFFFFu, cur_m.w, 1);
+            uint32_t xr_m = __shfl_down_sync(0xFFFFFFFFu, cur_m.x, 1);
+            if (lane == 0) xl_m = hx_ok ? hx_m : wall;
+            if (lane == 31) xr_m = hx_ok ? hx_m : wall;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const uint32_t ml = i == 0 ? xl_m : xk_get(cur_m, i > 0 ? i - 1 : 0);
+                const uint32_t mr = i == 3 ? xr_m : xk_get(cur_m, i < 3 ? i + 1 : 3);
+                const uint32_t ql = i == 0 ? xl_q : xk_get(cur_q, i > 0 ? i - 1 : 0);
+                const uint32_t qr = i == 3 ? xr_q : xk_get(cur_q, i < 3 ? i + 1 : 3);
+                const uint32_t mpz = z + 1 < p.D ? xk_get(nxt_m, i) : wall;
+                const uint32_t cnt = (uint32_t)(ml != wall) + (uint32_t)(mr != wall) +
+                                     (uint32_t)(xk_get(ym_m, i) != wall) +
+                                     (uint32_t)(xk_get(yp_m, i) != wall) +
+                                     (uint32_t)(xk_get(prv_m, i) != wall) + (uint32_t)(mpz != wall);
+                const uint32_t sq = ql + qr + xk_get(ym_q, i) + xk_get(yp_q, i) +
+                                    xk_get(prv_q, i) + xk_get(nxt_q, i);
+                const uint32_t m = xk_get(cur_m, i);
+                out[i] = m - xk_get(cur_q, i) * cnt + (m != wall ? sq : 0u);
+            }
+        }
+        if (in) {
+            *reinterpret_cast<uint4 *>(dst + zb + col) = make_uint4(out[0], out[1], out[2], out[3]);
+            mass_sum += (unsigned long long)out[0] + out[1] + (unsigned long long)out[2] + out[3];
+        }
+        prv_m = cur_m;
+        prv_q = cur_q;
+        cur_m = nxt_m;
+        cur_q = nxt_q;
+        nxt_m = nn_m;
+        hx_m = hx_next;
+        hy_m = hy_next;
+    }
+    for (int off = 16; off > 0; off >>= 1) mass_sum += __shfl_down_sync(0xFFFFFFFFu, mass_sum, off);
+    if (lane == 0) warp_sums[ty] = mass_sum;
+    __syncthreads();
+    if (ty == 0 && lane == 0) {
+        unsigned long long s = 0;
+        for (int w = 0; w < XK_MASS_BY; ++w) s += warp_sums[w];
         atomicAdd(total, s);
     }
 }
@@ -152,13 +359,38 @@ static MassParams mass_params(const xk_desc &d)
     return p;
 }
 
-cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, uint32_t *proj,
-                         unsigned long long *total, const xk_desc &d, cudaStream_t s)
+// planes per CTA: enough CTAs for about 2048 per generation
+static int mass_zchunk(const MassParams &p, int gx, int gy)
+{
+    if (const char *e = getenv("XK_MASS_ZC")) {
+        const int v = atoi(e);
+        if (v > 0) return v;
+    }
+    const int64_t tiles = (int64_t)gx * gy;
+    int64_t chunks = (2048 + tiles - 1) / tiles;
+    if (chunks > p.D) chunks = p.D;
+    if (chunks < 1) chunks = 1;
+    return (int)((p.D + chunks - 1) / chunks);
+}
+
+cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long *total,
+                         const xk_desc &d, cudaStream_t s)
 {
     const MassParams p = mass_params(d);
-    dim3 block(XK_MASS_BX, XK_MASS_BY);
-    dim3 grid((p.W + XK_MASS_BX - 1) / XK_MASS_BX, (p.H + XK_MASS_BY - 1) / XK_MASS_BY);
-    xk_k_mass<<<grid, block, 0, s>>>(src, dst, proj, total, p);
+    const bool vec = p.W % 4 == 0;
+    const int cells_x = 32 * (vec ? 4 : 1);
+    const int gx = (p.W + cells_x - 1) / cells_x, gy = (p.H + XK_MASS_BY - 1) / XK_MASS_BY;
+    const int zc = mass_zchunk(p, gx, gy);
+    dim3 block(32, XK_MASS_BY);
+    dim3 grid(gx, gy, (p.D + zc - 1) / zc);
+    // four CTAs per SM (64 registers) measured faster than three; XK_MASS_MINB=1 lifts the cap
+    static const int minb = getenv("XK_MASS_MINB") ? atoi(getenv("XK_MASS_MINB")) : 4;
+    if (vec && minb >= 4)
+        xk_k_mass_tiled<4><<<grid, block, 0, s>>>(src, dst, total, p, zc);
+    else if (vec)
+        xk_k_mass_tiled<1><<<grid, block, 0, s>>>(src, dst, total, p, zc);
+    else
+        xk_k_mass<1><<<grid, block, 0, s>>>(src, dst, total, p, zc);
     return cudaGetLastError();
 }
 

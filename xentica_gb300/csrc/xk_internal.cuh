@@ -118,8 +118,8 @@ cudaError_t xk_evolife_step(const uint64_t *src, uint64_t *dst, int32_t *col, co
                             float mut_thresh, cudaStream_t s);
 
 // mass-transfer family (mass.cu)
-cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, uint32_t *proj,
-                         unsigned long long *total, const xk_desc &d, cudaStream_t s);
+cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long *total,
+                         const xk_desc &d, cudaStream_t s);
 cudaError_t xk_mass_project(const uint32_t *src, uint32_t *proj, const xk_desc &d, cudaStream_t s);
 cudaError_t xk_mass_colors(const uint32_t *src, int32_t *col, int64_t n, cudaStream_t s);
 cudaError_t xk_mass_render(const uint32_t *proj, int32_t *img, const xk_desc &d, int width,
