@@ -50,10 +50,17 @@ def parse():
     ap.add_argument("--seed", type=int, default=2041)
     ap.add_argument("--plain-generations", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--workload", choices=("ensemble", "evolife", "mass"), default="ensemble",
+    ap.add_argument("--requests", type=int, default=256, help="serve: requests in the run")
+    ap.add_argument("--load", type=float, default=0.7,
+                    help="serve: offered load as a fraction of the measured capacity")
+    ap.add_argument("--quantum", type=int, default=128, help="serve: generations per round")
+    ap.add_argument("--serve-budget-gb", type=int, default=16, help="serve: HBM budget (GiB)")
+    ap.add_argument("--workload", choices=("ensemble", "evolife", "mass", "serve"),
+                    default="ensemble",
                     help="ensemble: the batched Life-like ensemble (default); evolife: EvoLife "
                          "1920x1080 with a render every generation; mass: 3-D sand transfer "
-                         "256^3 with the total checked every generation")
+                         "256^3 with the total checked every generation; serve: Poisson "
+                         "arrivals of 2-D/3-D requests through the serving loop")
     return ap.parse_args()
 
 
@@ -504,6 +511,97 @@ def run_mass(args, dist):
         print(json.dumps(line), flush=True)
 
 
+def run_serve(args, dist):
+    """Serving: ``--requests`` seeded requests (half 2-D Life-like, a quarter
+    3-D von Neumann Life-like, a quarter mass transfer) arrive as a Poisson
+    process whose rate offers ``--load`` of the capacity measured first with a
+    closed batch of the first 48 requests; latency is completion minus
+    submission, including admission waits."""
+    import threading
+    from xentica_gb300 import build as xk_build
+    from xentica_gb300 import _native as nat
+    from xentica_gb300 import serve
+    xk_build.build()
+    nat.set_device(dist.local)
+    specs = serve.serving_workload(args.requests, seed=args.seed + dist.rank)
+    ctx = multiprocessing.get_context("spawn")
+    with ctx.Pool(min(16, os.cpu_count())) as pool:
+        cells = pool.map(serve.make_cells, specs, chunksize=2)
+    work = [int(np.prod(sp["shape"])) * sp["generations"] for sp in specs]
+    srv = serve.Server(args.serve_budget_gb << 30, host_bytes=8 << 30, max_active=1024,
+                       quantum=args.quantum)
+
+    def run_batch(idx):
+        hs = [srv.submit(specs[i]["kind"], cells[i], specs[i]["rule"], specs[i]["generations"])
+              for i in idx]
+        for h in hs:
+            h.result(timeout=600)
+
+    small = [i for i in range(len(specs)) if work[i] < 5e8][:max(1, args.warmup * 4)]
+    run_batch(small)                                   # warm-up: kernels loaded, pools grown
+    probe = list(range(min(48, len(specs))))
+    t0 = time.perf_counter()
+    run_batch(probe)
+    capacity = sum(work[i] for i in probe) / (time.perf_counter() - t0)
+    rate = args.load * capacity / (sum(work) / len(work))
+    arrivals = serve.poisson_arrivals(rate, len(specs), seed=args.seed + 17)
+    handles = [None] * len(specs)
+    launches0 = srv.stats()["launches"]
+    clocks = Clocks(dist.local)
+    time.sleep(0.6)
+    dist.barrier()
+    start = time.perf_counter()
+
+    def submitter():
+        for i in range(len(specs)):
+            delay = start + arrivals[i] - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            handles[i] = srv.submit(specs[i]["kind"], cells[i], specs[i]["rule"],
+                                    specs[i]["generations"])
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    infos = []
+    for i in range(len(specs)):
+        while handles[i] is None:
+            time.sleep(0.0005)
+        handles[i].result(timeout=1800)
+        infos.append(handles[i].info())
+    th.join()
+    dist.barrier()
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    first = min(inf["submit_s"] for inf in infos)
+    last = max(inf["done_s"] for inf in infos)
+    span = dist.max(last - first)
+    value = sum(work) * dist.world / span
+    lat = serve.latency_summary([inf["done_s"] - inf["submit_s"] for inf in infos])
+    wait = serve.latency_summary([inf["admit_s"] - inf["submit_s"] for inf in infos])
+    h2d = sum(c.nbytes for c in cells)
+    kinds = {k: sum(1 for sp in specs if sp["kind"] == k) for k in ("life2d", "life3d", "mass")}
+    line = {"metric": "cell-updates/s (serving, Poisson arrivals)", "value": value,
+            "unit": "cell-updates/s", "n_gpus": dist.world, "steps": len(specs),
+            "warmup": len(small), "ms_per_step": span * 1000 / len(specs),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u32",
+            "data": "synthetic (seeded request mix)",
+            "config": {"workload": "serving: %d requests %s, 2-D sides log-uniform [32, 4096], "
+                                   "3-D sides log-uniform [64, 256], generations uniform "
+                                   "[100, 10000], Poisson arrivals" % (len(specs), kinds),
+                       "quantum": args.quantum, "budget_gib": args.serve_budget_gb,
+                       "l2": "state per request up to 67 MB; no flush"},
+            "rate_per_s": rate, "offered_load": args.load, "capacity_probe": capacity,
+            "latency_s": lat, "admission_wait_s": wait,
+            "device_bytes_peak": st["device_bytes_peak"],
+            "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d / len(specs),
+                    "d2h_bytes_per_step": h2d / len(specs),
+                    "note": "requests enter and leave through host memory"},
+            "gpu_launches": st["launches"] - launches0, "roofline": None, "clocks": clk}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -514,6 +612,8 @@ def main():
             run_evolife(args, dist)
         elif args.workload == "mass":
             run_mass(args, dist)
+        elif args.workload == "serve":
+            run_serve(args, dist)
         else:
             run_ours(args, dist)
     finally:

@@ -171,6 +171,90 @@ int xk_batch_step_noalloc(uint8_t *d_cells, int32_t count, const int32_t *width,
                           const int32_t *height, const uint32_t *rule, int32_t generations,
                           void *stream);
 
+/* ---- Serving: continuous batching of independent simulation requests ------
+ * No reference counterpart: the reference runs one model per Python object
+ * (xentica/core/base.py:591-728, stepped by the caller) and has no request
+ * loop.  A server owns a device arena of `budget_bytes` and a pinned host
+ * arena of `host_bytes` (each one allocation at creation), a worker thread and
+ * its CUDA streams.  Requests are admitted first come, first served, when their
+ * device bytes and result bytes fit and fewer than `max_active` run; each
+ * active request advances in rounds of at most `quantum` generations, a new
+ * round starting as soon as its previous one finished, so requests admitted
+ * while others run share the GPU with them.  2-D lattices that fit one CTA
+ * run together, one resident-kernel launch per shape class per round; larger
+ * and 3-D lattices run on their own streams.  Results wait in the pinned arena
+ * until xk_serve_result collects them.  A request computes exactly what it
+ * computes alone. */
+enum { XK_SERVE_LIFE2D = 1, XK_SERVE_LIFE3D_VN = 2, XK_SERVE_MASS3D = 3 };
+enum {
+    XK_REQ_PENDING = 0,      /* queued, waiting for memory or a slot          */
+    XK_REQ_ACTIVE = 1,       /* on the device                                 */
+    XK_REQ_DONE = 2,         /* result ready for xk_serve_result              */
+    XK_REQ_CANCELLED = 3,
+    XK_REQ_FAILED = 4
+};
+
+typedef struct xk_request {
+    int32_t kind;            /* XK_SERVE_*                                            */
+    int32_t reserved0;       /* 0                                                     */
+    int64_t size[3];         /* cells per axis, axis 0 fastest; size[2] = 1 for 2-D   */
+    uint32_t rule;           /* LIFE2D: B bits 0-8, S bits 9-17 (golly int, Moore,
+                                torus, LifelikeCA semantics); LIFE3D_VN: B bits 0-6,
+                                S bits 7-13 (6 von Neumann neighbours, torus);
+                                next = B(k) | S(k) & state.  MASS3D: unused (0)      */
+    int32_t reserved1;       /* 0                                                     */
+    int64_t generations;     /* >= 0                                                  */
+} xk_request;
+/* Cells are one byte (0/1) for the Life kinds and uint32 mass for MASS3D
+ * (the mass-transfer model: StaticBorder wall 2**32-1), axis 0 fastest. */
+
+typedef struct xk_request_info {
+    int32_t status;          /* XK_REQ_*                                               */
+    int32_t reserved;
+    int64_t generations_done;
+    double submit_s, admit_s, done_s;   /* seconds since server start; -1 not yet   */
+    uint64_t mass_total;     /* MASS3D: total mass after the last generation          */
+} xk_request_info;
+
+typedef struct xk_serve_stats {
+    int64_t submitted, admitted, completed, cancelled, rejected, failed;
+    int64_t pending, active;
+    int64_t device_bytes_in_use, device_bytes_peak, budget_bytes;
+    int64_t cell_updates;    /* cells x generations of completed requests             */
+    int64_t rounds, launches;/* worker rounds that launched work; kernel launches     */
+    double elapsed_s;
+} xk_serve_stats;
+
+typedef struct xk_server xk_server;
+
+int xk_serve_create(int64_t budget_bytes, int64_t host_bytes, int32_t max_active,
+                    int32_t quantum, xk_server **out);
+/* Cancels pending and active requests, waits for in-flight work, frees all. */
+int xk_serve_destroy(xk_server *srv);
+/* Device bytes a request is admitted with (validates it; host only). */
+int xk_serve_request_bytes(const xk_request *req, int64_t *bytes);
+/* Copies the cells; returns the request id.  Malformed requests and requests
+ * larger than the whole budget are rejected (XK_ERR_ARG / XK_ERR_OOM). */
+int xk_serve_submit(xk_server *srv, const xk_request *req, const void *host_cells, int64_t *id);
+int xk_serve_info(xk_server *srv, int64_t id, xk_request_info *info);
+/* Waits until the request is DONE, CANCELLED or FAILED, or the timeout
+ * passes (XK_ERR_TIMEOUT); info may be NULL. */
+int xk_serve_wait(xk_server *srv, int64_t id, double timeout_s, xk_request_info *info);
+/* Copies a DONE request's cells to host_out and forgets the request. */
+int xk_serve_result(xk_server *srv, int64_t id, void *host_out, int64_t cells);
+/* Pending: dropped at once; active: stops at its next round boundary. */
+int xk_serve_cancel(xk_server *srv, int64_t id);
+int xk_serve_stats_get(xk_server *srv, xk_serve_stats *st);
+
+/* The server's arena allocator on its own (host only, no CUDA): first-fit
+ * offsets in [0, capacity), 256-byte granules, neighbours merged on free. */
+typedef struct xk_arena xk_arena;
+int xk_arena_create(int64_t capacity, xk_arena **out);
+int xk_arena_alloc(xk_arena *a, int64_t bytes, int64_t *offset);   /* XK_ERR_OOM: no fit */
+int xk_arena_free(xk_arena *a, int64_t offset);
+int xk_arena_stats(xk_arena *a, int64_t *in_use, int64_t *largest_free, int32_t *free_ranges);
+int xk_arena_destroy(xk_arena *a);
+
 /* Select the CUDA device for handles created afterwards on this thread. */
 int xk_set_device(int32_t device);
 /* Page-lock (pin) caller-owned host memory for fast copies, and release it. */

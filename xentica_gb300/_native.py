@@ -46,6 +46,35 @@ class XkDesc(ctypes.Structure):
     ]
 
 
+XK_SERVE_LIFE2D, XK_SERVE_LIFE3D_VN, XK_SERVE_MASS3D = 1, 2, 3
+XK_REQ_PENDING, XK_REQ_ACTIVE, XK_REQ_DONE, XK_REQ_CANCELLED, XK_REQ_FAILED = 0, 1, 2, 3, 4
+XK_ERR_ARG, XK_ERR_CUDA, XK_ERR_OOM, XK_ERR_STATE, XK_ERR_TIMEOUT = -1, -2, -3, -5, -6
+
+
+class XkRequest(ctypes.Structure):
+    """Mirror of ``xk_request``."""
+
+    _fields_ = [("kind", _I32), ("reserved0", _I32), ("size", _I64 * 3), ("rule", _U32),
+                ("reserved1", _I32), ("generations", _I64)]
+
+
+class XkRequestInfo(ctypes.Structure):
+    """Mirror of ``xk_request_info``."""
+
+    _fields_ = [("status", _I32), ("reserved", _I32), ("generations_done", _I64),
+                ("submit_s", ctypes.c_double), ("admit_s", ctypes.c_double),
+                ("done_s", ctypes.c_double), ("mass_total", _U64)]
+
+
+class XkServeStats(ctypes.Structure):
+    """Mirror of ``xk_serve_stats``."""
+
+    _fields_ = [(name, _I64) for name in (
+        "submitted", "admitted", "completed", "cancelled", "rejected", "failed", "pending",
+        "active", "device_bytes_in_use", "device_bytes_peak", "budget_bytes", "cell_updates",
+        "rounds", "launches")] + [("elapsed_s", ctypes.c_double)]
+
+
 # name -> (restype, argtypes); every symbol declared in include/xk.h
 SIGNATURES = {
     "xk_model_create": (_I32, [ctypes.POINTER(XkDesc), ctypes.POINTER(_P)]),
@@ -72,6 +101,21 @@ SIGNATURES = {
     "xk_batch_total_cells": (_I64, [_P]),
     "xk_batch_launches": (_I64, [_P, _I32]),
     "xk_batch_step_noalloc": (_I32, [_P, _I32, _P, _P, _P, _I32, _P]),
+    "xk_serve_create": (_I32, [_I64, _I64, _I32, _I32, ctypes.POINTER(_P)]),
+    "xk_serve_destroy": (_I32, [_P]),
+    "xk_serve_request_bytes": (_I32, [ctypes.POINTER(XkRequest), ctypes.POINTER(_I64)]),
+    "xk_serve_submit": (_I32, [_P, ctypes.POINTER(XkRequest), _P, ctypes.POINTER(_I64)]),
+    "xk_serve_info": (_I32, [_P, _I64, ctypes.POINTER(XkRequestInfo)]),
+    "xk_serve_wait": (_I32, [_P, _I64, ctypes.c_double, ctypes.POINTER(XkRequestInfo)]),
+    "xk_serve_result": (_I32, [_P, _I64, _P, _I64]),
+    "xk_serve_cancel": (_I32, [_P, _I64]),
+    "xk_serve_stats_get": (_I32, [_P, ctypes.POINTER(XkServeStats)]),
+    "xk_arena_create": (_I32, [_I64, ctypes.POINTER(_P)]),
+    "xk_arena_alloc": (_I32, [_P, _I64, ctypes.POINTER(_I64)]),
+    "xk_arena_free": (_I32, [_P, _I64]),
+    "xk_arena_stats": (_I32, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
+                              ctypes.POINTER(_I32)]),
+    "xk_arena_destroy": (_I32, [_P]),
     "xk_set_device": (_I32, [_I32]),
     "xk_host_register": (_I32, [_P, _I64]),
     "xk_host_unregister": (_I32, [_P]),

@@ -205,6 +205,66 @@ cudaError_t xk_life_step_global(const uint32_t *src, uint32_t *dst, const LifeGe
 }
 
 // ---------------------------------------------------------------------------
+// 3-D von Neumann Life-like on a torus (the serving loop's 3-D requests),
+// bit-packed along x: row (y, z) is row z * H + y of the 2-D packing, so the
+// pack/unpack kernels above serve unchanged with H * D rows.  One thread per
+// word: the x neighbours come from the row's own words (torus wrap as in 2-D),
+// y and z neighbours are the same word of four other rows.  Six one-bit
+// inputs reduce to a 3-bit count with two full adders and a third on the
+// carries; the count and the cell's state select the rule bit through the
+// same multiplexer tree as in 2-D (counts 0..6).
+
+__global__ void __launch_bounds__(256)
+xk_k_life3d_vn(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, Life3Geo g,
+               LifeTable t)
+{
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t rows = (int64_t)g.H * g.D;
+    if (idx >= rows * g.wpr) return;
+    const int64_t r = idx / g.wpr;
+    const int j = (int)(idx - r * g.wpr);
+    const int z = (int)(r / g.H), y = (int)(r - (int64_t)z * g.H);
+    const int last = g.wpr - 1;
+    const int jl = j > 0 ? j - 1 : last, jr = j < last ? j + 1 : 0;
+    const int lshift = j > 0 ? 31 : g.rlast - 1;
+    const int top = j == last ? g.rlast - 1 : 31;
+    const uint32_t *row = src + r * g.wpr;
+    const RowVec v = xk_row_vec(__ldg(row + j), __ldg(row + jl), __ldg(row + jr), lshift, top, 0u,
+                                0u, 0, 0);
+    const int yu = y > 0 ? y - 1 : g.H - 1, yd = y + 1 < g.H ? y + 1 : 0;
+    const int zf = z > 0 ? z - 1 : g.D - 1, zb = z + 1 < g.D ? z + 1 : 0;
+    const uint32_t U = __ldg(src + ((int64_t)z * g.H + yu) * g.wpr + j);
+    const uint32_t Dn = __ldg(src + ((int64_t)z * g.H + yd) * g.wpr + j);
+    const uint32_t F = __ldg(src + ((int64_t)zf * g.H + y) * g.wpr + j);
+    const uint32_t B = __ldg(src + ((int64_t)zb * g.H + y) * g.wpr + j);
+    const uint32_t s1 = xk_lop3_xor3(v.L, v.R, U), c1 = xk_maj(v.L, v.R, U);
+    const uint32_t s2 = xk_lop3_xor3(Dn, F, B), c2 = xk_maj(Dn, F, B);
+    const uint32_t b0 = s1 ^ s2, c3 = s1 & s2;
+    const uint32_t b1 = xk_lop3_xor3(c1, c2, c3), b2 = xk_maj(c1, c2, c3);
+    uint32_t m[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) m[q] = xk_mux(b0, t.tab[2 * q], t.tab[2 * q + 1]);
+    uint32_t n[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) n[q] = xk_mux(b1, m[2 * q], m[2 * q + 1]);
+    const uint32_t dead = xk_mux(b2, n[0], n[1]);
+    const uint32_t live = xk_mux(b2, n[2], n[3]);
+    uint32_t out = xk_mux(v.C, dead, live);
+    if (j == last) out &= g.lastmask;
+    dst[idx] = out;
+}
+
+cudaError_t xk_life_step3d_vn(const uint32_t *src, uint32_t *dst, const Life3Geo &g,
+                              const LifeTable &t, cudaStream_t s)
+{
+    const int64_t total = (int64_t)g.H * g.D * g.wpr;
+    const int threads = 256;
+    const int64_t blocks = (total + threads - 1) / threads;
+    xk_k_life3d_vn<<<(unsigned)blocks, threads, 0, s>>>(src, dst, g, t);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // resident lattices: a whole lattice (W <= 1024) lives in shared memory for
 // all generations of a launch; one CTA per lattice.
 //

@@ -83,6 +83,15 @@ cudaError_t xk_life_color_step(const uint32_t *bits, int32_t *col, const LifeGeo
                                const int32_t *lut6, int fade_in, int fade_out, int smooth,
                                int plain, cudaStream_t s);
 
+// 3-D von Neumann Life-like on a torus, bit-packed along x; row (y, z) is row
+// z * H + y (pack/unpack with xk_life_geo(W, H * D, 1, 0))
+struct Life3Geo {
+    int32_t W, H, D, wpr, rlast;
+    uint32_t lastmask;
+};
+cudaError_t xk_life_step3d_vn(const uint32_t *src, uint32_t *dst, const Life3Geo &g,
+                              const LifeTable &t, cudaStream_t s);
+
 // byte-per-cell lattices (N-D, any neighbourhood; and the plain 2-D form)
 struct NdGeo {
     int32_t ndim, nbr, torus;
