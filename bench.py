@@ -55,9 +55,10 @@ def parse():
                     help="serve: offered load as a fraction of the measured capacity")
     ap.add_argument("--quantum", type=int, default=128, help="serve: generations per round")
     ap.add_argument("--serve-budget-gb", type=int, default=16, help="serve: HBM budget (GiB)")
-    ap.add_argument("--workload", choices=("ensemble", "evolife", "mass", "serve"),
+    ap.add_argument("--workload", choices=("ensemble", "life512", "evolife", "mass", "serve"),
                     default="ensemble",
-                    help="ensemble: the batched Life-like ensemble (default); evolife: EvoLife "
+                    help="ensemble: the batched Life-like ensemble (default); life512: Conway's "
+                         "Life 512x512 torus, 1000 generations per step; evolife: EvoLife "
                          "1920x1080 with a render every generation; mass: 3-D sand transfer "
                          "256^3 with the total checked every generation; serve: Poisson "
                          "arrivals of 2-D/3-D requests through the serving loop")
@@ -292,7 +293,9 @@ def run_ours(args, dist):
     time.sleep(0.6)                       # let the sampler start before the timed region
     dist.barrier()
     t_wall = time.perf_counter()
+    nat.load().xk_range_push(b"timed")
     step_ms = [ens.step(G) for _ in range(args.steps)]
+    nat.load().xk_range_pop()
     wall = time.perf_counter() - t_wall
     dist.barrier()
     clk = clocks.stop()
@@ -392,9 +395,11 @@ def run_evolife(args, dist):
     time.sleep(0.6)
     dist.barrier()
     step_ms = []
+    lib.xk_range_push(b"timed")
     for _ in range(args.steps):
         model.gpu.step(gens)
         step_ms.append(lib.xk_last_step_ms())
+    lib.xk_range_pop()
     dist.barrier()
     clk = clocks.stop()
     t0 = time.perf_counter()
@@ -467,11 +472,13 @@ def run_mass(args, dist):
     dist.barrier()
     step_ms = []
     conserved = True
+    lib.xk_range_push(b"timed")
     for _ in range(args.steps):
         model.gpu.step(gens)
         step_ms.append(lib.xk_last_step_ms())
         totals = model.gpu.mass_totals(gens)
         conserved &= bool((totals == total0).all())
+    lib.xk_range_pop()
     dist.barrier()
     clk = clocks.stop()
     t0 = time.perf_counter()
@@ -508,6 +515,134 @@ def run_mass(args, dist):
         line["cpu_baseline"] = {"value": n * 3 / el, "unit": "cell-updates/s",
                                 "cores": os.cpu_count(), "kind": "port",
                                 "sample": "3 generations of the full lattice, oracle (OpenMP)"}
+        print(json.dumps(line), flush=True)
+
+
+def life512_model():
+    """Conway's Life as the reference's examples/game_of_life.py:15-90 writes it,
+    on a 512x512 torus seeded Bernoulli(0.5) from a 64-bit integer seed."""
+    from xentica_gb300 import core, seeds
+    from xentica_gb300.core import color_effects
+
+    class GameOfLife(core.CellularAutomaton):
+        state = core.IntegerProperty(max_val=1)
+
+        class Topology:
+            dimensions = 2
+            lattice = core.OrthogonalLattice()
+            neighborhood = core.MooreNeighborhood()
+            border = core.TorusBorder()
+
+        def emit(self):
+            for buf in self.buffers:
+                buf.state = self.main.state
+
+        def absorb(self):
+            neighbors_alive = core.IntegerVariable()
+            for i in range(len(self.buffers)):
+                neighbors_alive += self.neighbors[i].buffer.state
+            is_born = (8 >> neighbors_alive) & 1
+            is_sustain = (12 >> neighbors_alive) & 1
+            self.main.state = is_born | is_sustain & self.main.state
+
+        @color_effects.MovingAverage
+        def color(self):
+            red = self.main.state * 255
+            green = self.main.state * 255
+            blue = self.main.state * 255
+            return (red, green, blue)
+
+    class Life512(core.Experiment):
+        word = 0x5EED0F11FE512A1B
+        size = (512, 512)
+        zoom = 1
+        pos = [0, 0]
+        seed = seeds.patterns.PrimordialSoup(vals={"state": seeds.random.RandInt(0, 1)})
+
+    return GameOfLife(Life512)
+
+
+def run_life512(args, dist):
+    """Life 512x512: K steps of 1000 generations (one resident launch each);
+    e2e through the public API (load the cells from the host, step 1000,
+    read the cells back); also the reference's calling pattern, 1000 calls of
+    model.step(); the final state is compared with the oracle."""
+    from xentica_gb300 import build as xk_build
+    from xentica_gb300 import _native as nat
+    xk_build.build()
+    nat.set_device(dist.local)
+    lib = nat.load()
+    model = life512_model()
+    n = model.cells_num
+    init = model.gpu.arrays.cells.get()[:n].copy()
+    colors0 = model.gpu.arrays.colors.get()
+    gens = 1000
+    for _ in range(args.warmup):
+        model.gpu.step(gens)
+    clocks = Clocks(dist.local)
+    time.sleep(0.6)
+    dist.barrier()
+    step_ms = []
+    lib.xk_range_push(b"timed")
+    for _ in range(args.steps):
+        model.gpu.step(gens)
+        step_ms.append(lib.xk_last_step_ms())
+    lib.xk_range_pop()
+    dist.barrier()
+    clk = clocks.stop()
+    total_gens = gens * (args.warmup + args.steps)
+    final = model.gpu.arrays.cells.get()[:n].copy()
+    dev_s = dist.max(sum(step_ms) / 1000.0)
+    value = float(n) * gens * args.steps * dist.world / dev_s
+    # end to end: host cells in, 1000 generations, host cells out
+    e2e = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        model.gpu.load(init, colors0)
+        model.gpu.step(gens)
+        out = model.gpu.arrays.cells.get()
+        e2e.append(time.perf_counter() - t0)
+    e2e_s = dist.max(sum(e2e))
+    # the reference's calling pattern: one step() per generation
+    model.gpu.load(init, colors0)
+    t0 = time.perf_counter()
+    for _ in range(gens):
+        model.step()
+    model.gpu.arrays.cells.get()
+    api_s = time.perf_counter() - t0
+    peak, peak_kind = measured_peak()
+    achieved = B_ALG * n * gens / (statistics.mean(step_ms) / 1000.0) / 1e9
+    line = {"metric": "cell-updates/s (Life 512x512)", "value": value, "unit": "cell-updates/s",
+            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dev_s * 1000 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded Bernoulli(0.5), 64-bit integer seed)",
+            "config": {"workload": "Conway's Life B3/S23 512x512 torus, 1000 generations per step",
+                       "l2": "256 KB state, L2 resident; no flush (latency-bound size)"},
+            "e2e": {"value": float(n) * gens * args.steps * dist.world / e2e_s,
+                    "unit": "cell-updates/s", "h2d_bytes_per_step": n + 12 * n,
+                    "d2h_bytes_per_step": n},
+            "api_step_loop": {"value": float(n) * gens / api_s, "unit": "cell-updates/s",
+                              "note": "1000 calls of model.step(), one generation each"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "note": "B_alg = 2 B per cell-update; the lattice stays in one CTA's "
+                                 "shared memory for all 1000 generations, so frac is "
+                                 "reference-format effective"},
+            "gpu_launches": args.steps, "clocks": clk}
+    if dist.rank == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        topo = O.Topology(model.size)
+        fld = topo.field(init, np.uint8)
+        col = np.zeros(3 * n, dtype=np.int32)
+        t0 = time.perf_counter()
+        O.life_run(topo, fld, col, total_gens)
+        el = time.perf_counter() - t0
+        line["parity"] = {"generations": total_gens, "bit_exact": bool(np.array_equal(fld[:n], final))}
+        line["cpu_baseline"] = {"value": n * total_gens / el, "unit": "cell-updates/s",
+                                "cores": os.cpu_count(), "kind": "port",
+                                "sample": "%d generations of the lattice, oracle (OpenMP)" % total_gens}
         print(json.dumps(line), flush=True)
 
 
@@ -610,6 +745,8 @@ def main():
             run_reference_arm(args, dist)
         elif args.workload == "evolife":
             run_evolife(args, dist)
+        elif args.workload == "life512":
+            run_life512(args, dist)
         elif args.workload == "mass":
             run_mass(args, dist)
         elif args.workload == "serve":

@@ -261,6 +261,11 @@ int xk_set_device(int32_t device);
 int xk_host_register(void *ptr, int64_t bytes);
 int xk_host_unregister(void *ptr);
 
+/* Named NVTX range around a region of host code, for profilers that filter
+ * kernels by range (ncu --nvtx-include "name/"); no reference counterpart. */
+int xk_range_push(const char *name);
+int xk_range_pop(void);
+
 /* Last error message of the calling thread ("" if none). */
 const char *xk_last_error(void);
 /* Name and SM count of the current device, for logs. */

@@ -25,13 +25,24 @@ def _topo(size):
 
 
 @pytest.mark.parametrize("size,high", [((33, 17, 9), 2 ** 32 - 1), ((64, 8, 31), 2 ** 20),
-                                       ((7, 129, 5), 100)])
+                                       ((7, 129, 5), 100), ((64, 24, 12), 2 ** 32 - 1),
+                                       ((128, 40, 20), "mixed")])
 def test_random_states_vs_oracle(size, high):
+    # widths that are multiples of 4 take the tiled kernel: small values its
+    # fast path, large ones (and the wall value) its exact path, "mixed" both
+    # in one launch, with values next to the 2^30 and 1431655765 boundaries
     model = _model(size)
     n = model.cells_num
     rng = np.random.RandomState(size[0])
-    cells = rng.randint(0, high, n, dtype=np.uint64).astype(np.uint32)
-    if high > 2 ** 31:
+    if high == "mixed":
+        cells = rng.poisson(4, n).astype(np.uint32)
+        edges = [2 ** 30 - 2, 2 ** 30 - 1, 2 ** 30, 2 ** 30 + 1, 1431655764, 1431655765,
+                 1431655766, WALL - 1, WALL]
+        where = rng.randint(0, n // 8, 24)          # the first z-slabs only
+        cells[where] = rng.choice(edges, where.size)
+    else:
+        cells = rng.randint(0, high, n, dtype=np.uint64).astype(np.uint32)
+    if high != "mixed" and high > 2 ** 31:
         cells[rng.randint(0, n, 20)] = WALL
     colors = np.zeros(3 * n, dtype=np.int32)
     model.gpu.load(cells, colors)
@@ -67,3 +78,25 @@ def test_multi_generation_call_equals_single_steps():
         b.step()
     assert np.array_equal(a.gpu.arrays.cells.get(), b.gpu.arrays.cells.get())
     assert np.array_equal(a.gpu.arrays.colors.get(), b.gpu.arrays.colors.get())
+
+
+@pytest.mark.parametrize("zc", ["1", "3", "8", "20"])
+def test_z_chunks_vs_oracle(zc, monkeypatch):
+    # planes per CTA forced (the automatic choice gives small lattices one);
+    # a few large cells put some CTAs on the exact path
+    monkeypatch.setenv("XK_MASS_ZC", zc)
+    size = (64, 24, 20)
+    model = _model(size)
+    n = model.cells_num
+    rng = np.random.RandomState(int(zc))
+    cells = rng.poisson(5, n).astype(np.uint32)
+    cells[rng.randint(0, n, 6)] = rng.choice([2 ** 30, 1431655766, WALL], 6)
+    model.gpu.load(cells, np.zeros(3 * n, dtype=np.int32))
+    topo = _topo(size)
+    fld = topo.field(cells, np.uint32)
+    col = np.zeros(3 * n, dtype=np.int32)
+    model.gpu.step(4)
+    totals = []
+    O.mass_run(topo, fld, col, 4, totals=totals)
+    assert np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n])
+    assert model.gpu.mass_totals(4).tolist() == totals

@@ -116,6 +116,8 @@ SIGNATURES = {
     "xk_arena_stats": (_I32, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                               ctypes.POINTER(_I32)]),
     "xk_arena_destroy": (_I32, [_P]),
+    "xk_range_push": (_I32, [ctypes.c_char_p]),
+    "xk_range_pop": (_I32, []),
     "xk_set_device": (_I32, [_I32]),
     "xk_host_register": (_I32, [_P, _I64]),
     "xk_host_unregister": (_I32, [_P]),

@@ -7,6 +7,8 @@
 #include <mutex>
 #include <new>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "xk_internal.cuh"
 
 // ---------------------------------------------------------------------------
@@ -625,5 +627,18 @@ extern "C" int xk_host_unregister(void *ptr)
 {
     XK_REQUIRE(ptr, XK_ERR_ARG, "xk_host_unregister: null pointer");
     XK_CUDA(cudaHostUnregister(ptr));
+    return XK_OK;
+}
+
+extern "C" int xk_range_push(const char *name)
+{
+    XK_REQUIRE(name, XK_ERR_ARG, "xk_range_push: null name");
+    nvtxRangePushA(name);
+    return XK_OK;
+}
+
+extern "C" int xk_range_pop(void)
+{
+    nvtxRangePop();
     return XK_OK;
 }

@@ -11,9 +11,10 @@
 //   m'         = m - sum_k sent_k + sum_k incoming_k
 // Colour (plain ColorEffect): min(m' * 32, 255) on every channel.
 //
-// Work split: a CTA owns a 32*V-wide, 8-row tile of a run of zc planes; a
-// thread owns V consecutive cells of one row (one 128-bit load and store per
-// plane when V = 4) and walks its z run with a three-plane register queue.
+// Two kernels: xk_k_mass_rows for widths that are a multiple of 4 (below)
+// and the generic xk_k_mass for any width.  Work split of the generic one: a
+// CTA owns a 32-wide, 8-row tile of a run of zc planes; a thread owns one
+// cell of a row and walks its z run with a three-plane register queue.
 // x neighbours come from the neighbouring lanes (shuffles; lanes 0 and 31
 // load the one cell beyond the warp), y neighbours are 128-bit loads of the
 // rows above and below (the neighbouring warps' own rows, so mostly L1
@@ -145,37 +146,37 @@ xk_k_mass(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
     }
 }
 
-// Tiled form for W % 4 == 0 (the usual case): the (m, m / 7) pairs of the
-// CTA's eight rows of plane z go through a double-buffered shared tile, so
-// every m / 7 is computed once, by the thread that loaded the cell; rows
-// y - 1 and y + 8 (the tile's halo) are loaded by warps 0 and 7 and the x
-// halo cells by lanes 0 and 31.  A thread's own column is a four-deep
-// register queue (planes z - 1 .. z + 2, the last one in flight).  Every
-// loaded cell is tested for the wall value once; while no CTA thread has met
-// one (a sticky flag OR-ed at the one barrier per plane) every on-board
-// neighbour counts in the "sent" sum, so
-//   m' = m - (m / 7) * (#on-board neighbours) + sum_k q_k,
-// else the exact per-neighbour form of the generic kernel is used.
-#define XK_MT_ROW 128
+// Helpers of the W % 4 == 0 kernel.  While a cell is below 2^30,
+// q = umulhi(m, 0x24924925) is m / 7 exactly (it is for all m < 1 431 655 765);
+// larger cells take the exact division.
+#define XK_MASS_SMALL 0x40000000u
 
-struct MassTile {
-    uint32_t m[2][XK_MASS_BY + 2][XK_MT_ROW];
-    uint32_t q[2][XK_MASS_BY + 2][XK_MT_ROW];
-};
-
-__device__ __forceinline__ uint4 xk_mass_ld4(const uint32_t *__restrict__ src, int64_t idx, bool ok,
+__device__ __forceinline__ uint4 xk_mass_ld4(const uint32_t *__restrict__ src, uint32_t off, bool ok,
                                               uint32_t wall)
 {
     uint4 u = make_uint4(wall, wall, wall, wall);
-    if (ok) u = __ldg(reinterpret_cast<const uint4 *>(src + idx));
+    if (ok) u = __ldg(reinterpret_cast<const uint4 *>(src + off));
     return u;
 }
 
-// q of four loaded cells (0 when off-board); marks a loaded wall value
-__device__ __forceinline__ uint4 xk_mass_q4(const uint4 m, bool ok, uint32_t wall, bool &seen)
+__device__ __forceinline__ uint32_t xk_div7(uint32_t m, bool small)
 {
-    seen |= ok && (m.x == wall || m.y == wall || m.z == wall || m.w == wall);
-    return ok ? make_uint4(m.x / 7u, m.y / 7u, m.z / 7u, m.w / 7u) : make_uint4(0u, 0u, 0u, 0u);
+    return small ? __umulhi(m, 0x24924925u) : m / 7u;
+}
+
+// q of four loaded cells (0 when off-board), exact; `big` marks a loaded
+// cell at or above 2^30
+__device__ __forceinline__ uint4 xk_mass_q4(const uint4 m, bool ok, bool &big)
+{
+    const bool b = ok && ((m.x | m.y | m.z | m.w) >= XK_MASS_SMALL);
+    big |= b;
+    uint4 q;
+    if (b)
+        q = make_uint4(m.x / 7u, m.y / 7u, m.z / 7u, m.w / 7u);
+    else
+        q = make_uint4(__umulhi(m.x, 0x24924925u), __umulhi(m.y, 0x24924925u),
+                       __umulhi(m.z, 0x24924925u), __umulhi(m.w, 0x24924925u));
+    return ok ? q : make_uint4(0u, 0u, 0u, 0u);
 }
 
 __device__ __forceinline__ uint32_t xk_get(const uint4 &u, int i)
@@ -183,12 +184,23 @@ __device__ __forceinline__ uint32_t xk_get(const uint4 &u, int i)
     return i == 0 ? u.x : i == 1 ? u.y : i == 2 ? u.z : u.w;
 }
 
+// Form for W % 4 == 0 (the usual case): a thread owns four consecutive
+// cells of one row (128-bit loads and stores) and walks its run of zc planes
+// with a register queue of planes z - 1 .. z + 2; the rows above and below and
+// the x halo cell of lanes 0 and 31 are loaded one plane ahead.  Each
+// loaded cell gets its q = m / 7 by the one-instruction division when it is
+// below 2^30.  No shared tile and no barrier: x neighbours are lane shuffles,
+// y neighbours the thread's own loads of the rows above and below (mostly L1
+// hits: they are the neighbouring warps' rows).  A warp takes the fast path
+// when none of the cells its lanes read is at or above 2^30 (__any_sync), so
+// no cell is the wall value and every on-board neighbour counts in the sent
+// sum:  m' = m - q * (#on-board neighbours) + sum_k q_k;  otherwise the exact
+// per-neighbour form of the generic kernel.
 template <int MINB>
 __global__ void __launch_bounds__(32 * XK_MASS_BY, MINB)
-xk_k_mass_tiled(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
-                unsigned long long *__restrict__ total, MassParams p, int zc)
+xk_k_mass_rows(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
+               unsigned long long *__restrict__ total, MassParams p, int zc)
 {
-    __shared__ __align__(16) MassTile t;
     __shared__ unsigned long long warp_sums[XK_MASS_BY];
     const int lane = threadIdx.x, ty = threadIdx.y;
     const int x0 = (blockIdx.x * 32 + lane) * 4;
@@ -196,73 +208,63 @@ xk_k_mass_tiled(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
     const int z0 = blockIdx.z * zc;
     const int z1 = min(z0 + zc, p.D);
     const bool in = x0 < p.W && y < p.H;
-    const int64_t plane = (int64_t)p.W * p.H;
-    const int64_t col = in ? (int64_t)y * p.W + x0 : 0;
+    const uint32_t plane = (uint32_t)p.W * (uint32_t)p.H;
     const uint32_t wall = p.wall;
-    // x halo: lane 0 owns the cell left of the warp's row, lane 31 the one right of it
+    uint32_t off = in ? (uint32_t)z0 * plane + (uint32_t)y * p.W + x0 : 0u;
     const bool hx_ok = in && ((lane == 0 && x0 > 0) || (lane == 31 && x0 + 4 < p.W));
-    const int64_t hx_col = lane == 0 ? col - 1 : col + 4;
-    // y halo rows: warp 0 loads row y - 1, warp 7 row y + 1 (of the tile's edge rows)
-    const bool hy_warp = ty == 0 || ty == XK_MASS_BY - 1;
-    const bool hy_ok = in && ((ty == 0 && y > 0) || (ty == XK_MASS_BY - 1 && y + 1 < p.H));
-    const int64_t hy_col = ty == 0 ? col - p.W : col + p.W;
-    const int hy_row = ty == 0 ? 0 : XK_MASS_BY + 1;
-    // on-board x/y neighbours of each of the four cells
+    const int hx_d = lane == 0 ? -1 : 4;
+    const bool has_ym = in && y > 0, has_yp = in && y + 1 < p.H;
     int cxy[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
         cxy[i] = (x0 + i > 0) + (x0 + i + 1 < p.W) + (y > 0) + (y + 1 < p.H);
 
-    bool seen = false;
-    uint4 prv_m = xk_mass_ld4(src, (int64_t)(z0 - 1) * plane + col, in && z0 > 0, wall);
-    uint4 prv_q = xk_mass_q4(prv_m, in && z0 > 0, wall, seen);
-    uint4 cur_m = xk_mass_ld4(src, (int64_t)z0 * plane + col, in, wall);
-    uint4 cur_q = xk_mass_q4(cur_m, in, wall, seen);
-    uint4 nxt_m = xk_mass_ld4(src, (int64_t)(z0 + 1) * plane + col, in && z0 + 1 < p.D, wall);
-    uint32_t hx_m = hx_ok ? __ldg(src + (int64_t)z0 * plane + hx_col) : wall;
-    uint4 hy_m = hy_warp ? xk_mass_ld4(src, (int64_t)z0 * plane + hy_col, hy_ok, wall)
-                         : make_uint4(wall, wall, wall, wall);
+    bool big = false;   // this thread has met a cell >= 2^30 in the last three planes
+    bool big_prv = false, big_cur = false;
+    uint4 prv_m = xk_mass_ld4(src, off - plane, in && z0 > 0, wall);
+    uint4 prv_q = xk_mass_q4(prv_m, in && z0 > 0, big_prv);
+    uint4 cur_m = xk_mass_ld4(src, off, in, wall);
+    uint4 cur_q = xk_mass_q4(cur_m, in, big_cur);
+    uint4 nxt_m = xk_mass_ld4(src, off + plane, in && z0 + 1 < p.D, wall);
+    // the rows above and below and the x halo of plane z + 1 are loaded while
+    // plane z is computed
+    uint4 ym_pf = xk_mass_ld4(src, off - p.W, has_ym, wall);
+    uint4 yp_pf = xk_mass_ld4(src, off + p.W, has_yp, wall);
+    uint32_t hx_pf = hx_ok ? __ldg(src + (off + hx_d)) : wall;
     unsigned long long mass_sum = 0;
     for (int z = z0; z < z1; ++z) {
-        const int b = z & 1;
-        const int64_t zb = (int64_t)z * plane;
-        // in flight for later planes: own column z + 2, halos of z + 1
-        const uint4 nn_m = xk_mass_ld4(src, zb + 2 * plane + col, in && z + 2 < p.D, wall);
-        const uint4 nxt_q = xk_mass_q4(nxt_m, in && z + 1 < p.D, wall, seen);
-        const uint32_t hx_q = hx_ok ? hx_m / 7u : 0u;
-        seen |= hx_ok && hx_m == wall;
-        *reinterpret_cast<uint4 *>(&t.m[b][ty + 1][lane * 4]) = cur_m;
-        *reinterpret_cast<uint4 *>(&t.q[b][ty + 1][lane * 4]) = cur_q;
-        if (hy_warp) {
-            const uint4 hy_q = xk_mass_q4(hy_m, hy_ok, wall, seen);
-            *reinterpret_cast<uint4 *>(&t.m[b][hy_row][lane * 4]) = hy_m;
-            *reinterpret_cast<uint4 *>(&t.q[b][hy_row][lane * 4]) = hy_q;
-        }
+        const uint4 nn_m = xk_mass_ld4(src, off + 2 * plane, in && z + 2 < p.D, wall);
+        const uint4 ym_m = ym_pf, yp_m = yp_pf;
+        const uint32_t hx_m = hx_pf;
         const bool more = z + 1 < z1;
-        const uint32_t hx_next = hx_ok && more ? __ldg(src + zb + plane + hx_col) : wall;
-        const uint4 hy_next = hy_warp ? xk_mass_ld4(src, zb + plane + hy_col, hy_ok && more, wall)
-                                      : make_uint4(wall, wall, wall, wall);
-        const bool walls = __syncthreads_or(seen);
-        const uint4 ym_q = *reinterpret_cast<const uint4 *>(&t.q[b][ty][lane * 4]);
-        const uint4 yp_q = *reinterpret_cast<const uint4 *>(&t.q[b][ty + 2][lane * 4]);
+        ym_pf = xk_mass_ld4(src, off + plane - p.W, has_ym && more, wall);
+        yp_pf = xk_mass_ld4(src, off + plane + p.W, has_yp && more, wall);
+        hx_pf = hx_ok && more ? __ldg(src + (off + plane + hx_d)) : wall;
+        bool big_nxt = false, big_y = false;
+        const uint4 nxt_q = xk_mass_q4(nxt_m, in && z + 1 < p.D, big_nxt);
+        const uint4 ym_q = xk_mass_q4(ym_m, has_ym, big_y);
+        const uint4 yp_q = xk_mass_q4(yp_m, has_yp, big_y);
+        const bool hx_big = hx_ok && hx_m >= XK_MASS_SMALL;
+        const uint32_t hx_q = hx_ok ? xk_div7(hx_m, !hx_big) : 0u;
+        big = big_prv || big_cur || big_nxt || big_y || hx_big;
         uint32_t xl_q = __shfl_up_sync(0xFFFFFFFFu, cur_q.w, 1);
         uint32_t xr_q = __shfl_down_sync(0xFFFFFFFFu, cur_q.x, 1);
         if (lane == 0) xl_q = hx_q;
         if (lane == 31) xr_q = hx_q;
         uint32_t out[4];
-        if (!walls) {
+        if (!__any_sync(0xFFFFFFFFu, big)) {
             const int cz = (z > 0) + (z + 1 < p.D);
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 const uint32_t ql = i == 0 ? xl_q : xk_get(cur_q, i > 0 ? i - 1 : 0);
                 const uint32_t qr = i == 3 ? xr_q : xk_get(cur_q, i < 3 ? i + 1 : 3);
-                const uint32_t sq = ql + qr + xk_get(ym_q, i) + xk_get(yp_q, i) +
-                                    xk_get(prv_q, i) + xk_get(nxt_q, i);
-                out[i] = xk_get(cur_m, i) - xk_get(cur_q, i) * (uint32_t)(cxy[i] + cz) + sq;
+                const uint32_t s1 = ql + qr + xk_get(ym_q, i);
+                const uint32_t s2 = xk_get(yp_q, i) + xk_get(prv_q, i) + xk_get(nxt_q, i);
+                out[i] = xk_get(cur_m, i) - xk_get(cur_q, i) * (uint32_t)(cxy[i] + cz) + s1 + s2;
             }
+            if (in)   // each value < 2^31 here, so pairs sum without overflow
+                mass_sum += (unsigned long long)(out[0] + out[1]) + (unsigned long long)(out[2] + out[3]);
         } else {
-            const uint4 ym_m = *reinterpret_cast<const uint4 *>(&t.m[b][ty][lane * 4]);
-            const uint4 yp_m = *reinterpret_cast<const uint4 *>(&t.m[b][ty + 2][lane * 4]);
             uint32_t xl_m = __shfl_up_sync(0xFFFFFFFFu, cur_m.w, 1);
             uint32_t xr_m = __shfl_down_sync(0xFFFFFFFFu, cur_m.x, 1);
             if (lane == 0) xl_m = hx_ok ? hx_m : wall;
@@ -273,30 +275,30 @@ xk_k_mass_tiled(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
                 const uint32_t mr = i == 3 ? xr_m : xk_get(cur_m, i < 3 ? i + 1 : 3);
                 const uint32_t ql = i == 0 ? xl_q : xk_get(cur_q, i > 0 ? i - 1 : 0);
                 const uint32_t qr = i == 3 ? xr_q : xk_get(cur_q, i < 3 ? i + 1 : 3);
-                const uint32_t mpz = z + 1 < p.D ? xk_get(nxt_m, i) : wall;
                 const uint32_t cnt = (uint32_t)(ml != wall) + (uint32_t)(mr != wall) +
                                      (uint32_t)(xk_get(ym_m, i) != wall) +
                                      (uint32_t)(xk_get(yp_m, i) != wall) +
-                                     (uint32_t)(xk_get(prv_m, i) != wall) + (uint32_t)(mpz != wall);
+                                     (uint32_t)(xk_get(prv_m, i) != wall) +
+                                     (uint32_t)(xk_get(nxt_m, i) != wall);
                 const uint32_t sq = ql + qr + xk_get(ym_q, i) + xk_get(yp_q, i) +
                                     xk_get(prv_q, i) + xk_get(nxt_q, i);
                 const uint32_t m = xk_get(cur_m, i);
                 out[i] = m - xk_get(cur_q, i) * cnt + (m != wall ? sq : 0u);
             }
+            if (in)
+                mass_sum += (unsigned long long)out[0] + out[1] + (unsigned long long)out[2] + out[3];
         }
-        if (in) {
-            *reinterpret_cast<uint4 *>(dst + zb + col) = make_uint4(out[0], out[1], out[2], out[3]);
-            mass_sum += (unsigned long long)out[0] + out[1] + (unsigned long long)out[2] + out[3];
-        }
+        if (in) *reinterpret_cast<uint4 *>(dst + off) = make_uint4(out[0], out[1], out[2], out[3]);
         prv_m = cur_m;
         prv_q = cur_q;
+        big_prv = big_cur;
         cur_m = nxt_m;
         cur_q = nxt_q;
+        big_cur = big_nxt;
         nxt_m = nn_m;
-        hx_m = hx_next;
-        hy_m = hy_next;
+        off += plane;
     }
-    for (int off = 16; off > 0; off >>= 1) mass_sum += __shfl_down_sync(0xFFFFFFFFu, mass_sum, off);
+    for (int o = 16; o > 0; o >>= 1) mass_sum += __shfl_down_sync(0xFFFFFFFFu, mass_sum, o);
     if (lane == 0) warp_sums[ty] = mass_sum;
     __syncthreads();
     if (ty == 0 && lane == 0) {
@@ -386,9 +388,9 @@ cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long 
     // four CTAs per SM (64 registers) measured faster than three; XK_MASS_MINB=1 lifts the cap
     static const int minb = getenv("XK_MASS_MINB") ? atoi(getenv("XK_MASS_MINB")) : 4;
     if (vec && minb >= 4)
-        xk_k_mass_tiled<4><<<grid, block, 0, s>>>(src, dst, total, p, zc);
+        xk_k_mass_rows<4><<<grid, block, 0, s>>>(src, dst, total, p, zc);
     else if (vec)
-        xk_k_mass_tiled<1><<<grid, block, 0, s>>>(src, dst, total, p, zc);
+        xk_k_mass_rows<1><<<grid, block, 0, s>>>(src, dst, total, p, zc);
     else
         xk_k_mass<1><<<grid, block, 0, s>>>(src, dst, total, p, zc);
     return cudaGetLastError();
