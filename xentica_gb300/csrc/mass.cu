@@ -146,9 +146,13 @@ xk_k_mass(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
     }
 }
 
-// Helpers of the W % 4 == 0 kernel.  While a cell is below 2^30,
-// q = umulhi(m, 0x24924925) is m / 7 exactly (it is for all m < 1 431 655 765);
-// larger cells take the exact division.
+// Helpers of the W % 4 == 0 kernel.  Division by the invariant 7 as a
+// multiply-high (Granlund and Montgomery, "Division by invariant integers
+// using multiplication", 1994): c = 0x24924925 = (2^32 + 3) / 7, so
+// umulhi(m, c) = floor(m / 7 + 3m / (7 * 2^32)), which is floor(m / 7) while
+// the error term stays below 1/7 (the smallest gap to the next integer), i.e.
+// for all m < 2^32 / 3 = 1 431 655 765.  Cells below 2^30 use it; larger
+// cells take the compiler's exact division.
 #define XK_MASS_SMALL 0x40000000u
 
 __device__ __forceinline__ uint4 xk_mass_ld4(const uint32_t *__restrict__ src, uint32_t off, bool ok,
