@@ -1,0 +1,64 @@
+"""GPU parity of the cluster path for single Life-like lattices.
+
+``XK_CLUSTER=n`` makes a model's multi-generation steps run on a cluster of
+(up to) n CTAs, whatever the tuner would pick; every lattice is compared cell
+by cell with the oracle, torus and static border (value 1), widths around the
+word size and up to 1024, heights from a few rows to more than one CTA holds.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from xentica_gb300 import core, seeds
+from tests.models import GameOfLife, GameOfLifeStatic
+
+
+class SoupExperiment(core.Experiment):
+    word = "CLUSTER SOUP"
+    size = (64, 64)
+    zoom = 1
+    pos = [0, 0]
+    seed = seeds.patterns.PrimordialSoup(vals={"state": seeds.random.RandInt(0, 1)})
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(512, 512), (33, 17), (1024, 40), (1, 9), (100, 301), (1000, 700), (32, 2), (7, 1024)]
+
+
+def _run(cls, size, forced, gens, monkeypatch, seed):
+    monkeypatch.setenv("XK_CLUSTER", str(forced))
+    exp = type("E", (SoupExperiment, ), {"size": size})
+    model = cls(exp)
+    n = model.cells_num
+    rng = np.random.RandomState(seed)
+    cells = (rng.random_sample(n) < 0.45).astype(np.uint8)
+    model.gpu.load(cells, np.zeros(3 * n, dtype=np.int32))
+    model.gpu.step(gens)
+    border = 1 if cls is GameOfLifeStatic else None
+    topo = O.Topology(size, "moore", border)
+    fld = topo.field(cells, np.uint8)
+    O.life_run(topo, fld, np.zeros(3 * n, np.int32), gens)
+    return model.gpu.arrays.cells.get()[:n], fld[:n]
+
+
+@pytest.mark.parametrize("forced", [2, 4, 8, 16])
+@pytest.mark.parametrize("cls", [GameOfLife, GameOfLifeStatic])
+def test_cluster_sizes_vs_oracle(cls, forced, monkeypatch):
+    for k, size in enumerate(SIZES):
+        got, want = _run(cls, size, forced, 37, monkeypatch, 10 * forced + k)
+        assert np.array_equal(got, want), (cls.__name__, size, forced)
+
+
+def test_long_run_and_tuner_choice(monkeypatch):
+    # 1000 generations (one launch) with the tuner's own choice
+    monkeypatch.delenv("XK_CLUSTER", raising=False)
+    exp = type("E", (SoupExperiment, ), {"size": (512, 512)})
+    model = GameOfLife(exp)
+    n = model.cells_num
+    cells = (np.random.RandomState(3).random_sample(n) < 0.5).astype(np.uint8)
+    model.gpu.load(cells, np.zeros(3 * n, dtype=np.int32))
+    model.gpu.step(1000)
+    topo = O.Topology((512, 512))
+    fld = topo.field(cells, np.uint8)
+    O.life_run(topo, fld, np.zeros(3 * n, np.int32), 1000)
+    assert np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n])

@@ -431,14 +431,17 @@ extern "C" int xk_batch_tune(xk_batch *b, int32_t generations, int32_t *chosen)
     for (int r : cand) {
         b->rows_per_band = r;
         if ((rc = plan_classes(b)) != XK_OK) break;
-        float ms = 0.f;
-        for (int rep = 0; rep < 2; ++rep) {
-            if ((rc = launch_batched(b, generations)) != XK_OK) break;   // builds the graph
+        // best of three timed launches after one that builds the graph
+        float ms = 1e30f;
+        if ((rc = launch_batched(b, generations)) != XK_OK) break;
+        for (int rep = 0; rep < 3; ++rep) {
+            float t = 0.f;
             cudaEventRecord(b->ev0, b->stream);
             if ((rc = launch_batched(b, generations)) != XK_OK) break;
             cudaEventRecord(b->ev1, b->stream);
             cudaEventSynchronize(b->ev1);
-            cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+            cudaEventElapsedTime(&t, b->ev0, b->ev1);
+            ms = std::min(ms, t);
         }
         if (rc != XK_OK) break;
         if (ms < best) {

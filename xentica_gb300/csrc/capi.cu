@@ -1,6 +1,7 @@
 // C-ABI of single models (include/xk.h): device state, layout conversion and
 // generation stepping for the kernel families.
 #include <math.h>
+#include <stdlib.h>
 #include <stdarg.h>
 #include <string.h>
 
@@ -110,6 +111,7 @@ struct xk_model {
     int64_t img_cap = 0;
     LifeInst *d_inst = nullptr;  // the lattice as a one-instance resident batch
     int resident = 0, res_threads = 0, res_smem = 0;
+    int cl_tuned = 0, cl_C = 0, cl_R = 0, cl_threads = 0;   // cluster plan (cl_C = 0: none)
     uint32_t rule0 = 0, rule1 = 0;
     int32_t lut[6] = {0, 0, 0, 0, 0, 0};
     int hf = 0;                  // colour is a function of the state alone
@@ -161,6 +163,62 @@ int xk_life_resident_config(int W, int H, int rows_per_band, int *threads, int *
 static int resident_plan_for(xk_model *m)
 {
     return xk_life_resident_config(m->lg.W, m->lg.H, 8, &m->res_threads, &m->res_smem);
+}
+
+// Multi-generation steps of a 2-D lattice run in one launch on the resident
+// kernel (one CTA) or on a cluster of 2..16 CTAs (cluster.cu).  On the first
+// such step the candidates are timed over 32 generations on the ping-pong
+// partner buffer (the state is not touched) and the fastest is kept;
+// lattices too large for one CTA take the fastest cluster that fits, else the
+// per-generation global kernel.  XK_CLUSTER=0 disables clusters and
+// XK_CLUSTER=n asks for a cluster of (up to) n CTAs.
+static int tune_cluster(xk_model *m)
+{
+    m->cl_tuned = 1;
+    m->cl_C = 0;
+    const char *env = getenv("XK_CLUSTER");
+    if (env && env[0]) {
+        const int want = atoi(env);
+        int C = 0, R = 0, th = 0;
+        if (want > 0 && xk_life_cluster_config(m->lg, want, &C, &R, &th)) {
+            m->cl_C = C;
+            m->cl_R = R;
+            m->cl_threads = th;
+        }
+        return XK_OK;
+    }
+    const LifeTable t = xk_life_table(m->rule0, m->rule1);
+    const size_t bytes = (size_t)m->lg.H * m->lg.wpr * 4;
+    uint32_t *scratch = m->bits[1 - m->cur];
+    XK_CUDA(cudaMemcpyAsync(scratch, m->bits[m->cur], bytes, cudaMemcpyDeviceToDevice, m->stream));
+    const int G = 32;
+    float best = 1e30f;
+    if (m->resident) {
+        XK_CUDA(cudaEventRecord(m->ev0, m->stream));
+        XK_CUDA(xk_life_step_resident(m->d_inst, 1, scratch, 0, G, m->lg.torus, m->lg.bfill, nullptr,
+                                      m->res_threads, m->res_smem, m->stream));
+        XK_CUDA(cudaEventRecord(m->ev1, m->stream));
+        XK_CUDA(cudaEventSynchronize(m->ev1));
+        XK_CUDA(cudaEventElapsedTime(&best, m->ev0, m->ev1));
+    }
+    static const int cand[] = {16, 8, 4, 2};
+    for (int want : cand) {
+        int C = 0, R = 0, th = 0;
+        if (!xk_life_cluster_config(m->lg, want, &C, &R, &th)) continue;
+        float ms = 0.f;
+        XK_CUDA(cudaEventRecord(m->ev0, m->stream));
+        XK_CUDA(xk_life_step_cluster(scratch, m->lg, t, G, C, R, th, m->stream));
+        XK_CUDA(cudaEventRecord(m->ev1, m->stream));
+        XK_CUDA(cudaEventSynchronize(m->ev1));
+        XK_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+        if (ms < best) {
+            best = ms;
+            m->cl_C = C;
+            m->cl_R = R;
+            m->cl_threads = th;
+        }
+    }
+    return XK_OK;
 }
 
 static void free_model(xk_model *m)
@@ -503,8 +561,23 @@ extern "C" int xk_step(xk_model *m, int64_t nsteps)
         int rc = materialize_colors(m);
         if (rc != XK_OK) return rc;
     }
+    if (m->layout == LAYOUT_BITS2D && colors_free && !m->cl_tuned) {
+        int rc = tune_cluster(m);
+        if (rc != XK_OK) return rc;
+    }
     XK_CUDA(cudaEventRecord(m->ev0, m->stream));
-    if (m->layout == LAYOUT_BITS2D && m->resident && colors_free) {
+    if (m->layout == LAYOUT_BITS2D && colors_free && m->cl_C) {
+        // whole lattice in the shared memory of a cluster; long runs are cut
+        // into launches of at most 4096 generations
+        const LifeTable t = xk_life_table(m->rule0, m->rule1);
+        int64_t left = nsteps;
+        while (left > 0) {
+            const int g = (int)(left > 4096 ? 4096 : left);
+            XK_CUDA(xk_life_step_cluster(m->bits[m->cur], m->lg, t, g, m->cl_C, m->cl_R,
+                                         m->cl_threads, m->stream));
+            left -= g;
+        }
+    } else if (m->layout == LAYOUT_BITS2D && m->resident && colors_free) {
         // whole lattice in shared memory; long runs are cut into launches of
         // at most 4096 generations
         int64_t left = nsteps;

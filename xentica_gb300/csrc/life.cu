@@ -40,120 +40,7 @@ LifeGeo xk_life_geo(int64_t W, int64_t H, int torus, int border_state)
     return g;
 }
 
-// ---------------------------------------------------------------------------
-// word-level logic
-
-// Three-input boolean functions as single lop3 instructions (PTX lop3.b32:
-// the immediate is the function evaluated on a = 0xF0, b = 0xCC, c = 0xAA).
-__device__ __forceinline__ uint32_t xk_lop3_mux(uint32_t sel, uint32_t a, uint32_t b)
-{
-    uint32_t d;   // sel ? b : a, bitwise
-    asm("lop3.b32 %0, %1, %2, %3, 0xAC;" : "=r"(d) : "r"(sel), "r"(a), "r"(b));
-    return d;
-}
-
-__device__ __forceinline__ uint32_t xk_lop3_maj(uint32_t a, uint32_t b, uint32_t c)
-{
-    uint32_t d;   // majority: carry of a full adder
-    asm("lop3.b32 %0, %1, %2, %3, 0xE8;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
-    return d;
-}
-
-__device__ __forceinline__ uint32_t xk_lop3_xor3(uint32_t a, uint32_t b, uint32_t c)
-{
-    uint32_t d;   // sum of a full adder
-    asm("lop3.b32 %0, %1, %2, %3, 0x96;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
-    return d;
-}
-
-__device__ __forceinline__ uint32_t xk_mux(uint32_t sel, uint32_t a, uint32_t b)
-{
-    return xk_lop3_mux(sel, a, b);
-}
-
-__device__ __forceinline__ uint32_t xk_maj(uint32_t a, uint32_t b, uint32_t c)
-{
-    return xk_lop3_maj(a, b, c);
-}
-
-// Next state of 32 cells.  (Lu, Cu, Ru) are the row above shifted so that bit
-// b holds the up-left, up and up-right neighbour of cell b; (Lm, Rm) the left
-// and right neighbours; (Ld, Cd, Rd) the row below; Cm the cells themselves.
-template <class Tab>
-__device__ __forceinline__ uint32_t xk_life_word(uint32_t Lu, uint32_t Cu, uint32_t Ru,
-                                                 uint32_t Lm, uint32_t Cm, uint32_t Rm,
-                                                 uint32_t Ld, uint32_t Cd, uint32_t Rd,
-                                                 const Tab &t)
-{
-    // neighbour count k = b0 + 2 b1 + 4 b2 + 8 b3 (k <= 8, so b3 implies k == 8)
-    const uint32_t su = xk_lop3_xor3(Lu, Cu, Ru), cu = xk_maj(Lu, Cu, Ru);
-    const uint32_t sd = xk_lop3_xor3(Ld, Cd, Rd), cd = xk_maj(Ld, Cd, Rd);
-    const uint32_t sm = Lm ^ Rm, cm = Lm & Rm;
-    const uint32_t b0 = xk_lop3_xor3(su, sd, sm), k1 = xk_maj(su, sd, sm);
-    const uint32_t tw = xk_lop3_xor3(cu, cd, cm), k2 = xk_maj(cu, cd, cm);
-    const uint32_t b1 = tw ^ k1, k3 = tw & k1;
-    const uint32_t b2 = k2 ^ k3, b3 = k2 & k3;
-    // rule lookup: multiplexer tree over (state, b2, b1, b0), then b3
-    uint32_t m[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) m[q] = xk_mux(b0, t.tab[2 * q], t.tab[2 * q + 1]);
-    uint32_t n[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) n[q] = xk_mux(b1, m[2 * q], m[2 * q + 1]);
-    const uint32_t dead = xk_mux(b2, n[0], n[1]);
-    const uint32_t live = xk_mux(b2, n[2], n[3]);
-    const uint32_t low = xk_mux(Cm, dead, live);
-    const uint32_t eight = xk_mux(Cm, t.t8[0], t.t8[1]);
-    return xk_mux(b3, low, eight);
-}
-
-// Same as xk_life_word, with the rows above and below already reduced to
-// their column sums: (su, cu) = FA(Lu, Cu, Ru) and (sd, cd) = FA(Ld, Cd, Rd).
-// A row's sums are computed once and reused while it is the row below and,
-// two rows later, the row above.
-template <class Tab>
-__device__ __forceinline__ uint32_t xk_life_word_fa(uint32_t su, uint32_t cu, uint32_t Lm,
-                                                    uint32_t Cm, uint32_t Rm, uint32_t sd,
-                                                    uint32_t cd, const Tab &t)
-{
-    const uint32_t sm = Lm ^ Rm, cm = Lm & Rm;
-    const uint32_t b0 = xk_lop3_xor3(su, sd, sm), k1 = xk_maj(su, sd, sm);
-    const uint32_t tw = xk_lop3_xor3(cu, cd, cm), k2 = xk_maj(cu, cd, cm);
-    const uint32_t b1 = tw ^ k1, k3 = tw & k1;
-    const uint32_t b2 = k2 ^ k3, b3 = k2 & k3;
-    uint32_t m[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) m[q] = xk_mux(b0, t.tab[2 * q], t.tab[2 * q + 1]);
-    uint32_t n[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) n[q] = xk_mux(b1, m[2 * q], m[2 * q + 1]);
-    const uint32_t dead = xk_mux(b2, n[0], n[1]);
-    const uint32_t live = xk_mux(b2, n[2], n[3]);
-    const uint32_t low = xk_mux(Cm, dead, live);
-    const uint32_t eight = xk_mux(Cm, t.t8[0], t.t8[1]);
-    return xk_mux(b3, low, eight);
-}
-
-// Neighbour vectors of word j of a row, given the row's word and the words
-// left and right of it (already wrapped).  lshift: bit of `left` that is
-// the cell left of bit 0; top: bit of R that receives the cell right of the
-// word's last cell.
-struct RowVec {
-    uint32_t L, C, R;
-};
-
-__device__ __forceinline__ RowVec xk_row_vec(uint32_t c, uint32_t left, uint32_t right,
-                                             int lshift, int top, uint32_t ledge, uint32_t redge,
-                                             int use_ledge, int use_redge)
-{
-    RowVec v;
-    uint32_t lb = use_ledge ? ledge : ((left >> lshift) & 1u);
-    uint32_t rb = use_redge ? redge : (right & 1u);
-    v.C = c;
-    v.L = (c << 1) | lb;
-    v.R = (c >> 1) | (rb << top);
-    return v;
-}
+#include "life_word.cuh"
 
 // ---------------------------------------------------------------------------
 // one generation straight from global memory (lattices too large for a CTA)
@@ -309,20 +196,6 @@ int64_t xk_life_resident_words(int W, int H, int threads)
     if (wpr > 32) return -1;
     ResidentPlan p = xk_resident_plan(wpr, H, threads);
     return (int64_t)p.L * p.G * wpr + 2LL * p.G * wpr + XK_TAB_WORDS;
-}
-
-// neighbour vectors of a torus row: left bit taken from `left` (already the
-// wrapped neighbour word), right bit from `right`; lpre moves the left
-// neighbour's bit to position 31, top / topbit place the right neighbour
-// after the row's last cell
-__device__ __forceinline__ RowVec xk_torus_vec(uint32_t c, uint32_t left, uint32_t right, int lpre,
-                                               int top, uint32_t topbit)
-{
-    RowVec v;
-    v.C = c;
-    v.L = __funnelshift_l(left << lpre, c, 1);
-    v.R = (c >> 1) | ((right << top) & topbit);
-    return v;
 }
 
 template <bool BYTES, bool TORUS>
