@@ -359,7 +359,7 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
                 uint32_t *dst = wp;
                 const uint32_t *src = wp + 2 * stride;
                 const uint32_t *src_end = wp + p.L * stride;
-#pragma unroll 2
+#pragma unroll 6
                 for (; src < src_end; src += stride, dst += stride) {
                     const uint32_t wnext = *src;
                     row(wd, dst);
