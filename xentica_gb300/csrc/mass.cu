@@ -200,6 +200,17 @@ __device__ __forceinline__ uint32_t xk_get(const uint4 &u, int i)
 // no cell is the wall value and every on-board neighbour counts in the sent
 // sum:  m' = m - q * (#on-board neighbours) + sum_k q_k;  otherwise the exact
 // per-neighbour form of the generic kernel.
+__device__ __forceinline__ uint4 xk_mass_ld4z(const uint32_t *__restrict__ src, uint32_t off, bool ok)
+{
+    uint4 u = make_uint4(0u, 0u, 0u, 0u);
+    if (ok) u = __ldg(reinterpret_cast<const uint4 *>(src + off));
+    return u;
+}
+
+__device__ __forceinline__ uint32_t xk_or4(const uint4 &u) { return u.x | u.y | u.z | u.w; }
+
+__device__ __forceinline__ uint32_t xk_q_small(uint32_t m) { return __umulhi(m, 0x24924925u); }
+
 template <int MINB>
 __global__ void __launch_bounds__(32 * XK_MASS_BY, MINB)
 xk_k_mass_rows(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
@@ -218,87 +229,85 @@ xk_k_mass_rows(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
     const bool hx_ok = in && ((lane == 0 && x0 > 0) || (lane == 31 && x0 + 4 < p.W));
     const int hx_d = lane == 0 ? -1 : 4;
     const bool has_ym = in && y > 0, has_yp = in && y + 1 < p.H;
-    int cxy[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-        cxy[i] = (x0 + i > 0) + (x0 + i + 1 < p.W) + (y > 0) + (y + 1 < p.H);
+    const bool has_xl = x0 > 0, has_xr = x0 + 4 < p.W;   // outside the thread's four cells
+    // on-board x/y neighbours of cells 0 and 3 (cells 1 and 2 have both x neighbours)
+    const int cy = (y > 0) + (y + 1 < p.H);
+    const int c0 = cy + 1 + (int)has_xl, c3 = cy + 1 + (int)has_xr;
 
-    bool big = false;   // this thread has met a cell >= 2^30 in the last three planes
-    bool big_prv = false, big_cur = false;
-    uint4 prv_m = xk_mass_ld4(src, off - plane, in && z0 > 0, wall);
-    uint4 prv_q = xk_mass_q4(prv_m, in && z0 > 0, big_prv);
-    uint4 cur_m = xk_mass_ld4(src, off, in, wall);
-    uint4 cur_q = xk_mass_q4(cur_m, in, big_cur);
-    uint4 nxt_m = xk_mass_ld4(src, off + plane, in && z0 + 1 < p.D, wall);
-    // the rows above and below and the x halo of plane z + 1 are loaded while
-    // plane z is computed
-    uint4 ym_pf = xk_mass_ld4(src, off - p.W, has_ym, wall);
-    uint4 yp_pf = xk_mass_ld4(src, off + p.W, has_yp, wall);
-    uint32_t hx_pf = hx_ok ? __ldg(src + (off + hx_d)) : wall;
+    // Off-board cells load as 0 (their q is 0, nothing comes in from them);
+    // the exact path counts on-board neighbours from the flags above.
+    uint4 prv_m = xk_mass_ld4z(src, off - plane, in && z0 > 0);
+    uint4 cur_m = xk_mass_ld4z(src, off, in);
+    uint4 nxt_m = xk_mass_ld4z(src, off + plane, in && z0 + 1 < p.D);
+    uint4 ym_pf = xk_mass_ld4z(src, off - p.W, has_ym);
+    uint4 yp_pf = xk_mass_ld4z(src, off + p.W, has_yp);
+    uint32_t hx_pf = hx_ok ? __ldg(src + (off + hx_d)) : 0u;
     unsigned long long mass_sum = 0;
     for (int z = z0; z < z1; ++z) {
-        const uint4 nn_m = xk_mass_ld4(src, off + 2 * plane, in && z + 2 < p.D, wall);
+        const uint4 nn_m = xk_mass_ld4z(src, off + 2 * plane, in && z + 2 < p.D);
         const uint4 ym_m = ym_pf, yp_m = yp_pf;
         const uint32_t hx_m = hx_pf;
         const bool more = z + 1 < z1;
-        ym_pf = xk_mass_ld4(src, off + plane - p.W, has_ym && more, wall);
-        yp_pf = xk_mass_ld4(src, off + plane + p.W, has_yp && more, wall);
-        hx_pf = hx_ok && more ? __ldg(src + (off + plane + hx_d)) : wall;
-        bool big_nxt = false, big_y = false;
-        const uint4 nxt_q = xk_mass_q4(nxt_m, in && z + 1 < p.D, big_nxt);
-        const uint4 ym_q = xk_mass_q4(ym_m, has_ym, big_y);
-        const uint4 yp_q = xk_mass_q4(yp_m, has_yp, big_y);
-        const bool hx_big = hx_ok && hx_m >= XK_MASS_SMALL;
-        const uint32_t hx_q = hx_ok ? xk_div7(hx_m, !hx_big) : 0u;
-        big = big_prv || big_cur || big_nxt || big_y || hx_big;
-        uint32_t xl_q = __shfl_up_sync(0xFFFFFFFFu, cur_q.w, 1);
-        uint32_t xr_q = __shfl_down_sync(0xFFFFFFFFu, cur_q.x, 1);
-        if (lane == 0) xl_q = hx_q;
-        if (lane == 31) xr_q = hx_q;
+        ym_pf = xk_mass_ld4z(src, off + plane - p.W, has_ym && more);
+        yp_pf = xk_mass_ld4z(src, off + plane + p.W, has_yp && more);
+        hx_pf = hx_ok && more ? __ldg(src + (off + plane + hx_d)) : 0u;
+        const uint32_t ors = xk_or4(prv_m) | xk_or4(cur_m) | xk_or4(nxt_m) | xk_or4(ym_m) |
+                             xk_or4(yp_m) | hx_m;
         uint32_t out[4];
-        if (!__any_sync(0xFFFFFFFFu, big)) {
+        if (!__any_sync(0xFFFFFFFFu, ors >= XK_MASS_SMALL)) {
+            // every cell the warp reads is below 2^30: no wall value, exact
+            // one-instruction q, every on-board neighbour counts
+            const uint32_t q0 = xk_q_small(cur_m.x), q1 = xk_q_small(cur_m.y);
+            const uint32_t q2 = xk_q_small(cur_m.z), q3 = xk_q_small(cur_m.w);
+            uint32_t xl = xk_q_small(__shfl_up_sync(0xFFFFFFFFu, cur_m.w, 1));
+            uint32_t xr = xk_q_small(__shfl_down_sync(0xFFFFFFFFu, cur_m.x, 1));
+            const uint32_t hq = xk_q_small(hx_m);
+            if (lane == 0) xl = hq;
+            if (lane == 31) xr = hq;
+            if (!has_xl && lane == 0) xl = 0u;
+            if (!has_xr && lane == 31) xr = 0u;
             const int cz = (z > 0) + (z + 1 < p.D);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const uint32_t ql = i == 0 ? xl_q : xk_get(cur_q, i > 0 ? i - 1 : 0);
-                const uint32_t qr = i == 3 ? xr_q : xk_get(cur_q, i < 3 ? i + 1 : 3);
-                const uint32_t s1 = ql + qr + xk_get(ym_q, i);
-                const uint32_t s2 = xk_get(yp_q, i) + xk_get(prv_q, i) + xk_get(nxt_q, i);
-                out[i] = xk_get(cur_m, i) - xk_get(cur_q, i) * (uint32_t)(cxy[i] + cz) + s1 + s2;
-            }
+            const uint32_t vz0 = xk_q_small(prv_m.x) + xk_q_small(nxt_m.x) + xk_q_small(ym_m.x) + xk_q_small(yp_m.x);
+            const uint32_t vz1 = xk_q_small(prv_m.y) + xk_q_small(nxt_m.y) + xk_q_small(ym_m.y) + xk_q_small(yp_m.y);
+            const uint32_t vz2 = xk_q_small(prv_m.z) + xk_q_small(nxt_m.z) + xk_q_small(ym_m.z) + xk_q_small(yp_m.z);
+            const uint32_t vz3 = xk_q_small(prv_m.w) + xk_q_small(nxt_m.w) + xk_q_small(ym_m.w) + xk_q_small(yp_m.w);
+            out[0] = cur_m.x - q0 * (uint32_t)(c0 + cz) + xl + q1 + vz0;
+            out[1] = cur_m.y - q1 * (uint32_t)(cy + 2 + cz) + q0 + q2 + vz1;
+            out[2] = cur_m.z - q2 * (uint32_t)(cy + 2 + cz) + q1 + q3 + vz2;
+            out[3] = cur_m.w - q3 * (uint32_t)(c3 + cz) + q2 + xr + vz3;
             if (in)   // each value < 2^31 here, so pairs sum without overflow
                 mass_sum += (unsigned long long)(out[0] + out[1]) + (unsigned long long)(out[2] + out[3]);
         } else {
-            uint32_t xl_m = __shfl_up_sync(0xFFFFFFFFu, cur_m.w, 1);
-            uint32_t xr_m = __shfl_down_sync(0xFFFFFFFFu, cur_m.x, 1);
-            if (lane == 0) xl_m = hx_ok ? hx_m : wall;
-            if (lane == 31) xr_m = hx_ok ? hx_m : wall;
+            // the reference's arithmetic per neighbour: sent to each on-board
+            // neighbour whose mass is not the wall, its share taken in while
+            // the cell itself is not the wall
+            const uint32_t xl_m = __shfl_up_sync(0xFFFFFFFFu, cur_m.w, 1);
+            const uint32_t xr_m = __shfl_down_sync(0xFFFFFFFFu, cur_m.x, 1);
+            const uint32_t left = lane == 0 ? hx_m : xl_m, right = lane == 31 ? hx_m : xr_m;
+            const bool zm = z > 0, zp = z + 1 < p.D, ym_on = y > 0, yp_on = y + 1 < p.H;
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const uint32_t ml = i == 0 ? xl_m : xk_get(cur_m, i > 0 ? i - 1 : 0);
-                const uint32_t mr = i == 3 ? xr_m : xk_get(cur_m, i < 3 ? i + 1 : 3);
-                const uint32_t ql = i == 0 ? xl_q : xk_get(cur_q, i > 0 ? i - 1 : 0);
-                const uint32_t qr = i == 3 ? xr_q : xk_get(cur_q, i < 3 ? i + 1 : 3);
-                const uint32_t cnt = (uint32_t)(ml != wall) + (uint32_t)(mr != wall) +
-                                     (uint32_t)(xk_get(ym_m, i) != wall) +
-                                     (uint32_t)(xk_get(yp_m, i) != wall) +
-                                     (uint32_t)(xk_get(prv_m, i) != wall) +
-                                     (uint32_t)(xk_get(nxt_m, i) != wall);
-                const uint32_t sq = ql + qr + xk_get(ym_q, i) + xk_get(yp_q, i) +
-                                    xk_get(prv_q, i) + xk_get(nxt_q, i);
                 const uint32_t m = xk_get(cur_m, i);
-                out[i] = m - xk_get(cur_q, i) * cnt + (m != wall ? sq : 0u);
+                const uint32_t ml = i == 0 ? left : xk_get(cur_m, i > 0 ? i - 1 : 0);
+                const uint32_t mr = i == 3 ? right : xk_get(cur_m, i < 3 ? i + 1 : 3);
+                const bool lo = i > 0 || has_xl, ro = i < 3 || has_xr;
+                const uint32_t nb[6] = {ml, mr, xk_get(ym_m, i), xk_get(yp_m, i), xk_get(prv_m, i),
+                                        xk_get(nxt_m, i)};
+                const bool on[6] = {lo, ro, ym_on, yp_on, zm, zp};
+                uint32_t cnt = 0, sq = 0;
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    cnt += (uint32_t)(on[k] && nb[k] != wall);
+                    sq += on[k] ? nb[k] / 7u : 0u;
+                }
+                out[i] = m - (m / 7u) * cnt + (m != wall ? sq : 0u);
             }
             if (in)
                 mass_sum += (unsigned long long)out[0] + out[1] + (unsigned long long)out[2] + out[3];
         }
         if (in) *reinterpret_cast<uint4 *>(dst + off) = make_uint4(out[0], out[1], out[2], out[3]);
         prv_m = cur_m;
-        prv_q = cur_q;
-        big_prv = big_cur;
         cur_m = nxt_m;
-        cur_q = nxt_q;
-        big_cur = big_nxt;
         nxt_m = nn_m;
         off += plane;
     }
