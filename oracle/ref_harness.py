@@ -205,6 +205,10 @@ def run_job(job):
         res["steps"] = np.int64(k)
         np.savez(job["out"], **res)
         return
+    if job.get("load_pickle"):
+        model.load(job["load_pickle"])
+        res["loaded_cells"] = model.gpu.arrays.cells.get()[:n]
+        res["loaded_colors"] = model.gpu.arrays.colors.get()
     viewport = (job.get("render") or {}).get("viewport")
     if viewport:
         model.set_viewport(tuple(viewport))
@@ -220,6 +224,12 @@ def run_job(job):
         res["colors_%d" % cp] = model.gpu.arrays.colors.get()
         if viewport:
             res["img_%d" % cp] = model.render()
+    if job.get("save_pickle"):
+        model.save(job["save_pickle"])
+    if job.get("load_pickle") or job.get("save_pickle"):
+        # the random streams after the load / save: the next draws
+        res["rng_standard"] = np.int64(model.random.standard.getrandbits(32))
+        res["rng_numpy"] = model.random.numpy.randint(0, 2 ** 31 - 1, 4)
     np.savez(job["out"], **res)
 
 

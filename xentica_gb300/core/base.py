@@ -26,7 +26,6 @@ import collections
 import functools
 import itertools
 import operator
-import pickle
 import threading
 from copy import deepcopy
 
@@ -39,6 +38,7 @@ from xentica_gb300.core.mixins import ACTIVE
 from xentica_gb300.core.properties import Property, ContainerProperty
 from xentica_gb300.core.renderers import RendererPlain
 from xentica_gb300.core.exceptions import XenticaException
+from xentica_gb300.utils import compat
 
 __all__ = ['BSCA', 'CellularAutomaton', 'CachedNeighbor']
 
@@ -376,18 +376,19 @@ class CellularAutomaton(Translator, metaclass=BSCA):
             return img.astype(np.uint8)
 
     def save(self, filename):
-        """Save the state (cells, colours, RNG) to ``filename``."""
+        """Save the state (cells, colours, RNG) to ``filename``, in the
+        reference's pickle layout (the reference can load it)."""
         with open(filename, "wb") as ca_file:
             ca_state = {
                 "cells": self.gpu.arrays.cells.get(),
                 "colors": self.gpu.arrays.colors.get(),
                 "random": self.random,
             }
-            pickle.dump(ca_state, ca_file)
+            compat.dump_state(ca_state, ca_file)
 
     def load(self, filename):
-        """Load a state saved by :meth:`save` (or by the reference)."""
+        """Load a state saved by :meth:`save` or by the reference."""
         with open(filename, "rb") as ca_file:
-            ca_state = pickle.load(ca_file)
+            ca_state = compat.load_state(ca_file)
             self.gpu.load(ca_state['cells'], ca_state['colors'])
             self.random.load(ca_state['random'])
