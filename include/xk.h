@@ -38,7 +38,7 @@ enum {
     XK_ERR_INVARIANT = -7     /* a conserved quantity changed              */
 };
 
-enum { XK_FAMILY_LIFE = 1, XK_FAMILY_EVOLIFE = 2, XK_FAMILY_MASS = 3 };
+enum { XK_FAMILY_LIFE = 1, XK_FAMILY_EVOLIFE = 2, XK_FAMILY_MASS = 3, XK_FAMILY_VM = 4 };
 enum { XK_COLOR_NONE = 0, XK_COLOR_PLAIN = 1, XK_COLOR_MOVING_AVERAGE = 2 };
 
 /* Model descriptor filled by the translator (xentica_gb300/core/templates.py)
@@ -113,6 +113,29 @@ int xk_render(xk_model *m, int32_t *host_img, int32_t width, int32_t height,
 /* Mass family: total mass after each of the last xk_step's generations
  * (count = that nsteps); the invariant the configuration checks. */
 int xk_mass_totals(xk_model *m, uint64_t *host_totals, int64_t count);
+
+/* Generic interpreter family (XK_FAMILY_VM): models no hand-written template
+ * implements run their traced emit and absorb programs, compiled to typed
+ * register instructions by xentica_gb300/core/vm.py, with the reference's
+ * execution model -- replaces the emit and absorb kernels the reference
+ * generates for the model (base.py:461-487) and their launches in step()
+ * (base.py:703-728).  The model keeps the reference's layout: N + 1 planes of
+ * state_bytes-wide containers and int32 x 3 colours. */
+typedef struct xk_vm_ins {
+    uint8_t op, ty;               /* opcode and C type (codes of core/vm.py)   */
+    uint16_t dst, a, b, c;        /* registers, or constant / parameter slot,
+                                     load kind / neighbour / plane            */
+    uint16_t reserved;
+} xk_vm_ins;
+#define XK_VM_MAX_REGS 256
+#define XK_VM_MAX_PARAMS 64
+/* which: 0 emit, 1 absorb.  Every instruction is checked against the model
+ * (registers < nregs <= XK_VM_MAX_REGS, slots, planes, neighbours). */
+int xk_vm_load(xk_model *m, int32_t which, const xk_vm_ins *code, int32_t ncode,
+               const uint64_t *consts, int32_t nconsts, int32_t nregs);
+/* Interactive parameter values (64-bit register images), bound at the next
+ * step, as the reference passes them per launch (base.py:717, :722). */
+int xk_vm_set_params(xk_model *m, const uint64_t *values, int32_t count);
 
 /* Wait for all work queued on the model's stream. */
 int xk_sync(xk_model *m);

@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 from xentica_gb300 import core, seeds
+from xentica_gb300.core import color_effects
 from xentica_gb300.bridge.base import Bridge
 from xentica_gb300.core.base import CellularAutomaton
 from xentica_gb300.core.exceptions import XenticaException
@@ -141,10 +142,31 @@ def test_no_init_val():
         Variable()
 
 
+class RawColorEffect(color_effects.ColorEffect):
+    """A colour effect with its own C text, which no GB300 kernel runs."""
+
+    def __call__(self):
+        self.effect = "new_r = new_r ^ 7;"
+        return super().__call__()
+
+
+class RawColorLife(GameOfLife):
+    @RawColorEffect
+    def color(self):
+        return (self.main.state * 255, 0, 0)
+
+
 def test_no_template_raises():
-    # inverting models are not a GB300 kernel family: construction fails loudly
+    # a model no family implements and the interpreter cannot run (C text
+    # of its own) fails loudly at construction
     with pytest.raises(XenticaException, match="No GB300 kernel template"):
-        InvertCA(InvertExperiment)
+        RawColorLife(GOLExperiment)
+
+
+def test_interpreter_takes_other_models():
+    # inverting models are not a hand-written family: the interpreter runs them
+    model = InvertCA(InvertExperiment)
+    assert type(model.gpu.template).__name__ == "VMTemplate"
 
 
 # -- properties (reference tests/core/test_properties.py) -------------------
@@ -409,3 +431,42 @@ def test_template_match_repeated_instances():
     evo = type("E", (BigBangExperiment, ), {"size": (128, 128)})
     for _ in range(2):
         assert type(EvoLife(evo).gpu.template).__name__ == "EvoLifeTemplate"
+
+
+def test_headless_viewer_keys_and_ppm(tmp_path):
+    from xentica_gb300.bridge.headless import HeadlessViewer, write_ppm
+    model = GameOfLife(type("E", (GOLExperiment, ), {"pos": [0, 0]}))
+    viewer = HeadlessViewer(model, (64, 36))
+    zoom, pos = model.zoom, list(model.pos)
+    for key in ("]", "]", "=", "right", "up", "spacebar", "f12", "unbound-key"):
+        viewer.press(key)
+    assert model.speed == 3 and model.zoom == zoom + 1 and model.paused
+    assert model.pos == [(pos[0] + 1) % model.size[0], (pos[1] + 1) % model.size[1]]
+    assert viewer.sysinfo.shown and viewer.running
+    viewer.press("escape")
+    assert not viewer.running
+    assert viewer.run(5) == 0                    # exited: no frame drawn
+    img = np.arange(2 * 3 * 3, dtype=np.uint8).reshape(2, 3, 3)
+    write_ppm(str(tmp_path / "f.ppm"), img)
+    raw = open(str(tmp_path / "f.ppm"), "rb").read()
+    assert raw == b"P6\n3 2\n255\n" + img.tobytes()
+
+
+def test_interpreter_bytecode_reproduces_fixtures(golden):
+    # the compiler's bytecode, run by the NumPy executor (the GPU kernel's
+    # semantics), against the reference's checksums on small fixtures
+    from tests import vm_cpu
+    from tests.models import build_from_job
+    from tests.test_oracle import crc
+    for case in ("gol_33x9", "static_31x5", "gol_color_fade", "gol_plain_color", "rule_highlife",
+                 "mass_24x20x12", "evolife_bigbang_mut_131x101"):
+        entry = golden[case]
+        model = build_from_job(entry["job"])
+        n = model.cells_num
+        fld = np.zeros(n * (len(model.buffers) + 1) + 1, dtype=model.main.dtype)
+        fld[:n] = model.gpu.arrays.cells.get()[:n]
+        col = np.zeros(3 * n, dtype=np.int32)
+        cp = min(int(c) for c in entry["steps"])
+        vm_cpu.step(model, fld, col, cp)
+        assert crc(fld[:n]) == entry["steps"][str(cp)]["cells"], case
+        assert crc(col) == entry["steps"][str(cp)]["colors"], case

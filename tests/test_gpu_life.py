@@ -7,7 +7,6 @@ with the oracle after every step.  Bit-exact throughout.
 """
 import binascii
 import os
-import pickle
 
 import numpy as np
 import pytest
@@ -93,8 +92,9 @@ def test_pause_and_save_load(tmp_path):
     for _ in range(500):
         ca2.step()
     assert binascii.crc32(ca2.gpu.arrays.cells.get()[:ca2.cells_num]) == 2981695958
+    from xentica_gb300.utils import compat
     with open(path, "rb") as fh:
-        state = pickle.load(fh)
+        state = compat.load_state(fh)     # the pickle names the reference's classes
     assert set(state) == {"cells", "colors", "random"}
 
 
@@ -134,3 +134,30 @@ def test_multi_step_equals_single_steps():
         a.step()
     b.gpu.step(64)
     assert np.array_equal(a.gpu.arrays.cells.get(), b.gpu.arrays.cells.get())
+
+
+def test_headless_viewer_frames_vs_oracle(tmp_path):
+    # the GUI loop of the reference without a window: key actions between
+    # frames, speed generations per frame, nothing while paused
+    from xentica_gb300.bridge.headless import HeadlessViewer, ppm_sink
+    # its own experiment: moving the view edits ``pos`` in place, which is the
+    # experiment class's list (as in the reference)
+    model = GameOfLife(type("E", (GOLExperiment, ), {"pos": [0, 0]}))
+    n = model.cells_num
+    init = model.gpu.arrays.cells.get()[:n].copy()
+    viewer = HeadlessViewer(model, (160, 90))
+    frames = []
+    keys = {2: ["]"], 4: ["="], 5: ["right", "up"], 7: ["spacebar"], 9: ["spacebar"],
+            11: ["escape"]}
+    sink = ppm_sink(str(tmp_path))
+    drawn = viewer.run(20, keys, lambda i, img: (frames.append(img), sink(i, img)))
+    assert drawn == 11 and model.timestep == 2 + 5 * 2 + 2 * 2
+    topo = O.Topology(model.size)
+    fld = topo.field(init, np.uint8)
+    col = np.zeros(3 * n, np.int32)
+    O.life_run(topo, fld, col, model.timestep)
+    smooth = model.constants["SMOOTH_FACTOR"].value if model.is_constant("SMOOTH_FACTOR") else 0
+    want = O.render(topo, col, 160, 90, zoom=model.zoom, dx=model.pos[0], dy=model.pos[1],
+                    smooth=smooth)
+    assert np.array_equal(frames[-1].ravel(), want.astype(np.uint8))
+    assert len(os.listdir(str(tmp_path))) == 11

@@ -16,7 +16,7 @@ LIBPATH = os.path.join(HERE, "libxk.so")
 XK_ABI_VERSION = 1
 XK_MAXDIM = 8
 XK_MAXNBR = 32
-XK_FAMILY_LIFE, XK_FAMILY_EVOLIFE, XK_FAMILY_MASS = 1, 2, 3
+XK_FAMILY_LIFE, XK_FAMILY_EVOLIFE, XK_FAMILY_MASS, XK_FAMILY_VM = 1, 2, 3, 4
 XK_COLOR_NONE, XK_COLOR_PLAIN, XK_COLOR_MOVING_AVERAGE = 0, 1, 2
 
 _I32, _U32, _I64, _U64 = ctypes.c_int32, ctypes.c_uint32, ctypes.c_int64, ctypes.c_uint64
@@ -101,6 +101,8 @@ SIGNATURES = {
     "xk_batch_total_cells": (_I64, [_P]),
     "xk_batch_launches": (_I64, [_P, _I32]),
     "xk_batch_step_noalloc": (_I32, [_P, _I32, _P, _P, _P, _I32, _P]),
+    "xk_vm_load": (_I32, [_P, _I32, _P, _I32, _P, _I32, _I32]),
+    "xk_vm_set_params": (_I32, [_P, _P, _I32]),
     "xk_serve_create": (_I32, [_I64, _I64, _I32, _I32, ctypes.POINTER(_P)]),
     "xk_serve_destroy": (_I32, [_P]),
     "xk_serve_request_bytes": (_I32, [ctypes.POINTER(XkRequest), ctypes.POINTER(_I64)]),

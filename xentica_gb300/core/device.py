@@ -76,6 +76,8 @@ class GPU:
                   "xk_model_create")
         self._lib = lib
         self._handle = handle
+        if hasattr(self.template, "after_create"):
+            self.template.after_create(lib, handle)
         self._rule = (desc.rule0, desc.rule1, list(desc.color_lut))
         self._upload(self._host_cells, self._host_colors)
         self._host_cells = None
@@ -101,6 +103,9 @@ class GPU:
 
     def _bind_params(self):
         tpl = self.template
+        if hasattr(tpl, "bind"):
+            tpl.bind(self._lib, self._handle)
+            return
         if not getattr(tpl, "param_names", None):
             return
         rule0, rule1, lut = tpl.rule_for(tpl.current_params())

@@ -16,7 +16,17 @@ Life-like family (``XK_FAMILY_LIFE``)
     only through their sum.  Interactive parameters are re-bound and the rule
     re-extracted whenever their values change (LifelikeCA,
     ``examples/game_of_life.py:183-203``).
+
+EvoLife (``XK_FAMILY_EVOLIFE``) and mass transfer (``XK_FAMILY_MASS``)
+    matched statement by statement against the canonical programs of
+    ``core/canonical.py``.
+
+Interpreter (``XK_FAMILY_VM``)
+    any other model whose programs hold no opaque C text: compiled to
+    register bytecode (``core/vm.py``) and run by the generic kernel.
 """
+import os
+
 import numpy as np
 
 from xentica_gb300 import _native as nat
@@ -329,13 +339,87 @@ class MassTemplate:
         return d
 
 
-FAMILIES = (LifeTemplate, EvoLifeTemplate, MassTemplate)
+class VMTemplate:
+    """Any other traced model: its emit and absorb programs, compiled to
+    register bytecode (``core/vm.py``), run on the generic interpreter kernel
+    with the reference's two-pass execution model and memory layout.  Tried
+    after every hand-written family; needs a plain or moving-average colour
+    and programs without opaque C text."""
+
+    family = nat.XK_FAMILY_VM
+
+    def __init__(self, model):
+        from xentica_gb300.core import vm
+        _topology(model)
+        self.model = model
+        params = []
+        try:
+            self.programs = [vm.compile_program(model.programs[key], params)
+                             for key in ("emit", "absorb")]
+        except XenticaException as exc:
+            raise NoTemplate(str(exc))
+        self.param_names = list(params)
+        color = _color_stmt(model.programs["absorb"])
+        if _color_stmt(model.programs["emit"]) is not None:
+            raise NoTemplate("emit writes a colour")
+        self.color = color
+        if color is not None and color.extra["kind"] not in ("plain", "moving_average"):
+            raise NoTemplate("colour effect %s" % color.extra["kind"])
+        self._bound = None
+
+    def descriptor(self):
+        d = _base_desc(self.model, self.family)
+        if self.color is None:
+            d.color_kind = nat.XK_COLOR_NONE
+        elif self.color.extra["kind"] == "plain":
+            d.color_kind = nat.XK_COLOR_PLAIN
+        else:
+            d.color_kind = nat.XK_COLOR_MOVING_AVERAGE
+            d.fade_in = int(self.color.extra["fade_in"])
+            d.fade_out = int(self.color.extra["fade_out"])
+            d.smooth = int(self.color.extra["smooth"])
+        return d
+
+    def after_create(self, lib, handle):
+        """Load both programs into the new device model."""
+        import ctypes
+        for which, prog in enumerate(self.programs):
+            nat.check(lib.xk_vm_load(handle, which, prog.code.ctypes.data_as(ctypes.c_void_p),
+                                     len(prog.code), prog.consts.ctypes.data_as(ctypes.c_void_p),
+                                     len(prog.consts), prog.nregs), "xk_vm_load")
+        self._bound = None
+
+    def bind(self, lib, handle):
+        """Send the interactive parameters' current values when they changed."""
+        from xentica_gb300.core import vm
+        if not self.param_names:
+            return
+        vals = []
+        for name in self.param_names:
+            param = self.model.meta.__dict__[name]
+            ctype = ir.ctype_of(param.ctype) if hasattr(param, "ctype") else ir.I32
+            vals.append(vm.pack_value(param.value, ctype))
+        if vals == self._bound:
+            return
+        arr = np.array(vals, dtype=np.uint64)
+        nat.check(lib.xk_vm_set_params(handle, nat.ptr(arr), len(arr)), "xk_vm_set_params")
+        self._bound = vals
+
+
+FAMILIES = (LifeTemplate, EvoLifeTemplate, MassTemplate, VMTemplate)
 
 
 def match(model):
-    """Template instance for ``model``; raises :class:`XenticaException`."""
+    """Template instance for ``model``; raises :class:`XenticaException`.
+
+    The hand-written families are tried first, the interpreter last;
+    ``XENTICA_GB300_TEMPLATE=vm`` in the environment runs every model on the
+    interpreter (for comparing the two on the same model)."""
     reasons = []
-    for family in FAMILIES:
+    families = FAMILIES
+    if os.environ.get("XENTICA_GB300_TEMPLATE", "") == "vm":
+        families = (VMTemplate, )
+    for family in families:
         try:
             return family(model)
         except NoTemplate as exc:

@@ -77,7 +77,7 @@ extern "C" int xk_device_info(char *buf, int32_t len)
 // ---------------------------------------------------------------------------
 // model object
 
-enum { LAYOUT_BITS2D = 1, LAYOUT_BYTES = 2, LAYOUT_CELLS64 = 3, LAYOUT_MASS = 4 };
+enum { LAYOUT_BITS2D = 1, LAYOUT_BYTES = 2, LAYOUT_CELLS64 = 3, LAYOUT_MASS = 4, LAYOUT_VM = 5 };
 
 // largest float t with (double)u < p  <=>  u <= t for every float u
 static float below_threshold(double p)
@@ -114,6 +114,12 @@ struct xk_model {
     int cl_tuned = 0, cl_C = 0, cl_R = 0, cl_threads = 0;   // cluster plan (cl_C = 0: none)
     uint32_t rule0 = 0, rule1 = 0;
     int32_t lut[6] = {0, 0, 0, 0, 0, 0};
+    uint8_t *fld = nullptr;      // interpreter: the reference's N + 1 planes
+    xk_vm_ins *vm_code[2] = {nullptr, nullptr};     // emit, absorb
+    uint64_t *vm_consts[2] = {nullptr, nullptr};
+    int vm_ncode[2] = {0, 0};
+    uint64_t *vm_params = nullptr;                  // XK_VM_MAX_PARAMS slots
+    VmGeo vg;
     int hf = 0;                  // colour is a function of the state alone
     int derived = 0;             // colours currently implied by the state
     int uploaded = 0;
@@ -230,6 +236,12 @@ static void free_model(xk_model *m)
         if (m->cells64[i]) cudaFree(m->cells64[i]);
         if (m->cells32[i]) cudaFree(m->cells32[i]);
     }
+    for (int i = 0; i < 2; ++i) {
+        if (m->vm_code[i]) cudaFree(m->vm_code[i]);
+        if (m->vm_consts[i]) cudaFree(m->vm_consts[i]);
+    }
+    if (m->fld) cudaFree(m->fld);
+    if (m->vm_params) cudaFree(m->vm_params);
     if (m->proj) cudaFree(m->proj);
     if (m->totals) cudaFree(m->totals);
     if (m->stage) cudaFree(m->stage);
@@ -278,7 +290,7 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
     const int64_t n = cells_of(d);
     XK_REQUIRE(n <= (1LL << 40), XK_ERR_ARG, "lattice of %lld cells too large", (long long)n);
     XK_REQUIRE(d.family == XK_FAMILY_LIFE || d.family == XK_FAMILY_EVOLIFE ||
-                   d.family == XK_FAMILY_MASS,
+                   d.family == XK_FAMILY_MASS || d.family == XK_FAMILY_VM,
                XK_ERR_UNSUPPORTED, "model family %d is not available in this build", d.family);
     if (d.family == XK_FAMILY_MASS)
         XK_REQUIRE(d.ndim == 3 && d.nbr == 6 && !d.torus && d.state_bytes == 4, XK_ERR_ARG,
@@ -309,7 +321,27 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
     XK_TRY(cudaEventCreate(&m->ev1));
     {
         const int border_state = (int)(d.border_value & 1u);
-        if (d.family == XK_FAMILY_MASS) {
+        if (d.family == XK_FAMILY_VM) {
+            m->layout = LAYOUT_VM;
+            const size_t bytes = (size_t)(d.nbr + 1) * n * d.state_bytes + 16;
+            XK_TRY(cudaMalloc(&m->fld, bytes));
+            XK_TRY(cudaMemsetAsync(m->fld, 0, bytes, m->stream));
+            XK_TRY(cudaMalloc(&m->vm_params, XK_VM_MAX_PARAMS * sizeof(uint64_t)));
+            XK_TRY(cudaMemsetAsync(m->vm_params, 0, XK_VM_MAX_PARAMS * sizeof(uint64_t), m->stream));
+            memset(&m->vg, 0, sizeof(m->vg));
+            m->vg.ndim = d.ndim;
+            m->vg.nbr = d.nbr;
+            m->vg.torus = d.torus;
+            m->vg.esz = d.state_bytes;
+            m->vg.n = n;
+            for (int i = 0; i < d.ndim; ++i) m->vg.size[i] = d.size[i];
+            memcpy(m->vg.delta, d.delta, sizeof(m->vg.delta));
+            m->vg.border = d.border_value;
+            m->vg.color_kind = d.color_kind;
+            m->vg.fade_in = d.fade_in;
+            m->vg.fade_out = d.fade_out;
+            m->vg.smooth = d.smooth;
+        } else if (d.family == XK_FAMILY_MASS) {
             m->layout = LAYOUT_MASS;
             XK_TRY(cudaMalloc(&m->cells32[0], (size_t)n * 4));
             XK_TRY(cudaMalloc(&m->cells32[1], (size_t)n * 4));
@@ -345,7 +377,7 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
             XK_TRY(cudaMalloc(&m->bytes[1], bytes));
             XK_TRY(cudaMemsetAsync(m->bytes[0], 0, bytes, m->stream));
         }
-        if (m->layout != LAYOUT_CELLS64 && m->layout != LAYOUT_MASS)
+        if (m->layout != LAYOUT_CELLS64 && m->layout != LAYOUT_MASS && m->layout != LAYOUT_VM)
             XK_TRY(cudaMalloc(&m->stage, (size_t)n * d.state_bytes + 16));
         XK_TRY(cudaMalloc(&m->col, (size_t)n * 3 * sizeof(int32_t)));
         XK_TRY(cudaMemsetAsync(m->col, 0, (size_t)n * 3 * sizeof(int32_t), m->stream));
@@ -375,8 +407,9 @@ extern "C" int xk_upload(xk_model *m, const void *host_main, int64_t ncells)
     XK_REQUIRE(ncells == m->n, XK_ERR_ARG, "xk_upload: %lld cells given, model has %lld",
                (long long)ncells, (long long)m->n);
     const int esz = m->d.state_bytes;
-    if (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_MASS) {
-        void *dst = m->layout == LAYOUT_MASS ? (void *)m->cells32[m->cur] : (void *)m->cells64[m->cur];
+    if (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_MASS || m->layout == LAYOUT_VM) {
+        void *dst = m->layout == LAYOUT_MASS ? (void *)m->cells32[m->cur]
+                    : m->layout == LAYOUT_VM ? (void *)m->fld : (void *)m->cells64[m->cur];
         XK_CUDA(cudaMemcpyAsync(dst, host_main, (size_t)m->n * esz, cudaMemcpyHostToDevice,
                                 m->stream));
         XK_CUDA(cudaStreamSynchronize(m->stream));
@@ -409,8 +442,9 @@ extern "C" int xk_download(xk_model *m, void *host_main, int64_t ncells)
     XK_REQUIRE(ncells == m->n, XK_ERR_ARG, "xk_download: %lld cells given, model has %lld",
                (long long)ncells, (long long)m->n);
     const int esz = m->d.state_bytes;
-    if (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_MASS) {
+    if (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_MASS || m->layout == LAYOUT_VM) {
         const void *src = m->layout == LAYOUT_MASS ? (const void *)m->cells32[m->cur]
+                          : m->layout == LAYOUT_VM ? (const void *)m->fld
                                                    : (const void *)m->cells64[m->cur];
         XK_CUDA(cudaMemcpyAsync(host_main, src, (size_t)m->n * esz, cudaMemcpyDeviceToHost,
                                 m->stream));
@@ -430,6 +464,7 @@ extern "C" int xk_download(xk_model *m, void *host_main, int64_t ncells)
 // write the colours implied by the state into m->col
 static int materialize_colors(xk_model *m)
 {
+    if (m->layout == LAYOUT_VM) return XK_OK;   // absorb writes the colours
     if (m->layout == LAYOUT_MASS) {
         XK_CUDA(xk_mass_colors(m->cells32[m->cur], m->col, m->n, m->stream));
         return XK_OK;
@@ -518,6 +553,19 @@ extern "C" int xk_step(xk_model *m, int64_t nsteps)
     XK_REQUIRE(nsteps >= 0, XK_ERR_ARG, "xk_step: negative step count");
     XK_REQUIRE(m->uploaded, XK_ERR_STATE, "xk_step before xk_upload");
     if (nsteps == 0) return XK_OK;
+    if (m->layout == LAYOUT_VM) {
+        XK_CUDA(cudaEventRecord(m->ev0, m->stream));
+        for (int64_t g = 0; g < nsteps; ++g)
+            for (int w = 0; w < 2; ++w)
+                XK_CUDA(xk_vm_run(m->vm_code[w], m->vm_ncode[w], m->vm_consts[w], m->vm_params,
+                                  m->fld, m->col, m->vg, m->stream));
+        XK_CUDA(cudaEventRecord(m->ev1, m->stream));
+        XK_CUDA(cudaEventSynchronize(m->ev1));
+        float ms = 0.f;
+        XK_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+        xk_set_last_step_ms(ms);
+        return XK_OK;
+    }
     if (m->layout == LAYOUT_MASS) {
         if (nsteps > m->totals_cap) {
             if (m->totals) cudaFree(m->totals);
@@ -713,5 +761,72 @@ extern "C" int xk_range_push(const char *name)
 extern "C" int xk_range_pop(void)
 {
     nvtxRangePop();
+    return XK_OK;
+}
+
+// opcodes and type codes of the interpreter (csrc/vm.cu, core/vm.py)
+static bool vm_check(const xk_model *m, const xk_vm_ins &in, int nconsts, int nregs, int pc)
+{
+    const int op = in.op;
+    auto reg = [&](int r) { return r >= 0 && r < nregs; };
+    if (in.ty > 8) return false;
+    switch (op) {
+    case 1: return reg(in.dst) && in.a < nconsts;                      // const
+    case 2: return reg(in.dst) && in.a < XK_VM_MAX_PARAMS;             // param
+    case 3:                                                            // load
+        if (!reg(in.dst) || in.a > 3 || in.c > m->d.nbr) return false;
+        return in.a < 2 || in.b < m->d.nbr;
+    case 4: case 30: case 31: case 32: case 41: case 42: case 50: case 51:
+        return reg(in.dst) && reg(in.a);
+    case 5: return reg(in.dst) && reg(in.a) && in.b <= 8;               // cvt
+    case 40: return reg(in.dst) && reg(in.a) && reg(in.b) && reg(in.c); // select
+    case 60: return reg(in.a) && in.b <= m->d.nbr;                     // store
+    case 61: return reg(in.a) && reg(in.b) && reg(in.c);               // colour
+    default:
+        if (op >= 10 && op <= 25) return reg(in.dst) && reg(in.a) && reg(in.b);
+        (void)pc;
+        return false;
+    }
+}
+
+extern "C" int xk_vm_load(xk_model *m, int32_t which, const xk_vm_ins *code, int32_t ncode,
+                          const uint64_t *consts, int32_t nconsts, int32_t nregs)
+{
+    XK_REQUIRE(m && (code || ncode == 0) && consts, XK_ERR_ARG, "xk_vm_load: null argument");
+    XK_REQUIRE(m->layout == LAYOUT_VM, XK_ERR_STATE, "xk_vm_load: not an interpreter model");
+    XK_REQUIRE(which == 0 || which == 1, XK_ERR_ARG, "xk_vm_load: program %d", which);
+    XK_REQUIRE(ncode >= 0 && nconsts >= 1 && nregs >= 1 && nregs <= XK_VM_MAX_REGS, XK_ERR_ARG,
+               "xk_vm_load: %d instructions, %d constants, %d registers", ncode, nconsts, nregs);
+    for (int pc = 0; pc < ncode; ++pc)
+        XK_REQUIRE(vm_check(m, code[pc], nconsts, nregs, pc), XK_ERR_ARG,
+                   "xk_vm_load: instruction %d (opcode %d) is malformed", pc, code[pc].op);
+    if (m->vm_code[which]) cudaFree(m->vm_code[which]);
+    if (m->vm_consts[which]) cudaFree(m->vm_consts[which]);
+    m->vm_code[which] = nullptr;
+    m->vm_consts[which] = nullptr;
+    m->vm_ncode[which] = 0;
+    if (ncode > 0) {
+        XK_CUDA(cudaMalloc(&m->vm_code[which], (size_t)ncode * sizeof(xk_vm_ins)));
+        XK_CUDA(cudaMemcpyAsync(m->vm_code[which], code, (size_t)ncode * sizeof(xk_vm_ins),
+                                cudaMemcpyHostToDevice, m->stream));
+    }
+    XK_CUDA(cudaMalloc(&m->vm_consts[which], (size_t)nconsts * sizeof(uint64_t)));
+    XK_CUDA(cudaMemcpyAsync(m->vm_consts[which], consts, (size_t)nconsts * sizeof(uint64_t),
+                            cudaMemcpyHostToDevice, m->stream));
+    XK_CUDA(cudaStreamSynchronize(m->stream));
+    m->vm_ncode[which] = ncode;
+    return XK_OK;
+}
+
+extern "C" int xk_vm_set_params(xk_model *m, const uint64_t *values, int32_t count)
+{
+    XK_REQUIRE(m && (values || count == 0), XK_ERR_ARG, "xk_vm_set_params: null argument");
+    XK_REQUIRE(m->layout == LAYOUT_VM, XK_ERR_STATE, "xk_vm_set_params: not an interpreter model");
+    XK_REQUIRE(count >= 0 && count <= XK_VM_MAX_PARAMS, XK_ERR_ARG, "xk_vm_set_params: %d values",
+               count);
+    if (count == 0) return XK_OK;
+    XK_CUDA(cudaMemcpyAsync(m->vm_params, values, (size_t)count * sizeof(uint64_t),
+                            cudaMemcpyHostToDevice, m->stream));
+    XK_CUDA(cudaStreamSynchronize(m->stream));
     return XK_OK;
 }

@@ -128,6 +128,19 @@ cudaError_t xk_render_colors(const int32_t *col, int32_t *img, const RenderGeo &
 
 int xk_sm_count();
 
+// generic interpreter (vm.cu)
+struct VmGeo {
+    int32_t ndim, nbr, torus, esz;
+    int64_t n;
+    int64_t size[XK_MAXDIM];
+    int8_t delta[XK_MAXNBR][XK_MAXDIM];
+    uint64_t border;             // static border: the whole off-board container
+    int32_t color_kind, fade_in, fade_out, smooth;
+};
+cudaError_t xk_vm_run(const xk_vm_ins *code, int ncode, const uint64_t *consts,
+                      const uint64_t *params, uint8_t *fld, int32_t *col, const VmGeo &g,
+                      cudaStream_t s);
+
 // EvoLife family (evolife.cu)
 cudaError_t xk_evolife_set_positional(const double *lut54);
 cudaError_t xk_evolife_step(const uint64_t *src, uint64_t *dst, int32_t *col, const xk_desc &d,
