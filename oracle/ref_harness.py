@@ -175,6 +175,11 @@ def bind_kernels(model, lib, threads):
 
 
 def run_job(job):
+    if job.get("py_random_seed") is not None:
+        # some example experiments draw from Python's global random stream when
+        # their module is imported; seed it so two processes build the same
+        import random
+        random.seed(job["py_random_seed"])
     model_cls = _load_obj(job["model"])
     exp_cls = _load_obj(job["experiment"])
     overrides = dict(job.get("exp_overrides", {}))

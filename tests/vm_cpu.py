@@ -135,13 +135,16 @@ def unary(op, ty, a):
 class Lattice:
     """Coordinates, neighbour indices and the static border of a model."""
 
-    def __init__(self, model):
-        self.n = model.cells_num
-        self.size = tuple(model.size)
-        deltas = model.topology.neighborhood.deltas
-        border = model.topology.border
-        self.torus = not hasattr(border, "value")
-        self.border = 0 if self.torus else int(border.value)
+    def __init__(self, model=None, size=None, deltas=None, torus=True, border=0):
+        if model is not None:
+            size = tuple(model.size)
+            deltas = model.topology.neighborhood.deltas
+            torus = not hasattr(model.topology.border, "value")
+            border = 0 if torus else int(model.topology.border.value)
+        self.size = tuple(int(s) for s in size)
+        self.n = int(np.prod(self.size))
+        self.torus = bool(torus)
+        self.border = int(border)
         idx = np.arange(self.n, dtype=np.int64)
         coords, rest = [], idx
         for s in self.size:
@@ -233,3 +236,19 @@ def step(model, fld, col, steps=1, params=None):
     for _ in range(steps):
         for p in progs:
             run(p, fld, col, lat, esz, vals, color)
+
+
+def replay(desc, programs, params, fld, col, steps):
+    """Run stored programs (``[(code, consts, nregs), ...]``) for a model
+    described by an ``XkDesc`` (as the GPU interpreter would)."""
+    size = [desc.size[i] for i in range(desc.ndim)]
+    deltas = [[desc.delta[k][i] for i in range(desc.ndim)] for k in range(desc.nbr)]
+    lat = Lattice(size=size, deltas=deltas, torus=desc.torus, border=desc.border_value)
+    color = None
+    if desc.color_kind == 2:
+        color = {"kind": "moving_average", "fade_in": desc.fade_in, "fade_out": desc.fade_out,
+                 "smooth": desc.smooth}
+    progs = [vm.VmProgram(code, consts, nregs, [], False) for code, consts, nregs in programs]
+    for _ in range(steps):
+        for p in progs:
+            run(p, fld, col, lat, fld.dtype.itemsize, list(params), color)
