@@ -14,15 +14,14 @@
 // round-to-nearest with no contraction (__fdiv_rn, __fmul_rn, __fadd_rn).
 #include <string.h>
 
+#include <mutex>
+
 #include "xk_internal.cuh"
 
 // GenomeColor.positional weights (double) per gene and channel
 __constant__ double c_evo_pos[18 * 3];
 
 __device__ __forceinline__ uint32_t xk_lcg(uint32_t x) { return (x * 58321u + 11113u) % 65535u; }
-
-// the uniform draw (float)x / 65535 of RandomProperty.uniform
-__device__ __forceinline__ float xk_uniform(uint32_t x) { return __fdiv_rn((float)x, 65535.0f); }
 
 // float -> unsigned int as the GPU converts: truncation, NaN -> 0
 __device__ __forceinline__ uint32_t xk_f2u(float v) { return __float2uint_rz(v); }
@@ -102,15 +101,70 @@ __device__ __forceinline__ void xk_evo_color_positional(uint32_t rule, uint32_t 
     rgb[2] = (int)xk_f2u(__fmul_rn(blue, (float)e));
 }
 
+// The random draws of the crossover are u(x) = RN(x / 65535) of the 16-bit
+// state x in [0, 65534]: a parent index trunc(RN(u(x) * n)) for n parents,
+// the start gene trunc(RN(u(x) * 18)) % 8, and a mutation iff u(x) <= t.
+// For each n (and 18) there is a multiplier K with floor(x * K / 2^32) equal
+// to the float expression for every x -- found once per process on the host
+// by trying multipliers near n * 2^32 / 65535 against all 65535 states with
+// the same IEEE single-precision operations -- so a draw is one umulhi.  The
+// mutation test is monotonic in x: x <= mut_x.
 struct EvoParams {
     int32_t W, H;
     uint32_t death_speed, max_genes;
-    float mut_thresh;          // mutated iff uniform <= mut_thresh ((double)u < p exactly)
+    int32_t mut_x;             // largest x with u(x) <= t (-1: none)
     int32_t mutation;          // mutation_prob > 0
     int32_t positional;
     int32_t color_kind;        // XK_COLOR_*
     int32_t fade_in, fade_out, smooth;
+    uint32_t kmul[9];          // parent draw for 0..8 parents (0: none)
+    uint32_t kstart;           // start-gene draw (n = 18)
 };
+
+static float evo_u(uint32_t x) { return (float)x / 65535.0f; }
+
+// K with floor(x * K / 2^32) == trunc(RN(u(x) * n)) for all x in [0, 65534]
+static uint32_t evo_find_multiplier(uint32_t n)
+{
+    static uint32_t want[65535];
+    for (uint32_t x = 0; x < 65535; ++x) want[x] = (uint32_t)(evo_u(x) * (float)n);
+    const uint64_t base = ((uint64_t)n << 32) / 65535;
+    for (uint64_t d = 0; d < 65536; ++d)
+        for (int sign = 0; sign < 2; ++sign) {
+            const int64_t k = (int64_t)base + (sign ? -(int64_t)d : (int64_t)d);
+            if (k <= 0 || k > 0xFFFFFFFFLL) continue;
+            bool ok = true;
+            for (uint32_t x = 0; x < 65535 && ok; ++x)
+                ok = (uint32_t)(((uint64_t)x * (uint64_t)k) >> 32) == want[x];
+            if (ok) return (uint32_t)k;
+        }
+    return 0;   // not reached for n <= 18 (checked by the EvoLife GPU tests)
+}
+
+static std::once_flag g_evo_once;
+static uint32_t g_evo_k[9], g_evo_kstart;
+
+static void evo_draws(EvoParams &p, float mut_thresh)
+{
+    std::call_once(g_evo_once, [] {
+        g_evo_k[0] = 0;
+        for (uint32_t n = 1; n <= 8; ++n) g_evo_k[n] = evo_find_multiplier(n);
+        g_evo_kstart = evo_find_multiplier(18);
+    });
+    memcpy(p.kmul, g_evo_k, sizeof(p.kmul));
+    p.kstart = g_evo_kstart;
+    if (!(evo_u(0) <= mut_thresh)) {
+        p.mut_x = -1;
+        return;
+    }
+    uint32_t lo = 0, hi = 65534;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) / 2;
+        if (evo_u(mid) <= mut_thresh) lo = mid;
+        else hi = mid - 1;
+    }
+    p.mut_x = (int32_t)lo;
+}
 
 #define XK_EVO_BX 32
 #define XK_EVO_BY 8
@@ -170,20 +224,20 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
     const uint32_t old_rule = rule, old_energy = energy;
     // genome_crossover(main, 18, *genomes, max_genes, mutation_prob)
     rng = xk_lcg(rng);
-    const uint32_t start_gene = xk_f2u(__fmul_rn(xk_uniform(rng), 18.0f)) % 8u;
-    const float nf = (float)n;
+    const uint32_t start_gene = __umulhi(rng, p.kstart) % 8u;
+    const uint32_t kn = p.kmul[n];
     uint32_t new_genome = 0, num_active = 0;
     uint32_t gene = start_gene;
     for (int step = 0; step < 18; ++step) {
         rng = xk_lcg(rng);
-        const uint32_t winner = xk_f2u(__fmul_rn(xk_uniform(rng), nf));
+        const uint32_t winner = __umulhi(rng, kn);
         uint32_t new_gene = (winner < n) ? ((gsm[winner][tid] >> gene) & 1u) : 0u;
         num_active += new_gene;
         new_gene *= (uint32_t)(num_active <= p.max_genes);
         uint32_t mutated = 0;
         if (p.mutation) {
             rng = xk_lcg(rng);
-            mutated = (uint32_t)(xk_uniform(rng) <= p.mut_thresh) & ((any >> gene) & 1u);
+            mutated = (uint32_t)((int32_t)rng <= p.mut_x) & ((any >> gene) & 1u);
         }
         new_genome += (new_gene ^ mutated) << gene;
         gene = gene == 17 ? 0 : gene + 1;
@@ -226,13 +280,13 @@ cudaError_t xk_evolife_step(const uint64_t *src, uint64_t *dst, int32_t *col, co
     p.H = (int32_t)d.size[1];
     p.death_speed = d.death_speed;
     p.max_genes = d.max_genes;
-    p.mut_thresh = mut_thresh;
     p.mutation = d.mutation_prob > 0.0;
     p.positional = d.positional;
     p.color_kind = d.color_kind;
     p.fade_in = d.fade_in;
     p.fade_out = d.fade_out;
     p.smooth = d.smooth;
+    evo_draws(p, mut_thresh);
     dim3 block(XK_EVO_BX, XK_EVO_BY);
     dim3 grid((p.W + XK_EVO_BX - 1) / XK_EVO_BX, (p.H + XK_EVO_BY - 1) / XK_EVO_BY);
     xk_k_evolife<<<grid, block, 0, s>>>(src, dst, col, p);
