@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--load", type=float, default=0.7,
                     help="serve: offered load as a fraction of the measured capacity")
     ap.add_argument("--quantum", type=int, default=128, help="serve: generations per round")
+    ap.add_argument("--sweep", default="", help="serve: extra offered loads after the main run, "
+                                                "comma-separated (e.g. 0.3,0.5,0.9)")
     ap.add_argument("--serve-budget-gb", type=int, default=16, help="serve: HBM budget (GiB)")
     ap.add_argument("--workload", choices=("ensemble", "life512", "evolife", "mass", "serve"),
                     default="ensemble",
@@ -679,47 +681,63 @@ def run_serve(args, dist):
     t0 = time.perf_counter()
     run_batch(probe)
     capacity = sum(work[i] for i in probe) / (time.perf_counter() - t0)
-    rate = args.load * capacity / (sum(work) / len(work))
-    arrivals = serve.poisson_arrivals(rate, len(specs), seed=args.seed + 17)
-    handles = [None] * len(specs)
-    launches0 = srv.stats()["launches"]
+    mean_work = sum(work) / len(work)
+
+    def open_loop(load, seed):
+        """Poisson arrivals offering ``load`` x capacity; returns the stats."""
+        rate = load * capacity / mean_work
+        arrivals = serve.poisson_arrivals(rate, len(specs), seed=seed)
+        handles = [None] * len(specs)
+        launches0 = srv.stats()["launches"]
+        dist.barrier()
+        start = time.perf_counter()
+
+        def submitter():
+            for i in range(len(specs)):
+                delay = start + arrivals[i] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                handles[i] = srv.submit(specs[i]["kind"], cells[i], specs[i]["rule"],
+                                        specs[i]["generations"])
+
+        th = threading.Thread(target=submitter)
+        th.start()
+        infos = []
+        for i in range(len(specs)):
+            while handles[i] is None:
+                time.sleep(0.0005)
+            handles[i].result(timeout=1800)
+            infos.append(handles[i].info())
+        th.join()
+        dist.barrier()
+        first = min(inf["submit_s"] for inf in infos)
+        last = max(inf["done_s"] for inf in infos)
+        span = dist.max(last - first)
+        lat = [inf["done_s"] - inf["submit_s"] for inf in infos]
+        return {"offered_load": load, "rate_per_s": rate,
+                "value": sum(work) * dist.world / span, "span_s": span,
+                "latency_s": serve.latency_summary(lat),
+                "admission_wait_s": serve.latency_summary(
+                    [inf["admit_s"] - inf["submit_s"] for inf in infos]),
+                # latency over the request's own work at the measured capacity
+                "slowdown": serve.latency_summary(
+                    [l * capacity / w for l, w in zip(lat, work)]),
+                "launches": srv.stats()["launches"] - launches0}
+
     clocks = Clocks(dist.local)
     time.sleep(0.6)
-    dist.barrier()
-    start = time.perf_counter()
-
-    def submitter():
-        for i in range(len(specs)):
-            delay = start + arrivals[i] - time.perf_counter()
-            if delay > 0:
-                time.sleep(delay)
-            handles[i] = srv.submit(specs[i]["kind"], cells[i], specs[i]["rule"],
-                                    specs[i]["generations"])
-
-    th = threading.Thread(target=submitter)
-    th.start()
-    infos = []
-    for i in range(len(specs)):
-        while handles[i] is None:
-            time.sleep(0.0005)
-        handles[i].result(timeout=1800)
-        infos.append(handles[i].info())
-    th.join()
-    dist.barrier()
+    main_run = open_loop(args.load, args.seed + 17)
     clk = clocks.stop()
+    sweep = [open_loop(float(v), args.seed + 17 + k)
+             for k, v in enumerate(args.sweep.split(",")) if v.strip()] if args.sweep else []
     st = srv.stats()
     srv.close()
-    first = min(inf["submit_s"] for inf in infos)
-    last = max(inf["done_s"] for inf in infos)
-    span = dist.max(last - first)
-    value = sum(work) * dist.world / span
-    lat = serve.latency_summary([inf["done_s"] - inf["submit_s"] for inf in infos])
-    wait = serve.latency_summary([inf["admit_s"] - inf["submit_s"] for inf in infos])
+    value = main_run["value"]
     h2d = sum(c.nbytes for c in cells)
     kinds = {k: sum(1 for sp in specs if sp["kind"] == k) for k in ("life2d", "life3d", "mass")}
     line = {"metric": "cell-updates/s (serving, Poisson arrivals)", "value": value,
             "unit": "cell-updates/s", "n_gpus": dist.world, "steps": len(specs),
-            "warmup": len(small), "ms_per_step": span * 1000 / len(specs),
+            "warmup": len(small), "ms_per_step": main_run["span_s"] * 1000 / len(specs),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u32",
             "data": "synthetic (seeded request mix)",
             "config": {"workload": "serving: %d requests %s, 2-D sides log-uniform [32, 4096], "
@@ -727,13 +745,16 @@ def run_serve(args, dist):
                                    "[100, 10000], Poisson arrivals" % (len(specs), kinds),
                        "quantum": args.quantum, "budget_gib": args.serve_budget_gb,
                        "l2": "state per request up to 67 MB; no flush"},
-            "rate_per_s": rate, "offered_load": args.load, "capacity_probe": capacity,
-            "latency_s": lat, "admission_wait_s": wait,
+            "rate_per_s": main_run["rate_per_s"], "offered_load": args.load,
+            "capacity_probe": capacity, "latency_s": main_run["latency_s"],
+            "admission_wait_s": main_run["admission_wait_s"], "slowdown": main_run["slowdown"],
+            "sweep": [{k: r[k] for k in ("offered_load", "rate_per_s", "value", "latency_s",
+                                          "slowdown")} for r in sweep],
             "device_bytes_peak": st["device_bytes_peak"],
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d / len(specs),
                     "d2h_bytes_per_step": h2d / len(specs),
                     "note": "requests enter and leave through host memory"},
-            "gpu_launches": st["launches"] - launches0, "roofline": None, "clocks": clk}
+            "gpu_launches": main_run["launches"], "roofline": None, "clocks": clk}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
 
