@@ -11,8 +11,10 @@ flush is needed between steps.
 Reported (one JSON line on rank 0):
   value   cell-updates/s over the K timed steps, device time (CUDA events on
           the launching stream), inputs resident in HBM;
-  e2e     the same through ``xk_batch_run`` with pinned host buffers: the host
-          -> device copy of the cells, 256 generations, and the copy back;
+  e2e     the same through ``xk_batch_run`` with pinned host buffers: every
+          cell crosses the host link in and out inside the timed region (the
+          largest lattices by the copy engines around their launches, the
+          others read and written by their kernels), 256 generations between;
   plain   the same lattices with one launch per lattice per generation;
   roofline, cpu_baseline, clocks, gpu_launches as the benchmark contract asks.
 

@@ -166,7 +166,13 @@ int xk_batch_step(xk_batch *b, int32_t generations);
 /* Plain form: one launch per instance per generation, reference layout
  * (one byte per cell), for comparison. */
 int xk_batch_step_plain(xk_batch *b, int32_t generations);
-/* End to end: upload host_in, run, download into host_out. */
+/* End to end: host_in -> `generations` -> host_out (host_in == host_out is
+ * allowed); the result is also left as the batch's device state.  When both
+ * buffers are page-locked (xk_host_register, cudaHostAlloc), lattices whose
+ * CTA fills an SM are copied in and out by the copy engines around their
+ * launches and every other lattice is read and written by its kernel over
+ * the host link; pageable buffers are copied in overlapped chunks
+ * (XK_E2E=chunks in the environment forces that form). */
 int xk_batch_run(xk_batch *b, const uint8_t *host_in, uint8_t *host_out,
                  int64_t total_cells, int32_t generations);
 /* Autotune the batched kernel's block size for this batch (timed on device). */
@@ -280,7 +286,8 @@ int xk_arena_destroy(xk_arena *a);
 
 /* Select the CUDA device for handles created afterwards on this thread. */
 int xk_set_device(int32_t device);
-/* Page-lock (pin) caller-owned host memory for fast copies, and release it. */
+/* Page-lock (pin) caller-owned host memory for fast copies and for kernels
+ * to read and write (mapped, portable), and release it. */
 int xk_host_register(void *ptr, int64_t bytes);
 int xk_host_unregister(void *ptr);
 

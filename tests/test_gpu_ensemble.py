@@ -87,3 +87,66 @@ def test_workload_generator_subsample():
     got = ens.download()
     want = _oracle(ens, cells, 5)
     assert np.array_equal(got, want)
+
+
+def _resident_ensemble(seed=5):
+    """Every lattice fits a CTA (no plain-path member), so ``run`` takes the
+    mapped or the pipelined form."""
+    sizes = [s for s in SIZES if s[0] <= 1024]
+    rng = np.random.RandomState(seed)
+    ens = Ensemble([w for w, _ in sizes], [h for _, h in sizes],
+                   [int(r) for r in rng.randint(0, 2 ** 18, len(sizes))])
+    cells = (rng.random_sample(ens.total_cells) < 0.35).astype(np.uint8)
+    return ens, cells
+
+
+@pytest.mark.parametrize("form", ["default", "chunks"])
+@pytest.mark.parametrize("buffers", ["pinned", "pinned-unaligned", "pinned-inplace", "pageable"])
+def test_end_to_end_forms(form, buffers, monkeypatch):
+    """Both forms of ``run`` (on page-locked buffers: the largest lattices
+    copied around their launches, the others read and written by the kernels
+    through the mapping; XK_E2E=chunks or pageable buffers: index-order
+    chunks) on page-locked buffers (also at an odd offset inside a registered
+    block, and in place) and on pageable ones give the oracle's cells and
+    leave them on the device."""
+    from xentica_gb300 import _native as nat
+    monkeypatch.setenv("XK_E2E", form)
+    ens, cells = _resident_ensemble()
+    want = _oracle(ens, cells, 13)
+    n = ens.total_cells
+    bufs = []
+    if buffers == "pageable":
+        src, dst = cells.copy(), np.zeros(n, dtype=np.uint8)
+    else:
+        skew = 17 if buffers == "pinned-unaligned" else 0
+        bufs = [nat.PinnedBuffer(n + 64), nat.PinnedBuffer(n + 64)]
+        src = bufs[0].array[skew:skew + n]
+        dst = src if buffers == "pinned-inplace" else bufs[1].array[skew:skew + n]
+        src[:] = cells
+        if dst is not src:
+            dst[:] = 0
+    ens.upload(cells)
+    ens.step(2)          # a captured step first, as a caller may do
+    ens.run(src, dst, 13)
+    for i in range(ens.count):
+        assert np.array_equal(ens.lattice(dst, i), ens.lattice(want, i)), "lattice %d" % i
+    assert np.array_equal(ens.download(), want)
+    out0 = np.zeros(n, dtype=np.uint8)
+    ens.run(want, out0, 0)
+    assert np.array_equal(out0, want)
+    for b in bufs:
+        b.release()
+
+
+@pytest.mark.parametrize("form", ["default", "chunks"])
+def test_end_to_end_rejects_non_binary_cells(form, monkeypatch):
+    from xentica_gb300 import _native as nat
+    monkeypatch.setenv("XK_E2E", form)
+    ens, cells = _resident_ensemble()
+    cells[3] = 2
+    pin_in, pin_out = nat.PinnedBuffer(ens.total_cells), nat.PinnedBuffer(ens.total_cells)
+    pin_in.array[:] = cells
+    with pytest.raises(XenticaException, match="0 or 1"):
+        ens.run(pin_in.array, pin_out.array, 3)
+    pin_in.array[3] = 1
+    ens.run(pin_in.array, pin_out.array, 3)   # the flag was cleared

@@ -51,6 +51,24 @@ struct xk_batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, fork = nullptr;
     std::vector<cudaEvent_t> joins;
     std::map<int, cudaGraphExec_t> graphs;
+    // end-to-end pipeline (xk_batch_run): instances cut into chunks of
+    // consecutive lattices; per chunk and class a run of descriptors
+    std::vector<int> cls_of;       // class of each instance (-1: plain path)
+    std::vector<int> chunk_first;  // chunk k = instances [chunk_first[k], chunk_first[k + 1])
+    std::vector<std::vector<std::pair<int, int>>> seg;   // [chunk][class] -> (first, count)
+    LifeInst *d_pipe = nullptr;
+    cudaStream_t out_stream = nullptr;
+    std::vector<cudaStream_t> pipe_streams;  // one per chunk: its class launches
+    std::vector<cudaEvent_t> pev;  // per chunk: input landed, generations done
+    // end to end on page-locked buffers: classes whose CTA has its SM to
+    // itself run from device memory in groups (staged by the copy engines);
+    // the others read and write the host buffers from the kernel (mapped)
+    bool e2e_planned = false;
+    std::vector<int> stage_cls, stage_first, stage_count;   // groups, as runs of h_inst
+    std::vector<int> mapped_cls;
+    std::vector<cudaStream_t> stage_streams;               // high priority
+    std::vector<cudaEvent_t> sev;                          // per group: landed, done
+    cudaEvent_t staged_in = nullptr;
 };
 
 static void destroy_graphs(xk_batch *b)
@@ -59,10 +77,35 @@ static void destroy_graphs(xk_batch *b)
     b->graphs.clear();
 }
 
+static void free_pipeline(xk_batch *b)
+{
+    for (auto e : b->pev) cudaEventDestroy(e);
+    b->pev.clear();
+    for (auto st : b->pipe_streams) cudaStreamDestroy(st);
+    b->pipe_streams.clear();
+    for (auto e : b->sev) cudaEventDestroy(e);
+    b->sev.clear();
+    for (auto st : b->stage_streams) cudaStreamDestroy(st);
+    b->stage_streams.clear();
+    if (b->staged_in) cudaEventDestroy(b->staged_in);
+    b->staged_in = nullptr;
+    b->stage_cls.clear();
+    b->stage_first.clear();
+    b->stage_count.clear();
+    b->mapped_cls.clear();
+    b->e2e_planned = false;
+    if (b->d_pipe) cudaFree(b->d_pipe);
+    b->d_pipe = nullptr;
+    b->seg.clear();
+    b->chunk_first.clear();
+}
+
 static void free_batch(xk_batch *b)
 {
     if (!b) return;
     destroy_graphs(b);
+    free_pipeline(b);
+    if (b->out_stream) cudaStreamDestroy(b->out_stream);
     for (auto &c : b->classes)
         if (c.stream) cudaStreamDestroy(c.stream);
     for (auto e : b->joins) cudaEventDestroy(e);
@@ -84,6 +127,8 @@ static inline uint32_t rule1_of(uint32_t golly) { return (golly & 511u) | ((goll
 static int plan_classes(xk_batch *b)
 {
     destroy_graphs(b);
+    free_pipeline(b);
+    b->cls_of.assign(b->n, -1);
     for (auto &c : b->classes)
         if (c.stream) cudaStreamDestroy(c.stream);
     for (auto e : b->joins) cudaEventDestroy(e);
@@ -121,6 +166,7 @@ static int plan_classes(xk_batch *b)
             b->classes.push_back(c);
         }
         Class &c = b->classes.back();
+        b->cls_of[it.idx] = (int)b->classes.size() - 1;
         c.smem = std::max(c.smem, it.smem);
         c.count++;
         LifeInst in;
@@ -390,6 +436,228 @@ extern "C" int xk_batch_step_plain(xk_batch *b, int32_t generations)
     return XK_OK;
 }
 
+// Chunks for the end-to-end pipeline: about XK_PIPE_CHUNKS runs of
+// consecutive lattices with equal cell counts, and per chunk and class the
+// descriptors of its lattices (built on the first pipelined run after the
+// class table changed).
+#define XK_PIPE_CHUNKS 8
+
+static int plan_pipeline(xk_batch *b)
+{
+    int K = XK_PIPE_CHUNKS;
+    if (const char *e = getenv("XK_PIPE_CHUNKS")) K = std::max(1, atoi(e));
+    K = std::min(K, b->n);
+    b->chunk_first.assign(1, 0);
+    const int64_t per = (b->total + K - 1) / K;
+    int64_t acc = 0;
+    for (int i = 0; i < b->n; ++i) {
+        acc += (int64_t)b->W[i] * b->H[i];
+        if (acc >= per * (int64_t)b->chunk_first.size() && i + 1 < b->n &&
+            (int)b->chunk_first.size() < K)
+            b->chunk_first.push_back(i + 1);
+    }
+    b->chunk_first.push_back(b->n);
+    const int nk = (int)b->chunk_first.size() - 1, nc = (int)b->classes.size();
+    std::vector<LifeInst> table;
+    b->seg.assign(nk, std::vector<std::pair<int, int>>(nc, {0, 0}));
+    for (int k = 0; k < nk; ++k)
+        for (int c = 0; c < nc; ++c) {
+            const int first = (int)table.size();
+            for (int i = b->chunk_first[k]; i < b->chunk_first[k + 1]; ++i)
+                if (b->cls_of[i] == c) {
+                    const Class &cl = b->classes[c];
+                    // the class table holds this instance's descriptor
+                    for (int j = cl.first; j < cl.first + cl.count; ++j)
+                        if (b->h_inst[j].off == b->off[i]) {
+                            table.push_back(b->h_inst[j]);
+                            break;
+                        }
+                }
+            b->seg[k][c] = {first, (int)table.size() - first};
+        }
+    if (!table.empty()) {
+        XK_CUDA(cudaMalloc(&b->d_pipe, table.size() * sizeof(LifeInst)));
+        XK_CUDA(cudaMemcpy(b->d_pipe, table.data(), table.size() * sizeof(LifeInst),
+                           cudaMemcpyHostToDevice));
+    }
+    if (!b->out_stream) XK_CUDA(cudaStreamCreateWithFlags(&b->out_stream, cudaStreamNonBlocking));
+    b->pev.assign((size_t)nk * 2, nullptr);
+    for (auto &e : b->pev) XK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    b->pipe_streams.assign(nk, nullptr);
+    for (auto &st : b->pipe_streams) XK_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    return XK_OK;
+}
+
+// End to end with the copies overlapped: chunk k's upload (b->stream), its
+// lattices' generations (stream k, after the upload, classes largest first)
+// and its download (out_stream, after its generations) run while other
+// chunks are in other stages; chunk k + 1's launches fill the SMs while
+// chunk k's last lattices finish.  Lattices only the plain path runs make
+// the call take the serial form.
+static int run_pipelined(xk_batch *b, const uint8_t *host_in, uint8_t *host_out, int generations)
+{
+    if (b->chunk_first.empty()) {
+        int rc = plan_pipeline(b);
+        if (rc != XK_OK) return rc;
+    }
+    const int nk = (int)b->chunk_first.size() - 1, nc = (int)b->classes.size();
+    XK_CUDA(cudaEventRecord(b->ev0, b->stream));
+    XK_CUDA(cudaStreamWaitEvent(b->out_stream, b->ev0, 0));
+    for (int k = 0; k < nk; ++k) {
+        const int i0 = b->chunk_first[k], i1 = b->chunk_first[k + 1];
+        const int64_t lo = b->off[i0], hi = b->off[i1 - 1] + (int64_t)b->W[i1 - 1] * b->H[i1 - 1];
+        cudaEvent_t in_done = b->pev[(size_t)k * 2], done = b->pev[(size_t)k * 2 + 1];
+        cudaStream_t st = b->pipe_streams[k];
+        XK_CUDA(cudaMemcpyAsync(b->cells + lo, host_in + lo, (size_t)(hi - lo),
+                                cudaMemcpyHostToDevice, b->stream));
+        XK_CUDA(cudaEventRecord(in_done, b->stream));
+        XK_CUDA(cudaStreamWaitEvent(st, in_done, 0));
+        for (int c = 0; c < nc; ++c) {
+            const auto sg = b->seg[k][c];
+            if (sg.second == 0) continue;
+            const Class &cl = b->classes[c];
+            XK_CUDA(xk_life_step_resident(b->d_pipe + sg.first, sg.second, b->cells, 1, generations,
+                                          1, 0u, b->bad, cl.threads, cl.smem, st));
+        }
+        XK_CUDA(cudaEventRecord(done, st));
+        XK_CUDA(cudaStreamWaitEvent(b->out_stream, done, 0));
+        XK_CUDA(cudaMemcpyAsync(host_out + lo, b->cells + lo, (size_t)(hi - lo),
+                                cudaMemcpyDeviceToHost, b->out_stream));
+    }
+    XK_CUDA(cudaEventRecord(b->fork, b->out_stream));
+    XK_CUDA(cudaStreamWaitEvent(b->stream, b->fork, 0));
+    XK_CUDA(cudaEventRecord(b->ev1, b->stream));
+    XK_CUDA(cudaEventSynchronize(b->ev1));
+    float ms = 0.f;
+    XK_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    xk_set_last_step_ms(ms);
+    return check_bad(b);
+}
+
+// Device address of a host range [p, p + bytes) when all of it is mapped
+// page-locked memory (cudaHostRegister / cudaHostAlloc), else null.
+static uint8_t *mapped_host(const void *p, int64_t bytes)
+{
+    cudaPointerAttributes a0, a1;
+    if (cudaPointerGetAttributes(&a0, p) != cudaSuccess ||
+        cudaPointerGetAttributes(&a1, (const uint8_t *)p + bytes - 1) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer ||
+        (uint8_t *)a1.devicePointer != (uint8_t *)a0.devicePointer + bytes - 1)
+        return nullptr;
+    return (uint8_t *)a0.devicePointer;
+}
+
+#define XK_STAGE_GROUP 16   // lattices per staged launch
+#define XK_STAGE_STREAMS 12
+
+static int plan_e2e(xk_batch *b)
+{
+    int lo = 0, hi = 0;
+    XK_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    for (int c = 0; c < (int)b->classes.size(); ++c) {
+        const Class &cl = b->classes[c];
+        if (xk_life_resident_ctas_per_sm(cl.threads, cl.smem) > 1) {
+            b->mapped_cls.push_back(c);
+            continue;
+        }
+        for (int j = 0; j < cl.count; j += XK_STAGE_GROUP) {
+            b->stage_cls.push_back(c);
+            b->stage_first.push_back(cl.first + j);
+            b->stage_count.push_back(std::min(XK_STAGE_GROUP, cl.count - j));
+        }
+    }
+    if (!b->stage_cls.empty()) {
+        b->stage_streams.assign(XK_STAGE_STREAMS, nullptr);
+        for (auto &st : b->stage_streams)
+            XK_CUDA(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, hi));
+        b->sev.assign(2 * b->stage_cls.size(), nullptr);
+        for (auto &e : b->sev) XK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    XK_CUDA(cudaEventCreateWithFlags(&b->staged_in, cudaEventDisableTiming));
+    if (!b->out_stream) XK_CUDA(cudaStreamCreateWithFlags(&b->out_stream, cudaStreamNonBlocking));
+    b->e2e_planned = true;
+    return XK_OK;
+}
+
+// queue the staged groups: per-lattice uploads on b->stream, one launch per
+// group on the high-priority streams, per-lattice downloads on out_stream
+static int enqueue_staged(xk_batch *b, const uint8_t *host_in, uint8_t *host_out, int generations)
+{
+    for (size_t g = 0; g < b->stage_cls.size(); ++g) {
+        const Class &cl = b->classes[b->stage_cls[g]];
+        const int first = b->stage_first[g], count = b->stage_count[g];
+        for (int j = first; j < first + count; ++j) {
+            const LifeInst &in = b->h_inst[j];
+            XK_CUDA(cudaMemcpyAsync(b->cells + in.off, host_in + in.off, (size_t)in.W * in.H,
+                                    cudaMemcpyHostToDevice, b->stream));
+        }
+        cudaEvent_t landed = b->sev[2 * g], done = b->sev[2 * g + 1];
+        cudaStream_t st = b->stage_streams[g % b->stage_streams.size()];
+        XK_CUDA(cudaEventRecord(landed, b->stream));
+        XK_CUDA(cudaStreamWaitEvent(st, landed, 0));
+        XK_CUDA(xk_life_step_resident_io(b->d_inst + first, count, b->cells, b->cells, nullptr, generations,
+                                         b->bad, cl.threads, cl.smem, st));
+        XK_CUDA(cudaEventRecord(done, st));
+        XK_CUDA(cudaStreamWaitEvent(b->out_stream, done, 0));
+        for (int j = first; j < first + count; ++j) {
+            const LifeInst &in = b->h_inst[j];
+            XK_CUDA(cudaMemcpyAsync(host_out + in.off, b->cells + in.off, (size_t)in.W * in.H,
+                                    cudaMemcpyDeviceToHost, b->out_stream));
+        }
+    }
+    return XK_OK;
+}
+
+// join the end-to-end streams on b->stream and time the run
+static int finish_e2e(xk_batch *b)
+{
+    XK_CUDA(cudaEventRecord(b->fork, b->out_stream));
+    XK_CUDA(cudaStreamWaitEvent(b->stream, b->fork, 0));
+    for (int c : b->mapped_cls) XK_CUDA(cudaStreamWaitEvent(b->stream, b->joins[c], 0));
+    XK_CUDA(cudaEventRecord(b->ev1, b->stream));
+    XK_CUDA(cudaEventSynchronize(b->ev1));
+    float ms = 0.f;
+    XK_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    xk_set_last_step_ms(ms);
+    return check_bad(b);
+}
+
+// End to end on page-locked buffers.  A CTA that has its SM to itself (the
+// largest lattices) would leave the SM idle while it read and wrote the host
+// link, so those lattices are copied in by the copy engines in launch order,
+// run from device memory in groups on high-priority streams, and copied out
+// as each group ends.  Every other CTA shares its SM, which keeps computing
+// while one CTA waits: those read their cells from host_in and write results
+// to host_out (and to the batch's device state) from the kernel; they are
+// released once the staged uploads are queued, so the largest lattices are
+// dispatched first.
+static int run_mapped(xk_batch *b, const uint8_t *host_in, uint8_t *host_out, const uint8_t *din,
+                      uint8_t *dout, int generations)
+{
+    if (!b->e2e_planned) {
+        int rc = plan_e2e(b);
+        if (rc != XK_OK) return rc;
+    }
+    int rc = set_class_attributes(b);
+    if (rc != XK_OK) return rc;
+    XK_CUDA(cudaEventRecord(b->ev0, b->stream));
+    XK_CUDA(cudaStreamWaitEvent(b->out_stream, b->ev0, 0));
+    rc = enqueue_staged(b, host_in, host_out, generations);
+    if (rc != XK_OK) return rc;
+    XK_CUDA(cudaEventRecord(b->staged_in, b->stream));
+    for (int c : b->mapped_cls) {
+        const Class &cl = b->classes[c];
+        XK_CUDA(cudaStreamWaitEvent(cl.stream, b->staged_in, 0));
+        XK_CUDA(xk_life_step_resident_io(b->d_inst + cl.first, cl.count, din, dout, b->cells, generations,
+                                         b->bad, cl.threads, cl.smem, cl.stream));
+        XK_CUDA(cudaEventRecord(b->joins[c], cl.stream));
+    }
+    return finish_e2e(b);
+}
+
 extern "C" int xk_batch_run(xk_batch *b, const uint8_t *host_in, uint8_t *host_out,
                             int64_t total_cells, int32_t generations)
 {
@@ -397,6 +665,16 @@ extern "C" int xk_batch_run(xk_batch *b, const uint8_t *host_in, uint8_t *host_o
     XK_REQUIRE(total_cells == b->total, XK_ERR_ARG, "xk_batch_run: %lld cells, batch has %lld",
                (long long)total_cells, (long long)b->total);
     XK_REQUIRE(generations >= 0, XK_ERR_ARG, "xk_batch_run: negative generations");
+    if (generations > 0 && b->big.empty() && !b->classes.empty()) {
+        // XK_E2E=chunks in the environment takes the chunked copies for
+        // page-locked buffers too
+        const char *form = getenv("XK_E2E");
+        const bool chunks = form && !strcmp(form, "chunks");
+        uint8_t *din = chunks ? nullptr : mapped_host(host_in, b->total);
+        uint8_t *dout = din ? mapped_host(host_out, b->total) : nullptr;
+        if (din && dout) return run_mapped(b, host_in, host_out, din, dout, generations);
+        return run_pipelined(b, host_in, host_out, generations);
+    }
     if (generations > 0 && graphs_enabled()) {
         cudaGraphExec_t g;
         int rc = graph_for(b, generations, &g);

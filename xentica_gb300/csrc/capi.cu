@@ -740,7 +740,7 @@ extern "C" int xk_set_device(int32_t device)
 extern "C" int xk_host_register(void *ptr, int64_t bytes)
 {
     XK_REQUIRE(ptr && bytes > 0, XK_ERR_ARG, "xk_host_register: bad buffer");
-    XK_CUDA(cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault));
+    XK_CUDA(cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterMapped | cudaHostRegisterPortable));
     return XK_OK;
 }
 

@@ -200,7 +200,7 @@ int64_t xk_life_resident_words(int W, int H, int threads)
 
 template <bool BYTES, bool TORUS>
 __global__ void __launch_bounds__(1024)
-xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
+xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out, void *mirror,
                    int generations, uint32_t bfill, unsigned int *__restrict__ bad)
 {
     extern __shared__ uint32_t sm[];
@@ -216,8 +216,9 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
     if (BYTES) {
         // one thread per word: 32 bytes in two 16-byte loads when the row
         // segment is whole and aligned, byte by byte otherwise
-        const uint8_t *src = (const uint8_t *)state + I.off;
+        const uint8_t *src = (const uint8_t *)in + I.off;
         unsigned int flag = 0;
+#pragma unroll 4
         for (int w = threadIdx.x; w < H * wpr; w += blockDim.x) {
             const int y = w / wpr, jj = w - y * wpr;
             const int b = y / p.L, i = y - b * p.L;
@@ -245,7 +246,7 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
         }
         if (flag) atomicOr(bad, 1u);
     } else {
-        const uint32_t *src = (const uint32_t *)state + I.off;
+        const uint32_t *src = (const uint32_t *)in + I.off;
         for (int w = threadIdx.x; w < H * wpr; w += blockDim.x) {
             const int y = w / wpr, jj = w - y * wpr;
             const int b = y / p.L, i = y - b * p.L;
@@ -399,14 +400,17 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
         __syncthreads();
     }
     if (BYTES) {
-        uint8_t *dst = (uint8_t *)state + I.off;
+        uint8_t *dst = (uint8_t *)out + I.off;
+        uint8_t *dst2 = mirror ? (uint8_t *)mirror + I.off : nullptr;
         for (int w = threadIdx.x; w < H * wpr; w += blockDim.x) {
             const int y = w / wpr, jj = w - y * wpr;
             const int b = y / p.L, i = y - b * p.L;
             const uint32_t word = lat[(i * p.G + b) * wpr + jj];
             const int x0 = jj * 32;
-            uint8_t *seg = dst + (int64_t)y * W + x0;
-            if (x0 + 32 <= W && ((uintptr_t)seg & 15u) == 0) {
+            const int64_t at = (int64_t)y * W + x0;
+            uint8_t *seg = dst + at;
+            if (x0 + 32 <= W && ((uintptr_t)seg & 15u) == 0 &&
+                (!dst2 || ((uintptr_t)(dst2 + at) & 15u) == 0)) {
                 uint64_t qq[4];
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
@@ -414,17 +418,25 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
                                  0x8040201008040201ull;
                     qq[k] = ((u + 0x7F7F7F7F7F7F7F7Full) >> 7) & 0x0101010101010101ull;
                 }
-                *(uint4 *)seg = make_uint4((uint32_t)qq[0], (uint32_t)(qq[0] >> 32), (uint32_t)qq[1],
-                                           (uint32_t)(qq[1] >> 32));
-                *(uint4 *)(seg + 16) = make_uint4((uint32_t)qq[2], (uint32_t)(qq[2] >> 32),
-                                                  (uint32_t)qq[3], (uint32_t)(qq[3] >> 32));
+                const uint4 lo = make_uint4((uint32_t)qq[0], (uint32_t)(qq[0] >> 32), (uint32_t)qq[1],
+                                            (uint32_t)(qq[1] >> 32));
+                const uint4 hi = make_uint4((uint32_t)qq[2], (uint32_t)(qq[2] >> 32), (uint32_t)qq[3],
+                                            (uint32_t)(qq[3] >> 32));
+                *(uint4 *)seg = lo;
+                *(uint4 *)(seg + 16) = hi;
+                if (dst2) {
+                    *(uint4 *)(dst2 + at) = lo;
+                    *(uint4 *)(dst2 + at + 16) = hi;
+                }
             } else {
                 const int nb = min(32, W - x0);
                 for (int k = 0; k < nb; ++k) seg[k] = (uint8_t)((word >> k) & 1u);
+                if (dst2)
+                    for (int k = 0; k < nb; ++k) dst2[at + k] = (uint8_t)((word >> k) & 1u);
             }
         }
     } else {
-        uint32_t *dst = (uint32_t *)state + I.off;
+        uint32_t *dst = (uint32_t *)out + I.off;
         for (int w = threadIdx.x; w < H * wpr; w += blockDim.x) {
             const int y = w / wpr, jj = w - y * wpr;
             const int b = y / p.L, i = y - b * p.L;
@@ -434,15 +446,15 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, void *__restrict__ state,
 }
 
 template <bool BYTES, bool TORUS>
-static cudaError_t xk_launch_resident(const LifeInst *inst, int ninst, void *state, int generations,
-                                      uint32_t bfill, unsigned int *bad, int threads, int smem_bytes,
-                                      cudaStream_t s)
+static cudaError_t xk_launch_resident(const LifeInst *inst, int ninst, const void *in, void *out,
+                                      void *mirror, int generations, uint32_t bfill, unsigned int *bad,
+                                      int threads, int smem_bytes, cudaStream_t s)
 {
     cudaError_t e = cudaFuncSetAttribute(xk_k_life_resident<BYTES, TORUS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
     if (e != cudaSuccess || ninst <= 0) return e;
-    xk_k_life_resident<BYTES, TORUS><<<ninst, threads, smem_bytes, s>>>(inst, state, generations,
-                                                                        bfill, bad);
+    xk_k_life_resident<BYTES, TORUS><<<ninst, threads, smem_bytes, s>>>(inst, in, out, mirror,
+                                                                        generations, bfill, bad);
     return cudaGetLastError();
 }
 
@@ -453,14 +465,36 @@ cudaError_t xk_life_step_resident(const LifeInst *inst, int ninst, void *state, 
                                   int threads, int smem_bytes, cudaStream_t s)
 {
     if (bytes_io)
-        return torus ? xk_launch_resident<true, true>(inst, ninst, state, generations, bfill, bad,
-                                                      threads, smem_bytes, s)
-                     : xk_launch_resident<true, false>(inst, ninst, state, generations, bfill, bad,
-                                                       threads, smem_bytes, s);
-    return torus ? xk_launch_resident<false, true>(inst, ninst, state, generations, bfill, bad,
-                                                   threads, smem_bytes, s)
-                 : xk_launch_resident<false, false>(inst, ninst, state, generations, bfill, bad,
-                                                    threads, smem_bytes, s);
+        return torus ? xk_launch_resident<true, true>(inst, ninst, state, state, nullptr, generations,
+                                                      bfill, bad, threads, smem_bytes, s)
+                     : xk_launch_resident<true, false>(inst, ninst, state, state, nullptr, generations,
+                                                       bfill, bad, threads, smem_bytes, s);
+    return torus ? xk_launch_resident<false, true>(inst, ninst, state, state, nullptr, generations,
+                                                   bfill, bad, threads, smem_bytes, s)
+                 : xk_launch_resident<false, false>(inst, ninst, state, state, nullptr, generations,
+                                                    bfill, bad, threads, smem_bytes, s);
+}
+
+// CTAs of the one-byte torus resident kernel one SM holds at once
+int xk_life_resident_ctas_per_sm(int threads, int smem_bytes)
+{
+    int n = 0;
+    if (cudaFuncSetAttribute(xk_k_life_resident<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem_bytes) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, xk_k_life_resident<true, true>, threads,
+                                                      smem_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return n;
+}
+
+cudaError_t xk_life_step_resident_io(const LifeInst *inst, int ninst, const uint8_t *in, uint8_t *out,
+                                     uint8_t *mirror, int generations, unsigned int *bad, int threads,
+                                     int smem_bytes, cudaStream_t s)
+{
+    return xk_launch_resident<true, true>(inst, ninst, in, out, mirror, generations, 0u, bad, threads,
+                                          smem_bytes, s);
 }
 
 // ---------------------------------------------------------------------------

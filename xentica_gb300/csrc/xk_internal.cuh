@@ -74,6 +74,15 @@ cudaError_t xk_life_step_global(const uint32_t *src, uint32_t *dst, const LifeGe
 cudaError_t xk_life_step_resident(const LifeInst *inst, int ninst, void *state, int bytes_io,
                                   int generations, int torus, uint32_t bfill, unsigned int *bad,
                                   int threads, int smem_bytes, cudaStream_t s);
+// torus, one byte per cell: lattices read from `in`, results written to
+// `out` and, when `mirror` is not null, also to `mirror` (the same offsets);
+// `in` and `out` may be device addresses of mapped host memory
+cudaError_t xk_life_step_resident_io(const LifeInst *inst, int ninst, const uint8_t *in, uint8_t *out,
+                                     uint8_t *mirror, int generations, unsigned int *bad, int threads,
+                                     int smem_bytes, cudaStream_t s);
+// CTAs of that kernel one SM holds at once with this block size and
+// shared memory (1 when the query fails)
+int xk_life_resident_ctas_per_sm(int threads, int smem_bytes);
 // threads and dynamic shared memory of the resident kernel for one lattice;
 // rows_per_band: target band length (controls the number of warps)
 int xk_life_resident_config(int W, int H, int rows_per_band, int *threads, int *smem_bytes);
