@@ -19,11 +19,15 @@
 LifeTable xk_life_table(uint32_t rule0, uint32_t rule1)
 {
     LifeTable t;
-    for (int s = 0; s < 2; ++s) {
-        uint32_t r = s ? rule1 : rule0;
-        for (int k = 0; k < 8; ++k) t.tab[s * 8 + k] = ((r >> k) & 1u) ? 0xFFFFFFFFu : 0u;
-        t.t8[s] = ((r >> 8) & 1u) ? 0xFFFFFFFFu : 0u;
+    auto mask = [](uint32_t r, int n) { return 0u - ((r >> n) & 1u); };
+    for (int q = 0; q < 8; ++q) {
+        const uint32_t r = q < 4 ? rule0 : rule1;
+        const int n = 2 * (q & 3);
+        t.a[q] = mask(r, n);
+        t.k[q] = xk_mux_coef(mask(r, n), mask(r, n + 1));
     }
+    t.a8 = mask(rule0, 8);
+    t.k8 = xk_mux_coef(mask(rule0, 8), mask(rule1, 8));
     return t;
 }
 
@@ -130,7 +134,7 @@ xk_k_life3d_vn(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, Lif
     const uint32_t b1 = xk_lop3_xor3(c1, c2, c3), b2 = xk_maj(c1, c2, c3);
     uint32_t m[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) m[q] = xk_mux(b0, t.tab[2 * q], t.tab[2 * q + 1]);
+    for (int q = 0; q < 8; ++q) m[q] = xk_imux(b0, t.a[q], t.k[q]);
     uint32_t n[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) n[q] = xk_mux(b1, m[2 * q], m[2 * q + 1]);
@@ -253,11 +257,15 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
             lat[(i * p.G + b) * wpr + jj] = src[w];
         }
     }
-    if (threadIdx.x < 18) {
-        const uint32_t r = threadIdx.x < 8 ? I.rule0 : threadIdx.x < 16 ? I.rule1
-                                                     : (threadIdx.x == 16 ? I.rule0 : I.rule1);
-        const int k = threadIdx.x < 16 ? (threadIdx.x & 7) : 8;
-        tabs[threadIdx.x] = 0u - ((r >> k) & 1u);
+    if (threadIdx.x < 9) {
+        // first-level multiplexer coefficients (LifeTable) of this rule
+        const int q = threadIdx.x;
+        const uint32_t r = q < 4 ? I.rule0 : I.rule1;
+        const int n = 2 * (q & 3);
+        const uint32_t A = q < 8 ? 0u - ((r >> n) & 1u) : 0u - ((I.rule0 >> 8) & 1u);
+        const uint32_t B = q < 8 ? 0u - ((r >> (n + 1)) & 1u) : 0u - ((I.rule1 >> 8) & 1u);
+        tabs[2 * q] = A;
+        tabs[2 * q + 1] = xk_mux_coef(A, B);
     }
 
     const int q = lane / p.P, j = lane - q * p.P;
@@ -286,9 +294,12 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
     __syncthreads();
     LifeTable t;
 #pragma unroll
-    for (int k = 0; k < 16; ++k) t.tab[k] = tabs[k];
-    t.t8[0] = tabs[16];
-    t.t8[1] = tabs[17];
+    for (int q = 0; q < 8; ++q) {
+        t.a[q] = tabs[2 * q];
+        t.k[q] = tabs[2 * q + 1];
+    }
+    t.a8 = tabs[16];
+    t.k8 = tabs[17];
 
     for (int gen = 0; gen < generations; ++gen) {
         if (active) {

@@ -1,6 +1,7 @@
 // Word-level Life-like logic shared by the bit-sliced kernels (life.cu,
 // cluster.cu): 32 cells per 32-bit word, neighbour counts from carry-save
-// adders and the rule from a multiplexer tree over warp-uniform masks.
+// adders and the rule from a multiplexer tree over warp-uniform masks (its
+// first level as integer multiply-adds, LifeTable).
 #pragma once
 
 #include <stdint.h>
@@ -38,6 +39,13 @@ __device__ __forceinline__ uint32_t xk_maj(uint32_t a, uint32_t b, uint32_t c)
     return xk_lop3_maj(a, b, c);
 }
 
+// sel ? B : A for warp-uniform masks A, B (0 or ~0) given as A and
+// k = xk_mux_coef(A, B): one integer multiply-add
+__device__ __forceinline__ uint32_t xk_imux(uint32_t sel, uint32_t a, uint32_t k)
+{
+    return sel * k + a;
+}
+
 // Next state of 32 cells.  (Lu, Cu, Ru) are the row above shifted so that bit
 // b holds the up-left, up and up-right neighbour of cell b; (Lm, Rm) the left
 // and right neighbours; (Ld, Cd, Rd) the row below; Cm the cells themselves.
@@ -58,14 +66,14 @@ __device__ __forceinline__ uint32_t xk_life_word(uint32_t Lu, uint32_t Cu, uint3
     // rule lookup: multiplexer tree over (state, b2, b1, b0), then b3
     uint32_t m[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) m[q] = xk_mux(b0, t.tab[2 * q], t.tab[2 * q + 1]);
+    for (int q = 0; q < 8; ++q) m[q] = xk_imux(b0, t.a[q], t.k[q]);
     uint32_t n[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) n[q] = xk_mux(b1, m[2 * q], m[2 * q + 1]);
     const uint32_t dead = xk_mux(b2, n[0], n[1]);
     const uint32_t live = xk_mux(b2, n[2], n[3]);
     const uint32_t low = xk_mux(Cm, dead, live);
-    const uint32_t eight = xk_mux(Cm, t.t8[0], t.t8[1]);
+    const uint32_t eight = xk_imux(Cm, t.a8, t.k8);
     return xk_mux(b3, low, eight);
 }
 
@@ -85,14 +93,14 @@ __device__ __forceinline__ uint32_t xk_life_word_fa(uint32_t su, uint32_t cu, ui
     const uint32_t b2 = k2 ^ k3, b3 = k2 & k3;
     uint32_t m[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) m[q] = xk_mux(b0, t.tab[2 * q], t.tab[2 * q + 1]);
+    for (int q = 0; q < 8; ++q) m[q] = xk_imux(b0, t.a[q], t.k[q]);
     uint32_t n[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) n[q] = xk_mux(b1, m[2 * q], m[2 * q + 1]);
     const uint32_t dead = xk_mux(b2, n[0], n[1]);
     const uint32_t live = xk_mux(b2, n[2], n[3]);
     const uint32_t low = xk_mux(Cm, dead, live);
-    const uint32_t eight = xk_mux(Cm, t.t8[0], t.t8[1]);
+    const uint32_t eight = xk_imux(Cm, t.a8, t.k8);
     return xk_mux(b3, low, eight);
 }
 

@@ -30,13 +30,23 @@ void xk_set_last_step_ms(double ms);
 // Life-like bit-packed lattices: cell x of row y is bit (x & 31) of word
 // y * wpr + (x >> 5); padding bits past the row's last cell are always 0.
 
-// Rule truth table as warp-uniform masks: tab[s * 8 + k] is all-ones when a
-// cell in state s with k live neighbours lives next generation (k < 8);
-// t8[s] the same for k == 8.
+// The rule as the coefficients of the multiplexer tree's first level.  The
+// truth-table masks T[s][n] (0 or ~0: the next state of a cell in state s
+// with n live neighbours) are paired by the count's bit 0, and
+// `sel ? B : A` over masks A, B is the integer multiply-add sel * k + A with
+// k = 0 (A == B), 1 (A = 0, B = ~0) or ~0 (A = ~0, B = 0), exactly, on the
+// FMA pipe instead of the logic pipe.  Pair q < 4: A = T[0][2q],
+// B = T[0][2q + 1]; q >= 4: the same for T[1][2(q - 4)].  a8/k8: the count-8
+// pair (T[0][8], T[1][8]) selected by the cell's state.
 struct LifeTable {
-    uint32_t tab[16];
-    uint32_t t8[2];
+    uint32_t a[8], k[8];
+    uint32_t a8, k8;
 };
+
+__host__ __device__ inline uint32_t xk_mux_coef(uint32_t A, uint32_t B)
+{
+    return A == B ? 0u : (A ? 0xFFFFFFFFu : 1u);
+}
 
 LifeTable xk_life_table(uint32_t rule0, uint32_t rule1);
 
