@@ -168,16 +168,30 @@ cudaError_t xk_life_step3d_vn(const uint32_t *src, uint32_t *dst, const Life3Geo
 // the first and last row of every band are copied to a halo area before the
 // generation starts, so neighbouring bands read the previous generation.
 //
-// Shared layout interleaves the bands' rows (local row i of band b at
-// (i * G + b) * wpr) so that the groups of a warp hit consecutive words; the
-// rule table sits after the halo and is read into registers once (a value
-// loaded from shared memory is never recomputed per use).
+// Shared layout is warp-major: the bands of warp w hold their local row i at
+// words (w * L + i) * 32 + lane, lane = group * P + column word, so a warp's
+// accesses to one row hit 32 consecutive words and a lane's next row is
+// always 32 words further on (a constant stride: the unrolled band loop
+// addresses its rows with immediate offsets).  The rule table sits after the
+// halo and is read into registers once.
 
 #define XK_TAB_WORDS 32
 
 struct ResidentPlan {
     int P, gpw, G, L, nb;  // lanes per group, groups per warp, groups, band length, live bands
 };
+
+// shared word of local row i, column word jj of band b (warp-major layout)
+__host__ __device__ __forceinline__ int xk_res_at(const ResidentPlan &p, int b, int i, int jj)
+{
+    return ((b / p.gpw) * p.L + i) * 32 + (b % p.gpw) * p.P + jj;
+}
+
+// shared words of the lattice area: L rows of 32 words per warp holding bands
+__host__ __device__ __forceinline__ int64_t xk_res_lat_words(const ResidentPlan &p)
+{
+    return (int64_t)p.L * ((p.G + p.gpw - 1) / p.gpw) * 32;
+}
 
 __host__ __device__ inline ResidentPlan xk_resident_plan(int wpr, int H, int threads)
 {
@@ -199,7 +213,7 @@ int64_t xk_life_resident_words(int W, int H, int threads)
     const int wpr = (W + 31) / 32;
     if (wpr > 32) return -1;
     ResidentPlan p = xk_resident_plan(wpr, H, threads);
-    return (int64_t)p.L * p.G * wpr + 2LL * p.G * wpr + XK_TAB_WORDS;
+    return xk_res_lat_words(p) + 2LL * p.G * wpr + XK_TAB_WORDS;
 }
 
 template <bool BYTES, bool TORUS>
@@ -212,7 +226,7 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
     const int wpr = I.wpr, H = I.H, W = I.W;
     const ResidentPlan p = xk_resident_plan(wpr, H, blockDim.x);
     uint32_t *lat = sm;
-    uint32_t *halo = sm + (int64_t)p.L * p.G * wpr;   // [band][2][wpr]
+    uint32_t *halo = sm + xk_res_lat_words(p);       // [band][2][wpr]
     uint32_t *tabs = halo + 2 * p.G * wpr;            // rule table
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
@@ -246,7 +260,7 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
                     word |= (v != 0u) << k;
                 }
             }
-            lat[(i * p.G + b) * wpr + jj] = word;
+            lat[xk_res_at(p, b, i, jj)] = word;
         }
         if (flag) atomicOr(bad, 1u);
     } else {
@@ -254,7 +268,7 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
         for (int w = threadIdx.x; w < H * wpr; w += blockDim.x) {
             const int y = w / wpr, jj = w - y * wpr;
             const int b = y / p.L, i = y - b * p.L;
-            lat[(i * p.G + b) * wpr + jj] = src[w];
+            lat[xk_res_at(p, b, i, jj)] = src[w];
         }
     }
     if (threadIdx.x < 9) {
@@ -303,13 +317,13 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
 
     for (int gen = 0; gen < generations; ++gen) {
         if (active) {
-            halo[(band * 2 + 0) * wpr + j] = lat[(0 * p.G + band) * wpr + j];
-            halo[(band * 2 + 1) * wpr + j] = lat[((y1 - 1 - y0) * p.G + band) * wpr + j];
+            halo[(band * 2 + 0) * wpr + j] = lat[xk_res_at(p, band, 0, j)];
+            halo[(band * 2 + 1) * wpr + j] = lat[xk_res_at(p, band, y1 - 1 - y0, j)];
         }
         __syncthreads();
         RowVec vu, vm, vd;
         const uint32_t wu = (!TORUS && bc == 0) ? bfill : halo[(hup * 2 + 1) * wpr + jc];
-        const uint32_t wm = lat[bc * wpr + jc];
+        const uint32_t wm = lat[xk_res_at(p, bc, 0, jc)];
         if (TORUS) {
             uint32_t l = __shfl_sync(0xFFFFFFFFu, wu, src_l), r = __shfl_sync(0xFFFFFFFFu, wu, src_r);
             vu = xk_torus_vec(wu, l, r, lpre, top, topbit);
@@ -334,8 +348,8 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
             uint32_t su = xk_lop3_xor3(vu.L, vu.C, vu.R), cu = xk_maj(vu.L, vu.C, vu.R);
             uint32_t sm_ = xk_lop3_xor3(vm.L, vm.C, vm.R), cm_ = xk_maj(vm.L, vm.C, vm.R);
             uint32_t Lm = vm.L, Cm = vm.C, Rm = vm.R;
-            const int stride = p.G * wpr;                       // words between band rows
-            uint32_t *wp = lat + bc * wpr + jc;                 // this lane's word of row i
+            constexpr int stride = 32;                          // words between band rows
+            uint32_t *wp = lat + xk_res_at(p, bc, 0, jc);       // this lane's word of row i
             const uint32_t whalo = halo[(hdn * 2 + 0) * wpr + jc];
             auto band_rows = [&](auto fullw_tag) {
                 constexpr bool FULLW = decltype(fullw_tag)::value;
@@ -390,7 +404,7 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
                 const bool row_ok = active && y < y1;
                 uint32_t wd;
                 bool off_d = false;
-                if (y + 1 < y1) wd = lat[((i + 1) * p.G + bc) * wpr + jc];
+                if (y + 1 < y1) wd = lat[xk_res_at(p, bc, i + 1, jc)];
                 else if (y + 1 < H) wd = halo[((bc + 1) * 2 + 0) * wpr + jc];
                 else if (TORUS) wd = halo[(0 * 2 + 0) * wpr + jc];
                 else { wd = bfill; off_d = true; }
@@ -403,7 +417,7 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
                     if (off_d) vd.L = vd.C = vd.R = bfill;
                 }
                 const uint32_t out = xk_life_word(vu.L, vu.C, vu.R, vm.L, vm.C, vm.R, vd.L, vd.C, vd.R, t);
-                if (row_ok) lat[(i * p.G + bc) * wpr + jc] = out & outmask;
+                if (row_ok) lat[xk_res_at(p, bc, i, jc)] = out & outmask;
                 vu = vm;
                 vm = vd;
             }
@@ -416,7 +430,7 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
         for (int w = threadIdx.x; w < H * wpr; w += blockDim.x) {
             const int y = w / wpr, jj = w - y * wpr;
             const int b = y / p.L, i = y - b * p.L;
-            const uint32_t word = lat[(i * p.G + b) * wpr + jj];
+            const uint32_t word = lat[xk_res_at(p, b, i, jj)];
             const int x0 = jj * 32;
             const int64_t at = (int64_t)y * W + x0;
             uint8_t *seg = dst + at;
@@ -451,7 +465,7 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
         for (int w = threadIdx.x; w < H * wpr; w += blockDim.x) {
             const int y = w / wpr, jj = w - y * wpr;
             const int b = y / p.L, i = y - b * p.L;
-            dst[w] = lat[(i * p.G + b) * wpr + jj];
+            dst[w] = lat[xk_res_at(p, b, i, jj)];
         }
     }
 }
