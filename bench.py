@@ -172,6 +172,16 @@ def traffic_per_cell():
     return None
 
 
+def committed_traffic(name):
+    """DRAM bytes per launch of a kernel from its committed ncu summary
+    (``profiles/<name>_traffic.json``), or None."""
+    path = os.path.join(ROOT, "profiles", name + "_traffic.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            return float(json.load(fh)["dram_bytes_per_launch"])
+    return None
+
+
 def workload(args, rank):
     from xentica_gb300.batch import ensemble_workload
     ctx = multiprocessing.get_context("spawn")
@@ -424,10 +434,12 @@ def run_evolife(args, dist):
                                    "modular colour, MovingAverage(18, 3)",
                        "l2": "state + colours (41 MB) fit in L2"},
             "render_ms_per_frame": render_ms,
-            "roofline": {"bound": "alu", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": committed_traffic("evolife"),
                          "note": "40 B per cell-update of state and colour traffic; the "
-                                 "kernel is integer-ALU bound (genome crossover)"},
+                                 "kernel itself is bound by integer instruction issue "
+                                 "(genome crossover), not by HBM"},
             "clocks": clk}
     if dist.rank == 0:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -505,7 +517,9 @@ def run_mass(args, dist):
             "mass_conserved": conserved, "render_ms_per_frame": render_ms,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
-                         "note": "8 B per cell-update (uint32 read + write)"},
+                         "traffic": committed_traffic("mass_tma"),
+                         "note": "8 B per cell-update (uint32 read + write); traffic: "
+                                 "DRAM bytes of one launch (one generation)"},
             "clocks": clk}
     if dist.rank == 0:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -629,7 +643,8 @@ def run_life512(args, dist):
             "api_step_loop": {"value": float(n) * gens / api_s, "unit": "cell-updates/s",
                               "note": "1000 calls of model.step(), one generation each"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": committed_traffic("life_cluster"),
                          "note": "B_alg = 2 B per cell-update; the lattice stays in the "
                                  "shared memory of one CTA or of a thread-block cluster "
                                  "(whichever the first step's tuning found faster) for all "

@@ -24,13 +24,27 @@ def _topo(size):
     return O.Topology(size, "von_neumann", border=WALL)
 
 
+@pytest.fixture(params=["tma", "tma-general", "rows"])
+def kernel_form(request, monkeypatch):
+    """Widths that are multiples of 4: the TMA form (default; its fast-only
+    instantiation when the uploaded total is below 2^30, its general one
+    otherwise or with XK_MASS_GENERAL=1) and the register-queue form
+    (XK_MASS_KERNEL=rows)."""
+    if request.param == "rows":
+        monkeypatch.setenv("XK_MASS_KERNEL", "rows")
+    if request.param == "tma-general":
+        monkeypatch.setenv("XK_MASS_GENERAL", "1")
+    return request.param
+
+
 @pytest.mark.parametrize("size,high", [((33, 17, 9), 2 ** 32 - 1), ((64, 8, 31), 2 ** 20),
                                        ((7, 129, 5), 100), ((64, 24, 12), 2 ** 32 - 1),
                                        ((128, 40, 20), "mixed")])
-def test_random_states_vs_oracle(size, high):
-    # widths that are multiples of 4 take the tiled kernel: small values its
-    # fast path, large ones (and the wall value) its exact path, "mixed" both
-    # in one launch, with values next to the 2^30 and 1431655765 boundaries
+def test_random_states_vs_oracle(size, high, kernel_form):
+    # widths that are multiples of 4 take the tiled kernels: small values
+    # their fast path, large ones (and the wall value) their exact path,
+    # "mixed" both in one launch, with values next to the 2^30 and
+    # 1431655765 boundaries
     model = _model(size)
     n = model.cells_num
     rng = np.random.RandomState(size[0])
@@ -61,7 +75,7 @@ def test_random_states_vs_oracle(size, high):
     assert np.array_equal(model.render(), img)
 
 
-def test_mass_conserved_long_run():
+def test_mass_conserved_long_run(kernel_form):
     model = _model((96, 80, 40))
     before = int(model.gpu.arrays.cells.get()[:model.cells_num].astype(np.uint64).sum())
     model.gpu.step(500)
@@ -81,7 +95,7 @@ def test_multi_generation_call_equals_single_steps():
 
 
 @pytest.mark.parametrize("zc", ["1", "3", "8", "20"])
-def test_z_chunks_vs_oracle(zc, monkeypatch):
+def test_z_chunks_vs_oracle(zc, monkeypatch, kernel_form):
     # planes per CTA forced (the automatic choice gives small lattices one);
     # a few large cells put some CTAs on the exact path
     monkeypatch.setenv("XK_MASS_ZC", zc)
@@ -100,3 +114,25 @@ def test_z_chunks_vs_oracle(zc, monkeypatch):
     O.mass_run(topo, fld, col, 4, totals=totals)
     assert np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n])
     assert model.gpu.mass_totals(4).tolist() == totals
+
+
+@pytest.mark.parametrize("size", [(4, 3, 1), (132, 9, 2), (256, 17, 3), (8, 1, 5), (260, 8, 7)])
+def test_tile_edges_vs_oracle(size, kernel_form):
+    # partial tiles in x (a second 128-cell tile mostly off the lattice), y
+    # (heights not a multiple of the tile's 8 rows) and z (one to seven
+    # planes), with a few cells at or above 2^30 in some runs
+    model = _model(size)
+    n = model.cells_num
+    rng = np.random.RandomState(sum(size))
+    cells = rng.poisson(6, n).astype(np.uint32)
+    if size[0] > 8:
+        cells[rng.randint(0, n, 3)] = rng.choice([2 ** 30, WALL], 3)
+    model.gpu.load(cells, np.zeros(3 * n, dtype=np.int32))
+    topo = _topo(size)
+    fld = topo.field(cells, np.uint32)
+    col = np.zeros(3 * n, dtype=np.int32)
+    model.gpu.step(3)
+    totals = []
+    O.mass_run(topo, fld, col, 3, totals=totals)
+    assert np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n])
+    assert model.gpu.mass_totals(3).tolist() == totals

@@ -104,6 +104,7 @@ struct xk_model {
     int proj_valid = 0;
     unsigned long long *totals = nullptr;       // mass: total after each generation
     int64_t totals_cap = 0, totals_count = 0;
+    bool mass_small = false;                    // mass: uploaded total below 2^30
     int cur = 0;
     void *stage = nullptr;       // reference-layout staging + validity flag
     int32_t *col = nullptr;      // colours (3 int32 per cell) when materialised
@@ -412,6 +413,19 @@ extern "C" int xk_upload(xk_model *m, const void *host_main, int64_t ncells)
                     : m->layout == LAYOUT_VM ? (void *)m->fld : (void *)m->cells64[m->cur];
         XK_CUDA(cudaMemcpyAsync(dst, host_main, (size_t)m->n * esz, cudaMemcpyHostToDevice,
                                 m->stream));
+        if (m->layout == LAYOUT_MASS) {
+            // the total decides the kernel for good: mass is conserved
+            if (m->totals_cap < 1) {
+                XK_CUDA(cudaMalloc(&m->totals, sizeof(unsigned long long)));
+                m->totals_cap = 1;
+            }
+            unsigned long long tot = 0;
+            XK_CUDA(xk_mass_sum((const uint32_t *)dst, m->n, m->totals, m->stream));
+            XK_CUDA(cudaMemcpyAsync(&tot, m->totals, sizeof(tot), cudaMemcpyDeviceToHost, m->stream));
+            XK_CUDA(cudaStreamSynchronize(m->stream));
+            m->mass_small = tot < (1ull << 30);
+            m->totals_count = 0;
+        }
         XK_CUDA(cudaStreamSynchronize(m->stream));
         m->proj_valid = 0;
         m->uploaded = 1;
@@ -578,7 +592,7 @@ extern "C" int xk_step(xk_model *m, int64_t nsteps)
         XK_CUDA(cudaEventRecord(m->ev0, m->stream));
         for (int64_t g = 0; g < nsteps; ++g) {
             XK_CUDA(xk_mass_step(m->cells32[m->cur], m->cells32[1 - m->cur], m->totals + g, m->d,
-                                 m->stream));
+                                 m->mass_small, m->stream));
             m->cur = 1 - m->cur;
         }
         XK_CUDA(cudaEventRecord(m->ev1, m->stream));
@@ -588,6 +602,10 @@ extern "C" int xk_step(xk_model *m, int64_t nsteps)
         xk_set_last_step_ms(ms);
         m->totals_count = nsteps;
         m->proj_valid = 0;
+        if (xk_mass_take_wait_failure()) {
+            xk_set_error("mass-transfer step: a CTA gave up waiting for a tensor copy");
+            return XK_ERR_TIMEOUT;
+        }
         return XK_OK;
     }
     if (m->layout == LAYOUT_CELLS64) {

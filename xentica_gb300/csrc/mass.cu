@@ -11,8 +11,10 @@
 //   m'         = m - sum_k sent_k + sum_k incoming_k
 // Colour (plain ColorEffect): min(m' * 32, 255) on every channel.
 //
-// Two kernels: xk_k_mass_rows for widths that are a multiple of 4 (below)
-// and the generic xk_k_mass for any width.  Work split of the generic one: a
+// Three kernels: xk_k_mass_tma (tensor copies into a shared-memory ring,
+// widths that are a multiple of 4: the default), xk_k_mass_rows (the same
+// widths, register queue and plain loads; XK_MASS_KERNEL=rows) and the
+// generic xk_k_mass for any width.  Work split of the generic one: a
 // CTA owns a 32-wide, 8-row tile of a run of zc planes; a thread owns one
 // cell of a row and walks its z run with a three-plane register queue.
 // x neighbours come from the neighbouring lanes (shuffles; lanes 0 and 31
@@ -26,7 +28,12 @@
 // holds).  Each CTA adds its cells' new mass to the generation's total with
 // one 64-bit atomic.  Colours and the RendererPlain projection are derived
 // from the state when they are read, not every generation.
+#include <cuda.h>          // CUtensorMap and its enums (types only; no driver link)
+#include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
+
 #include <cstdlib>
+#include <cstring>
+#include <mutex>
 
 #include "xk_internal.cuh"
 
@@ -321,6 +328,273 @@ xk_k_mass_rows(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
     }
 }
 
+// ---------------------------------------------------------------------------
+// TMA form (W % 4 == 0, the default): a CTA owns a 128-cell by XK_MT_BY-row
+// tile of a run of zc planes.  Each plane of the tile, with one halo row
+// above and below and four halo columns either side, arrives in shared
+// memory by one tensor copy (cp.async.bulk.tensor, issued by one thread into
+// a ring of XK_MT_STAGES stages, completion on an mbarrier); coordinates off
+// the lattice read as 0, which is exactly what an off-board neighbour
+// contributes in the fast path.  Each cell's q = m / 7 is computed once,
+// when its plane arrives, and written to a q tile (three of them in turn, so
+// one barrier per plane separates writers and readers); a thread owns four
+// consecutive cells of a row and keeps q of planes z - 1, z, z + 1 of its own
+// column in registers, reads the q of the rows above and below from the q
+// tile, the x neighbours from its lanes (shuffles) and, at the tile's edge,
+// from the tile's halo columns.  The barrier also ORs a flag: some cell of
+// the plane's tile or halo is at or above 2^30 (so the one-instruction q may
+// be inexact, or a wall value is inside).  A plane whose tile saw such a
+// cell in planes z - 1 .. z + 1 takes the exact per-neighbour form for the
+// whole CTA, reading the neighbours from global memory.  When the uploaded
+// lattice's total mass is below 2^30, no cell can ever reach 2^30 (mass is
+// conserved and never negative) and the fast-only instantiation runs: plain
+// barriers, no flag and no exact path, so fewer registers.
+#define XK_MT_BY 8
+#define XK_MT_STAGES 4
+#define XK_MT_COLS 136                                  // 4 + 128 + 4
+#define XK_MT_ROWS (XK_MT_BY + 2)
+#define XK_MT_TILE_WORDS (XK_MT_COLS * XK_MT_ROWS)
+#define XK_MT_STAGE_BYTES (XK_MT_TILE_WORDS * 4)
+#define XK_MT_STAGE_STRIDE (((XK_MT_STAGE_BYTES + 127) / 128) * 128)
+#define XK_MT_SMEM \
+    (128 + XK_MT_STAGES * XK_MT_STAGE_STRIDE + 3 * XK_MT_STAGE_BYTES + 8 * XK_MT_STAGES + 8 * XK_MT_BY + 16)
+#define XK_MT_SPIN (1u << 20)                           // try_wait rounds before giving up
+
+// set when a CTA gave up waiting for a tensor copy (never expected)
+__device__ unsigned int xk_mass_wait_failed;
+
+__device__ __forceinline__ uint32_t xk_smem_addr(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ bool xk_mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t done;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    return done != 0;
+}
+
+// bounded wait for the copy of one stage; false after XK_MT_SPIN rounds
+__device__ __forceinline__ bool xk_mbar_wait(uint32_t bar, uint32_t parity)
+{
+    for (uint32_t i = 0; i < XK_MT_SPIN; ++i)
+        if (xk_mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// one thread: plane z of the tile (x from x_lo, y from y_lo) into a stage
+__device__ __forceinline__ void xk_mt_issue(const CUtensorMap *tm, uint32_t stage, uint32_t bar, int x_lo,
+                                            int y_lo, int z)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                 :
+                 : "r"(bar), "r"((uint32_t)XK_MT_STAGE_BYTES)
+                 : "memory");
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
+                 "[%0], [%1, {%2, %3, %4}], [%5];"
+                 :
+                 : "r"(stage), "l"(reinterpret_cast<uint64_t>(tm)), "r"(x_lo), "r"(y_lo), "r"(z),
+                   "r"(bar)
+                 : "memory");
+}
+
+// the barrier of a plane; the general kernel also ORs the flags of its threads
+template <bool GENERAL>
+__device__ __forceinline__ bool xk_mt_barrier(bool flag)
+{
+    if (GENERAL) return __syncthreads_or(flag);
+    __syncthreads();
+    return false;
+}
+
+// q of four cells, and whether one of them is at or above 2^30
+__device__ __forceinline__ uint4 xk_mt_q4(const uint4 m, bool &big)
+{
+    big |= (m.x | m.y | m.z | m.w) >= XK_MASS_SMALL;
+    return make_uint4(xk_q_small(m.x), xk_q_small(m.y), xk_q_small(m.z), xk_q_small(m.w));
+}
+
+template <int MINB, bool GENERAL>
+__global__ void __launch_bounds__(32 * XK_MT_BY, MINB)
+xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict__ src,
+              uint32_t *__restrict__ dst, unsigned long long *__restrict__ total, MassParams p, int zc)
+{
+    extern __shared__ __align__(128) uint8_t xk_mt_raw[];
+    // tensor copies land on 128-byte boundaries: round the window's start up
+    uint8_t *base = xk_mt_raw + ((128u - (xk_smem_addr(xk_mt_raw) & 127u)) & 127u);
+    uint8_t *stages = base;
+    uint32_t *qt = reinterpret_cast<uint32_t *>(base + XK_MT_STAGES * XK_MT_STAGE_STRIDE);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(qt + 3 * XK_MT_TILE_WORDS);
+    unsigned long long *warp_sums = reinterpret_cast<unsigned long long *>(bars + XK_MT_STAGES);
+    volatile int *fail = reinterpret_cast<volatile int *>(warp_sums + XK_MT_BY);
+
+    const int lane = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + lane;
+    const int x_lo = blockIdx.x * 128 - 4, y_lo = blockIdx.y * XK_MT_BY - 1;
+    const int x0 = blockIdx.x * 128 + lane * 4, y = blockIdx.y * XK_MT_BY + ty;
+    const int z0 = blockIdx.z * zc, z1 = min(z0 + zc, p.D);
+    const int nplanes = z1 - z0 + 2;                  // planes z0 - 1 .. z1
+    const bool in = x0 < p.W && y < p.H;              // W % 4 == 0: all four cells or none
+    const uint32_t plane = (uint32_t)p.W * (uint32_t)p.H;
+    const uint32_t bar0 = xk_smem_addr(bars), stage0 = xk_smem_addr(stages);
+
+    if (tid == 0) {
+        *fail = 0;
+        for (int s = 0; s < XK_MT_STAGES; ++s)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8 * s) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        for (int k = 0; k < XK_MT_STAGES && k < nplanes; ++k)
+            xk_mt_issue(&tm, stage0 + k * XK_MT_STAGE_STRIDE, bar0 + 8 * k, x_lo, y_lo, z0 - 1 + k);
+    }
+    __syncthreads();
+
+    // own cells of a stage (row ty + 1, columns 4 + 4 lane ..); the halo
+    // column this lane converts when it is lane 0 or 31 (every lane reads one,
+    // in bounds, so the code has no lane-dependent branch)
+    const int own = (ty + 1) * XK_MT_COLS + 4 + 4 * lane;
+    const int hcol = (ty + 1) * XK_MT_COLS + (lane == 0 ? 3 : 4 + 128);
+    const bool hlane = lane == 0 || lane == 31;
+    const bool hrow = ty == 0 || ty == XK_MT_BY - 1;
+    const int hrow_at = (ty == 0 ? 0 : XK_MT_BY + 1) * XK_MT_COLS + 4 + 4 * lane;
+    uint32_t *const qt0 = qt, *const qt1 = qt + XK_MT_TILE_WORDS, *const qt2 = qt + 2 * XK_MT_TILE_WORDS;
+    int st_idx = 0;                                   // ring stage of the next plane taken
+    uint32_t par = 0;                                 // its mbarrier phase parity
+    // next plane of the ring: wait for it, return this thread's cells; the q
+    // of its cells and of the halo cells it converts go to q tile qdst (null:
+    // own cells only).  A wait that gives up marks `fail`, which every thread
+    // reads after the next barrier.
+    auto take = [&](uint32_t *qdst, uint4 &m, uint4 &q, bool &big) {
+        if (!xk_mbar_wait(bar0 + 8 * st_idx, par)) *fail = 1;
+        const uint32_t *st = reinterpret_cast<const uint32_t *>(stages + st_idx * XK_MT_STAGE_STRIDE);
+        m = *reinterpret_cast<const uint4 *>(st + own);
+        q = xk_mt_q4(m, big);
+        if (qdst) {
+            *reinterpret_cast<uint4 *>(qdst + own) = q;
+            const uint32_t hm = st[hcol];
+            if (hlane) {
+                big |= hm >= XK_MASS_SMALL;
+                qdst[hcol] = xk_q_small(hm);
+            }
+            if (hrow) {
+                const uint4 rm = *reinterpret_cast<const uint4 *>(st + hrow_at);
+                *reinterpret_cast<uint4 *>(qdst + hrow_at) = xk_mt_q4(rm, big);
+            }
+        }
+    };
+    // after the barrier that follows the last read of the plane just taken
+    // (ring index k): its stage receives plane k + XK_MT_STAGES
+    int k_taken = -1;
+    auto advance = [&]() {
+        ++k_taken;
+        if (tid == 0 && k_taken + XK_MT_STAGES < nplanes)
+            xk_mt_issue(&tm, stage0 + st_idx * XK_MT_STAGE_STRIDE, bar0 + 8 * st_idx, x_lo, y_lo,
+                        z0 - 1 + k_taken + XK_MT_STAGES);
+        if (++st_idx == XK_MT_STAGES) {
+            st_idx = 0;
+            par ^= 1u;
+        }
+    };
+
+    // three register sets (m, q) take the roles previous / current / next
+    // plane in turn, and three q tiles the roles current / next: plane
+    // z0 + j uses tile j % 3 and set (j + 1) % 3
+    uint4 m0, q0, m1, q1, m2, q2;
+    bool b_prev = false, b_cur = false;
+    take(nullptr, m0, q0, b_prev);                    // plane z0 - 1: q of the own column
+    b_prev = xk_mt_barrier<GENERAL>(b_prev);
+    if (*fail) {
+        if (tid == 0) atomicOr(&xk_mass_wait_failed, 1u);
+        return;
+    }
+    advance();
+    take(qt0, m1, q1, b_cur);                         // plane z0
+    b_cur = xk_mt_barrier<GENERAL>(b_cur);
+    if (*fail) {
+        if (tid == 0) atomicOr(&xk_mass_wait_failed, 1u);
+        return;
+    }
+    advance();
+
+    // on-board neighbours in x and y of the four cells
+    const int cy = (y > 0) + (y + 1 < p.H);
+    const uint32_t c0 = cy + 1 + (x0 > 0), c3 = cy + 1 + (x0 + 4 < p.W), c12 = cy + 2;
+    unsigned long long mass_sum = 0;
+    uint32_t off = in ? (uint32_t)z0 * plane + (uint32_t)y * p.W + x0 : 0u;
+    int z = z0;
+    // one plane: take plane z + 1 into (mn, qn) and tile qnext, then compute
+    // plane z from tile qcur, qp (z - 1), (mc, qc) (z) and qn (z + 1)
+    auto step = [&](const uint4 &qp, const uint4 &mc, const uint4 &qc, uint4 &mn, uint4 &qn,
+                    const uint32_t *qcur, uint32_t *qnext) -> bool {
+        bool b_t = false;
+        take(qnext, mn, qn, b_t);
+        const bool b_next = xk_mt_barrier<GENERAL>(b_t);
+        if (*fail) return false;
+        advance();
+        const uint32_t cz = (uint32_t)((z > 0) + (z + 1 < p.D));
+        uint32_t out[4];
+        if (!GENERAL || !(b_prev | b_cur | b_next)) {
+            const uint4 up = *reinterpret_cast<const uint4 *>(qcur + own - XK_MT_COLS);
+            const uint4 dn = *reinterpret_cast<const uint4 *>(qcur + own + XK_MT_COLS);
+            const uint32_t hl = qcur[own - 1], hr = qcur[own + 4];
+            const uint32_t sl = __shfl_up_sync(0xFFFFFFFFu, qc.w, 1);
+            const uint32_t sr = __shfl_down_sync(0xFFFFFFFFu, qc.x, 1);
+            const uint32_t xl = lane == 0 ? hl : sl, xr = lane == 31 ? hr : sr;
+            out[0] = mc.x - qc.x * (c0 + cz) + xl + qc.y + up.x + dn.x + qp.x + qn.x;
+            out[1] = mc.y - qc.y * (c12 + cz) + qc.x + qc.z + up.y + dn.y + qp.y + qn.y;
+            out[2] = mc.z - qc.z * (c12 + cz) + qc.y + qc.w + up.z + dn.z + qp.z + qn.z;
+            out[3] = mc.w - qc.w * (c3 + cz) + qc.z + xr + up.w + dn.w + qp.w + qn.w;
+        } else if (GENERAL && in) {
+            // the reference's arithmetic per neighbour, neighbours from global memory
+            const uint32_t wall = p.wall;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const uint32_t m = xk_get(mc, i);
+                const uint32_t o = off + i;
+                const bool on[6] = {x0 + i > 0, x0 + i + 1 < p.W, y > 0, y + 1 < p.H, z > 0, z + 1 < p.D};
+                const uint32_t at[6] = {o - 1, o + 1, o - p.W, o + p.W, o - plane, o + plane};
+                uint32_t cnt = 0, sq = 0;
+#pragma unroll
+                for (int n = 0; n < 6; ++n) {
+                    const uint32_t nb = on[n] ? __ldg(src + at[n]) : 0u;
+                    cnt += (uint32_t)(on[n] && nb != wall);
+                    sq += on[n] ? nb / 7u : 0u;
+                }
+                out[i] = m - (m / 7u) * cnt + (m != wall ? sq : 0u);
+            }
+        }
+        if (in) {
+            *reinterpret_cast<uint4 *>(dst + off) = make_uint4(out[0], out[1], out[2], out[3]);
+            mass_sum += (unsigned long long)out[0] + out[1] + (unsigned long long)out[2] + out[3];
+        }
+        b_prev = b_cur;
+        b_cur = b_next;
+        off += plane;
+        return ++z < z1;
+    };
+    bool go = true;
+    while (go) {
+        go = step(q0, m1, q1, m2, q2, qt0, qt1) && step(q1, m2, q2, m0, q0, qt1, qt2) &&
+             step(q2, m0, q0, m1, q1, qt2, qt0);
+    }
+    if (*fail) {
+        if (tid == 0) atomicOr(&xk_mass_wait_failed, 1u);
+        return;
+    }
+    for (int o = 16; o > 0; o >>= 1) mass_sum += __shfl_down_sync(0xFFFFFFFFu, mass_sum, o);
+    if (lane == 0) warp_sums[ty] = mass_sum;
+    __syncthreads();
+    if (tid == 0) {
+        unsigned long long s = 0;
+        for (int w = 0; w < XK_MT_BY; ++w) s += warp_sums[w];
+        atomicAdd(total, s);
+    }
+}
+
 // column colour sums of a state (after an upload, before any step)
 __global__ void xk_k_mass_project(const uint32_t *__restrict__ src, uint32_t *__restrict__ proj,
                                   MassParams p)
@@ -374,25 +648,81 @@ static MassParams mass_params(const xk_desc &d)
     return p;
 }
 
-// planes per CTA: enough CTAs for about 2048 per generation
-static int mass_zchunk(const MassParams &p, int gx, int gy)
+// planes per CTA: enough CTAs for about `target` per generation (2048 for
+// the register-queue forms; 1024 for the TMA form, whose CTAs load two halo
+// planes per run and fill a four-stage ring before their first plane)
+static int mass_zchunk(const MassParams &p, int gx, int gy, int target = 2048)
 {
     if (const char *e = getenv("XK_MASS_ZC")) {
         const int v = atoi(e);
         if (v > 0) return v;
     }
     const int64_t tiles = (int64_t)gx * gy;
-    int64_t chunks = (2048 + tiles - 1) / tiles;
+    int64_t chunks = (target + tiles - 1) / tiles;
     if (chunks > p.D) chunks = p.D;
     if (chunks < 1) chunks = 1;
     return (int)((p.D + chunks - 1) / chunks);
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library)
+static PFN_cuTensorMapEncodeTiled_v12000 xk_tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// XK_MASS_KERNEL=rows in the environment selects the register-queue form
+// for widths that are a multiple of 4 instead of the TMA form
+static bool mass_tma_enabled()
+{
+    const char *v = getenv("XK_MASS_KERNEL");
+    return !(v && !strcmp(v, "rows"));
+}
+
 cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long *total,
-                         const xk_desc &d, cudaStream_t s)
+                         const xk_desc &d, bool small, cudaStream_t s)
 {
     const MassParams p = mass_params(d);
     const bool vec = p.W % 4 == 0;
+    if (vec && mass_tma_enabled()) {
+        PFN_cuTensorMapEncodeTiled_v12000 enc = xk_tensor_map_encoder();
+        if (!enc) return cudaErrorNotSupported;
+        CUtensorMap tm;
+        const cuuint64_t dims[3] = {(cuuint64_t)p.W, (cuuint64_t)p.H, (cuuint64_t)p.D};
+        const cuuint64_t strides[2] = {(cuuint64_t)p.W * 4, (cuuint64_t)p.W * p.H * 4};
+        const cuuint32_t box[3] = {XK_MT_COLS, XK_MT_ROWS, 1};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        if (enc(&tm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<uint32_t *>(src), dims, strides, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return cudaErrorInvalidValue;
+        const int gx = (p.W + 127) / 128, gy = (p.H + XK_MT_BY - 1) / XK_MT_BY;
+        const int zc = mass_zchunk(p, gx, gy, 1024);
+        dim3 block(32, XK_MT_BY);
+        dim3 grid(gx, gy, (p.D + zc - 1) / zc);
+        // a lattice whose total mass is below 2^30 keeps every cell below 2^30
+        // (mass is conserved and never negative), so no cell can need the exact
+        // form and no wall value can be inside: the fast-only instantiation.
+        // XK_MASS_GENERAL=1 in the environment takes the general one anyway.
+        const char *g = getenv("XK_MASS_GENERAL");
+        if (small && !(g && g[0] == '1'))
+            xk_k_mass_tma<4, false><<<grid, block, XK_MT_SMEM, s>>>(tm, src, dst, total, p, zc);
+        else
+            xk_k_mass_tma<4, true><<<grid, block, XK_MT_SMEM, s>>>(tm, src, dst, total, p, zc);
+        return cudaGetLastError();
+    }
     const int cells_x = 32 * (vec ? 4 : 1);
     const int gx = (p.W + cells_x - 1) / cells_x, gy = (p.H + XK_MASS_BY - 1) / XK_MASS_BY;
     const int zc = mass_zchunk(p, gx, gy);
@@ -407,6 +737,36 @@ cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long 
     else
         xk_k_mass<1><<<grid, block, 0, s>>>(src, dst, total, p, zc);
     return cudaGetLastError();
+}
+
+__global__ void xk_k_mass_sum(const uint32_t *__restrict__ src, int64_t n, unsigned long long *__restrict__ out)
+{
+    unsigned long long s = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s += src[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
+cudaError_t xk_mass_sum(const uint32_t *src, int64_t n, unsigned long long *out, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    if (blocks < 1) blocks = 1;
+    xk_k_mass_sum<<<(unsigned)blocks, 256, 0, s>>>(src, n, out);
+    return cudaGetLastError();
+}
+
+// copy of the TMA kernel's give-up flag, cleared; true when a CTA gave up
+// waiting for a tensor copy since the last call
+bool xk_mass_take_wait_failure()
+{
+    unsigned int v = 0, z = 0;
+    if (cudaMemcpyFromSymbol(&v, xk_mass_wait_failed, sizeof(v)) != cudaSuccess) return false;
+    if (v) cudaMemcpyToSymbol(xk_mass_wait_failed, &z, sizeof(z));
+    return v != 0;
 }
 
 cudaError_t xk_mass_project(const uint32_t *src, uint32_t *proj, const xk_desc &d, cudaStream_t s)

@@ -323,7 +323,7 @@ static int enqueue_round(xk_server *s, Req *q, int64_t chunk)
         unsigned long long *tot = (unsigned long long *)(base + 2 * rnd(4 * q->n));
         XK_CUDA(cudaMemsetAsync(tot, 0, (size_t)chunk * 8, q->stream));
         for (int64_t g = 0; g < chunk; ++g) {
-            XK_CUDA(xk_mass_step(m[q->cur], m[1 - q->cur], tot + g, q->md, q->stream));
+            XK_CUDA(xk_mass_step(m[q->cur], m[1 - q->cur], tot + g, q->md, false, q->stream));
             q->cur ^= 1;
         }
     }

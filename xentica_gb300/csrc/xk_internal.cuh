@@ -166,8 +166,15 @@ cudaError_t xk_evolife_step(const uint64_t *src, uint64_t *dst, int32_t *col, co
                             float mut_thresh, cudaStream_t s);
 
 // mass-transfer family (mass.cu)
+// small: the lattice's total mass is below 2^30 (then every cell stays below
+// it for good), which allows the fast-only kernel
 cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long *total,
-                         const xk_desc &d, cudaStream_t s);
+                         const xk_desc &d, bool small, cudaStream_t s);
+// total of n cells into *out (64-bit)
+cudaError_t xk_mass_sum(const uint32_t *src, int64_t n, unsigned long long *out, cudaStream_t s);
+// true when a mass-transfer CTA gave up waiting for a tensor copy since the
+// last call (the flag is cleared)
+bool xk_mass_take_wait_failure();
 cudaError_t xk_mass_project(const uint32_t *src, uint32_t *proj, const xk_desc &d, cudaStream_t s);
 cudaError_t xk_mass_colors(const uint32_t *src, int32_t *col, int64_t n, cudaStream_t s);
 cudaError_t xk_mass_render(const uint32_t *proj, int32_t *img, const xk_desc &d, int width,
