@@ -282,13 +282,22 @@ def run_reference_arm(args, dist):
 def run_ours(args, dist):
     from xentica_gb300 import build as xk_build
     from xentica_gb300 import _native as nat
+    t_host = time.perf_counter()
     widths, heights, rules, dens, cells = workload(args, dist.rank)   # before any GPU call
+    host_seed_s = time.perf_counter() - t_host
     xk_build.build()
     nat.set_device(dist.local)
-    from xentica_gb300.batch import Ensemble
+    from xentica_gb300.batch import Ensemble, ensemble_seeds
     ens = Ensemble(widths, heights, rules)
     total = ens.total_cells
     G = args.generations
+    # the same cells drawn on the device (MT19937 per lattice), checked bit for bit
+    seeds = ensemble_seeds(args.instances, args.seed + 7919 * dist.rank)[4]
+    ens.seed_bernoulli(seeds, dens)
+    seed_ms = ens.seed_bernoulli(seeds, dens)
+    seed_exact = bool(np.array_equal(ens.download(), cells))
+    if not seed_exact:
+        raise SystemExit("device seeding disagrees with the host draw")
     ens.upload(cells)
     rows_per_band = ens.tune(G)
     ens.upload(cells)
@@ -356,6 +365,11 @@ def run_ours(args, dist):
                     "d2h_bytes_per_step": total, "ms_per_step": e2e_s * 1000 / args.steps},
             "plain": {"value": plain_value, "unit": "cell-updates/s", "generations": pg,
                       "batched_over_plain": value / dist.world / plain_value},
+            "seeding": {"device_ms": seed_ms, "host_s": host_seed_s, "bit_exact": seed_exact,
+                        "note": "the %d lattices' Bernoulli cells drawn on the device (one "
+                                "MT19937 stream per lattice, NumPy's random_sample) against "
+                                "the host draw (RandomState per lattice, %d processes)"
+                                % (args.instances, min(32, os.cpu_count() or 1))},
             "gpu_launches": launches, "wall_s": wall, "roofline": roofline, "clocks": clk}
     if dist.rank == 0:
         line["cpu_baseline"] = cpu_sample(widths, heights, rules, cells, ens.offsets,

@@ -175,6 +175,14 @@ int xk_batch_step_plain(xk_batch *b, int32_t generations);
  * (XK_E2E=chunks in the environment forces that form). */
 int xk_batch_run(xk_batch *b, const uint8_t *host_in, uint8_t *host_out,
                  int64_t total_cells, int32_t generations);
+/* Seed every instance on the device: cell j of instance i =
+ * (RandomState(seeds[i]).random_sample(W_i * H_i)[j] < p[i]), bit for bit
+ * NumPy's legacy MT19937 stream (the draw a seed pattern makes through
+ * xentica/seeds/random.py:22-54 LocalRandom.numpy; the reference's seeds are
+ * host NumPy arrays packed by xentica/core/base.py:510-524), so a huge
+ * ensemble needs no host array.  One CTA per instance; last_step_ms is the
+ * device time. */
+int xk_batch_seed_bernoulli(xk_batch *b, const uint32_t *seeds, const double *p);
 /* Autotune the batched kernel's block size for this batch (timed on device). */
 int xk_batch_tune(xk_batch *b, int32_t generations, int32_t *chosen_rows_per_band);
 int64_t xk_batch_total_cells(const xk_batch *b);

@@ -96,6 +96,7 @@ SIGNATURES = {
     "xk_batch_download": (_I32, [_P, _P, _I64]),
     "xk_batch_step": (_I32, [_P, _I32]),
     "xk_batch_step_plain": (_I32, [_P, _I32]),
+    "xk_batch_seed_bernoulli": (_I32, [_P, _P, _P]),
     "xk_batch_run": (_I32, [_P, _P, _P, _I64, _I32]),
     "xk_batch_tune": (_I32, [_P, _I32, ctypes.POINTER(_I32)]),
     "xk_batch_total_cells": (_I64, [_P]),

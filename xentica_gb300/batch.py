@@ -18,7 +18,7 @@ from xentica_gb300 import _native as nat
 from xentica_gb300.core.exceptions import XenticaException
 from xentica_gb300.tools.rules import LifeLike
 
-__all__ = ['Ensemble', 'ensemble_workload', 'hash64']
+__all__ = ['Ensemble', 'ensemble_workload', 'ensemble_seeds', 'hash64']
 
 
 def hash64(base_seed, index):
@@ -36,6 +36,20 @@ def _seed_state(args):
     return (rng.random_sample(n) < p).astype(np.uint8)
 
 
+def ensemble_seeds(count=4096, base_seed=2041, sides=(64, 128, 256, 512, 1024)):
+    """The seeded ensemble without its cells: ``(widths, heights, rules,
+    densities, seeds)``, ``seeds[i]`` the 32-bit RandomState seed of lattice
+    ``i``'s cells (see :func:`ensemble_workload`; :meth:`Ensemble.seed_bernoulli`
+    draws the same cells on the device)."""
+    rng = np.random.RandomState(hash64(base_seed, 0) & 0xFFFFFFFF)
+    widths = rng.choice(sides, count).astype(np.int32)
+    heights = rng.choice(sides, count).astype(np.int32)
+    rules = rng.randint(0, 2 ** 18, count).astype(np.uint32)
+    dens = rng.uniform(0.1, 0.6, count)
+    seeds = np.array([hash64(base_seed, i + 1) & 0xFFFFFFFF for i in range(count)], dtype=np.uint32)
+    return widths, heights, rules, dens, seeds
+
+
 def ensemble_workload(count=4096, base_seed=2041, sides=(64, 128, 256, 512, 1024), pool=None):
     """Seeded ensemble: sizes, rules, densities and initial states.
 
@@ -45,12 +59,8 @@ def ensemble_workload(count=4096, base_seed=2041, sides=(64, 128, 256, 512, 1024
     ``RandomState(hash64(base_seed, i + 1)).random_sample(n) < p``.
     ``pool`` (a ``multiprocessing`` pool) parallelises the cell draws.
     """
-    rng = np.random.RandomState(hash64(base_seed, 0) & 0xFFFFFFFF)
-    widths = rng.choice(sides, count).astype(np.int32)
-    heights = rng.choice(sides, count).astype(np.int32)
-    rules = rng.randint(0, 2 ** 18, count).astype(np.uint32)
-    dens = rng.uniform(0.1, 0.6, count)
-    jobs = [(hash64(base_seed, i + 1), int(widths[i]) * int(heights[i]), float(dens[i]))
+    widths, heights, rules, dens, seeds = ensemble_seeds(count, base_seed, sides)
+    jobs = [(int(seeds[i]), int(widths[i]) * int(heights[i]), float(dens[i]))
             for i in range(count)]
     parts = pool.map(_seed_state, jobs, chunksize=16) if pool else [_seed_state(j) for j in jobs]
     return widths, heights, rules, dens, np.concatenate(parts)
@@ -136,6 +146,20 @@ class Ensemble:
     def launches(self, generations):
         """Kernel launches one :meth:`step` of ``generations`` makes."""
         return int(self._lib.xk_batch_launches(self._handle, int(generations)))
+
+    def seed_bernoulli(self, seeds, densities):
+        """Draw every lattice's cells on the device: cell ``j`` of lattice
+        ``i`` is ``RandomState(seeds[i]).random_sample(n_i)[j] < densities[i]``,
+        bit for bit (the cells :func:`ensemble_workload` makes on the host
+        when given the seeds of :func:`ensemble_seeds`).  Returns the device
+        time in ms."""
+        seeds = np.ascontiguousarray(seeds, dtype=np.uint32)
+        dens = np.ascontiguousarray(densities, dtype=np.float64)
+        if seeds.size != self.count or dens.size != self.count:
+            raise XenticaException("one seed and one density per lattice")
+        nat.check(self._lib.xk_batch_seed_bernoulli(self._handle, nat.ptr(seeds), nat.ptr(dens)),
+                  "xk_batch_seed_bernoulli")
+        return self._lib.xk_last_step_ms()
 
     def tune(self, generations):
         """Pick the resident kernel's band length by timing; returns it."""

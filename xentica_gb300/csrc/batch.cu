@@ -411,6 +411,36 @@ extern "C" int xk_batch_step(xk_batch *b, int32_t generations)
     return check_bad(b);
 }
 
+extern "C" int xk_batch_seed_bernoulli(xk_batch *b, const uint32_t *seeds, const double *p)
+{
+    XK_REQUIRE(b && seeds && p, XK_ERR_ARG, "xk_batch_seed_bernoulli: null argument");
+    std::vector<XkSeedJob> jobs(b->n);
+    for (int i = 0; i < b->n; ++i) {
+        jobs[i].off = b->off[i];
+        jobs[i].n = (int64_t)b->W[i] * b->H[i];
+        jobs[i].seed = seeds[i];
+        jobs[i].pad = 0;
+        jobs[i].p = p[i];
+    }
+    // the longest streams first: their CTAs start in the first wave
+    std::stable_sort(jobs.begin(), jobs.end(),
+                     [](const XkSeedJob &a, const XkSeedJob &c) { return a.n > c.n; });
+    XkSeedJob *d_jobs = nullptr;
+    XK_CUDA(cudaMallocAsync(&d_jobs, jobs.size() * sizeof(XkSeedJob), b->stream));
+    cudaError_t e = cudaMemcpyAsync(d_jobs, jobs.data(), jobs.size() * sizeof(XkSeedJob),
+                                    cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev0, b->stream);
+    if (e == cudaSuccess) e = xk_seed_bernoulli(d_jobs, b->n, b->cells, b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev1, b->stream);
+    cudaFreeAsync(d_jobs, b->stream);
+    XK_CUDA(e);
+    XK_CUDA(cudaEventSynchronize(b->ev1));
+    float ms = 0.f;
+    XK_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    xk_set_last_step_ms(ms);
+    return XK_OK;
+}
+
 extern "C" int xk_batch_step_plain(xk_batch *b, int32_t generations)
 {
     XK_REQUIRE(b, XK_ERR_ARG, "xk_batch_step_plain: null batch");

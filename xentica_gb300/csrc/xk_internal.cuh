@@ -165,6 +165,15 @@ cudaError_t xk_evolife_set_positional(const double *lut54);
 cudaError_t xk_evolife_step(const uint64_t *src, uint64_t *dst, int32_t *col, const xk_desc &d,
                             float mut_thresh, cudaStream_t s);
 
+// Bernoulli seeds (seed.cu): cells[off .. off + n) of a lattice =
+// RandomState(seed).random_sample(n) < p, bit for bit
+struct XkSeedJob {
+    int64_t off, n;
+    uint32_t seed, pad;
+    double p;
+};
+cudaError_t xk_seed_bernoulli(const XkSeedJob *jobs, int count, uint8_t *cells, cudaStream_t s);
+
 // mass-transfer family (mass.cu)
 // small: the lattice's total mass is below 2^30 (then every cell stays below
 // it for good), which allows the fast-only kernel
