@@ -32,16 +32,20 @@ def _oracle_step(model, fld, col, steps):
                   smooth=info["smooth"])
 
 
-@pytest.mark.parametrize("legacy,mutation", [(True, 0.0), (False, 0.2), (True, 0.0001)])
-def test_random_states_vs_oracle(legacy, mutation):
+@pytest.mark.parametrize("legacy,mutation,live", [(True, 0.0, 0.6), (False, 0.2, 0.6),
+                                                  (True, 0.0001, 0.6), (True, 0.0, 0.02),
+                                                  (False, 0.2, 0.02), (True, 0.0001, 0.005)])
+def test_random_states_vs_oracle(legacy, mutation, live):
+    # live: share of cells with a rule; sparse lattices put whole warps of
+    # cells with no parent on the composed-RNG path
     w, h = 131, 103          # at least the BigBang seed area (100 x 100)
     model = _model((w, h), legacy, mutation_prob=mutation, death_speed=9, max_genes=7,
                    fade_in=30, fade_out=7)
-    rng = np.random.RandomState(int(mutation * 1e4) + legacy)
+    rng = np.random.RandomState(int(mutation * 1e4) + legacy + int(live * 1000))
     n = w * h
     energy = rng.randint(0, 300, n).astype(np.uint64)
-    rule = rng.randint(0, 2 ** 18, n).astype(np.uint64) * (rng.random_sample(n) < 0.6)
-    rnd = rng.randint(0, 2 ** 16 - 1, n).astype(np.uint64)
+    rule = rng.randint(0, 2 ** 18, n).astype(np.uint64) * (rng.random_sample(n) < live)
+    rnd = rng.randint(0, 2 ** 16, n).astype(np.uint64)     # 65535 included
     cells = energy + (rule << np.uint64(9)) + (rnd << np.uint64(27))
     colors = rng.randint(0, 256, 3 * n).astype(np.int32)
     model.gpu.load(cells, colors)

@@ -119,6 +119,7 @@ struct EvoParams {
     int32_t fade_in, fade_out, smooth;
     uint32_t kmul[9];          // parent draw for 0..8 parents (0: none)
     uint32_t kstart;           // start-gene draw (n = 18)
+    uint32_t jump_a, jump_c;   // the crossover's RNG advances as one map x -> (a x + c) % 65535
 };
 
 static float evo_u(uint32_t x) { return (float)x / 65535.0f; }
@@ -139,6 +140,23 @@ static uint32_t evo_find_multiplier(uint32_t n)
             if (ok) return (uint32_t)k;
         }
     return 0;   // not reached for n <= 18 (checked by the EvoLife GPU tests)
+}
+
+// The crossover advances the RNG once for the start gene and once (twice
+// with mutation) per gene: 19 or 37 applications of x -> (58321 x + 11113)
+// mod 65535, composed into one affine map.  For every 16-bit x the composed
+// a x + c stays below 2^32 (a, c < 65535).
+static void evo_jump(EvoParams &p)
+{
+    const uint64_t m = 65535;
+    uint64_t a = 1, c = 0;
+    const int steps = 1 + 18 * (p.mutation ? 2 : 1);
+    for (int k = 0; k < steps; ++k) {
+        a = (58321 * a) % m;
+        c = (58321 * c + 11113) % m;
+    }
+    p.jump_a = (uint32_t)a;
+    p.jump_c = (uint32_t)c;
 }
 
 static std::once_flag g_evo_once;
@@ -222,25 +240,32 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
         }
     }
     const uint32_t old_rule = rule, old_energy = energy;
-    // genome_crossover(main, 18, *genomes, max_genes, mutation_prob)
-    rng = xk_lcg(rng);
-    const uint32_t start_gene = __umulhi(rng, p.kstart) % 8u;
-    const uint32_t kn = p.kmul[n];
-    uint32_t new_genome = 0, num_active = 0;
-    uint32_t gene = start_gene;
-    for (int step = 0; step < 18; ++step) {
+    // genome_crossover(main, 18, *genomes, max_genes, mutation_prob).  With
+    // no parent, every gene is 0 (no winner, and a mutation needs a gene that
+    // some parent has): only the RNG advances, by the composed map.
+    uint32_t new_genome = 0;
+    if (n == 0) {
+        rng = (p.jump_a * rng + p.jump_c) % 65535u;
+    } else {
         rng = xk_lcg(rng);
-        const uint32_t winner = __umulhi(rng, kn);
-        uint32_t new_gene = (winner < n) ? ((gsm[winner][tid] >> gene) & 1u) : 0u;
-        num_active += new_gene;
-        new_gene *= (uint32_t)(num_active <= p.max_genes);
-        uint32_t mutated = 0;
-        if (p.mutation) {
+        const uint32_t start_gene = __umulhi(rng, p.kstart) % 8u;
+        const uint32_t kn = p.kmul[n];
+        uint32_t num_active = 0;
+        uint32_t gene = start_gene;
+        for (int step = 0; step < 18; ++step) {
             rng = xk_lcg(rng);
-            mutated = (uint32_t)((int32_t)rng <= p.mut_x) & ((any >> gene) & 1u);
+            const uint32_t winner = __umulhi(rng, kn);
+            uint32_t new_gene = (winner < n) ? ((gsm[winner][tid] >> gene) & 1u) : 0u;
+            num_active += new_gene;
+            new_gene *= (uint32_t)(num_active <= p.max_genes);
+            uint32_t mutated = 0;
+            if (p.mutation) {
+                rng = xk_lcg(rng);
+                mutated = (uint32_t)((int32_t)rng <= p.mut_x) & ((any >> gene) & 1u);
+            }
+            new_genome += (new_gene ^ mutated) << gene;
+            gene = gene == 17 ? 0 : gene + 1;
         }
-        new_genome += (new_gene ^ mutated) << gene;
-        gene = gene == 17 ? 0 : gene + 1;
     }
     rule = new_genome + rule * (uint32_t)(new_genome == 0);
     const uint32_t is_live = (uint32_t)(old_energy < 255u) &
@@ -287,6 +312,7 @@ cudaError_t xk_evolife_step(const uint64_t *src, uint64_t *dst, int32_t *col, co
     p.fade_out = d.fade_out;
     p.smooth = d.smooth;
     evo_draws(p, mut_thresh);
+    evo_jump(p);
     dim3 block(XK_EVO_BX, XK_EVO_BY);
     dim3 grid((p.W + XK_EVO_BX - 1) / XK_EVO_BX, (p.H + XK_EVO_BY - 1) / XK_EVO_BY);
     xk_k_evolife<<<grid, block, 0, s>>>(src, dst, col, p);
