@@ -35,6 +35,17 @@ __device__ __forceinline__ uint32_t xk_spread_nibbles(uint32_t b)
     return b;
 }
 
+// bit j of the result = bit (s + j) mod 18 of v (v < 2^18, s < 18), and back
+__device__ __forceinline__ uint32_t xk_rot18(uint32_t v, uint32_t s)
+{
+    return ((v >> s) | (v << (18u - s))) & 0x3FFFFu;
+}
+
+__device__ __forceinline__ uint32_t xk_unrot18(uint32_t w, uint32_t s)
+{
+    return ((w << s) | (w >> (18u - s))) & 0x3FFFFu;
+}
+
 __device__ __forceinline__ int xk_ma_clamp(int v, int old, int fade_in, int fade_out)
 {
     int m = v < old + fade_in ? v : old + fade_in;
@@ -228,16 +239,13 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
         const uint32_t fit = np * (uint32_t)(np == (uint32_t)(g + 1));
         num_fit = num_fit > fit ? num_fit : fit;
     }
-    // parents: rules with the winning birth count, compacted in neighbour order
+    // parents: rules with the winning birth count, in neighbour order
     uint32_t n = 0, any = 0;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         const uint32_t genome = nr[k] * (((nr[k] & 510u) >> num_fit) & 1u);
-        if (genome > 0) {
-            gsm[n][tid] = genome;
-            ++n;
-            any |= genome;
-        }
+        n += genome > 0;
+        any |= genome;
     }
     const uint32_t old_rule = rule, old_energy = energy;
     // genome_crossover(main, 18, *genomes, max_genes, mutation_prob).  With
@@ -249,23 +257,38 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
     } else {
         rng = xk_lcg(rng);
         const uint32_t start_gene = __umulhi(rng, p.kstart) % 8u;
+        // genes are visited from start_gene, wrapping at 18: the parents and
+        // the mutation mask are rotated so that step j reads bit j (the
+        // unrolled loop then shifts by constants), the result rotated back
+        uint32_t slot = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t genome = nr[k] * (((nr[k] & 510u) >> num_fit) & 1u);
+            if (genome > 0) {
+                gsm[slot][tid] = xk_rot18(genome, start_gene);
+                ++slot;
+            }
+        }
+        const uint32_t any_rot = xk_rot18(any, start_gene);
         const uint32_t kn = p.kmul[n];
-        uint32_t num_active = 0;
-        uint32_t gene = start_gene;
-        for (int step = 0; step < 18; ++step) {
+        uint32_t num_active = 0, rot_genome = 0;
+#pragma unroll
+        for (int j = 0; j < 18; ++j) {
             rng = xk_lcg(rng);
+            // winner < n for every state: the multiplier reproduces
+            // trunc(RN(u * n)) with u = x / 65535 < 1
             const uint32_t winner = __umulhi(rng, kn);
-            uint32_t new_gene = (winner < n) ? ((gsm[winner][tid] >> gene) & 1u) : 0u;
+            uint32_t new_gene = (gsm[winner][tid] >> j) & 1u;
             num_active += new_gene;
             new_gene *= (uint32_t)(num_active <= p.max_genes);
             uint32_t mutated = 0;
             if (p.mutation) {
                 rng = xk_lcg(rng);
-                mutated = (uint32_t)((int32_t)rng <= p.mut_x) & ((any >> gene) & 1u);
+                mutated = (uint32_t)((int32_t)rng <= p.mut_x) & ((any_rot >> j) & 1u);
             }
-            new_genome += (new_gene ^ mutated) << gene;
-            gene = gene == 17 ? 0 : gene + 1;
+            rot_genome |= (new_gene ^ mutated) << j;
         }
+        new_genome = xk_unrot18(rot_genome, start_gene);
     }
     rule = new_genome + rule * (uint32_t)(new_genome == 0);
     const uint32_t is_live = (uint32_t)(old_energy < 255u) &
