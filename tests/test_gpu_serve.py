@@ -17,6 +17,7 @@ from xentica_gb300.core.exceptions import XenticaException
 pytestmark = pytest.mark.gpu
 
 WALL = 2 ** 32 - 1
+BIG_MASS_SHAPE = (16, 12, 10)      # mass requests of this shape get cells at and above 2^30
 
 
 def oracle_result(kind, cells, rule, generations):
@@ -47,7 +48,8 @@ SPECS = [  # kind, shape, rule, generations
     ("life2d", (5, 33), 3 | (12 << 9), 9),
     ("life3d", (13, 17, 20), 0b0001100_0000100, 40),
     ("life3d", (7, 5, 9), 0b0011000_0001010, 3),
-    ("mass", (12, 20, 24), 0, 45),           # W % 4 == 0: tiled kernel
+    ("mass", (12, 20, 24), 0, 45),           # W % 4 == 0: TMA kernel, fast-only (small total)
+    ("mass", BIG_MASS_SHAPE, 0, 20),         # large masses and walls: TMA kernel, general form
     ("mass", (7, 9, 23), 0, 30),             # generic kernel
     ("life2d", (64, 64), 6152, 0),           # zero generations: the input back
 ]
@@ -56,7 +58,11 @@ SPECS = [  # kind, shape, rule, generations
 def _cells(kind, shape, seed):
     rng = np.random.RandomState(seed)
     if kind == "mass":
-        return rng.poisson(6, shape).astype(np.uint32)
+        cells = rng.poisson(6, shape).astype(np.uint32)
+        if shape == BIG_MASS_SHAPE:
+            flat = cells.reshape(-1)
+            flat[rng.randint(0, flat.size, 12)] = rng.choice([2 ** 30, 1431655766, WALL], 12)
+        return cells
     return (rng.random_sample(shape) < 0.4).astype(np.uint8)
 
 

@@ -81,6 +81,7 @@ struct Req {
     int threads = 0, smem = 0;
     double t_submit = -1, t_admit = -1, t_done = -1;
     uint64_t mass_total = 0;
+    bool mass_small = false;   // initial total below 2^30
 };
 
 struct Group {
@@ -323,7 +324,7 @@ static int enqueue_round(xk_server *s, Req *q, int64_t chunk)
         unsigned long long *tot = (unsigned long long *)(base + 2 * rnd(4 * q->n));
         XK_CUDA(cudaMemsetAsync(tot, 0, (size_t)chunk * 8, q->stream));
         for (int64_t g = 0; g < chunk; ++g) {
-            XK_CUDA(xk_mass_step(m[q->cur], m[1 - q->cur], tot + g, q->md, false, q->stream));
+            XK_CUDA(xk_mass_step(m[q->cur], m[1 - q->cur], tot + g, q->md, q->mass_small, q->stream));
             q->cur ^= 1;
         }
     }
@@ -697,9 +698,15 @@ extern "C" int xk_serve_submit(xk_server *s, const xk_request *req, const void *
                              (unsigned)src[i]);
                 return XK_ERR_ARG;
             }
-    } else if (req->generations == 0) {
+    } else {
+        // the initial total: the result's total when no generation runs, and
+        // below 2^30 the fast-only kernel (mass is conserved, so every cell
+        // stays below 2^30)
         const uint32_t *m = (const uint32_t *)host_cells;
-        for (int64_t i = 0; i < q->n; ++i) q->mass_total += m[i];
+        uint64_t total = 0;
+        for (int64_t i = 0; i < q->n; ++i) total += m[i];
+        q->mass_small = total < (1ull << 30);
+        if (req->generations == 0) q->mass_total = total;
     }
     q->input.assign(src, src + q->n * q->esz);
     {
