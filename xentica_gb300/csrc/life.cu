@@ -271,15 +271,23 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
             lat[xk_res_at(p, b, i, jj)] = src[w];
         }
     }
-    if (threadIdx.x < 9) {
-        // first-level multiplexer coefficients (LifeTable) of this rule
+    if (threadIdx.x < 10) {
+        // first-level multiplexer coefficients (LifeTable9) of this rule:
+        // masks of dead D[n] = rule0 bit n, live L[n] = rule1 bit n - 1
+        auto D = [&](int n) { return 0u - ((I.rule0 >> n) & 1u); };
+        auto L = [&](int n) { return 0u - ((I.rule1 >> (n > 0 ? n - 1 : 0)) & 1u); };
         const int q = threadIdx.x;
-        const uint32_t r = q < 4 ? I.rule0 : I.rule1;
-        const int n = 2 * (q & 3);
-        const uint32_t A = q < 8 ? 0u - ((r >> n) & 1u) : 0u - ((I.rule0 >> 8) & 1u);
-        const uint32_t B = q < 8 ? 0u - ((r >> (n + 1)) & 1u) : 0u - ((I.rule1 >> 8) & 1u);
-        tabs[2 * q] = A;
-        tabs[2 * q + 1] = xk_mux_coef(A, B);
+        if (q < 8) {
+            const uint32_t A = q < 4 ? D(2 * q) : L(2 * (q - 4));
+            const uint32_t B = q < 4 ? D(2 * q + 1) : L(2 * (q - 4) + 1);
+            tabs[2 * q] = A;
+            tabs[2 * q + 1] = xk_mux_coef(A, B);
+        } else if (q == 8) {
+            tabs[16] = D(8);
+        } else {
+            tabs[17] = L(8);
+            tabs[18] = xk_mux_coef(L(8), L(9));
+        }
     }
 
     const int q = lane / p.P, j = lane - q * p.P;
@@ -306,14 +314,15 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
     const int hdn = bc + 1 < p.nb ? bc + 1 : 0;         // band holding the row below
     const bool full = (H % p.L) == 0;                   // every band has L rows
     __syncthreads();
-    LifeTable t;
+    LifeTable9 t;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         t.a[q] = tabs[2 * q];
         t.k[q] = tabs[2 * q + 1];
     }
-    t.a8 = tabs[16];
-    t.k8 = tabs[17];
+    t.d8 = tabs[16];
+    t.a9 = tabs[17];
+    t.k9 = tabs[18];
 
     for (int gen = 0; gen < generations; ++gen) {
         if (active) {
@@ -347,7 +356,7 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
             // per CTA and taken outside the row loop.
             uint32_t su = xk_lop3_xor3(vu.L, vu.C, vu.R), cu = xk_maj(vu.L, vu.C, vu.R);
             uint32_t sm_ = xk_lop3_xor3(vm.L, vm.C, vm.R), cm_ = xk_maj(vm.L, vm.C, vm.R);
-            uint32_t Lm = vm.L, Cm = vm.C, Rm = vm.R;
+            uint32_t Cm = vm.C;
             constexpr int stride = 32;                          // words between band rows
             uint32_t *wp = lat + xk_res_at(p, bc, 0, jc);       // this lane's word of row i
             const uint32_t whalo = halo[(hdn * 2 + 0) * wpr + jc];
@@ -366,16 +375,14 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
                         Rd = d.R;
                     }
                     const uint32_t sd = xk_lop3_xor3(Ld, wd, Rd), cd = xk_maj(Ld, wd, Rd);
-                    uint32_t out = xk_life_word_fa(su, cu, Lm, Cm, Rm, sd, cd, t);
+                    uint32_t out = xk_life_word9(su, cu, sm_, cm_, sd, cd, Cm, t);
                     if (!FULLW) out &= outmask;
                     if (active) *dst = out;
                     su = sm_;
                     cu = cm_;
                     sm_ = sd;
                     cm_ = cd;
-                    Lm = Ld;
                     Cm = wd;
-                    Rm = Rd;
                 };
                 if (p.L == 1) {
                     row(whalo, wp);
@@ -416,7 +423,9 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
                     vd = xk_row_vec(wd, l, r, lshift, top, edge, edge, use_le, use_re);
                     if (off_d) vd.L = vd.C = vd.R = bfill;
                 }
-                const uint32_t out = xk_life_word(vu.L, vu.C, vu.R, vm.L, vm.C, vm.R, vd.L, vd.C, vd.R, t);
+                const uint32_t out = xk_life_word9(
+                    xk_lop3_xor3(vu.L, vu.C, vu.R), xk_maj(vu.L, vu.C, vu.R), xk_lop3_xor3(vm.L, vm.C, vm.R),
+                    xk_maj(vm.L, vm.C, vm.R), xk_lop3_xor3(vd.L, vd.C, vd.R), xk_maj(vd.L, vd.C, vd.R), vm.C, t);
                 if (row_ok) lat[xk_res_at(p, bc, i, jc)] = out & outmask;
                 vu = vm;
                 vm = vd;

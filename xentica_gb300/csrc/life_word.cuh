@@ -6,6 +6,8 @@
 
 #include <stdint.h>
 
+#include "xk_internal.cuh"
+
 // Three-input boolean functions as single lop3 instructions (PTX lop3.b32:
 // the immediate is the function evaluated on a = 0xF0, b = 0xCC, c = 0xAA).
 __device__ __forceinline__ uint32_t xk_lop3_mux(uint32_t sel, uint32_t a, uint32_t b)
@@ -102,6 +104,34 @@ __device__ __forceinline__ uint32_t xk_life_word_fa(uint32_t su, uint32_t cu, ui
     const uint32_t low = xk_mux(Cm, dead, live);
     const uint32_t eight = xk_imux(Cm, t.a8, t.k8);
     return xk_mux(b3, low, eight);
+}
+
+// Next state of 32 cells from the column sums (s, c) = FA(L, C, R) of the
+// rows above (u), at (m) and below (d) -- the 3 x 3 block including the cell
+// -- and the cells themselves (C).  A row's sums are computed once, when it
+// is the row below, and reused twice; the count n9 = (su + sm + sd) +
+// 2 (cu + cm + cd) <= 9 needs one fewer logic instruction than the
+// neighbour count of xk_life_word_fa, and the rule is indexed by it
+// (LifeTable9).
+__device__ __forceinline__ uint32_t xk_life_word9(uint32_t su, uint32_t cu, uint32_t sm, uint32_t cm,
+                                                  uint32_t sd, uint32_t cd, uint32_t C,
+                                                  const LifeTable9 &t)
+{
+    const uint32_t b0 = xk_lop3_xor3(su, sm, sd), k1 = xk_maj(su, sm, sd);
+    const uint32_t tw = xk_lop3_xor3(cu, cm, cd), k2 = xk_maj(cu, cm, cd);
+    const uint32_t b1 = tw ^ k1, k3 = tw & k1;
+    const uint32_t b2 = k2 ^ k3, b3 = k2 & k3;   // b3: n9 is 8 or 9, so b1 = b2 = 0
+    uint32_t m[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) m[q] = xk_imux(b0, t.a[q], t.k[q]);
+    uint32_t n[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) n[q] = xk_mux(b1, m[2 * q], m[2 * q + 1]);
+    const uint32_t dead = xk_mux(b2, n[0], n[1]);
+    const uint32_t live = xk_mux(b2, n[2], n[3]);
+    const uint32_t low = xk_mux(C, dead, live);
+    const uint32_t high = xk_mux(C, t.d8, xk_imux(b0, t.a9, t.k9));
+    return xk_mux(b3, low, high);
 }
 
 // Neighbour vectors of word j of a row, given the row's word and the words

@@ -43,6 +43,17 @@ struct LifeTable {
     uint32_t a8, k8;
 };
 
+// The same rule over the count n9 of the 3 x 3 block including the cell
+// (0..9; a live cell's n9 is its neighbour count + 1): dead D[n] = T[0][n],
+// live L[n] = T[1][n - 1] (L[0] never occurs and repeats L[1]).  Pairs by
+// the count's bit 0: q < 4 (D[2q], D[2q + 1]), q >= 4 (L[2(q - 4)],
+// L[2(q - 4) + 1]); n9 of 8 or 9: D[8] for a dead cell, the pair (L[8], L[9])
+// (a9, k9) for a live one.
+struct LifeTable9 {
+    uint32_t a[8], k[8];
+    uint32_t d8, a9, k9;
+};
+
 __host__ __device__ inline uint32_t xk_mux_coef(uint32_t A, uint32_t B)
 {
     return A == B ? 0u : (A ? 0xFFFFFFFFu : 1u);
