@@ -292,7 +292,7 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
     XK_REQUIRE(n <= (1LL << 40), XK_ERR_ARG, "lattice of %lld cells too large", (long long)n);
     XK_REQUIRE(d.family == XK_FAMILY_LIFE || d.family == XK_FAMILY_EVOLIFE ||
                    d.family == XK_FAMILY_MASS || d.family == XK_FAMILY_VM,
-               XK_ERR_UNSUPPORTED, "model family %d is not available in this build", d.family);
+               XK_ERR_UNSUPPORTED, "model family %d has no kernel in this library", d.family);
     if (d.family == XK_FAMILY_MASS)
         XK_REQUIRE(d.ndim == 3 && d.nbr == 6 && !d.torus && d.state_bytes == 4, XK_ERR_ARG,
                    "mass transfer needs a 3-D von Neumann lattice of 32-bit cells with a wall");
