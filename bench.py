@@ -770,6 +770,17 @@ def run_serve(args, dist):
     srv.close()
     value = main_run["value"]
     h2d = sum(c.nbytes for c in cells)
+    # algorithmic bytes of the mix in the reference's format: 2 B per Life-like
+    # cell-update (uint8 read + write), 8 B per mass-transfer one (uint32)
+    alg_bytes = sum(w * (8 if sp["kind"] == "mass" else 2) for w, sp in zip(work, specs))
+    peak, peak_kind = measured_peak()
+    achieved = alg_bytes * dist.world / main_run["span_s"] / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                "note": "whole mix over the run's span (arrivals at %.0f %% of capacity, so the "
+                        "GPU idles between requests); 2 B per Life-like and 8 B per "
+                        "mass-transfer cell-update; many kernels, so no single traffic figure"
+                        % (100 * args.load)}
     kinds = {k: sum(1 for sp in specs if sp["kind"] == k) for k in ("life2d", "life3d", "mass")}
     line = {"metric": "cell-updates/s (serving, Poisson arrivals)", "value": value,
             "unit": "cell-updates/s", "n_gpus": dist.world, "steps": len(specs),
@@ -790,7 +801,7 @@ def run_serve(args, dist):
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d / len(specs),
                     "d2h_bytes_per_step": h2d / len(specs),
                     "note": "requests enter and leave through host memory"},
-            "gpu_launches": main_run["launches"], "roofline": None, "clocks": clk}
+            "gpu_launches": main_run["launches"], "roofline": roofline, "clocks": clk}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
 
