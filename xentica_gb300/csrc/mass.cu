@@ -34,6 +34,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 
 #include "xk_internal.cuh"
 
@@ -491,9 +492,13 @@ xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict
     int k_taken = -1;
     auto advance = [&]() {
         ++k_taken;
-        if (tid == 0 && k_taken + XK_MT_STAGES < nplanes)
-            xk_mt_issue(&tm, stage0 + st_idx * XK_MT_STAGE_STRIDE, bar0 + 8 * st_idx, x_lo, y_lo,
-                        z0 - 1 + k_taken + XK_MT_STAGES);
+        // warp 0 alone (a warp-uniform branch: the other warps skip the
+        // issue code instead of running it predicated off), lane 0 issues
+        if (ty == 0 && k_taken + XK_MT_STAGES < nplanes) {
+            if (lane == 0)
+                xk_mt_issue(&tm, stage0 + st_idx * XK_MT_STAGE_STRIDE, bar0 + 8 * st_idx, x_lo, y_lo,
+                            z0 - 1 + k_taken + XK_MT_STAGES);
+        }
         if (++st_idx == XK_MT_STAGES) {
             st_idx = 0;
             par ^= 1u;
@@ -523,7 +528,9 @@ xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict
     // on-board neighbours in x and y of the four cells
     const int cy = (y > 0) + (y + 1 < p.H);
     const uint32_t c0 = cy + 1 + (x0 > 0), c3 = cy + 1 + (x0 + 4 < p.W), c12 = cy + 2;
-    unsigned long long mass_sum = 0;
+    // the fast-only form runs when the lattice's whole total is below 2^30,
+    // so every partial sum of its cells fits 32 bits
+    typename std::conditional<GENERAL, unsigned long long, uint32_t>::type mass_sum = 0;
     uint32_t off = in ? (uint32_t)z0 * plane + (uint32_t)y * p.W + x0 : 0u;
     int z = z0;
     // one plane: take plane z + 1 into (mn, qn) and tile qnext, then compute
@@ -569,7 +576,10 @@ xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict
         }
         if (in) {
             *reinterpret_cast<uint4 *>(dst + off) = make_uint4(out[0], out[1], out[2], out[3]);
-            mass_sum += (unsigned long long)out[0] + out[1] + (unsigned long long)out[2] + out[3];
+            if (GENERAL)
+                mass_sum += (unsigned long long)out[0] + out[1] + (unsigned long long)out[2] + out[3];
+            else
+                mass_sum += out[0] + out[1] + out[2] + out[3];
         }
         b_prev = b_cur;
         b_cur = b_next;
