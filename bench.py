@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--plain-generations", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--requests", type=int, default=256, help="serve: requests in the run")
+    ap.add_argument("--mass-side", type=int, default=256, help="mass: lattice side (a cube)")
     ap.add_argument("--load", type=float, default=0.7,
                     help="serve: offered load as a fraction of the measured capacity")
     ap.add_argument("--quantum", type=int, default=128, help="serve: generations per round")
@@ -482,9 +483,10 @@ def run_evolife(args, dist):
 
 
 def run_mass(args, dist):
-    """Mass transfer 256^3, Poisson(4) masses: K steps of 100 generations; the
-    total mass of every generation (reduced inside the kernel) is checked
-    against the initial total after each step; z-projection render timed."""
+    """Mass transfer 256^3 (``--mass-side``), Poisson(4) masses: K steps of 100
+    generations; the total mass of every generation (reduced inside the
+    kernel) is checked against the initial total after each step;
+    z-projection render timed."""
     from xentica_gb300 import build as xk_build
     from xentica_gb300 import _native as nat
     from xentica_gb300 import core, seeds
@@ -493,15 +495,17 @@ def run_mass(args, dist):
     nat.set_device(dist.local)
     lib = nat.load()
 
+    side = args.mass_side
+
     class SandPiles(core.Experiment):
         word = "SAND PILES 3D"
-        size = (256, 256, 256)
+        size = (side, side, side)
         zoom = 1
         pos = [0, 0]
         seed = seeds.patterns.PrimordialSoup(vals={"mass": seeds.random.RandPoisson(4)})
 
     model = MassTransferProgram(SandPiles)
-    model.set_viewport((256, 256))
+    model.set_viewport((side, side))
     n = model.cells_num
     total0 = int(model.gpu.arrays.cells.get()[:n].astype(np.uint64).sum())
     gens = 100
@@ -535,13 +539,14 @@ def run_mass(args, dist):
             "warmup": args.warmup, "ms_per_step": dev_s * 1000 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
             "data": "synthetic (seeded Poisson(4) masses)",
-            "config": {"workload": "mass transfer 256^3 von Neumann, StaticBorder wall, "
-                                   "100 generations per step, total checked every generation",
-                       "l2": "state (2 x 64 MB) close to L2 size; no flush"},
+            "config": {"workload": "mass transfer %d^3 von Neumann, StaticBorder wall, "
+                                   "100 generations per step, total checked every generation" % side,
+                       "l2": "state (2 x %.0f MB)%s; no flush" % (
+                           4 * n / 2 ** 20, " close to L2 size" if side == 256 else "")},
             "mass_conserved": conserved, "render_ms_per_frame": render_ms,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": committed_traffic("mass_tma"),
+                         "traffic": committed_traffic("mass_tma") if side == 256 else None,
                          "note": "8 B per cell-update (uint32 read + write); traffic: "
                                  "DRAM bytes of one launch (one generation)"},
             "clocks": clk}
