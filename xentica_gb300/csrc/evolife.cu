@@ -207,6 +207,7 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
     const int y = blockIdx.y * XK_EVO_BY + threadIdx.y;
     const int tid = threadIdx.y * XK_EVO_BX + threadIdx.x;
     if (x >= p.W || y >= p.H) return;   // no block-wide synchronisation below
+    xk_grid_dep_wait();                 // launched as a dependent of the previous generation
     const int xl = x > 0 ? x - 1 : p.W - 1, xr = x < p.W - 1 ? x + 1 : 0;
     const int yu = y > 0 ? y - 1 : p.H - 1, yd = y < p.H - 1 ? y + 1 : 0;
     const int nxs[8] = {xl, xl, xl, x, x, xr, xr, xr};
@@ -338,6 +339,5 @@ cudaError_t xk_evolife_step(const uint64_t *src, uint64_t *dst, int32_t *col, co
     evo_jump(p);
     dim3 block(XK_EVO_BX, XK_EVO_BY);
     dim3 grid((p.W + XK_EVO_BX - 1) / XK_EVO_BX, (p.H + XK_EVO_BY - 1) / XK_EVO_BY);
-    xk_k_evolife<<<grid, block, 0, s>>>(src, dst, col, p);
-    return cudaGetLastError();
+    return xk_launch_pdl(xk_k_evolife, grid, block, 0, s, src, dst, col, p);
 }

@@ -56,6 +56,7 @@ xk_k_life_global(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, L
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t total = (int64_t)g.H * g.wpr;
     if (idx >= total) return;
+    xk_grid_dep_wait();       // launched as a dependent of the previous generation
     const int y = (int)(idx / g.wpr);
     const int j = (int)(idx - (int64_t)y * g.wpr);
     const int last = g.wpr - 1;
@@ -91,8 +92,7 @@ cudaError_t xk_life_step_global(const uint32_t *src, uint32_t *dst, const LifeGe
     const int64_t total = (int64_t)g.H * g.wpr;
     const int threads = 256;
     const int64_t blocks = (total + threads - 1) / threads;
-    xk_k_life_global<<<(unsigned)blocks, threads, 0, s>>>(src, dst, g, t);
-    return cudaGetLastError();
+    return xk_launch_pdl(xk_k_life_global, dim3((unsigned)blocks), dim3(threads), 0, s, src, dst, g, t);
 }
 
 // ---------------------------------------------------------------------------
@@ -112,6 +112,7 @@ xk_k_life3d_vn(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, Lif
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t rows = (int64_t)g.H * g.D;
     if (idx >= rows * g.wpr) return;
+    xk_grid_dep_wait();       // launched as a dependent of the previous generation
     const int64_t r = idx / g.wpr;
     const int j = (int)(idx - r * g.wpr);
     const int z = (int)(r / g.H), y = (int)(r - (int64_t)z * g.H);
@@ -151,8 +152,7 @@ cudaError_t xk_life_step3d_vn(const uint32_t *src, uint32_t *dst, const Life3Geo
     const int64_t total = (int64_t)g.H * g.D * g.wpr;
     const int threads = 256;
     const int64_t blocks = (total + threads - 1) / threads;
-    xk_k_life3d_vn<<<(unsigned)blocks, threads, 0, s>>>(src, dst, g, t);
-    return cudaGetLastError();
+    return xk_launch_pdl(xk_k_life3d_vn, dim3((unsigned)blocks), dim3(threads), 0, s, src, dst, g, t);
 }
 
 // ---------------------------------------------------------------------------

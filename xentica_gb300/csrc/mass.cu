@@ -449,9 +449,16 @@ xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict
         for (int s = 0; s < XK_MT_STAGES; ++s)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8 * s) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // launched as a programmatic dependent of the previous generation: all of
+    // the above overlaps its last CTAs; every thread waits here for that
+    // grid to complete (and its writes to be visible) before any global
+    // access -- the previous generation still reads the buffer this one
+    // writes.  Without a programmatic launch this returns at once.
+    xk_grid_dep_wait();
+    if (tid == 0)
         for (int k = 0; k < XK_MT_STAGES && k < nplanes; ++k)
             xk_mt_issue(&tm, stage0 + k * XK_MT_STAGE_STRIDE, bar0 + 8 * k, x_lo, y_lo, z0 - 1 + k);
-    }
     __syncthreads();
 
     // own cells of a stage (row ty + 1, columns 4 + 4 lane ..); the halo
@@ -727,11 +734,12 @@ cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long 
         // form and no wall value can be inside: the fast-only instantiation.
         // XK_MASS_GENERAL=1 in the environment takes the general one anyway.
         const char *g = getenv("XK_MASS_GENERAL");
-        if (small && !(g && g[0] == '1'))
-            xk_k_mass_tma<4, false><<<grid, block, XK_MT_SMEM, s>>>(tm, src, dst, total, p, zc);
-        else
-            xk_k_mass_tma<4, true><<<grid, block, XK_MT_SMEM, s>>>(tm, src, dst, total, p, zc);
-        return cudaGetLastError();
+        const bool fast = small && !(g && g[0] == '1');
+        // programmatic dependent launch: this generation's CTAs may start
+        // their set-up while the previous generation's last CTAs run
+        if (fast)
+            return xk_launch_pdl(xk_k_mass_tma<4, false>, grid, block, XK_MT_SMEM, s, tm, src, dst, total, p, zc);
+        return xk_launch_pdl(xk_k_mass_tma<4, true>, grid, block, XK_MT_SMEM, s, tm, src, dst, total, p, zc);
     }
     const int cells_x = 32 * (vec ? 4 : 1);
     const int gx = (p.W + cells_x - 1) / cells_x, gy = (p.H + XK_MASS_BY - 1) / XK_MASS_BY;

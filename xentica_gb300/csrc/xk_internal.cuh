@@ -1,6 +1,9 @@
 // Internal declarations shared by the libxk translation units.
 #pragma once
 
+#include <stdlib.h>
+#include <string.h>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -175,6 +178,37 @@ cudaError_t xk_vm_run(const xk_vm_ins *code, int ncode, const uint64_t *consts,
 cudaError_t xk_evolife_set_positional(const double *lut54);
 cudaError_t xk_evolife_step(const uint64_t *src, uint64_t *dst, int32_t *col, const xk_desc &d,
                             float mut_thresh, cudaStream_t s);
+
+// Programmatic dependent launch for kernels that run once per generation: the
+// launch may begin while the previous kernel in the stream finishes, and the
+// kernel calls xk_grid_dep_wait() before its first global-memory access
+// (which returns once that kernel has completed and its writes are
+// visible).  XK_PDL=0 in the environment launches plainly.
+__device__ __forceinline__ void xk_grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+inline bool xk_pdl_enabled()
+{
+    const char *v = getenv("XK_PDL");
+    return !(v && v[0] == '0');
+}
+
+template <typename... KArgs, typename... Args>
+cudaError_t xk_launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                          Args... args)
+{
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr.val.programmaticStreamSerializationAllowed = 1;
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = &attr;
+    cfg.numAttrs = xk_pdl_enabled() ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
 
 // Bernoulli seeds (seed.cu): cells[off .. off + n) of a lattice =
 // RandomState(seed).random_sample(n) < p, bit for bit
