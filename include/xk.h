@@ -103,7 +103,9 @@ int xk_life_set_rule(xk_model *m, uint32_t rule0, uint32_t rule1, const int32_t 
 int xk_set_color_mode(xk_model *m, int32_t history_free);
 
 /* Replaces CellularAutomaton.step (base.py:703-728): nsteps generations of
- * emit + absorb + colour, fused. */
+ * emit + absorb + colour, fused.  XK_ERR_TIMEOUT: a mass-transfer kernel gave
+ * up waiting for one of its tensor copies (a bounded wait; the state is then
+ * unspecified). */
 int xk_step(xk_model *m, int64_t nsteps);
 
 /* Replaces CellularAutomaton.render (base.py:730-753): width*height*3 int32. */
