@@ -162,8 +162,11 @@ cudaError_t xk_life_step3d_vn(const uint32_t *src, uint32_t *dst, const Life3Geo
 // Lanes are grouped: a group of P = next_pow2(wpr) lanes covers one row, lane
 // j of the group owning column word j.  The lattice's rows are cut into one
 // band of consecutive rows per group; a group walks down its band keeping the
-// neighbour vectors of three rows in registers, so every generation costs one
-// shared load, two shuffles and one shared store per 32 cells.  Updates are
+// column sums (s, c) = FA(L, C, R) of three rows and the cells of the middle
+// row in registers (each row's sums are computed once, when it is the row
+// below), so every generation costs one shared load, two shuffles and one
+// shared store per 32 cells.  The rule is indexed by the count of the 3 x 3
+// block including the cell (LifeTable9, xk_life_word9).  Updates are
 // in place: a lane only ever touches its own column word of its own band, and
 // the first and last row of every band are copied to a halo area before the
 // generation starts, so neighbouring bands read the previous generation.
