@@ -13,6 +13,14 @@
 //
 // The plain form is the reference's execution model on the same GPU: one
 // launch per instance per generation over the byte layout.
+//
+// End to end (xk_batch_run, host buffers in and out): on page-locked buffers,
+// classes whose CTA has its SM to itself are staged by the copy engines
+// around grouped launches on high-priority streams while every other class
+// reads and writes the host buffers from its kernel (run_mapped); pageable
+// buffers go through index-order chunks whose uploads, launches and
+// downloads overlap (run_pipelined).  Seeds: xk_batch_seed_bernoulli draws
+// every instance's cells on the device (seed.cu).
 #include <stdlib.h>
 #include <string.h>
 

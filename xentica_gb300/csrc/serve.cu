@@ -24,7 +24,8 @@
 //             bit-sliced launch per generation on the request's stream;
 //   life3d    3-D von Neumann Life-like: bit-packed along x like global2d, one
 //             launch per generation;
-//   mass3d    mass transfer: uint32 ping-pong with the per-generation totals.
+//   mass3d    mass transfer: uint32 ping-pong with the per-generation totals
+//             (the fast-only kernel when the submitted total is below 2^30).
 // Full rounds of the per-request paths are captured once as a CUDA graph (per
 // ping-pong parity) and replayed, so a round costs the worker one launch.
 // A request's cells see exactly the arithmetic they see alone: every kernel
