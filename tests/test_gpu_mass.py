@@ -136,3 +136,26 @@ def test_tile_edges_vs_oracle(size, kernel_form):
     O.mass_run(topo, fld, col, 3, totals=totals)
     assert np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n])
     assert model.gpu.mass_totals(3).tolist() == totals
+
+
+@pytest.mark.parametrize("general", [False, True])
+@pytest.mark.parametrize("size", [(33, 17, 9), (171, 20, 9), (5, 3, 2), (1, 1, 1), (97, 1, 4), (63, 65, 3)])
+def test_odd_widths_vs_oracle(size, general, monkeypatch):
+    # widths that are not a multiple of 4: the generic kernels (one cell per
+    # thread); small totals take its fast-only form, XK_MASS_GENERAL=1 the
+    # exact one
+    if general:
+        monkeypatch.setenv("XK_MASS_GENERAL", "1")
+    model = _model(size)
+    n = model.cells_num
+    rng = np.random.RandomState(sum(size) + general)
+    cells = rng.poisson(5, n).astype(np.uint32)
+    model.gpu.load(cells, np.zeros(3 * n, dtype=np.int32))
+    topo = _topo(size)
+    fld = topo.field(cells, np.uint32)
+    col = np.zeros(3 * n, dtype=np.int32)
+    model.gpu.step(4)
+    totals = []
+    O.mass_run(topo, fld, col, 4, totals=totals)
+    assert np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n])
+    assert model.gpu.mass_totals(4).tolist() == totals

@@ -95,6 +95,7 @@ xk_k_mass(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
     const bool has_xl = in && x0 > 0, has_xr = in && x0 + V < p.W;
     const uint32_t wall = p.wall;
     MassRow<V> prv, cur, nxt, ym, yp;
+    xk_grid_dep_wait();       // launched as a dependent of the previous generation
     xk_mass_load<V>(src, (int64_t)(z0 - 1) * plane + col, in && z0 > 0, wall, prv);
     xk_mass_load<V>(src, (int64_t)z0 * plane + col, in && z0 < p.D, wall, cur);
     unsigned long long mass_sum = 0;
@@ -218,6 +219,81 @@ __device__ __forceinline__ uint4 xk_mass_ld4z(const uint32_t *__restrict__ src, 
 __device__ __forceinline__ uint32_t xk_or4(const uint4 &u) { return u.x | u.y | u.z | u.w; }
 
 __device__ __forceinline__ uint32_t xk_q_small(uint32_t m) { return __umulhi(m, 0x24924925u); }
+
+// The generic form's fast-only counterpart (any width): used when the
+// lattice's total mass is below 2^30, so no cell reaches 2^30 and no wall
+// value is inside (see the TMA kernel).  One cell per thread marching its z
+// run; q = m / 7 by the one-instruction division; off-board neighbours read
+// as 0 and the cell's on-board neighbours are counted once:
+//   m' = m - q * (#on-board neighbours) + sum_k q_k.
+__global__ void __launch_bounds__(32 * XK_MASS_BY)
+xk_k_mass_small(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
+                unsigned long long *__restrict__ total, MassParams p, int zc)
+{
+    __shared__ unsigned long long warp_sums[XK_MASS_BY];
+    const int lane = threadIdx.x;
+    const int x = blockIdx.x * 32 + lane;
+    const int y = blockIdx.y * XK_MASS_BY + threadIdx.y;
+    const int z0 = blockIdx.z * zc;
+    const int z1 = min(z0 + zc, p.D);
+    const bool in = x < p.W && y < p.H;
+    const uint32_t plane = (uint32_t)p.W * (uint32_t)p.H;
+    uint32_t off = in ? (uint32_t)z0 * plane + (uint32_t)y * p.W + x : 0u;
+    const bool has_xl = in && x > 0, has_xr = in && x + 1 < p.W;
+    const bool has_ym = in && y > 0, has_yp = in && y + 1 < p.H;
+    const uint32_t cxy = (uint32_t)has_xl + has_xr + has_ym + has_yp;
+    auto ld = [&](uint32_t o, bool ok) { return ok ? __ldg(src + o) : 0u; };
+    xk_grid_dep_wait();       // launched as a dependent of the previous generation
+    uint32_t q_prv = xk_q_small(ld(off - plane, in && z0 > 0));
+    uint32_t m_cur = ld(off, in);
+    uint32_t q_cur = xk_q_small(m_cur);
+    uint32_t m_nxt = ld(off + plane, in && z0 + 1 < p.D);
+    uint32_t q_nxt = xk_q_small(m_nxt);
+    // the rows above and below and the cell beyond the warp (lanes 0 and 31)
+    // are loaded one plane ahead
+    const bool edge_l = lane == 0 && has_xl, edge_r = lane == 31 && has_xr;
+    uint32_t ym_pf = ld(off - p.W, has_ym), yp_pf = ld(off + p.W, has_yp);
+    uint32_t hl_pf = ld(off - 1, edge_l), hr_pf = ld(off + 1, edge_r);
+    uint32_t sum = 0;         // below 2^30: the whole lattice's total is
+    for (int z = z0; z < z1; ++z) {
+        const uint32_t m_nn = ld(off + 2 * plane, in && z + 2 < p.D);
+        const uint32_t ym_m = ym_pf, yp_m = yp_pf, hl_m = hl_pf, hr_m = hr_pf;
+        const bool more = z + 1 < z1;
+        ym_pf = ld(off + plane - p.W, has_ym && more);
+        yp_pf = ld(off + plane + p.W, has_yp && more);
+        hl_pf = ld(off + plane - 1, edge_l && more);
+        hr_pf = ld(off + plane + 1, edge_r && more);
+        const uint32_t qy = xk_q_small(ym_m) + xk_q_small(yp_m);
+        // x neighbours from the neighbouring lanes (same row); lanes 0 and 31
+        // take the cell beyond the warp
+        const uint32_t sl = __shfl_up_sync(0xFFFFFFFFu, q_cur, 1);
+        const uint32_t sr = __shfl_down_sync(0xFFFFFFFFu, q_cur, 1);
+        const uint32_t hl = lane == 0 ? xk_q_small(hl_m) : sl;
+        const uint32_t hr = lane == 31 ? xk_q_small(hr_m) : sr;
+        const uint32_t ql = has_xl ? hl : 0u, qr = has_xr ? hr : 0u;
+        const uint32_t cz = (uint32_t)((z > 0) + (z + 1 < p.D));
+        const uint32_t out = m_cur - q_cur * (cxy + cz) + ql + qr + qy + q_prv + q_nxt;
+        if (in) {
+            dst[off] = out;
+            sum += out;
+        }
+        q_prv = q_cur;
+        m_cur = m_nxt;
+        q_cur = q_nxt;
+        m_nxt = m_nn;
+        q_nxt = xk_q_small(m_nn);
+        off += plane;
+    }
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xFFFFFFFFu, sum, o);
+    if (lane == 0) warp_sums[threadIdx.y] = sum;
+    __syncthreads();
+    if (threadIdx.y == 0 && lane == 0) {
+        unsigned long long t = 0;
+        for (int w = 0; w < XK_MASS_BY; ++w) t += warp_sums[w];
+        atomicAdd(total, t);
+    }
+}
+
 
 template <int MINB>
 __global__ void __launch_bounds__(32 * XK_MASS_BY, MINB)
@@ -752,8 +828,10 @@ cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long 
         xk_k_mass_rows<4><<<grid, block, 0, s>>>(src, dst, total, p, zc);
     else if (vec)
         xk_k_mass_rows<1><<<grid, block, 0, s>>>(src, dst, total, p, zc);
+    else if (small && !(getenv("XK_MASS_GENERAL") && getenv("XK_MASS_GENERAL")[0] == '1'))
+        return xk_launch_pdl(xk_k_mass_small, grid, block, 0, s, src, dst, total, p, zc);
     else
-        xk_k_mass<1><<<grid, block, 0, s>>>(src, dst, total, p, zc);
+        return xk_launch_pdl(xk_k_mass<1>, grid, block, 0, s, src, dst, total, p, zc);
     return cudaGetLastError();
 }
 
