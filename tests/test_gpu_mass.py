@@ -138,17 +138,20 @@ def test_tile_edges_vs_oracle(size, kernel_form):
     assert model.gpu.mass_totals(3).tolist() == totals
 
 
-@pytest.mark.parametrize("general", [False, True])
+@pytest.mark.parametrize("form", ["tma", "tma-general", "generic", "generic-exact"])
 @pytest.mark.parametrize("size", [(33, 17, 9), (171, 20, 9), (5, 3, 2), (1, 1, 1), (97, 1, 4), (63, 65, 3)])
-def test_odd_widths_vs_oracle(size, general, monkeypatch):
-    # widths that are not a multiple of 4: the generic kernels (one cell per
-    # thread); small totals take its fast-only form, XK_MASS_GENERAL=1 the
-    # exact one
-    if general:
+def test_odd_widths_vs_oracle(size, form, monkeypatch):
+    # widths that are not a multiple of 4: rows at a pitch padded to 4 cells;
+    # the TMA kernel (its fast-only form for small totals, XK_MASS_GENERAL=1
+    # the general one) or, with XK_MASS_KERNEL=rows, the generic one-cell
+    # kernels; results, colours and totals against the oracle
+    if form.endswith("general") or form.endswith("exact"):
         monkeypatch.setenv("XK_MASS_GENERAL", "1")
+    if form.startswith("generic"):
+        monkeypatch.setenv("XK_MASS_KERNEL", "rows")
     model = _model(size)
     n = model.cells_num
-    rng = np.random.RandomState(sum(size) + general)
+    rng = np.random.RandomState(sum(size) + len(form))
     cells = rng.poisson(5, n).astype(np.uint32)
     model.gpu.load(cells, np.zeros(3 * n, dtype=np.int32))
     topo = _topo(size)
@@ -159,3 +162,9 @@ def test_odd_widths_vs_oracle(size, general, monkeypatch):
     O.mass_run(topo, fld, col, 4, totals=totals)
     assert np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n])
     assert model.gpu.mass_totals(4).tolist() == totals
+    assert np.array_equal(model.gpu.arrays.colors.get(), col)
+    model.gpu.load(cells, np.zeros(3 * n, dtype=np.int32))   # a second upload over the stepped state
+    model.gpu.step(1)
+    fld = topo.field(cells, np.uint32)
+    O.mass_run(topo, fld, np.zeros(3 * n, dtype=np.int32), 1)
+    assert np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n])

@@ -344,9 +344,12 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
             m->vg.smooth = d.smooth;
         } else if (d.family == XK_FAMILY_MASS) {
             m->layout = LAYOUT_MASS;
-            XK_TRY(cudaMalloc(&m->cells32[0], (size_t)n * 4));
-            XK_TRY(cudaMalloc(&m->cells32[1], (size_t)n * 4));
-            XK_TRY(cudaMemsetAsync(m->cells32[0], 0, (size_t)n * 4, m->stream));
+            // pitched rows (xk_mass_pitch); padding cells stay 0
+            const size_t bytes = (size_t)xk_mass_pitch(d.size[0]) * d.size[1] * d.size[2] * 4;
+            XK_TRY(cudaMalloc(&m->cells32[0], bytes));
+            XK_TRY(cudaMalloc(&m->cells32[1], bytes));
+            XK_TRY(cudaMemsetAsync(m->cells32[0], 0, bytes, m->stream));
+            XK_TRY(cudaMemsetAsync(m->cells32[1], 0, bytes, m->stream));
             XK_TRY(cudaMalloc(&m->proj, (size_t)d.size[0] * d.size[1] * 4));
         } else if (d.family == XK_FAMILY_EVOLIFE) {
             m->layout = LAYOUT_CELLS64;
@@ -411,8 +414,16 @@ extern "C" int xk_upload(xk_model *m, const void *host_main, int64_t ncells)
     if (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_MASS || m->layout == LAYOUT_VM) {
         void *dst = m->layout == LAYOUT_MASS ? (void *)m->cells32[m->cur]
                     : m->layout == LAYOUT_VM ? (void *)m->fld : (void *)m->cells64[m->cur];
-        XK_CUDA(cudaMemcpyAsync(dst, host_main, (size_t)m->n * esz, cudaMemcpyHostToDevice,
-                                m->stream));
+        if (m->layout == LAYOUT_MASS) {
+            // W cells per row into rows of the pitch; the padding keeps its 0s
+            const int64_t W = m->d.size[0];
+            XK_CUDA(cudaMemcpy2DAsync(dst, (size_t)xk_mass_pitch(W) * 4, host_main, (size_t)W * 4,
+                                      (size_t)W * 4, (size_t)(m->n / W), cudaMemcpyHostToDevice,
+                                      m->stream));
+        } else {
+            XK_CUDA(cudaMemcpyAsync(dst, host_main, (size_t)m->n * esz, cudaMemcpyHostToDevice,
+                                    m->stream));
+        }
         if (m->layout == LAYOUT_MASS) {
             // the total decides the kernel for good: mass is conserved
             if (m->totals_cap < 1) {
@@ -420,7 +431,8 @@ extern "C" int xk_upload(xk_model *m, const void *host_main, int64_t ncells)
                 m->totals_cap = 1;
             }
             unsigned long long tot = 0;
-            XK_CUDA(xk_mass_sum((const uint32_t *)dst, m->n, m->totals, m->stream));
+            XK_CUDA(xk_mass_sum((const uint32_t *)dst, xk_mass_pitch(m->d.size[0]) * (m->n / m->d.size[0]),
+                                m->totals, m->stream));
             XK_CUDA(cudaMemcpyAsync(&tot, m->totals, sizeof(tot), cudaMemcpyDeviceToHost, m->stream));
             XK_CUDA(cudaStreamSynchronize(m->stream));
             m->mass_small = tot < (1ull << 30);
@@ -460,8 +472,15 @@ extern "C" int xk_download(xk_model *m, void *host_main, int64_t ncells)
         const void *src = m->layout == LAYOUT_MASS ? (const void *)m->cells32[m->cur]
                           : m->layout == LAYOUT_VM ? (const void *)m->fld
                                                    : (const void *)m->cells64[m->cur];
-        XK_CUDA(cudaMemcpyAsync(host_main, src, (size_t)m->n * esz, cudaMemcpyDeviceToHost,
-                                m->stream));
+        if (m->layout == LAYOUT_MASS) {
+            const int64_t W = m->d.size[0];
+            XK_CUDA(cudaMemcpy2DAsync(host_main, (size_t)W * 4, src, (size_t)xk_mass_pitch(W) * 4,
+                                      (size_t)W * 4, (size_t)(m->n / W), cudaMemcpyDeviceToHost,
+                                      m->stream));
+        } else {
+            XK_CUDA(cudaMemcpyAsync(host_main, src, (size_t)m->n * esz, cudaMemcpyDeviceToHost,
+                                    m->stream));
+        }
         XK_CUDA(cudaStreamSynchronize(m->stream));
         return XK_OK;
     }
@@ -480,7 +499,7 @@ static int materialize_colors(xk_model *m)
 {
     if (m->layout == LAYOUT_VM) return XK_OK;   // absorb writes the colours
     if (m->layout == LAYOUT_MASS) {
-        XK_CUDA(xk_mass_colors(m->cells32[m->cur], m->col, m->n, m->stream));
+        XK_CUDA(xk_mass_colors(m->cells32[m->cur], m->col, m->d, m->stream));
         return XK_OK;
     }
     if (!m->derived) return XK_OK;

@@ -42,6 +42,7 @@
 
 struct MassParams {
     int32_t W, H, D;
+    int32_t P;          // row pitch in cells: W rounded up to a multiple of 4
     uint32_t wall;
 };
 
@@ -89,8 +90,8 @@ xk_k_mass(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
     const int z0 = blockIdx.z * zc;
     const int z1 = min(z0 + zc, p.D);
     const bool in = x0 < p.W && y < p.H;
-    const int64_t plane = (int64_t)p.W * p.H;
-    const int64_t col = in ? (int64_t)y * p.W + x0 : 0;
+    const int64_t plane = (int64_t)p.P * p.H;
+    const int64_t col = in ? (int64_t)y * p.P + x0 : 0;
     const bool has_ym = in && y > 0, has_yp = in && y + 1 < p.H;
     const bool has_xl = in && x0 > 0, has_xr = in && x0 + V < p.W;
     const uint32_t wall = p.wall;
@@ -102,8 +103,8 @@ xk_k_mass(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
     for (int z = z0; z < z1; ++z) {
         const int64_t zb = (int64_t)z * plane;
         xk_mass_load<V>(src, zb + plane + col, in && z + 1 < p.D, wall, nxt);
-        xk_mass_load<V>(src, zb + col - p.W, has_ym, wall, ym);
-        xk_mass_load<V>(src, zb + col + p.W, has_yp, wall, yp);
+        xk_mass_load<V>(src, zb + col - p.P, has_ym, wall, ym);
+        xk_mass_load<V>(src, zb + col + p.P, has_yp, wall, yp);
         uint32_t lm = __shfl_up_sync(0xFFFFFFFFu, cur.m[V - 1], 1);
         uint32_t lq = __shfl_up_sync(0xFFFFFFFFu, cur.q[V - 1], 1);
         uint32_t rm = __shfl_down_sync(0xFFFFFFFFu, cur.m[0], 1);
@@ -237,8 +238,8 @@ xk_k_mass_small(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
     const int z0 = blockIdx.z * zc;
     const int z1 = min(z0 + zc, p.D);
     const bool in = x < p.W && y < p.H;
-    const uint32_t plane = (uint32_t)p.W * (uint32_t)p.H;
-    uint32_t off = in ? (uint32_t)z0 * plane + (uint32_t)y * p.W + x : 0u;
+    const uint32_t plane = (uint32_t)p.P * (uint32_t)p.H;
+    uint32_t off = in ? (uint32_t)z0 * plane + (uint32_t)y * p.P + x : 0u;
     const bool has_xl = in && x > 0, has_xr = in && x + 1 < p.W;
     const bool has_ym = in && y > 0, has_yp = in && y + 1 < p.H;
     const uint32_t cxy = (uint32_t)has_xl + has_xr + has_ym + has_yp;
@@ -252,15 +253,15 @@ xk_k_mass_small(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
     // the rows above and below and the cell beyond the warp (lanes 0 and 31)
     // are loaded one plane ahead
     const bool edge_l = lane == 0 && has_xl, edge_r = lane == 31 && has_xr;
-    uint32_t ym_pf = ld(off - p.W, has_ym), yp_pf = ld(off + p.W, has_yp);
+    uint32_t ym_pf = ld(off - p.P, has_ym), yp_pf = ld(off + p.P, has_yp);
     uint32_t hl_pf = ld(off - 1, edge_l), hr_pf = ld(off + 1, edge_r);
     uint32_t sum = 0;         // below 2^30: the whole lattice's total is
     for (int z = z0; z < z1; ++z) {
         const uint32_t m_nn = ld(off + 2 * plane, in && z + 2 < p.D);
         const uint32_t ym_m = ym_pf, yp_m = yp_pf, hl_m = hl_pf, hr_m = hr_pf;
         const bool more = z + 1 < z1;
-        ym_pf = ld(off + plane - p.W, has_ym && more);
-        yp_pf = ld(off + plane + p.W, has_yp && more);
+        ym_pf = ld(off + plane - p.P, has_ym && more);
+        yp_pf = ld(off + plane + p.P, has_yp && more);
         hl_pf = ld(off + plane - 1, edge_l && more);
         hr_pf = ld(off + plane + 1, edge_r && more);
         const uint32_t qy = xk_q_small(ym_m) + xk_q_small(yp_m);
@@ -307,9 +308,9 @@ xk_k_mass_rows(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
     const int z0 = blockIdx.z * zc;
     const int z1 = min(z0 + zc, p.D);
     const bool in = x0 < p.W && y < p.H;
-    const uint32_t plane = (uint32_t)p.W * (uint32_t)p.H;
+    const uint32_t plane = (uint32_t)p.P * (uint32_t)p.H;
     const uint32_t wall = p.wall;
-    uint32_t off = in ? (uint32_t)z0 * plane + (uint32_t)y * p.W + x0 : 0u;
+    uint32_t off = in ? (uint32_t)z0 * plane + (uint32_t)y * p.P + x0 : 0u;
     const bool hx_ok = in && ((lane == 0 && x0 > 0) || (lane == 31 && x0 + 4 < p.W));
     const int hx_d = lane == 0 ? -1 : 4;
     const bool has_ym = in && y > 0, has_yp = in && y + 1 < p.H;
@@ -323,8 +324,8 @@ xk_k_mass_rows(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
     uint4 prv_m = xk_mass_ld4z(src, off - plane, in && z0 > 0);
     uint4 cur_m = xk_mass_ld4z(src, off, in);
     uint4 nxt_m = xk_mass_ld4z(src, off + plane, in && z0 + 1 < p.D);
-    uint4 ym_pf = xk_mass_ld4z(src, off - p.W, has_ym);
-    uint4 yp_pf = xk_mass_ld4z(src, off + p.W, has_yp);
+    uint4 ym_pf = xk_mass_ld4z(src, off - p.P, has_ym);
+    uint4 yp_pf = xk_mass_ld4z(src, off + p.P, has_yp);
     uint32_t hx_pf = hx_ok ? __ldg(src + (off + hx_d)) : 0u;
     unsigned long long mass_sum = 0;
     for (int z = z0; z < z1; ++z) {
@@ -332,8 +333,8 @@ xk_k_mass_rows(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
         const uint4 ym_m = ym_pf, yp_m = yp_pf;
         const uint32_t hx_m = hx_pf;
         const bool more = z + 1 < z1;
-        ym_pf = xk_mass_ld4z(src, off + plane - p.W, has_ym && more);
-        yp_pf = xk_mass_ld4z(src, off + plane + p.W, has_yp && more);
+        ym_pf = xk_mass_ld4z(src, off + plane - p.P, has_ym && more);
+        yp_pf = xk_mass_ld4z(src, off + plane + p.P, has_yp && more);
         hx_pf = hx_ok && more ? __ldg(src + (off + plane + hx_d)) : 0u;
         const uint32_t ors = xk_or4(prv_m) | xk_or4(cur_m) | xk_or4(nxt_m) | xk_or4(ym_m) |
                              xk_or4(yp_m) | hx_m;
@@ -516,8 +517,10 @@ xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict
     const int x0 = blockIdx.x * 128 + lane * 4, y = blockIdx.y * XK_MT_BY + ty;
     const int z0 = blockIdx.z * zc, z1 = min(z0 + zc, p.D);
     const int nplanes = z1 - z0 + 2;                  // planes z0 - 1 .. z1
-    const bool in = x0 < p.W && y < p.H;              // W % 4 == 0: all four cells or none
-    const uint32_t plane = (uint32_t)p.W * (uint32_t)p.H;
+    // a thread's four cells start at x0; when W is not a multiple of 4 the
+    // last quad of a row is partly in the row's padding (pitch P)
+    const bool in = x0 < p.W && y < p.H;
+    const uint32_t plane = (uint32_t)p.P * (uint32_t)p.H;
     const uint32_t bar0 = xk_smem_addr(bars), stage0 = xk_smem_addr(stages);
 
     if (tid == 0) {
@@ -610,11 +613,15 @@ xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict
 
     // on-board neighbours in x and y of the four cells
     const int cy = (y > 0) + (y + 1 < p.H);
-    const uint32_t c0 = cy + 1 + (x0 > 0), c3 = cy + 1 + (x0 + 4 < p.W), c12 = cy + 2;
+    // per cell: x neighbours on the lattice (0 for cells in the padding)
+    const uint32_t c0 = cy + (x0 > 0) + (x0 + 1 < p.W), c1 = cy + 1 + (x0 + 2 < p.W);
+    const uint32_t c2 = cy + 1 + (x0 + 3 < p.W), c3 = cy + 1 + (x0 + 4 < p.W);
+    // cells at or beyond W (padding) are written as 0
+    const bool v1 = x0 + 1 < p.W, v2 = x0 + 2 < p.W, v3 = x0 + 3 < p.W;
     // the fast-only form runs when the lattice's whole total is below 2^30,
     // so every partial sum of its cells fits 32 bits
     typename std::conditional<GENERAL, unsigned long long, uint32_t>::type mass_sum = 0;
-    uint32_t off = in ? (uint32_t)z0 * plane + (uint32_t)y * p.W + x0 : 0u;
+    uint32_t off = in ? (uint32_t)z0 * plane + (uint32_t)y * p.P + x0 : 0u;
     int z = z0;
     // one plane: take plane z + 1 into (mn, qn) and tile qnext, then compute
     // plane z from tile qcur, qp (z - 1), (mc, qc) (z) and qn (z + 1)
@@ -635,8 +642,8 @@ xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict
             const uint32_t sr = __shfl_down_sync(0xFFFFFFFFu, qc.x, 1);
             const uint32_t xl = lane == 0 ? hl : sl, xr = lane == 31 ? hr : sr;
             out[0] = mc.x - qc.x * (c0 + cz) + xl + qc.y + up.x + dn.x + qp.x + qn.x;
-            out[1] = mc.y - qc.y * (c12 + cz) + qc.x + qc.z + up.y + dn.y + qp.y + qn.y;
-            out[2] = mc.z - qc.z * (c12 + cz) + qc.y + qc.w + up.z + dn.z + qp.z + qn.z;
+            out[1] = mc.y - qc.y * (c1 + cz) + qc.x + qc.z + up.y + dn.y + qp.y + qn.y;
+            out[2] = mc.z - qc.z * (c2 + cz) + qc.y + qc.w + up.z + dn.z + qp.z + qn.z;
             out[3] = mc.w - qc.w * (c3 + cz) + qc.z + xr + up.w + dn.w + qp.w + qn.w;
         } else if (GENERAL && in) {
             // the reference's arithmetic per neighbour, neighbours from global memory
@@ -646,7 +653,7 @@ xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict
                 const uint32_t m = xk_get(mc, i);
                 const uint32_t o = off + i;
                 const bool on[6] = {x0 + i > 0, x0 + i + 1 < p.W, y > 0, y + 1 < p.H, z > 0, z + 1 < p.D};
-                const uint32_t at[6] = {o - 1, o + 1, o - p.W, o + p.W, o - plane, o + plane};
+                const uint32_t at[6] = {o - 1, o + 1, o - p.P, o + p.P, o - plane, o + plane};
                 uint32_t cnt = 0, sq = 0;
 #pragma unroll
                 for (int n = 0; n < 6; ++n) {
@@ -657,6 +664,9 @@ xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict
                 out[i] = m - (m / 7u) * cnt + (m != wall ? sq : 0u);
             }
         }
+        out[1] = v1 ? out[1] : 0u;
+        out[2] = v2 ? out[2] : 0u;
+        out[3] = v3 ? out[3] : 0u;
         if (in) {
             *reinterpret_cast<uint4 *>(dst + off) = make_uint4(out[0], out[1], out[2], out[3]);
             if (GENERAL)
@@ -688,26 +698,35 @@ xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict
     }
 }
 
-// column colour sums of a state (after an upload, before any step)
+// column colour sums of a state (pitched rows; the sums are W * H, unpadded);
+// grid: x over a row's cells, y striding over the rows
 __global__ void xk_k_mass_project(const uint32_t *__restrict__ src, uint32_t *__restrict__ proj,
                                   MassParams p)
 {
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t plane = (int64_t)p.W * p.H;
-    if (c >= plane) return;
-    uint32_t s = 0;
-    for (int z = 0; z < p.D; ++z) s += xk_mass_color(src[(int64_t)z * plane + c]);
-    proj[c] = s;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= p.W) return;
+    const int64_t plane = (int64_t)p.P * p.H;
+    for (int64_t y = blockIdx.y; y < p.H; y += gridDim.y) {
+        uint32_t s = 0;
+        for (int z = 0; z < p.D; ++z) s += xk_mass_color(src[(int64_t)z * plane + y * p.P + x]);
+        proj[y * p.W + x] = s;
+    }
 }
 
-__global__ void xk_k_mass_colors(const uint32_t *__restrict__ src, int32_t *__restrict__ col, int64_t n)
+// colours of every cell in the reference's order (3 ints per cell, no
+// padding); grid: x over a row's cells, y striding over the H * D rows
+__global__ void xk_k_mass_colors(const uint32_t *__restrict__ src, int32_t *__restrict__ col, MassParams p)
 {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int v = (int)xk_mass_color(src[i]);
-    col[3 * i] = v;
-    col[3 * i + 1] = v;
-    col[3 * i + 2] = v;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= p.W) return;
+    const int64_t rows = (int64_t)p.H * p.D;
+    for (int64_t row = blockIdx.y; row < rows; row += gridDim.y) {
+        const int v = (int)xk_mass_color(src[row * p.P + x]);
+        const int64_t i = row * p.W + x;
+        col[3 * i] = v;
+        col[3 * i + 1] = v;
+        col[3 * i + 2] = v;
+    }
 }
 
 // RendererPlain over axes (0, 1) from the column sums: the float sum of a
@@ -737,6 +756,7 @@ static MassParams mass_params(const xk_desc &d)
     p.W = (int32_t)d.size[0];
     p.H = (int32_t)d.size[1];
     p.D = (int32_t)d.size[2];
+    p.P = (int32_t)xk_mass_pitch(p.W);
     p.wall = d.wall;
     return p;
 }
@@ -789,12 +809,14 @@ cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long 
 {
     const MassParams p = mass_params(d);
     const bool vec = p.W % 4 == 0;
-    if (vec && mass_tma_enabled()) {
+    if (mass_tma_enabled()) {
         PFN_cuTensorMapEncodeTiled_v12000 enc = xk_tensor_map_encoder();
         if (!enc) return cudaErrorNotSupported;
         CUtensorMap tm;
         const cuuint64_t dims[3] = {(cuuint64_t)p.W, (cuuint64_t)p.H, (cuuint64_t)p.D};
-        const cuuint64_t strides[2] = {(cuuint64_t)p.W * 4, (cuuint64_t)p.W * p.H * 4};
+        // logical width W with the pitched row stride: columns at or beyond W
+        // read as 0 like every other off-lattice coordinate
+        const cuuint64_t strides[2] = {(cuuint64_t)p.P * 4, (cuuint64_t)p.P * p.H * 4};
         const cuuint32_t box[3] = {XK_MT_COLS, XK_MT_ROWS, 1};
         const cuuint32_t estr[3] = {1, 1, 1};
         if (enc(&tm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<uint32_t *>(src), dims, strides, box, estr,
@@ -868,14 +890,17 @@ bool xk_mass_take_wait_failure()
 cudaError_t xk_mass_project(const uint32_t *src, uint32_t *proj, const xk_desc &d, cudaStream_t s)
 {
     const MassParams p = mass_params(d);
-    const int64_t plane = (int64_t)p.W * p.H;
-    xk_k_mass_project<<<(unsigned)((plane + 255) / 256), 256, 0, s>>>(src, proj, p);
+    const unsigned gy = (unsigned)(p.H < 65535 ? p.H : 65535);
+    xk_k_mass_project<<<dim3((unsigned)((p.W + 255) / 256), gy), 256, 0, s>>>(src, proj, p);
     return cudaGetLastError();
 }
 
-cudaError_t xk_mass_colors(const uint32_t *src, int32_t *col, int64_t n, cudaStream_t s)
+cudaError_t xk_mass_colors(const uint32_t *src, int32_t *col, const xk_desc &d, cudaStream_t s)
 {
-    xk_k_mass_colors<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, col, n);
+    const MassParams p = mass_params(d);
+    const int64_t rows = (int64_t)p.H * p.D;
+    const unsigned gy = (unsigned)(rows < 65535 ? rows : 65535);
+    xk_k_mass_colors<<<dim3((unsigned)((p.W + 255) / 256), gy), 256, 0, s>>>(src, col, p);
     return cudaGetLastError();
 }
 

@@ -105,6 +105,13 @@ uint32_t life3d_rule1(uint32_t r) { return (r & 127u) | ((r >> 7) & 127u); }
 }  // namespace
 
 // device/host bytes of a request (validates it)
+// cells of a mass-transfer request's device buffers: rows at the pitch of
+// xk_mass_pitch (padding cells hold 0)
+static int64_t mass_pitched_cells(const xk_request &r)
+{
+    return xk_mass_pitch(r.size[0]) * r.size[1] * r.size[2];
+}
+
 static int request_layout(const xk_request *q, int64_t *n_out, int64_t *esz_out, int64_t *dev,
                           int64_t *host)
 {
@@ -134,7 +141,7 @@ static int request_layout(const xk_request *q, int64_t *n_out, int64_t *esz_out,
         *esz_out = 1;
     } else {
         XK_REQUIRE(q->rule == 0, XK_ERR_ARG, "serve: mass-transfer requests take rule 0");
-        *dev = 2 * rnd(4 * n) + rnd(8 * XK_SERVE_MAX_QUANTUM);
+        *dev = 2 * rnd(4 * mass_pitched_cells(*q)) + rnd(8 * XK_SERVE_MAX_QUANTUM);
         *esz_out = 4;
     }
     *host = rnd(n * *esz_out) + XK_ARENA_ALIGN;
@@ -240,8 +247,15 @@ static int admit(xk_server *s, Req *q, bool *admitted)
     uint8_t *base = s->dev_base + doff;
     const xk_request &r = q->r;
     // pageable source: the call returns once the bytes are staged
-    XK_CUDA(cudaMemcpyAsync(base, q->input.data(), (size_t)(q->n * q->esz), cudaMemcpyHostToDevice,
-                            q->stream));
+    if (r.kind == XK_SERVE_MASS3D) {
+        const int64_t W = r.size[0];
+        XK_CUDA(cudaMemsetAsync(base, 0, (size_t)(4 * mass_pitched_cells(r)), q->stream));
+        XK_CUDA(cudaMemcpy2DAsync(base, (size_t)xk_mass_pitch(W) * 4, q->input.data(), (size_t)W * 4,
+                                  (size_t)W * 4, (size_t)(q->n / W), cudaMemcpyHostToDevice, q->stream));
+    } else {
+        XK_CUDA(cudaMemcpyAsync(base, q->input.data(), (size_t)(q->n * q->esz), cudaMemcpyHostToDevice,
+                                q->stream));
+    }
     if (r.kind == XK_SERVE_LIFE2D) {
         q->rule0 = life2d_rule0(r.rule);
         q->rule1 = life2d_rule1(r.rule);
@@ -321,8 +335,9 @@ static int enqueue_round(xk_server *s, Req *q, int64_t chunk)
             q->cur ^= 1;
         }
     } else {
-        uint32_t *m[2] = {(uint32_t *)base, (uint32_t *)(base + rnd(4 * q->n))};
-        unsigned long long *tot = (unsigned long long *)(base + 2 * rnd(4 * q->n));
+        const int64_t pn = mass_pitched_cells(q->r);
+        uint32_t *m[2] = {(uint32_t *)base, (uint32_t *)(base + rnd(4 * pn))};
+        unsigned long long *tot = (unsigned long long *)(base + 2 * rnd(4 * pn));
         XK_CUDA(cudaMemsetAsync(tot, 0, (size_t)chunk * 8, q->stream));
         for (int64_t g = 0; g < chunk; ++g) {
             XK_CUDA(xk_mass_step(m[q->cur], m[1 - q->cur], tot + g, q->md, q->mass_small, q->stream));
@@ -425,12 +440,20 @@ static int start_result_copy(xk_server *s, Req *q)
         XK_CUDA(xk_life_unpack(w, base, 1, q->lg, q->stream));
         s->st.launches++;
     } else if (q->path == PATH_MASS3D) {
-        src = base + (q->cur ? rnd(4 * q->n) : 0);
+        const int64_t pn = mass_pitched_cells(q->r);
+        src = base + (q->cur ? rnd(4 * pn) : 0);
         if (q->r.generations > 0) {
-            const unsigned long long *tot = (const unsigned long long *)(base + 2 * rnd(4 * q->n));
+            const unsigned long long *tot = (const unsigned long long *)(base + 2 * rnd(4 * pn));
             XK_CUDA(cudaMemcpyAsync(hst + rnd(q->n * q->esz), tot + (q->last_chunk - 1), 8,
                                     cudaMemcpyDeviceToHost, q->stream));
         }
+        const int64_t W = q->r.size[0];
+        XK_CUDA(cudaMemcpy2DAsync(hst, (size_t)W * 4, src, (size_t)xk_mass_pitch(W) * 4, (size_t)W * 4,
+                                  (size_t)(q->n / W), cudaMemcpyDeviceToHost, q->stream));
+        XK_CUDA(cudaEventRecord(q->ev, q->stream));
+        q->ev_pending = true;
+        q->draining = true;
+        return XK_OK;
     }
     XK_CUDA(cudaMemcpyAsync(hst, src, (size_t)(q->n * q->esz), cudaMemcpyDeviceToHost, q->stream));
     XK_CUDA(cudaEventRecord(q->ev, q->stream));

@@ -220,6 +220,10 @@ struct XkSeedJob {
 cudaError_t xk_seed_bernoulli(const XkSeedJob *jobs, int count, uint8_t *cells, cudaStream_t s);
 
 // mass-transfer family (mass.cu)
+// Mass-transfer state on the device: rows of W cells at a pitch of W rounded
+// up to a multiple of 4 (so a row starts on 16 bytes, as the tensor copies
+// need); the padding cells hold 0.
+inline int64_t xk_mass_pitch(int64_t W) { return (W + 3) / 4 * 4; }
 // small: the lattice's total mass is below 2^30 (then every cell stays below
 // it for good), which allows the fast-only kernel
 cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long *total,
@@ -230,6 +234,6 @@ cudaError_t xk_mass_sum(const uint32_t *src, int64_t n, unsigned long long *out,
 // last call (the flag is cleared)
 bool xk_mass_take_wait_failure();
 cudaError_t xk_mass_project(const uint32_t *src, uint32_t *proj, const xk_desc &d, cudaStream_t s);
-cudaError_t xk_mass_colors(const uint32_t *src, int32_t *col, int64_t n, cudaStream_t s);
+cudaError_t xk_mass_colors(const uint32_t *src, int32_t *col, const xk_desc &d, cudaStream_t s);
 cudaError_t xk_mass_render(const uint32_t *proj, int32_t *img, const xk_desc &d, int width,
                            int height, int zoom, int dx, int dy, cudaStream_t s);
