@@ -41,6 +41,7 @@ LifeGeo xk_life_geo(int64_t W, int64_t H, int torus, int border_state)
     g.lastmask = g.rlast == 32 ? 0xFFFFFFFFu : ((1u << g.rlast) - 1u);
     g.torus = torus;
     g.bfill = border_state ? 0xFFFFFFFFu : 0u;
+    g.div_wpr = xk_div_magic((uint64_t)g.wpr, (uint64_t)g.H * (uint64_t)g.wpr);
     return g;
 }
 
@@ -53,12 +54,11 @@ __global__ void __launch_bounds__(256)
 xk_k_life_global(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, LifeGeo g,
                  LifeTable t)
 {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t total = (int64_t)g.H * g.wpr;
-    if (idx >= total) return;
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (uint32_t)g.H * (uint32_t)g.wpr) return;
     xk_grid_dep_wait();       // launched as a dependent of the previous generation
-    const int y = (int)(idx / g.wpr);
-    const int j = (int)(idx - (int64_t)y * g.wpr);
+    const int y = (int)xk_divu(idx, (uint32_t)g.wpr, g.div_wpr);
+    const int j = (int)(idx - (uint32_t)y * g.wpr);
     const int last = g.wpr - 1;
     const int jl = j > 0 ? j - 1 : last, jr = j < last ? j + 1 : 0;
     const int lshift = j > 0 ? 31 : g.rlast - 1;
@@ -90,6 +90,7 @@ cudaError_t xk_life_step_global(const uint32_t *src, uint32_t *dst, const LifeGe
                                 const LifeTable &t, cudaStream_t s)
 {
     const int64_t total = (int64_t)g.H * g.wpr;
+    if (total > 0xFFFFFFFFll) return cudaErrorInvalidValue;   // 32-bit word indices
     const int threads = 256;
     const int64_t blocks = (total + threads - 1) / threads;
     return xk_launch_pdl(xk_k_life_global, dim3((unsigned)blocks), dim3(threads), 0, s, src, dst, g, t);
@@ -109,13 +110,12 @@ __global__ void __launch_bounds__(256)
 xk_k_life3d_vn(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, Life3Geo g,
                LifeTable t)
 {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t rows = (int64_t)g.H * g.D;
-    if (idx >= rows * g.wpr) return;
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (uint32_t)g.H * (uint32_t)g.D * (uint32_t)g.wpr) return;
     xk_grid_dep_wait();       // launched as a dependent of the previous generation
-    const int64_t r = idx / g.wpr;
-    const int j = (int)(idx - r * g.wpr);
-    const int z = (int)(r / g.H), y = (int)(r - (int64_t)z * g.H);
+    const uint32_t r = xk_divu(idx, (uint32_t)g.wpr, g.div_wpr);
+    const int j = (int)(idx - r * (uint32_t)g.wpr);
+    const int z = (int)xk_divu(r, (uint32_t)g.H, g.div_h), y = (int)(r - (uint32_t)z * g.H);
     const int last = g.wpr - 1;
     const int jl = j > 0 ? j - 1 : last, jr = j < last ? j + 1 : 0;
     const int lshift = j > 0 ? 31 : g.rlast - 1;
@@ -150,6 +150,7 @@ cudaError_t xk_life_step3d_vn(const uint32_t *src, uint32_t *dst, const Life3Geo
                               const LifeTable &t, cudaStream_t s)
 {
     const int64_t total = (int64_t)g.H * g.D * g.wpr;
+    if (total > 0xFFFFFFFFll) return cudaErrorInvalidValue;   // 32-bit word indices
     const int threads = 256;
     const int64_t blocks = (total + threads - 1) / threads;
     return xk_launch_pdl(xk_k_life3d_vn, dim3((unsigned)blocks), dim3(threads), 0, s, src, dst, g, t);

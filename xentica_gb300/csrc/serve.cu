@@ -290,6 +290,9 @@ static int admit(xk_server *s, Req *q, bool *admitted)
         q->g3.wpr = q->lg.wpr;
         q->g3.rlast = q->lg.rlast;
         q->g3.lastmask = q->lg.lastmask;
+        q->g3.div_wpr = xk_div_magic((uint64_t)q->g3.wpr,
+                                     (uint64_t)q->g3.H * (uint64_t)q->g3.D * (uint64_t)q->g3.wpr);
+        q->g3.div_h = xk_div_magic((uint64_t)q->g3.H, (uint64_t)q->g3.H * (uint64_t)q->g3.D);
         uint32_t *w0 = (uint32_t *)(base + rnd(q->n + 16));
         XK_CUDA(xk_life_pack(base, 1, w0, q->lg, q->stream));
         s->st.launches++;

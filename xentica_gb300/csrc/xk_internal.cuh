@@ -69,7 +69,24 @@ struct LifeGeo {
     uint32_t lastmask;         // valid bits of a row's last word
     int32_t torus;             // 1: wrap; 0: off-board cells read as bfill
     uint32_t bfill;            // 0 or ~0: static border state replicated
+    uint32_t div_wpr;          // xk_div_magic(wpr, H * wpr)
 };
+
+// n / d for every n < N as umulhi(n, m) with m = ceil(2^32 / d): exact when
+// N * (m d - 2^32) < 2^32 (then n / d + n e / (d 2^32) stays below the next
+// integer); 0 when that does not hold or d < 2, meaning a plain division
+inline uint32_t xk_div_magic(uint64_t d, uint64_t N)
+{
+    if (d < 2 || d >= (1ull << 32)) return 0;
+    const uint64_t m = ((1ull << 32) + d - 1) / d;
+    const uint64_t e = m * d - (1ull << 32);
+    return (e == 0 || N < (1ull << 32) / e) && N <= 0xFFFFFFFFull ? (uint32_t)m : 0u;
+}
+
+__device__ __forceinline__ uint32_t xk_divu(uint32_t n, uint32_t d, uint32_t m)
+{
+    return m ? __umulhi(n, m) : n / d;
+}
 
 LifeGeo xk_life_geo(int64_t W, int64_t H, int torus, int border_state);
 
@@ -121,6 +138,7 @@ cudaError_t xk_life_color_step(const uint32_t *bits, int32_t *col, const LifeGeo
 struct Life3Geo {
     int32_t W, H, D, wpr, rlast;
     uint32_t lastmask;
+    uint32_t div_wpr, div_h;   // xk_div_magic(wpr, H * D * wpr), xk_div_magic(H, H * D)
 };
 cudaError_t xk_life_step3d_vn(const uint32_t *src, uint32_t *dst, const Life3Geo &g,
                               const LifeTable &t, cudaStream_t s);
