@@ -1,9 +1,11 @@
 """GPU parity of the cluster path for single Life-like lattices.
 
 ``XK_CLUSTER=n`` makes a model's multi-generation steps run on a cluster of
-(up to) n CTAs, whatever the tuner would pick; every lattice is compared cell
-by cell with the oracle, torus and static border (value 1), widths around the
-word size and up to 1024, heights from a few rows to more than one CTA holds.
+(up to) n CTAs, whatever the tuner would pick, and ``XK_CLUSTER_BAND=b`` sets
+the rows each lane group walks (b = 1 .. 4, and 5 for bands that do not
+divide a CTA's rows); every lattice is compared cell by cell with the oracle,
+torus and static border (value 1), widths around the word size and up to
+1024, heights from a few rows to more than one CTA holds.
 """
 import numpy as np
 import pytest
@@ -25,8 +27,9 @@ pytestmark = pytest.mark.gpu
 SIZES = [(512, 512), (33, 17), (1024, 40), (1, 9), (100, 301), (1000, 700), (32, 2), (7, 1024)]
 
 
-def _run(cls, size, forced, gens, monkeypatch, seed):
+def _run(cls, size, forced, gens, monkeypatch, seed, band=2):
     monkeypatch.setenv("XK_CLUSTER", str(forced))
+    monkeypatch.setenv("XK_CLUSTER_BAND", str(band))
     exp = type("E", (SoupExperiment, ), {"size": size})
     model = cls(exp)
     n = model.cells_num
@@ -41,17 +44,19 @@ def _run(cls, size, forced, gens, monkeypatch, seed):
     return model.gpu.arrays.cells.get()[:n], fld[:n]
 
 
+@pytest.mark.parametrize("band", [1, 2, 4, 5])
 @pytest.mark.parametrize("forced", [2, 4, 8, 16])
 @pytest.mark.parametrize("cls", [GameOfLife, GameOfLifeStatic])
-def test_cluster_sizes_vs_oracle(cls, forced, monkeypatch):
+def test_cluster_sizes_vs_oracle(cls, forced, band, monkeypatch):
     for k, size in enumerate(SIZES):
-        got, want = _run(cls, size, forced, 37, monkeypatch, 10 * forced + k)
-        assert np.array_equal(got, want), (cls.__name__, size, forced)
+        got, want = _run(cls, size, forced, 37, monkeypatch, 10 * forced + k, band)
+        assert np.array_equal(got, want), (cls.__name__, size, forced, band)
 
 
 def test_long_run_and_tuner_choice(monkeypatch):
     # 1000 generations (one launch) with the tuner's own choice
     monkeypatch.delenv("XK_CLUSTER", raising=False)
+    monkeypatch.delenv("XK_CLUSTER_BAND", raising=False)
     exp = type("E", (SoupExperiment, ), {"size": (512, 512)})
     model = GameOfLife(exp)
     n = model.cells_num

@@ -174,11 +174,12 @@ static int resident_plan_for(xk_model *m)
 
 // Multi-generation steps of a 2-D lattice run in one launch on the resident
 // kernel (one CTA) or on a cluster of 2..16 CTAs (cluster.cu).  On the first
-// such step the candidates are timed over 32 generations on the ping-pong
-// partner buffer (the state is not touched) and the fastest is kept;
-// lattices too large for one CTA take the fastest cluster that fits, else the
-// per-generation global kernel.  XK_CLUSTER=0 disables clusters and
-// XK_CLUSTER=n asks for a cluster of (up to) n CTAs.
+// such step the candidates (cluster sizes, and bands of 1, 2 or 4 rows per
+// lane group) are timed over 32 generations on the ping-pong partner buffer
+// (the state is not touched) and the fastest is kept; lattices too large for
+// one CTA take the fastest cluster that fits, else the per-generation global
+// kernel.  XK_CLUSTER=0 disables clusters and XK_CLUSTER=n asks for a cluster
+// of (up to) n CTAs, with bands of XK_CLUSTER_BAND rows (default 2).
 static int tune_cluster(xk_model *m)
 {
     m->cl_tuned = 1;
@@ -186,15 +187,16 @@ static int tune_cluster(xk_model *m)
     const char *env = getenv("XK_CLUSTER");
     if (env && env[0]) {
         const int want = atoi(env);
+        const char *benv = getenv("XK_CLUSTER_BAND");
+        const int band = benv && benv[0] ? atoi(benv) : 2;
         int C = 0, R = 0, th = 0;
-        if (want > 0 && xk_life_cluster_config(m->lg, want, &C, &R, &th)) {
+        if (want > 0 && xk_life_cluster_config(m->lg, want, band, &C, &R, &th)) {
             m->cl_C = C;
             m->cl_R = R;
             m->cl_threads = th;
         }
         return XK_OK;
     }
-    const LifeTable t = xk_life_table(m->rule0, m->rule1);
     const size_t bytes = (size_t)m->lg.H * m->lg.wpr * 4;
     uint32_t *scratch = m->bits[1 - m->cur];
     XK_CUDA(cudaMemcpyAsync(scratch, m->bits[m->cur], bytes, cudaMemcpyDeviceToDevice, m->stream));
@@ -209,12 +211,14 @@ static int tune_cluster(xk_model *m)
         XK_CUDA(cudaEventElapsedTime(&best, m->ev0, m->ev1));
     }
     static const int cand[] = {16, 8, 4, 2};
-    for (int want : cand) {
+    static const int bands[] = {1, 2, 4};
+    for (int k = 0; k < 12; ++k) {
+        const int want = cand[k / 3], band = bands[k % 3];
         int C = 0, R = 0, th = 0;
-        if (!xk_life_cluster_config(m->lg, want, &C, &R, &th)) continue;
+        if (!xk_life_cluster_config(m->lg, want, band, &C, &R, &th)) continue;
         float ms = 0.f;
         XK_CUDA(cudaEventRecord(m->ev0, m->stream));
-        XK_CUDA(xk_life_step_cluster(scratch, m->lg, t, G, C, R, th, m->stream));
+        XK_CUDA(xk_life_step_cluster(scratch, m->lg, m->rule0, m->rule1, G, C, R, th, m->stream));
         XK_CUDA(cudaEventRecord(m->ev1, m->stream));
         XK_CUDA(cudaEventSynchronize(m->ev1));
         XK_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
@@ -654,11 +658,10 @@ extern "C" int xk_step(xk_model *m, int64_t nsteps)
     if (m->layout == LAYOUT_BITS2D && colors_free && m->cl_C) {
         // whole lattice in the shared memory of a cluster; long runs are cut
         // into launches of at most 4096 generations
-        const LifeTable t = xk_life_table(m->rule0, m->rule1);
         int64_t left = nsteps;
         while (left > 0) {
             const int g = (int)(left > 4096 ? 4096 : left);
-            XK_CUDA(xk_life_step_cluster(m->bits[m->cur], m->lg, t, g, m->cl_C, m->cl_R,
+            XK_CUDA(xk_life_step_cluster(m->bits[m->cur], m->lg, m->rule0, m->rule1, g, m->cl_C, m->cl_R,
                                          m->cl_threads, m->stream));
             left -= g;
         }

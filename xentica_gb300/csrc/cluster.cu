@@ -1,22 +1,29 @@
 // One Life-like lattice on a thread-block cluster (single-model path).
 //
 // The resident kernel runs a lattice on one CTA, i.e. one SM.  Here the rows
-// of a bit-packed lattice (W <= 1024) are cut into C bands, one per CTA of a
-// cluster of C (up to 16) CTAs; each CTA keeps its band in shared memory,
-// double-buffered by generation parity, for every generation of the launch.
-// The row above a band and the row below it belong to the neighbouring CTAs
-// and are read straight from their shared memory (distributed shared memory,
-// cluster.map_shared_rank).  One cluster barrier per generation orders it all:
-// after barrier g every CTA has finished generation g - 1, so buffer g & 1
-// holds generation g everywhere and nobody still reads buffer (g + 1) & 1,
-// which generation g overwrites.  The barrier is the hardware cluster barrier
-// (every thread of every CTA arrives once per generation; no CTA leaves the
-// loop early), so there is no software spin to bound.
+// of a bit-packed lattice (W <= 1024) are cut into C slabs of R rows, one per
+// CTA of a cluster of C (up to 16) CTAs, and each CTA keeps its slab in shared
+// memory for every generation of the launch, in the resident kernel's band
+// layout (a group of P = next_pow2(wpr) lanes per row, each group walking down
+// a band of L rows with the column sums of three rows in registers, the rule
+// indexed by the 3 x 3 block count: xk_life_word9).  Updates are in place.
 //
-// Inside a band, P = next_pow2(wpr) lanes cover one row (lane j owns column
-// word j) and each group of P lanes walks down a run of consecutive rows
-// keeping three rows' neighbour vectors in registers, as in the resident
-// kernel; the neighbour count and rule are xk_life_word's.
+// Each band's first and last row are also kept in a halo area, which the
+// bands next to it read; the slab's first row also goes to the CTA above's
+// "row below" slot and its last row to the CTA below's "row above" slot
+// (remote stores to distributed shared memory).  Halos and slots are
+// double-buffered by generation parity: generation g reads the parity-g
+// buffers (all local loads) and, as it computes a band's first and last row,
+// stores them straight from registers into the parity-(g + 1) buffers, last
+// read by generation g - 1.  One cluster barrier starts every generation: it
+// orders the stores of generation g - 1 before the loads of generation g and
+// the loads of generation g - 1 before the stores of generation g (release /
+// acquire at cluster scope; every thread of every CTA arrives once per
+// generation and no CTA leaves the loop early).  It is the hardware cluster
+// barrier, so there is no software spin to bound.  A last barrier after the
+// loop keeps every CTA's shared memory alive until the remote stores of the
+// final generation have landed.  A lane only ever touches its own column word
+// of its own band.
 #include <cooperative_groups.h>
 
 #include <string.h>
@@ -26,11 +33,23 @@
 
 namespace cg = cooperative_groups;
 
-template <bool TORUS>
-__global__ void __launch_bounds__(1024)
-xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable t, int generations, int R)
+// shared words: slab of the widest CTA (R rows), halos [2][G][2][wpr], slots
+// [2][2][wpr]; the offsets are the same in every CTA of the cluster, which
+// the remote stores rely on
+static inline int64_t cluster_words(int wpr, int R, int threads)
 {
-    extern __shared__ uint32_t band[];   // [2][R][wpr]
+    const ResidentPlan p = xk_resident_plan(wpr, R, threads);
+    return xk_res_lat_words(p) + 4LL * p.G * wpr + 4LL * wpr;
+}
+
+// TORUS: wrap, else static border; FULLW: torus rows of whole words (each
+// neighbour vector one funnel shift); LB: every band of the widest CTA has
+// exactly LB rows (1, 2 or 4; the row loop is unrolled), 0 for any length
+template <bool TORUS, bool FULLW, int LB>
+__global__ void __launch_bounds__(1024)
+xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t, int generations, int R)
+{
+    extern __shared__ uint32_t sm[];
     cg::cluster_group cluster = cg::this_cluster();
     const int C = (int)cluster.num_blocks();
     const int c = (int)cluster.block_rank();
@@ -38,27 +57,33 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable t, int gener
     const int r0 = c * R;
     const int Rc = min(H, r0 + R) - r0;                       // rows of this CTA (>= 1)
     const int cu = c > 0 ? c - 1 : C - 1, cd = c + 1 < C ? c + 1 : 0;
-    const int Ru = min(H, cu * R + R) - cu * R;               // rows of the CTA above
-    const bool top_off = !TORUS && c == 0, bot_off = !TORUS && c == C - 1;
-    const uint32_t *up_band = cluster.map_shared_rank(band, cu);
-    const uint32_t *dn_band = cluster.map_shared_rank(band, cd);
-    const int buf = R * wpr;
+    const ResidentPlan pw = xk_resident_plan(wpr, R, blockDim.x);
+    const ResidentPlan p = xk_resident_plan(wpr, Rc, blockDim.x);
+    uint32_t *lat = sm;
+    uint32_t *halo = sm + xk_res_lat_words(pw);               // [parity][band][first, last][wpr]
+    uint32_t *slot = halo + 4 * pw.G * wpr;                   // [parity][above, below][wpr]
+    uint32_t *slot_up = cluster.map_shared_rank(slot, cu);
+    uint32_t *slot_dn = cluster.map_shared_rank(slot, cd);
+    const int hwords = 2 * pw.G * wpr;
 
-    for (int w = threadIdx.x; w < Rc * wpr; w += blockDim.x) band[w] = bits[(int64_t)r0 * wpr + w];
+    for (int w = threadIdx.x; w < Rc * wpr; w += blockDim.x) {
+        const int y = w / wpr, jj = w - y * wpr;
+        const int b = y / p.L, i = y - b * p.L;
+        lat[xk_res_at(p, b, i, jj)] = bits[(int64_t)r0 * wpr + w];
+    }
 
-    int P = 1;
-    while (P < wpr) P <<= 1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int gpw = 32 / P;
-    const int groups = (int)(blockDim.x / 32) * gpw;
-    const int q = lane / P, j = lane - q * P;
-    const int grp = warp * gpw + q;
-    const int L = (Rc + groups - 1) / groups;                 // rows per group
-    const int gy0 = grp * L, gy1 = min(Rc, gy0 + L);
-    const bool jok = j < wpr;
-    const int jc = jok ? j : wpr - 1;
+    const int q = lane / p.P, j = lane - q * p.P;
+    const int band = warp * p.gpw + q;
+    const bool active = band < p.nb && j < wpr;
+    // clamped indices: idle lanes compute on valid (ignored) words, so the
+    // shuffles always see the whole warp
+    const int bc = band < p.nb ? band : p.nb - 1;
+    const int jc = j < wpr ? j : wpr - 1;
+    const int y0 = bc * p.L;
+    const int y1 = min(Rc, y0 + p.L);
     const int last = wpr - 1;
-    const int gbase = q * P;
+    const int gbase = q * p.P;
     const int src_l = gbase + (jc > 0 ? jc - 1 : last);
     const int src_r = gbase + (jc < last ? jc + 1 : 0);
     const int lshift = jc > 0 ? 31 : g.rlast - 1;
@@ -68,70 +93,119 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable t, int gener
     const uint32_t outmask = jc == last ? g.lastmask : 0xFFFFFFFFu;
     const uint32_t edge = g.bfill & 1u;
     const int use_le = (!TORUS) && jc == 0, use_re = (!TORUS) && jc == last;
+    const bool first_band = bc == 0, last_band = bc == p.nb - 1;
+    const bool top_off = !TORUS && c == 0 && first_band;      // row above is off the lattice
+    const bool bot_off = !TORUS && c == C - 1 && last_band;   // row below is off the lattice
+    uint32_t *wp = lat + xk_res_at(p, bc, 0, jc);             // this lane's word of band row i: wp[32 i]
 
-    cluster.sync();   // every band loaded before anyone reads a neighbour's
-    for (int gen = 0; gen < generations; ++gen) {
-        const int pb = (gen & 1) * buf;
-        const uint32_t *cur = band + pb;
-        uint32_t *nxt = band + (buf - pb);
-        // word of local row y (-1 .. Rc) at this lane's column; rows outside
-        // the band come from the neighbouring CTAs (or the static border)
-        auto fetch = [&](int y, bool &off) -> uint32_t {
-            off = false;
-            if (y < 0) {
-                if (top_off) { off = true; return g.bfill; }
-                return up_band[pb + (Ru - 1) * wpr + jc];
-            }
-            if (y >= Rc) {
-                if (bot_off) { off = true; return g.bfill; }
-                return dn_band[pb + jc];
-            }
-            return cur[y * wpr + jc];
-        };
-        auto vec = [&](uint32_t w, bool off) -> RowVec {
-            const uint32_t l = __shfl_sync(0xFFFFFFFFu, w, src_l);
-            const uint32_t r = __shfl_sync(0xFFFFFFFFu, w, src_r);
-            RowVec v;
-            if (TORUS) {
-                v = xk_torus_vec(w, l, r, lpre, top, topbit);
-            } else {
-                v = xk_row_vec(w, l, r, lshift, top, edge, edge, use_le, use_re);
-                if (off) v.L = v.C = v.R = g.bfill;
-            }
-            return v;
-        };
-        // every lane runs L iterations so the shuffles always see the whole
-        // warp; groups past the band's end compute and discard
-        const int ys = min(gy0, Rc);
-        bool off;
-        uint32_t w = fetch(ys - 1, off);
-        RowVec vu = vec(w, off);
-        w = fetch(ys, off);
-        RowVec vm = vec(w, off);
-        for (int i = 0; i < L; ++i) {
-            const int y = ys + i;
-            w = fetch(min(y + 1, Rc), off);
-            const RowVec vd = vec(w, off);
-            const uint32_t out = xk_life_word(vu.L, vu.C, vu.R, vm.L, vm.C, vm.R, vd.L, vd.C,
-                                                 vd.R, t) & outmask;
-            if (jok && y < gy1) nxt[y * wpr + j] = out;
-            vu = vm;
-            vm = vd;
+    // column sums (s, c) = FA(L, C, R) of the row whose word at this lane's
+    // column is w
+    auto colsum = [&](uint32_t w, uint32_t &s, uint32_t &cy) {
+        const uint32_t l = __shfl_sync(0xFFFFFFFFu, w, src_l);
+        const uint32_t r = __shfl_sync(0xFFFFFFFFu, w, src_r);
+        if (FULLW) {
+            const uint32_t L = __funnelshift_l(l, w, 1), Rr = __funnelshift_r(w, r, 1);
+            s = xk_lop3_xor3(L, w, Rr);
+            cy = xk_maj(L, w, Rr);
+            return;
         }
+        const RowVec v = TORUS ? xk_torus_vec(w, l, r, lpre, top, topbit)
+                               : xk_row_vec(w, l, r, lshift, top, edge, edge, use_le, use_re);
+        s = xk_lop3_xor3(v.L, v.C, v.R);
+        cy = xk_maj(v.L, v.C, v.R);
+    };
+
+    // a band's first row goes to its halo and, for the slab's first band, to
+    // the CTA above ("row below" slot); its last row likewise downwards
+    const bool send_up = active && band == 0, send_dn = active && band == p.nb - 1;
+    auto publish = [&](int npar, int i, uint32_t w) {
+        if (!active) return;
+        if (i == 0) {
+            halo[npar * hwords + (band * 2 + 0) * wpr + j] = w;
+            if (send_up) slot_up[(npar * 2 + 1) * wpr + j] = w;
+        }
+        if (i == y1 - 1 - y0) {
+            halo[npar * hwords + (band * 2 + 1) * wpr + j] = w;
+            if (send_dn) slot_dn[(npar * 2 + 0) * wpr + j] = w;
+        }
+    };
+
+    cluster.sync();   // every CTA running (before any remote store) and every slab loaded
+    publish(0, 0, wp[0]);
+    publish(0, y1 - 1 - y0, wp[32 * (y1 - 1 - y0)]);
+    for (int gen = 0; gen < generations; ++gen) {
+        const int par = gen & 1;
+        const uint32_t *hp = halo + par * hwords;
         cluster.sync();
+        const uint32_t wu = first_band ? slot[(par * 2 + 0) * wpr + jc] : hp[((bc - 1) * 2 + 1) * wpr + jc];
+        const uint32_t wl = last_band ? slot[(par * 2 + 1) * wpr + jc] : hp[((bc + 1) * 2 + 0) * wpr + jc];
+        uint32_t su, cu_, sm_, cm_, Cm = wp[0];
+        colsum(wu, su, cu_);
+        if (top_off) su = cu_ = g.bfill;
+        colsum(Cm, sm_, cm_);
+        auto row = [&](int i) {
+            const int y = y0 + i;
+            const bool below = y + 1 >= y1;                       // next row is the band's neighbour
+            const uint32_t wd = below ? wl : wp[32 * (i + 1)];
+            uint32_t sd, cd_;
+            colsum(wd, sd, cd_);
+            if (below && bot_off) sd = cd_ = g.bfill;
+            uint32_t out = xk_life_word9(su, cu_, sm_, cm_, sd, cd_, Cm, t);
+            if (!FULLW) out &= outmask;
+            if (active && y < y1) {
+                wp[32 * i] = out;
+                publish(par ^ 1, i, out);
+            }
+            su = sm_;
+            cu_ = cm_;
+            sm_ = sd;
+            cm_ = cd_;
+            Cm = wd;
+        };
+        if (LB > 0) {
+#pragma unroll
+            for (int i = 0; i < LB; ++i) row(i);
+        } else {
+#pragma unroll 2
+            for (int i = 0; i < p.L; ++i) row(i);
+        }
     }
-    const uint32_t *fin = band + (generations & 1) * buf;
-    for (int w = threadIdx.x; w < Rc * wpr; w += blockDim.x) bits[(int64_t)r0 * wpr + w] = fin[w];
+    cluster.sync();
+    for (int w = threadIdx.x; w < Rc * wpr; w += blockDim.x) {
+        const int y = w / wpr, jj = w - y * wpr;
+        const int b = y / p.L, i = y - b * p.L;
+        bits[(int64_t)r0 * wpr + w] = lat[xk_res_at(p, b, i, jj)];
+    }
 }
 
-template <bool TORUS>
-static cudaError_t cluster_attrs(size_t smem)
+typedef void (*ClusterKernel)(uint32_t *, LifeGeo, LifeTable9, int, int);
+
+template <bool TORUS, bool FULLW>
+static ClusterKernel cluster_kernel_l(int L)
 {
-    cudaError_t e = cudaFuncSetAttribute(xk_k_life_cluster<TORUS>,
-                                         cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    switch (L) {
+    case 1: return xk_k_life_cluster<TORUS, FULLW, 1>;
+    case 2: return xk_k_life_cluster<TORUS, FULLW, 2>;
+    case 4: return xk_k_life_cluster<TORUS, FULLW, 4>;
+    default: return xk_k_life_cluster<TORUS, FULLW, 0>;
+    }
+}
+
+// the instantiation for a lattice and launch shape (L: band length of the
+// widest CTA)
+static ClusterKernel cluster_kernel(const LifeGeo &g, int R, int threads)
+{
+    const int L = xk_resident_plan(g.wpr, R, threads).L;
+    if (!g.torus) return cluster_kernel_l<false, false>(L);
+    if (g.rlast == 32) return cluster_kernel_l<true, true>(L);
+    return cluster_kernel_l<true, false>(L);
+}
+
+static cudaError_t cluster_attrs(ClusterKernel k, size_t smem)
+{
+    cudaError_t e = cudaFuncSetAttribute((const void *)k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(xk_k_life_cluster<TORUS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem);
+    return cudaFuncSetAttribute((const void *)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 static void cluster_cfg(cudaLaunchConfig_t &cfg, cudaLaunchAttribute &attr, int C, int threads,
@@ -150,22 +224,42 @@ static void cluster_cfg(cudaLaunchConfig_t &cfg, cudaLaunchAttribute &attr, int 
     cfg.numAttrs = 1;
 }
 
-// rows per CTA and threads for a cluster of (up to) C CTAs; 0 if the lattice
-// does not fit or no such cluster can be resident on this device
-int xk_life_cluster_config(const LifeGeo &g, int C, int *C_out, int *R, int *threads)
+LifeTable9 xk_life_table9(uint32_t rule0, uint32_t rule1)
 {
-    if (g.wpr > 32 || C < 2 || C > 16 || g.H < C) return 0;
+    // dead D[n] = rule0 bit n, live L[n] = rule1 bit n - 1 (n: 3 x 3 count)
+    auto D = [&](int n) { return 0u - ((rule0 >> n) & 1u); };
+    auto L = [&](int n) { return 0u - ((rule1 >> (n > 0 ? n - 1 : 0)) & 1u); };
+    LifeTable9 t;
+    for (int q = 0; q < 8; ++q) {
+        const uint32_t A = q < 4 ? D(2 * q) : L(2 * (q - 4));
+        const uint32_t B = q < 4 ? D(2 * q + 1) : L(2 * (q - 4) + 1);
+        t.a[q] = A;
+        t.k[q] = xk_mux_coef(A, B);
+    }
+    t.d8 = D(8);
+    t.a9 = L(8);
+    t.k9 = xk_mux_coef(L(8), L(9));
+    return t;
+}
+
+// rows per CTA and threads for a cluster of (up to) C CTAs whose lane groups
+// walk bands of about `band` rows; 0 if the lattice does not fit or no such
+// cluster can be resident on this device
+int xk_life_cluster_config(const LifeGeo &g, int C, int band, int *C_out, int *R, int *threads)
+{
+    if (g.wpr > 32 || C < 2 || C > 16 || g.H < C || band < 1) return 0;
     const int rows = (g.H + C - 1) / C;
     const int Cr = (g.H + rows - 1) / rows;                    // no empty CTA
     if (Cr < 2) return 0;
-    const size_t smem = 2ull * rows * g.wpr * 4;
-    if ((int64_t)smem > xk_max_smem_optin()) return 0;
     int P = 1;
     while (P < g.wpr) P <<= 1;
-    int th = ((P * rows + 31) / 32) * 32;
+    const int groups = (rows + band - 1) / band;
+    int th = ((P * groups + 31) / 32) * 32;
     th = th < 32 ? 32 : (th > 1024 ? 1024 : th);
-    const bool torus = g.torus != 0;
-    if ((torus ? cluster_attrs<true>(smem) : cluster_attrs<false>(smem)) != cudaSuccess) {
+    const size_t smem = 4ull * cluster_words(g.wpr, rows, th);
+    if ((int64_t)smem > xk_max_smem_optin()) return 0;
+    const ClusterKernel k = cluster_kernel(g, rows, th);
+    if (cluster_attrs(k, smem) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
@@ -173,8 +267,7 @@ int xk_life_cluster_config(const LifeGeo &g, int C, int *C_out, int *R, int *thr
     cudaLaunchAttribute attr;
     cluster_cfg(cfg, attr, Cr, th, smem, 0);
     int active = 0;
-    cudaError_t e = torus ? cudaOccupancyMaxActiveClusters(&active, xk_k_life_cluster<true>, &cfg)
-                          : cudaOccupancyMaxActiveClusters(&active, xk_k_life_cluster<false>, &cfg);
+    cudaError_t e = cudaOccupancyMaxActiveClusters(&active, (const void *)k, &cfg);
     if (e != cudaSuccess || active < 1) {
         cudaGetLastError();
         return 0;
@@ -185,16 +278,16 @@ int xk_life_cluster_config(const LifeGeo &g, int C, int *C_out, int *R, int *thr
     return 1;
 }
 
-cudaError_t xk_life_step_cluster(uint32_t *bits, const LifeGeo &g, const LifeTable &t,
+cudaError_t xk_life_step_cluster(uint32_t *bits, const LifeGeo &g, uint32_t rule0, uint32_t rule1,
                                  int generations, int C, int R, int threads, cudaStream_t s)
 {
-    const size_t smem = 2ull * R * g.wpr * 4;
-    const bool torus = g.torus != 0;
-    cudaError_t e = torus ? cluster_attrs<true>(smem) : cluster_attrs<false>(smem);
+    const size_t smem = 4ull * cluster_words(g.wpr, R, threads);
+    const ClusterKernel k = cluster_kernel(g, R, threads);
+    cudaError_t e = cluster_attrs(k, smem);
     if (e != cudaSuccess) return e;
+    const LifeTable9 t = xk_life_table9(rule0, rule1);
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr;
     cluster_cfg(cfg, attr, C, threads, smem, s);
-    if (torus) return cudaLaunchKernelEx(&cfg, xk_k_life_cluster<true>, bits, g, t, generations, R);
-    return cudaLaunchKernelEx(&cfg, xk_k_life_cluster<false>, bits, g, t, generations, R);
+    return cudaLaunchKernelEx(&cfg, k, bits, g, t, generations, R);
 }

@@ -181,37 +181,6 @@ cudaError_t xk_life_step3d_vn(const uint32_t *src, uint32_t *dst, const Life3Geo
 
 #define XK_TAB_WORDS 32
 
-struct ResidentPlan {
-    int P, gpw, G, L, nb;  // lanes per group, groups per warp, groups, band length, live bands
-};
-
-// shared word of local row i, column word jj of band b (warp-major layout)
-__host__ __device__ __forceinline__ int xk_res_at(const ResidentPlan &p, int b, int i, int jj)
-{
-    return ((b / p.gpw) * p.L + i) * 32 + (b % p.gpw) * p.P + jj;
-}
-
-// shared words of the lattice area: L rows of 32 words per warp holding bands
-__host__ __device__ __forceinline__ int64_t xk_res_lat_words(const ResidentPlan &p)
-{
-    return (int64_t)p.L * ((p.G + p.gpw - 1) / p.gpw) * 32;
-}
-
-__host__ __device__ inline ResidentPlan xk_resident_plan(int wpr, int H, int threads)
-{
-    ResidentPlan p;
-    int P = 1;
-    while (P < wpr) P <<= 1;
-    p.P = P;
-    p.gpw = 32 / P;
-    int groups = (threads / 32) * p.gpw;
-    if (groups > H) groups = H;
-    p.G = groups;
-    p.L = (H + groups - 1) / groups;
-    p.nb = (H + p.L - 1) / p.L;
-    return p;
-}
-
 int64_t xk_life_resident_words(int W, int H, int threads)
 {
     const int wpr = (W + 31) / 32;

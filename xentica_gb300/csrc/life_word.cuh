@@ -169,3 +169,38 @@ __device__ __forceinline__ RowVec xk_torus_vec(uint32_t c, uint32_t left, uint32
     return v;
 }
 
+// Band layout of a lattice held in shared memory (life.cu's resident kernel,
+// cluster.cu): a group of P = next_pow2(wpr) lanes covers one row, the rows
+// are cut into bands of L consecutive rows, one per group, and local row i
+// of band b, column word jj, sits at ((b / gpw) * L + i) * 32 + (b % gpw) * P
+// + jj (warp-major: a lane's next row is always 32 words further on).
+struct ResidentPlan {
+    int P, gpw, G, L, nb;  // lanes per group, groups per warp, groups, band length, live bands
+};
+
+// shared word of local row i, column word jj of band b (warp-major layout)
+__host__ __device__ __forceinline__ int xk_res_at(const ResidentPlan &p, int b, int i, int jj)
+{
+    return ((b / p.gpw) * p.L + i) * 32 + (b % p.gpw) * p.P + jj;
+}
+
+// shared words of the lattice area: L rows of 32 words per warp holding bands
+__host__ __device__ __forceinline__ int64_t xk_res_lat_words(const ResidentPlan &p)
+{
+    return (int64_t)p.L * ((p.G + p.gpw - 1) / p.gpw) * 32;
+}
+
+__host__ __device__ inline ResidentPlan xk_resident_plan(int wpr, int H, int threads)
+{
+    ResidentPlan p;
+    int P = 1;
+    while (P < wpr) P <<= 1;
+    p.P = P;
+    p.gpw = 32 / P;
+    int groups = (threads / 32) * p.gpw;
+    if (groups > H) groups = H;
+    p.G = groups;
+    p.L = (H + groups - 1) / groups;
+    p.nb = (H + p.L - 1) / p.L;
+    return p;
+}

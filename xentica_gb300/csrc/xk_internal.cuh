@@ -145,9 +145,11 @@ cudaError_t xk_life_step3d_vn(const uint32_t *src, uint32_t *dst, const Life3Geo
 
 // one lattice (W <= 1024) on a thread-block cluster of C CTAs, R rows each,
 // in place on its bit-packed words (cluster.cu); config returns 0 when no
-// cluster of (up to) C CTAs fits
-int xk_life_cluster_config(const LifeGeo &g, int C, int *C_out, int *R, int *threads);
-cudaError_t xk_life_step_cluster(uint32_t *bits, const LifeGeo &g, const LifeTable &t,
+// cluster of (up to) C CTAs whose lane groups walk bands of about `band` rows
+// fits
+LifeTable9 xk_life_table9(uint32_t rule0, uint32_t rule1);
+int xk_life_cluster_config(const LifeGeo &g, int C, int band, int *C_out, int *R, int *threads);
+cudaError_t xk_life_step_cluster(uint32_t *bits, const LifeGeo &g, uint32_t rule0, uint32_t rule1,
                                  int generations, int C, int R, int threads, cudaStream_t s);
 
 // byte-per-cell lattices (N-D, any neighbourhood; and the plain 2-D form)
