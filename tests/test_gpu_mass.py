@@ -3,8 +3,9 @@
 Fixture cases (reference checksums) replay through ``test_gpu_life``'s
 fixture test; here: random states with large masses (unsigned wrap-around of
 the reference's arithmetic, cells equal to the wall value) compared with the
-oracle cell by cell, image parity, and conservation of the total mass over a
-long run read from the kernel's own per-generation totals.
+oracle cell by cell, image parity, conservation of the total mass over a
+long run read from the kernel's own per-generation totals, and step
+transitions after long runs checked against the oracle.
 """
 import numpy as np
 import pytest
@@ -83,6 +84,25 @@ def test_mass_conserved_long_run(kernel_form):
     assert totals.tolist() == [before] * 500
     after = int(model.gpu.arrays.cells.get()[:model.cells_num].astype(np.uint64).sum())
     assert after == before
+
+
+@pytest.mark.parametrize("size,gens", [((256, 256, 256), 2000), ((171, 205, 43), 3000)])
+def test_long_run_step_transitions(size, gens):
+    # after a long GPU run, one and then two more generations agree with the
+    # oracle started from the GPU state: the 256^3 lattice of the mass
+    # benchmark, and a width that is not a multiple of 4 (pitched rows)
+    model = _model(size)
+    model.gpu.step(gens)
+    n = model.cells_num
+    topo = _topo(size)
+    fld = topo.field(model.gpu.main_plane(), np.uint32)
+    col = np.zeros(3 * n, dtype=np.int32)
+    model.gpu.step(1)
+    O.mass_run(topo, fld, col, 1)
+    assert np.array_equal(model.gpu.main_plane(), fld[:n])
+    model.gpu.step(2)
+    O.mass_run(topo, fld, col, 2)
+    assert np.array_equal(model.gpu.main_plane(), fld[:n])
 
 
 def test_multi_generation_call_equals_single_steps():
