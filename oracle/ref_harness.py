@@ -92,6 +92,9 @@ def _install_stubs():
 def _load_obj(spec):
     mod_name, attr = spec.rsplit(":", 1)
     if mod_name.endswith(".py"):
+        if not os.path.isabs(mod_name):   # relative to the repository root
+            mod_name = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                    mod_name)
         name = "xk_refjob_" + hashlib.md5(mod_name.encode()).hexdigest()[:8]
         sp = importlib.util.spec_from_file_location(name, mod_name)
         mod = importlib.util.module_from_spec(sp)

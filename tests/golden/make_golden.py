@@ -23,7 +23,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 from ref_harness import run_reference  # noqa: E402
 
 GOL = "examples.game_of_life"
-REF_MODELS = os.path.join(HERE, "ref_models.py")
+REF_MODELS = "tests/golden/ref_models.py"   # relative to the repository root
 
 # name -> job (see ref_harness.py for the keys)
 CASES = {
