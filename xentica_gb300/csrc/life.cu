@@ -169,8 +169,12 @@ cudaError_t xk_life_step3d_vn(const uint32_t *src, uint32_t *dst, const Life3Geo
 // shared store per 32 cells.  The rule is indexed by the count of the 3 x 3
 // block including the cell (LifeTable9, xk_life_word9).  Updates are
 // in place: a lane only ever touches its own column word of its own band, and
-// the first and last row of every band are copied to a halo area before the
-// generation starts, so neighbouring bands read the previous generation.
+// the first and last row of every band are copied to a halo area, so
+// neighbouring bands read the previous generation.  The halos are
+// double-buffered by generation parity: generation g reads the parity-g
+// halos and, once its band is done, copies its new first and last row into
+// the parity-(g + 1) halos, last read by generation g - 1; one barrier per
+// generation (at its end) then orders everything.
 //
 // Shared layout is warp-major: the bands of warp w hold their local row i at
 // words (w * L + i) * 32 + lane, lane = group * P + column word, so a warp's
@@ -186,7 +190,7 @@ int64_t xk_life_resident_words(int W, int H, int threads)
     const int wpr = (W + 31) / 32;
     if (wpr > 32) return -1;
     ResidentPlan p = xk_resident_plan(wpr, H, threads);
-    return xk_res_lat_words(p) + 2LL * p.G * wpr + XK_TAB_WORDS;
+    return xk_res_lat_words(p) + 4LL * p.G * wpr + XK_TAB_WORDS;
 }
 
 template <bool BYTES, bool TORUS>
@@ -199,8 +203,8 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
     const int wpr = I.wpr, H = I.H, W = I.W;
     const ResidentPlan p = xk_resident_plan(wpr, H, blockDim.x);
     uint32_t *lat = sm;
-    uint32_t *halo = sm + xk_res_lat_words(p);       // [band][2][wpr]
-    uint32_t *tabs = halo + 2 * p.G * wpr;            // rule table
+    uint32_t *halo = sm + xk_res_lat_words(p);       // [parity][band][first, last][wpr]
+    uint32_t *tabs = halo + 4 * p.G * wpr;            // rule table
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
     // load: global row-major -> band-interleaved shared layout
@@ -297,14 +301,23 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
     t.a9 = tabs[17];
     t.k9 = tabs[18];
 
-    for (int gen = 0; gen < generations; ++gen) {
+    const int hw = 2 * p.G * wpr;                      // halo words per parity
+    // a band's first and last row into the halos of parity `par`
+    const uint32_t *first_row = lat + xk_res_at(p, bc, 0, jc);
+    const int last_off = 32 * (y1 - 1 - y0);            // warp-major: rows 32 words apart
+    uint32_t *hslot = halo + (bc * 2) * wpr + jc;
+    auto publish = [&](int par) {
         if (active) {
-            halo[(band * 2 + 0) * wpr + j] = lat[xk_res_at(p, band, 0, j)];
-            halo[(band * 2 + 1) * wpr + j] = lat[xk_res_at(p, band, y1 - 1 - y0, j)];
+            hslot[par * hw] = first_row[0];
+            hslot[par * hw + wpr] = first_row[last_off];
         }
-        __syncthreads();
+    };
+    publish(0);
+    __syncthreads();
+    for (int gen = 0; gen < generations; ++gen) {
+        const uint32_t *hc = halo + (gen & 1) * hw;
         RowVec vu, vm, vd;
-        const uint32_t wu = (!TORUS && bc == 0) ? bfill : halo[(hup * 2 + 1) * wpr + jc];
+        const uint32_t wu = (!TORUS && bc == 0) ? bfill : hc[(hup * 2 + 1) * wpr + jc];
         const uint32_t wm = lat[xk_res_at(p, bc, 0, jc)];
         if (TORUS) {
             uint32_t l = __shfl_sync(0xFFFFFFFFu, wu, src_l), r = __shfl_sync(0xFFFFFFFFu, wu, src_r);
@@ -332,7 +345,7 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
             uint32_t Cm = vm.C;
             constexpr int stride = 32;                          // words between band rows
             uint32_t *wp = lat + xk_res_at(p, bc, 0, jc);       // this lane's word of row i
-            const uint32_t whalo = halo[(hdn * 2 + 0) * wpr + jc];
+            const uint32_t whalo = hc[(hdn * 2 + 0) * wpr + jc];
             auto band_rows = [&](auto fullw_tag) {
                 constexpr bool FULLW = decltype(fullw_tag)::value;
                 auto row = [&](uint32_t wd, uint32_t *dst) {
@@ -385,8 +398,8 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
                 uint32_t wd;
                 bool off_d = false;
                 if (y + 1 < y1) wd = lat[xk_res_at(p, bc, i + 1, jc)];
-                else if (y + 1 < H) wd = halo[((bc + 1) * 2 + 0) * wpr + jc];
-                else if (TORUS) wd = halo[(0 * 2 + 0) * wpr + jc];
+                else if (y + 1 < H) wd = hc[((bc + 1) * 2 + 0) * wpr + jc];
+                else if (TORUS) wd = hc[(0 * 2 + 0) * wpr + jc];
                 else { wd = bfill; off_d = true; }
                 const uint32_t l = __shfl_sync(0xFFFFFFFFu, wd, src_l);
                 const uint32_t r = __shfl_sync(0xFFFFFFFFu, wd, src_r);
@@ -404,6 +417,7 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
                 vm = vd;
             }
         }
+        publish((gen & 1) ^ 1);
         __syncthreads();
     }
     if (BYTES) {
