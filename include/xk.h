@@ -187,6 +187,10 @@ int xk_batch_run(xk_batch *b, const uint8_t *host_in, uint8_t *host_out,
 int xk_batch_seed_bernoulli(xk_batch *b, const uint32_t *seeds, const double *p);
 /* Autotune the batched kernel's block size for this batch (timed on device). */
 int xk_batch_tune(xk_batch *b, int32_t generations, int32_t *chosen_rows_per_band);
+/* Set the band length (rows per lane group, 1..1024) the tuner would choose,
+ * e.g. from a cached tuning result, without timing; and read it back. */
+int xk_batch_set_band(xk_batch *b, int32_t rows_per_band);
+int32_t xk_batch_band(const xk_batch *b);
 int64_t xk_batch_total_cells(const xk_batch *b);
 /* Kernel launches one xk_batch_step makes (one per instance class, plus
  * per-generation launches for instances too large for a CTA). */

@@ -19,6 +19,13 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU and the built libxk.so")
 
 
+@pytest.fixture(autouse=True)
+def _no_tuning_cache(monkeypatch):
+    """Tests time their own tuning runs: the persistent tuning cache is off
+    unless a test points ``XK_TUNE_CACHE`` at a file of its own."""
+    monkeypatch.setenv("XK_TUNE_CACHE", "off")
+
+
 @pytest.fixture(scope="session")
 def golden():
     with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as fh:

@@ -4,10 +4,13 @@ Mixed sizes exercise every kernel path: resident in shared memory with one or
 many row groups per warp, partial last words, the in-place 1024-wide case, and
 lattices too wide for a CTA (plain per-generation launches).
 """
+import json
+
 import numpy as np
 import pytest
 
 import oracle as O
+from xentica_gb300 import _native as nat
 from xentica_gb300.batch import Ensemble, ensemble_workload
 from xentica_gb300.core.exceptions import XenticaException
 
@@ -68,6 +71,28 @@ def test_plain_run_and_tune_agree():
     assert np.array_equal(ens.download(), cells)   # tuning leaves the state alone
     ens.step(9)
     assert np.array_equal(ens.download(), plain)
+
+
+def test_tuning_cache_applies_the_stored_band(monkeypatch, tmp_path):
+    # the first tune times and stores its choice; a second ensemble of the
+    # same sizes takes it from the cache (xk_batch_set_band) and steps to the
+    # same cells as the plain form
+    monkeypatch.setenv("XK_TUNE_CACHE", str(tmp_path / "tune.json"))
+    ens, cells = _ensemble(3)
+    ens.upload(cells)
+    ens.step_plain(9)
+    plain = ens.download()
+    chosen = ens.tune(9)
+    assert ens.band == chosen
+    assert list(json.loads((tmp_path / "tune.json").read_text()).values()) == [chosen]
+    again, _ = _ensemble(3)
+    for band in (2, 32):
+        nat.check(again._lib.xk_batch_set_band(again._handle, band), "xk_batch_set_band")
+        assert again.band == band
+    assert again.tune(9) == chosen and again.band == chosen
+    again.upload(cells)
+    again.step(9)
+    assert np.array_equal(again.download(), plain)
 
 
 def test_rejects_non_binary_cells():

@@ -1,0 +1,119 @@
+"""The autotuning cache (``xentica_gb300.tuning``) on the CPU, with a fake
+library standing in for ``libxk.so``: where the file lives, what the keys
+distinguish, that a stored choice is applied without timing and that a miss
+times and stores."""
+import json
+
+import numpy as np
+import pytest
+
+from xentica_gb300 import tuning
+
+
+class FakeLib:
+    """Records the tuning calls a batch handle would get."""
+
+    def __init__(self, device=b"GB300 sm_103 SMs=152 smem_optin=232448", best=16):
+        self.device, self.best = device, best
+        self.tuned, self.set = [], []
+
+    def xk_device_info(self, buf, n):
+        buf.value = self.device[:n - 1]
+        return 0
+
+    def xk_batch_tune(self, handle, generations, chosen):
+        self.tuned.append(generations)
+        chosen._obj.value = self.best
+        return 0
+
+    def xk_batch_set_band(self, handle, rows):
+        self.set.append(rows)
+        return 0
+
+
+W = np.array([64, 128, 1024], np.int32)
+H = np.array([64, 256, 512], np.int32)
+
+
+def test_cache_path(monkeypatch, tmp_path):
+    monkeypatch.setenv("XK_TUNE_CACHE", str(tmp_path / "t.json"))
+    assert tuning.cache_path() == str(tmp_path / "t.json")
+    for off in ("off", "0", "", "none"):
+        monkeypatch.setenv("XK_TUNE_CACHE", off)
+        assert tuning.cache_path() is None
+    monkeypatch.delenv("XK_TUNE_CACHE")
+    monkeypatch.setenv("XDG_CACHE_HOME", str(tmp_path))
+    assert tuning.cache_path() == str(tmp_path / "xentica_gb300" / "tune.json")
+
+
+def test_keys_distinguish_workload_device_and_build():
+    base = tuning.ensemble_key("dev", "lib", W, H, 256)
+    assert base == tuning.ensemble_key("dev", "lib", W.copy(), H.copy(), 256)
+    others = [tuning.ensemble_key("dev2", "lib", W, H, 256),
+              tuning.ensemble_key("dev", "lib2", W, H, 256),
+              tuning.ensemble_key("dev", "lib", W, H, 128),
+              tuning.ensemble_key("dev", "lib", H, W, 256),
+              tuning.ensemble_key("dev", "lib", W[:2], H[:2], 256)]
+    assert len(set(others + [base])) == len(others) + 1
+
+
+def test_file_round_trip_and_bad_files(tmp_path):
+    path = tmp_path / "sub" / "t.json"
+    cache = tuning.TuneCache(str(path))
+    assert cache.get("a") is None                  # no file yet
+    cache.put("a", 4)
+    cache.put("b", 8)                              # merged, not overwritten
+    assert cache.get("a") == 4 and cache.get("b") == 8
+    assert json.loads(path.read_text()) == {"a": 4, "b": 8}
+    path.write_text("{not json")
+    assert cache.get("a") is None                  # a damaged file is a miss
+    cache.put("c", 2)
+    assert json.loads(path.read_text()) == {"c": 2}
+
+
+def test_miss_times_and_stores_then_hit_applies(monkeypatch, tmp_path):
+    monkeypatch.setenv("XK_TUNE_CACHE", str(tmp_path / "t.json"))
+    lib = FakeLib(best=16)
+    assert tuning.tuned_band(lib, None, W, H, 256, library="L1") == 16
+    assert lib.tuned == [256] and lib.set == []
+    lib.best = 2                                   # a new timing would now disagree
+    assert tuning.tuned_band(lib, None, W, H, 256, library="L1") == 16
+    assert lib.tuned == [256] and lib.set == [16]  # applied, not timed
+    # another generation count, library build or device: timed again
+    assert tuning.tuned_band(lib, None, W, H, 64, library="L1") == 2
+    assert tuning.tuned_band(lib, None, W, H, 256, library="L2") == 2
+    other = FakeLib(device=b"another device", best=32)
+    assert tuning.tuned_band(other, None, W, H, 256, library="L1") == 32
+    assert lib.tuned == [256, 64, 256] and other.tuned == [256]
+
+
+def test_cache_off(monkeypatch, tmp_path):
+    monkeypatch.setenv("XK_TUNE_CACHE", str(tmp_path / "t.json"))
+    lib = FakeLib(best=8)
+    assert tuning.tuned_band(lib, None, W, H, 256, cache=False, library="L") == 8
+    assert tuning.tuned_band(lib, None, W, H, 256, cache=False, library="L") == 8
+    assert lib.tuned == [256, 256] and not (tmp_path / "t.json").exists()
+    monkeypatch.setenv("XK_TUNE_CACHE", "off")
+    assert tuning.tuned_band(lib, None, W, H, 256, library="L") == 8
+    assert lib.tuned == [256, 256, 256]
+
+
+@pytest.mark.parametrize("bad", [0, 5000, "8", None, 2.5])
+def test_invalid_entries_are_ignored(monkeypatch, tmp_path, bad):
+    path = tmp_path / "t.json"
+    monkeypatch.setenv("XK_TUNE_CACHE", str(path))
+    key = tuning.ensemble_key(FakeLib().device.decode(), "L", W, H, 256)
+    path.write_text(json.dumps({key: bad}))
+    lib = FakeLib(best=4)
+    assert tuning.tuned_band(lib, None, W, H, 256, library="L") == 4
+    assert lib.tuned == [256] and lib.set == []
+    assert json.loads(path.read_text())[key] == 4
+
+
+def test_library_id_tracks_the_file(tmp_path):
+    f = tmp_path / "libxk.so"
+    f.write_bytes(b"one")
+    a = tuning.library_id(str(f))
+    assert a == tuning.library_id(str(f))
+    f.write_bytes(b"two!")
+    assert tuning.library_id(str(f)) != a

@@ -15,6 +15,7 @@ import ctypes
 import numpy as np
 
 from xentica_gb300 import _native as nat
+from xentica_gb300 import tuning
 from xentica_gb300.core.exceptions import XenticaException
 from xentica_gb300.tools.rules import LifeLike
 
@@ -161,9 +162,16 @@ class Ensemble:
                   "xk_batch_seed_bernoulli")
         return self._lib.xk_last_step_ms()
 
-    def tune(self, generations):
-        """Pick the resident kernel's band length by timing; returns it."""
-        chosen = ctypes.c_int32()
-        nat.check(self._lib.xk_batch_tune(self._handle, int(generations), ctypes.byref(chosen)),
-                  "xk_batch_tune")
-        return chosen.value
+    def tune(self, generations, cache=True):
+        """Pick the resident kernel's band length by timing; returns it.  With
+        ``cache`` the choice is kept in the tuning cache
+        (:mod:`xentica_gb300.tuning`, keyed by device, library build, lattice
+        sizes and ``generations``) and a later tune of the same workload
+        applies it without timing."""
+        return tuning.tuned_band(self._lib, self._handle, self.widths, self.heights,
+                                 int(generations), cache=cache)
+
+    @property
+    def band(self):
+        """Rows per lane group of the resident kernel's bands (the tuned choice)."""
+        return int(self._lib.xk_batch_band(self._handle))

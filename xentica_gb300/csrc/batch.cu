@@ -731,6 +731,27 @@ extern "C" int xk_batch_run(xk_batch *b, const uint8_t *host_in, uint8_t *host_o
     return check_bad(b);
 }
 
+extern "C" int xk_batch_set_band(xk_batch *b, int32_t rows_per_band)
+{
+    XK_REQUIRE(b, XK_ERR_ARG, "xk_batch_set_band: null batch");
+    XK_REQUIRE(rows_per_band >= 1 && rows_per_band <= 1024, XK_ERR_ARG,
+               "xk_batch_set_band: rows per band must be 1..1024, got %d", (int)rows_per_band);
+    if (rows_per_band == b->rows_per_band) return XK_OK;
+    const int old = b->rows_per_band;
+    b->rows_per_band = rows_per_band;
+    const int rc = plan_classes(b);
+    if (rc != XK_OK) {
+        b->rows_per_band = old;
+        plan_classes(b);
+    }
+    return rc;
+}
+
+extern "C" int32_t xk_batch_band(const xk_batch *b)
+{
+    return b ? b->rows_per_band : 0;
+}
+
 extern "C" int xk_batch_tune(xk_batch *b, int32_t generations, int32_t *chosen)
 {
     XK_REQUIRE(b && chosen, XK_ERR_ARG, "xk_batch_tune: null argument");
