@@ -117,3 +117,11 @@ def test_library_id_tracks_the_file(tmp_path):
     assert a == tuning.library_id(str(f))
     f.write_bytes(b"two!")
     assert tuning.library_id(str(f)) != a
+
+
+def test_unidentifiable_library_tunes_without_cache(monkeypatch, tmp_path):
+    monkeypatch.setenv("XK_TUNE_CACHE", str(tmp_path / "t.json"))
+    monkeypatch.setattr(tuning, "library_id", lambda: (_ for _ in ()).throw(OSError("gone")))
+    lib = FakeLib(best=8)
+    assert tuning.tuned_band(lib, None, W, H, 256) == 8
+    assert lib.tuned == [256] and not (tmp_path / "t.json").exists()

@@ -107,7 +107,11 @@ def tuned_band(lib, handle, widths, heights, generations, cache=True, library=No
     path = cache_path() if cache else None
     store = key = None
     if path is not None:
-        lib_id = library if library is not None else library_id()
+        try:
+            lib_id = library if library is not None else library_id()
+        except OSError:
+            path = None   # no library file to identify: tune without the cache
+    if path is not None:
         key = ensemble_key(device_id(lib), lib_id, widths, heights, generations)
         store = TuneCache(path)
         hit = store.get(key)
