@@ -98,7 +98,7 @@ def test_cache_off(monkeypatch, tmp_path):
     assert lib.tuned == [256, 256, 256]
 
 
-@pytest.mark.parametrize("bad", [0, 5000, "8", None, 2.5])
+@pytest.mark.parametrize("bad", [0, 5000, "8", None, 2.5, True])
 def test_invalid_entries_are_ignored(monkeypatch, tmp_path, bad):
     path = tmp_path / "t.json"
     monkeypatch.setenv("XK_TUNE_CACHE", str(path))

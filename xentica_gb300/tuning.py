@@ -115,7 +115,7 @@ def tuned_band(lib, handle, widths, heights, generations, cache=True, library=No
         key = ensemble_key(device_id(lib), lib_id, widths, heights, generations)
         store = TuneCache(path)
         hit = store.get(key)
-        if isinstance(hit, int) and 1 <= hit <= 1024:
+        if isinstance(hit, int) and not isinstance(hit, bool) and 1 <= hit <= 1024:
             nat.check(lib.xk_batch_set_band(handle, hit), "xk_batch_set_band")
             return hit
     chosen = ctypes.c_int32()
