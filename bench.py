@@ -18,9 +18,20 @@ Reported (one JSON line on rank 0):
   plain   the same lattices with one launch per lattice per generation;
   roofline, cpu_baseline, clocks, gpu_launches as the benchmark contract asks.
 
-``--impl reference`` times the reference's own kernels (its translator's
-LifelikeCA source compiled for the CPU, ``oracle/_ref``) on the host cores
-instead, with the same metric.
+  parity  one lattice of each of the 25 size classes, snapshotted before one
+          more timed-configuration step (the tuned band, the captured graph)
+          and compared with the oracle after it, outside the timed region;
+  extras  the other configurations, each with its own value, e2e, roofline,
+          cpu_baseline, clocks and parity: Life 512^2 (1000 generations per
+          launch), EvoLife 1920x1080 with a rendered frame every generation,
+          mass transfer 256^3 with a projection frame and the total checked
+          every generation, and the serving loop (Poisson arrivals, p50/p99
+          latency, a sweep of offered loads).  ``--extras none`` leaves them out.
+
+``--workload life512 | evolife | mass | serve`` prints one of the extras as
+its own line (with the given ``--steps``/``--warmup``).  ``--impl reference``
+times the reference's own kernels (its translator's LifelikeCA source compiled
+for the CPU, ``oracle/_ref``) on the host cores instead, with the same metric.
 """
 import argparse
 import json
@@ -59,6 +70,9 @@ def parse():
     ap.add_argument("--quantum", type=int, default=128, help="serve: generations per round")
     ap.add_argument("--sweep", default="", help="serve: extra offered loads after the main run, "
                                                 "comma-separated (e.g. 0.3,0.5,0.9)")
+    ap.add_argument("--extras", default="life512,evolife,mass,serve",
+                    help="default run: the other configurations measured after the ensemble "
+                         "(comma-separated, or 'none')")
     ap.add_argument("--serve-budget-gb", type=int, default=16, help="serve: HBM budget (GiB)")
     ap.add_argument("--workload", choices=("ensemble", "life512", "evolife", "mass", "serve"),
                     default="ensemble",
@@ -284,6 +298,35 @@ def run_reference_arm(args, dist):
     print(json.dumps(line), flush=True)
 
 
+def ensemble_parity(ens, widths, heights, G):
+    """One lattice of each size class: snapshot, one more step of G
+    generations in the timed configuration, the oracle from the snapshot."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    picks, seen = [], set()
+    for i in range(ens.count):
+        key = (int(widths[i]), int(heights[i]))
+        if key not in seen:
+            seen.add(key)
+            picks.append(i)
+    before = ens.download()
+    ens.step(G)
+    after = ens.download()
+    exact = True
+    for i in picks:
+        w, h, rule = int(ens.widths[i]), int(ens.heights[i]), int(ens.rules[i])
+        topo = O.Topology((w, h))
+        fld = topo.field(ens.lattice(before, i).ravel(), np.uint8)
+        O.life_run(topo, fld, np.zeros(topo.cells * 3, np.int32), G, born=rule & 511,
+                   sustain=rule >> 9)
+        exact &= bool(np.array_equal(fld[:topo.cells], ens.lattice(after, i).ravel()))
+    return {"lattices": len(picks), "size_classes": len(seen), "generations": G,
+            "band": ens.band, "bit_exact": exact,
+            "note": "one lattice of every size class, from the state after the timed steps, "
+                    "one more %d-generation step of the timed configuration against the "
+                    "oracle" % G}
+
+
 def run_ours(args, dist):
     from xentica_gb300 import build as xk_build
     from xentica_gb300 import _native as nat
@@ -306,7 +349,7 @@ def run_ours(args, dist):
     ens.upload(cells)
     rows_per_band = ens.tune(G)
     ens.upload(cells)
-    # self-check of the timed paths on this workload: batched == e2e == plain
+    # self-check of the timed paths on this workload: batched == e2e
     ens.step(G)
     after = ens.download()
     pin_in, pin_out = nat.PinnedBuffer(total), nat.PinnedBuffer(total)
@@ -330,6 +373,7 @@ def run_ours(args, dist):
     dev_s = dist.max(sum(step_ms) / 1000.0)
     updates = float(total) * G * args.steps
     value = updates * dist.world / dev_s
+    parity = ensemble_parity(ens, widths, heights, G)
     # end to end: pinned host in -> device -> 256 generations -> pinned host out
     ens.run(pin_in.array, pin_out.array, G)
     dist.barrier()
@@ -380,117 +424,197 @@ def run_ours(args, dist):
                                 "MT19937 stream per lattice, NumPy's random_sample) against "
                                 "the host draw (RandomState per lattice, %d processes)"
                                 % (args.instances, min(32, os.cpu_count() or 1))},
+            "parity": parity,
             "gpu_launches": launches, "wall_s": wall, "roofline": roofline, "clocks": clk}
     if dist.rank == 0:
         line["cpu_baseline"] = cpu_sample(widths, heights, rules, cells, ens.offsets,
                                           args.cpu_seconds, os.cpu_count())
         line["cpu_baseline"].pop("seconds")
+    pin_in.release()
+    pin_out.release()
+    del ens
+    extras = [e.strip() for e in args.extras.split(",") if e.strip() and e.strip() != "none"]
+    if extras:
+        line["extras"] = {}
+        small = argparse.Namespace(**vars(args))
+        small.cpu_seconds = 4.0
+        for name in extras:
+            fn = {"life512": life512_line, "evolife": evolife_line, "mass": mass_line,
+                  "serve": serve_line}[name]
+            steps, warmup = {"life512": (10, 3), "evolife": (5, 3), "mass": (5, 3),
+                             "serve": (None, 3)}[name]
+            small.steps, small.warmup = steps, warmup
+            if name == "serve" and not small.sweep:
+                small.sweep = "0.3,0.5,0.9"
+            sub = fn(small, dist)
+            if sub is not None:
+                line["extras"][name] = sub
+    if dist.rank == 0:
         print(json.dumps(line), flush=True)
 
 
-def evolife_experiment():
-    """CrossbreedingExperiment2 of the reference (examples/evolife.py:447-488)."""
+def c2_experiment():
+    """The EvoLife configuration: 1920x1080 torus, every cell seeded with a
+    uniform random energy (0..255), genome (0..2^18-1) and random state
+    (0..2^16-1) -- PrimordialSoup over the reference's EvoLife
+    (examples/evolife.py:20-128) with its default death_speed 15, max_genes 9
+    and mutation_prob 0, and CrossbreedingExperiment's MovingAverage fades
+    18/3 (examples/evolife.py:137-144)."""
     from xentica_gb300 import core, seeds
     from xentica_gb300.seeds.random import RandInt
-    from xentica_gb300.tools.rules import LifeLike
 
-    class Crossbreeding(core.Experiment):
-        word = "FUTURE BREEDING MACHINE 2041"
+    class PrimordialEvoLife(core.Experiment):
+        word = "EVOLIFE PRIMORDIAL SOUP 1920X1080"
         size = (1920, 1080)
         zoom = 1
         pos = [0, 0]
         fade_in = 18
         fade_out = 3
-        death_speed = 25
+        death_speed = 15
         max_genes = 9
-        mutation_prob = 0.0001
-        seed = (seeds.patterns.PrimordialSoup(vals={"rng": RandInt(0, 2 ** 16 - 1)})
-                + seeds.patterns.BigBang(pos=(0, 0), size=(1280, 720), vals={
-                    "energy": 0, "rule": +RandInt(0, 1) * LifeLike.golly2int("B3/S23"),
-                    "rng": 0 + RandInt(0, 2 ** 16 - 1)})
-                + seeds.patterns.BigBang(pos=(380, 280), size=(440, 340), vals={
-                    "energy": 0, "rule": LifeLike.golly2int("B35678/S5678") * RandInt(0, 1),
-                    "rng": RandInt(0, 2 ** 16 - 1)}))
-    return Crossbreeding
+        mutation_prob = 0.0
+        seed = seeds.patterns.PrimordialSoup(vals={
+            "energy": RandInt(0, 255), "rule": RandInt(0, 2 ** 18 - 1),
+            "rng": RandInt(0, 2 ** 16 - 1)})
+    return PrimordialEvoLife
 
 
-def run_evolife(args, dist):
-    """EvoLife 1920x1080: K steps of 100 generations, each generation
-    followed by a full-frame render (image copied to the host)."""
+def evolife_line(args, dist):
+    """EvoLife 1920x1080 (c2_experiment): K steps of 100 generations, each
+    generation followed by a full-frame render (RendererPlain, zoom 1) into a
+    device frame buffer -- the reference's step() + render() pair per frame.
+    e2e: the state and colours loaded from the host, then 100 generations
+    with every frame copied to page-locked host memory.  Parity: the oracle
+    started from the GPU state after the timed steps, two more generations
+    (state, colours and both frames compared)."""
     from xentica_gb300 import build as xk_build
     from xentica_gb300 import _native as nat
     from xentica_gb300.core.canonical import EvoLifeProgram
+    import torch
     xk_build.build()
     nat.set_device(dist.local)
     lib = nat.load()
-    model = EvoLifeProgram(evolife_experiment())
-    model.set_viewport(model.size)
+    model = EvoLifeProgram(c2_experiment())
+    W, H = model.size
+    model.set_viewport((W, H))
     n = model.cells_num
     gens = 100
-    model.gpu.step(1)
+    fb = W * H * 3
+    dev_frames = torch.empty(gens * fb, dtype=torch.uint8, device="cuda:%d" % dist.local)
+
+    def step_device():
+        return model.gpu.step_frames(gens, W, H, 1, 0, 0, dev_frames.data_ptr(), on_device=True)
+
+    step_device()
     for _ in range(args.warmup):
-        model.gpu.step(gens)
+        step_device()
     clocks = Clocks(dist.local)
     time.sleep(0.6)
     dist.barrier()
-    step_ms = []
     lib.xk_range_push(b"timed")
-    for _ in range(args.steps):
-        model.gpu.step(gens)
-        step_ms.append(lib.xk_last_step_ms())
+    step_ms = [step_device() for _ in range(args.steps)]
     lib.xk_range_pop()
     dist.barrier()
     clk = clocks.stop()
-    t0 = time.perf_counter()
-    for _ in range(5):
-        model.render()
-    render_ms = (time.perf_counter() - t0) / 5 * 1000
     dev_s = dist.max(sum(step_ms) / 1000.0)
     value = float(n) * gens * args.steps * dist.world / dev_s
-    bytes_per_update = 8 * 2 + 12 * 2      # uint64 state read+write, int3 colour read+write
+    # e2e: host state in, 100 generations, every frame to pinned host memory
+    cells = model.gpu.arrays.cells.get()[:n].copy()
+    colors = model.gpu.arrays.colors.get()
+    host = nat.PinnedBuffer(gens * fb)
+    frames = host.array.reshape(gens, fb)
+    e2e = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        model.gpu.load(cells, colors)
+        model.gpu.step_frames(gens, W, H, 1, 0, 0, frames.reshape(-1))
+        e2e.append(time.perf_counter() - t0)
+    e2e_s = dist.max(sum(e2e))
+    host.release()
+    generations_done = gens * (1 + args.warmup + args.steps)
     peak, peak_kind = measured_peak()
-    achieved = bytes_per_update * n * gens / (statistics.mean(step_ms) / 1000.0) / 1e9
-    line = {"metric": "cell-updates/s (EvoLife)", "value": value, "unit": "cell-updates/s",
-            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": dev_s * 1000 / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-            "data": "synthetic (seeded CrossbreedingExperiment2 layout)",
-            "config": {"workload": "EvoLife 1920x1080 torus, 100 generations per step, "
-                                   "modular colour, MovingAverage(18, 3)",
-                       "l2": "state + colours (41 MB) fit in L2"},
-            "render_ms_per_frame": render_ms,
+    mean_ms = statistics.mean(step_ms)
+    bytes_per_update = 8 * 2 + 12 * 2 + 12   # uint64 state r+w, int3 colour r+w, int3 pixel
+    achieved = bytes_per_update * n * gens / (mean_ms / 1000.0) / 1e9
+    line = {"metric": "cell-updates/s (EvoLife, frame every generation)", "value": value,
+            "unit": "cell-updates/s", "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_s * 1000 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (seeded PrimordialSoup: uniform random energy, genome, RNG state)",
+            "config": {"workload": "EvoLife 1920x1080 torus, uniform random genomes, "
+                                   "death_speed 15, max_genes 9, MovingAverage(18, 3), "
+                                   "100 generations per step, each followed by a 1920x1080 "
+                                   "RendererPlain frame (uint8 RGB)",
+                       "generations_at_end": generations_done,
+                       "l2": "state + colours (41 MB) fit in L2; frames (622 MB per step) "
+                             "stream to HBM"},
+            "e2e": {"value": float(n) * gens * args.steps * dist.world / e2e_s,
+                    "unit": "cell-updates/s", "h2d_bytes_per_step": n * 8 + n * 12,
+                    "d2h_bytes_per_step": gens * fb,
+                    "note": "state and colours loaded from the host, every frame copied to "
+                            "page-locked host memory"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": committed_traffic("evolife"),
-                         "note": "40 B per cell-update of state and colour traffic; the "
-                                 "kernel itself is bound by integer instruction issue "
-                                 "(genome crossover), not by HBM"},
-            "clocks": clk}
+                         "kernel": "xk_k_evolife + xk_k_render<uint8> per generation",
+                         "algorithmic_bytes_per_generation": bytes_per_update * n,
+                         "note": "B_alg = 52 B per cell-update (8 B state and 12 B colour read "
+                                 "and written, 12 B int3 pixel written); the kernel is bound by "
+                                 "integer instruction issue (genome crossover), not by HBM"},
+            "gpu_launches": 2 * gens * args.steps, "clocks": clk}
     if dist.rank == 0:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O
+        tpl = model.gpu.template
+        info = tpl.color.extra
         topo = O.Topology(model.size)
         fld = topo.field(model.gpu.arrays.cells.get()[:n], np.uint64)
         col = model.gpu.arrays.colors.get()
-        t0 = time.perf_counter()
-        O.evolife_run(topo, fld, col, 2, death_speed=25, max_genes=9, mutation_prob=0.0001,
-                      fade_in=18, fade_out=3)
-        el = time.perf_counter() - t0
+        smooth = model.constants["SMOOTH_FACTOR"].value \
+            if model.is_constant("SMOOTH_FACTOR") else 0
+        got = model.step_frames(2)
+        gpu_cells = model.gpu.arrays.cells.get()[:n]
+        gpu_col = model.gpu.arrays.colors.get()
+        exact, el = True, 0.0
+        for g in range(2):
+            t0 = time.perf_counter()
+            O.evolife_run(topo, fld, col, 1, death_speed=15, max_genes=9, mutation_prob=0.0,
+                          fade_in=info["fade_in"], fade_out=info["fade_out"],
+                          smooth=info["smooth"])
+            img = O.render(topo, col, W, H, smooth=smooth).astype(np.uint8)
+            el += time.perf_counter() - t0
+            exact &= bool(np.array_equal(got[g], img))
+        exact &= bool(np.array_equal(gpu_cells, fld[:n])) and bool(np.array_equal(gpu_col, col))
+        line["parity"] = {"generations_before": generations_done + gens,
+                          "checked_generations": 2, "bit_exact": exact,
+                          "note": "oracle started from the GPU state after the timed steps: "
+                                  "cells, colours and both frames"}
         line["cpu_baseline"] = {"value": n * 2 / el, "unit": "cell-updates/s",
                                 "cores": os.cpu_count(), "kind": "port",
-                                "sample": "2 generations of the full lattice, oracle (OpenMP)"}
+                                "sample": "2 generations of the full lattice, each with its "
+                                          "render, oracle (OpenMP)"}
+        return line
+    return None
+
+
+def run_evolife(args, dist):
+    line = evolife_line(args, dist)
+    if line is not None:
         print(json.dumps(line), flush=True)
 
 
-def run_mass(args, dist):
-    """Mass transfer 256^3 (``--mass-side``), Poisson(4) masses: K steps of 100
-    generations; the total mass of every generation (reduced inside the
-    kernel) is checked against the initial total after each step;
-    z-projection render timed."""
+def mass_line(args, dist):
+    """Mass transfer ``--mass-side``^3 (256), Poisson(4) masses: K steps of 100
+    generations, each generation followed by the z-projection frame
+    (RendererPlain over axes 0, 1) into a device frame buffer; the total
+    mass of every generation (reduced inside the kernel) checked against the
+    initial total after each step.  Parity: the oracle from the GPU state
+    after the timed steps, two more generations."""
     from xentica_gb300 import build as xk_build
     from xentica_gb300 import _native as nat
     from xentica_gb300 import core, seeds
     from xentica_gb300.core.canonical import MassTransferProgram
+    import torch
     xk_build.build()
     nat.set_device(dist.local)
     lib = nat.load()
@@ -507,10 +631,18 @@ def run_mass(args, dist):
     model = MassTransferProgram(SandPiles)
     model.set_viewport((side, side))
     n = model.cells_num
-    total0 = int(model.gpu.arrays.cells.get()[:n].astype(np.uint64).sum())
+    init = model.gpu.arrays.cells.get()[:n].copy()
+    total0 = int(init.astype(np.uint64).sum())
     gens = 100
+    fb = side * side * 3
+    dev_frames = torch.empty(gens * fb, dtype=torch.uint8, device="cuda:%d" % dist.local)
+
+    def step_device():
+        return model.gpu.step_frames(gens, side, side, 1, 0, 0, dev_frames.data_ptr(),
+                                     on_device=True)
+
     for _ in range(args.warmup):
-        model.gpu.step(gens)
+        step_device()
     clocks = Clocks(dist.local)
     time.sleep(0.6)
     dist.barrier()
@@ -518,50 +650,80 @@ def run_mass(args, dist):
     conserved = True
     lib.xk_range_push(b"timed")
     for _ in range(args.steps):
-        model.gpu.step(gens)
-        step_ms.append(lib.xk_last_step_ms())
+        step_ms.append(step_device())
         totals = model.gpu.mass_totals(gens)
         conserved &= bool((totals == total0).all())
     lib.xk_range_pop()
     dist.barrier()
     clk = clocks.stop()
-    t0 = time.perf_counter()
-    for _ in range(5):
-        model.render()
-    render_ms = (time.perf_counter() - t0) / 5 * 1000
     dev_s = dist.max(sum(step_ms) / 1000.0)
     value = float(n) * gens * args.steps * dist.world / dev_s
-    bytes_per_update = 4 * 2           # uint32 mass read + write
+    # e2e: host masses in, 100 generations, every frame to pinned host memory
+    host = nat.PinnedBuffer(gens * fb)
+    colors0 = model.gpu.arrays.colors.get()
+    e2e = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        model.gpu.load(init, colors0)
+        model.gpu.step_frames(gens, side, side, 1, 0, 0, host.array)
+        e2e.append(time.perf_counter() - t0)
+    e2e_s = dist.max(sum(e2e))
+    host.release()
+    bytes_per_update = 4 * 2 + 4           # uint32 mass read + write, projection re-read
     peak, peak_kind = measured_peak()
     achieved = bytes_per_update * n * gens / (statistics.mean(step_ms) / 1000.0) / 1e9
-    line = {"metric": "cell-updates/s (mass transfer 3-D)", "value": value,
-            "unit": "cell-updates/s", "n_gpus": dist.world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": dev_s * 1000 / args.steps,
+    line = {"metric": "cell-updates/s (mass transfer 3-D, frame every generation)",
+            "value": value, "unit": "cell-updates/s", "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1000 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
             "data": "synthetic (seeded Poisson(4) masses)",
             "config": {"workload": "mass transfer %d^3 von Neumann, StaticBorder wall, "
-                                   "100 generations per step, total checked every generation" % side,
+                                   "100 generations per step, each followed by the %dx%d "
+                                   "z-projection frame; total checked every generation"
+                                   % (side, side, side),
                        "l2": "state (2 x %.0f MB)%s; no flush" % (
                            4 * n / 2 ** 20, " close to L2 size" if side == 256 else "")},
-            "mass_conserved": conserved, "render_ms_per_frame": render_ms,
+            "mass_conserved": conserved,
+            "e2e": {"value": float(n) * gens * args.steps * dist.world / e2e_s,
+                    "unit": "cell-updates/s", "h2d_bytes_per_step": 4 * n,
+                    "d2h_bytes_per_step": gens * fb,
+                    "note": "masses loaded from the host, every frame copied to page-locked "
+                            "host memory"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": committed_traffic("mass_tma") if side == 256 else None,
-                         "note": "8 B per cell-update (uint32 read + write); traffic: "
-                                 "DRAM bytes of one launch (one generation)"},
-            "clocks": clk}
+                         "kernel": "xk_k_mass_tma + projection + frame per generation",
+                         "algorithmic_bytes_per_generation": bytes_per_update * n,
+                         "note": "B_alg = 12 B per cell-update (uint32 read + write, the "
+                                 "projection's re-read of the state); traffic: DRAM bytes of "
+                                 "one mass-transfer launch (one generation)"},
+            "gpu_launches": 3 * gens * args.steps, "clocks": clk}
     if dist.rank == 0:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O
         topo = O.Topology(model.size, "von_neumann", border=2 ** 32 - 1)
         fld = topo.field(model.gpu.arrays.cells.get()[:n], np.uint32)
         col = model.gpu.arrays.colors.get()
+        model.gpu.step(2)
         t0 = time.perf_counter()
-        O.mass_run(topo, fld, col, 3)
+        totals = []
+        O.mass_run(topo, fld, col, 2, totals=totals)
         el = time.perf_counter() - t0
-        line["cpu_baseline"] = {"value": n * 3 / el, "unit": "cell-updates/s",
+        exact = bool(np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n]))
+        exact &= model.gpu.mass_totals(2).tolist() == totals
+        line["parity"] = {"checked_generations": 2, "bit_exact": exact,
+                          "note": "oracle started from the GPU state after the timed steps "
+                                  "(cells and per-generation totals)"}
+        line["cpu_baseline"] = {"value": n * 2 / el, "unit": "cell-updates/s",
                                 "cores": os.cpu_count(), "kind": "port",
-                                "sample": "3 generations of the full lattice, oracle (OpenMP)"}
+                                "sample": "2 generations of the full lattice, oracle (OpenMP)"}
+        return line
+    return None
+
+
+def run_mass(args, dist):
+    line = mass_line(args, dist)
+    if line is not None:
         print(json.dumps(line), flush=True)
 
 
@@ -609,7 +771,7 @@ def life512_model():
     return GameOfLife(Life512)
 
 
-def run_life512(args, dist):
+def life512_line(args, dist):
     """Life 512x512: K steps of 1000 generations (one launch each);
     e2e through the public API (load the cells from the host, step 1000,
     read the cells back); also the reference's calling pattern, 1000 calls of
@@ -647,7 +809,7 @@ def run_life512(args, dist):
         t0 = time.perf_counter()
         model.gpu.load(init, colors0)
         model.gpu.step(gens)
-        out = model.gpu.arrays.cells.get()
+        model.gpu.arrays.cells.get()
         e2e.append(time.perf_counter() - t0)
     e2e_s = dist.max(sum(e2e))
     # the reference's calling pattern: one step() per generation
@@ -674,6 +836,7 @@ def run_life512(args, dist):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": committed_traffic("life_cluster"),
+                         "kernel": "xk_k_life_cluster (or the resident kernel, as tuned)",
                          "note": "B_alg = 2 B per cell-update; the lattice stays in the "
                                  "shared memory of one CTA or of a thread-block cluster "
                                  "(whichever the first step's tuning found faster) for all "
@@ -688,14 +851,23 @@ def run_life512(args, dist):
         t0 = time.perf_counter()
         O.life_run(topo, fld, col, total_gens)
         el = time.perf_counter() - t0
-        line["parity"] = {"generations": total_gens, "bit_exact": bool(np.array_equal(fld[:n], final))}
+        line["parity"] = {"generations": total_gens,
+                          "bit_exact": bool(np.array_equal(fld[:n], final))}
         line["cpu_baseline"] = {"value": n * total_gens / el, "unit": "cell-updates/s",
                                 "cores": os.cpu_count(), "kind": "port",
-                                "sample": "%d generations of the lattice, oracle (OpenMP)" % total_gens}
+                                "sample": "%d generations of the lattice, oracle (OpenMP)"
+                                          % total_gens}
+        return line
+    return None
+
+
+def run_life512(args, dist):
+    line = life512_line(args, dist)
+    if line is not None:
         print(json.dumps(line), flush=True)
 
 
-def run_serve(args, dist):
+def serve_line(args, dist):
     """Serving: ``--requests`` seeded requests (half 2-D Life-like, a quarter
     3-D von Neumann Life-like, a quarter mass transfer) arrive as a Poisson
     process whose rate offers ``--load`` of the capacity measured first with a
@@ -752,7 +924,9 @@ def run_serve(args, dist):
         for i in range(len(specs)):
             while handles[i] is None:
                 time.sleep(0.0005)
-            handles[i].result(timeout=1800)
+            res = handles[i].result(timeout=1800)
+            if i in keep:
+                keep[i] = res
             infos.append(handles[i].info())
         th.join()
         dist.barrier()
@@ -770,10 +944,19 @@ def run_serve(args, dist):
                     [l * capacity / w for l, w in zip(lat, work)]),
                 "launches": srv.stats()["launches"] - launches0}
 
+    # parity sample: the two requests of each kind with the least work, their
+    # results from the main run compared with the oracle afterwards
+    keep = {}
+    for kind in ("life2d", "life3d", "mass"):
+        idx = sorted((i for i in range(len(specs)) if specs[i]["kind"] == kind),
+                     key=lambda i: work[i])[:2]
+        keep.update({i: None for i in idx})
     clocks = Clocks(dist.local)
     time.sleep(0.6)
     main_run = open_loop(args.load, args.seed + 17)
     clk = clocks.stop()
+    sample = dict(keep)
+    keep = {}
     sweep = [open_loop(float(v), args.seed + 17 + k)
              for k, v in enumerate(args.sweep.split(",")) if v.strip()] if args.sweep else []
     st = srv.stats()
@@ -813,6 +996,41 @@ def run_serve(args, dist):
                     "note": "requests enter and leave through host memory"},
             "gpu_launches": main_run["launches"], "roofline": roofline, "clocks": clk}
     if dist.rank == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        exact, el, updates = True, 0.0, 0
+        for i, got in sample.items():
+            sp = specs[i]
+            shape = tuple(reversed(sp["shape"]))          # (w, h[, d])
+            t0 = time.perf_counter()
+            if sp["kind"] == "mass":
+                topo = O.Topology(shape, "von_neumann", border=2 ** 32 - 1)
+                fld = topo.field(cells[i].ravel(), np.uint32)
+                O.mass_run(topo, fld, np.zeros(topo.cells * 3, np.int32), sp["generations"])
+            else:
+                nbr = 8 if sp["kind"] == "life2d" else 6
+                topo = O.Topology(shape) if sp["kind"] == "life2d" else \
+                    O.Topology(shape, "von_neumann")
+                fld = topo.field(cells[i].ravel(), np.uint8)
+                O.life_run(topo, fld, np.zeros(topo.cells * 3, np.int32), sp["generations"],
+                           born=sp["rule"] & ((1 << (nbr + 1)) - 1), sustain=sp["rule"] >> (nbr + 1))
+            el += time.perf_counter() - t0
+            updates += work[i]
+            exact &= bool(np.array_equal(np.asarray(got).ravel(), fld[:topo.cells]))
+        line["parity"] = {"requests": len(sample), "bit_exact": exact,
+                          "note": "the two requests of each kind with the least work, results "
+                                  "of the main run against the oracle"}
+        line["cpu_baseline"] = {"value": updates / el, "unit": "cell-updates/s",
+                                "cores": os.cpu_count(), "kind": "port",
+                                "sample": "the %d parity requests (%.2g cell-updates), oracle "
+                                          "(OpenMP)" % (len(sample), updates)}
+        return line
+    return None
+
+
+def run_serve(args, dist):
+    line = serve_line(args, dist)
+    if line is not None:
         print(json.dumps(line), flush=True)
 
 

@@ -112,6 +112,18 @@ int xk_step(xk_model *m, int64_t nsteps);
 int xk_render(xk_model *m, int32_t *host_img, int32_t width, int32_t height,
               int32_t zoom, int32_t dx, int32_t dy);
 
+/* Replaces the viewer loop's step() + render() pair (base.py:703-753, called
+ * once per frame by the Moire bridge): nsteps generations, each followed by a
+ * RendererPlain frame of the viewport as uint8 RGB -- what render() returns,
+ * img.get().astype(np.uint8) -- written to frames + g * width * height * 3
+ * for generation g.  frames_on_device = 0: `frames` is host memory (frames
+ * pass through a ring of 4 device frames and are copied on a second stream
+ * while the next generations run; page-locked memory makes the copies
+ * asynchronous); 1: `frames` is a device buffer of nsteps frames.
+ * last_step_ms covers every generation, render and copy. */
+int xk_step_frames(xk_model *m, int64_t nsteps, int32_t width, int32_t height, int32_t zoom,
+                   int32_t dx, int32_t dy, uint8_t *frames, int32_t frames_on_device);
+
 /* Mass family: total mass after each of the last xk_step's generations
  * (count = that nsteps); the invariant the configuration checks. */
 int xk_mass_totals(xk_model *m, uint64_t *host_totals, int64_t count);
@@ -203,10 +215,12 @@ int64_t xk_batch_launches(const xk_batch *b, int32_t generations);
  * 0/1), advanced in place by `generations` on `stream` (a cudaStream_t, NULL
  * for the default stream); the call returns when the work is done.  The only
  * other device memory used is a file-scope array sized for
- * XK_NOALLOC_MAX_LATTICES lattice descriptors (~128 KB), held by every device
- * that loads the library until exit.  Every call shares it, so calls whose
- * GPU work overlaps race; the first call on a device looks the array up
- * (cudaGetSymbolAddress) and should come before any stream capture.  More
+ * XK_NOALLOC_MAX_LATTICES lattice descriptors of 40 bytes plus a 256-byte
+ * flag slot (164,096 bytes, about 160 KB), held by every device that loads
+ * the library until exit.  Every call shares it, so calls whose GPU work
+ * overlaps race; the first call on a device (and the first after its context
+ * was reset) looks the array up (cudaGetSymbolAddress) and should come
+ * before any stream capture.  More
  * lattices, or lattices wider than 1024 cells or too large for one CTA, are
  * rejected with an error. */
 #define XK_NOALLOC_MAX_LATTICES 4096

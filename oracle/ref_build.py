@@ -19,7 +19,22 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 SIDES = (64, 128, 256, 512, 1024)
-REFERENCE = os.environ.get("XK_REFERENCE_SRC", "/root/reference")
+
+
+def reference_root(required=False):
+    """The reference checkout: ``$XK_REFERENCE_SRC``, else a checkout named
+    ``reference`` beside this repository.  Returns None when neither holds
+    the ``xentica`` package, or exits with a message when ``required``."""
+    env = os.environ.get("XK_REFERENCE_SRC")
+    beside = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+    for root in ([env] if env else []) + [beside]:
+        if os.path.isdir(os.path.join(root, "xentica")):
+            return os.path.abspath(root)
+    if required:
+        raise SystemExit("reference checkout not found: set XK_REFERENCE_SRC to the directory "
+                         "holding the xentica package (tried %s)"
+                         % ", ".join(([env] if env else []) + [beside]))
+    return None
 
 
 def _generate(ref_root):
@@ -45,8 +60,9 @@ def build():
     os.makedirs(REF_DIR, exist_ok=True)
     sys.path.insert(0, HERE)
     from ref_harness import compile_cpp
-    if os.path.isdir(os.path.join(REFERENCE, "xentica")):
-        _generate(REFERENCE)
+    root = reference_root()
+    if root:
+        _generate(root)
     for cpp in sorted(glob.glob(os.path.join(REF_DIR, "ref_lifelike_*.cpp"))):
         so = cpp[:-4] + ".so"
         if not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(cpp):

@@ -140,5 +140,12 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    # usage: make_golden.py [reference checkout] [case ...]
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # usage: make_golden.py [reference checkout] [case ...]; without the
+    # argument the checkout is $XK_REFERENCE_SRC or one named "reference"
+    # beside this repository
+    if len(sys.argv) > 1:
+        main(sys.argv[1])
+    else:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import ref_build
+        main(ref_build.reference_root(required=True))

@@ -363,6 +363,24 @@ class CrossbreedingExperiment2(CrossbreedingExperiment):
     mutation_prob = 0.0001
 
 
+class PrimordialSoupExperiment(RegularExperiment):
+    """Every cell of a 1920x1080 torus seeded with a uniform random energy,
+    genome and random state; EvoLife's default meta-parameters (death_speed 15,
+    max_genes 9, no mutation) and CrossbreedingExperiment's fades 18/3."""
+    word = "EVOLIFE PRIMORDIAL SOUP 1920X1080"
+    size = (1920, 1080)
+    zoom = 1
+    pos = [0, 0]
+    fade_in = 18
+    fade_out = 3
+    death_speed = 15
+    max_genes = 9
+    mutation_prob = 0.0
+    seed = seeds.patterns.PrimordialSoup(vals={
+        "energy": RandInt(0, 255), "rule": RandInt(0, 2 ** 18 - 1),
+        "rng": RandInt(0, 2 ** 16 - 1)})
+
+
 class BigBangExperiment(RegularExperiment):
     death_speed = 0
     max_genes = 9

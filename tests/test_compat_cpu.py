@@ -39,9 +39,9 @@ def test_round_trip_and_reference_class_path(tmp_path):
 
 def _reference_root():
     import ref_build
-    root = ref_build.REFERENCE
-    if not os.path.isdir(os.path.join(root, "xentica")):
-        pytest.skip("reference source not available")
+    root = ref_build.reference_root()
+    if root is None or not os.path.isdir(os.path.join(root, "xentica")):
+        pytest.skip("reference source not available (set XK_REFERENCE_SRC)")
     return root
 
 

@@ -35,9 +35,9 @@ EXAMPLES = [  # model, experiment, overrides (smaller lattices that hold the see
 def _reference_root():
     sys.path.insert(0, os.path.join(os.path.dirname(HERE), "oracle"))
     import ref_build
-    root = ref_build.REFERENCE
-    if not os.path.isdir(os.path.join(root, "examples")):
-        pytest.skip("reference source not available")
+    root = ref_build.reference_root()
+    if root is None or not os.path.isdir(os.path.join(root, "examples")):
+        pytest.skip("reference source not available (set XK_REFERENCE_SRC)")
     return root
 
 

@@ -54,6 +54,80 @@ def test_batched_matches_oracle(generations):
         assert np.array_equal(ens.lattice(got, i), ens.lattice(want, i)), "lattice %d %s" % (i, SIZES[i])
 
 
+_ORACLE_CACHE = {}
+
+
+def _oracle_cached(ens, cells, generations, key):
+    if (key, generations) not in _ORACLE_CACHE:
+        _ORACLE_CACHE[(key, generations)] = _oracle(ens, cells, generations)
+    return _ORACLE_CACHE[(key, generations)]
+
+
+@pytest.mark.parametrize("generations", [1, 17, 256])
+@pytest.mark.parametrize("band", [2, 4, 8, 16, 32])
+def test_every_band_matches_oracle(band, generations):
+    """Every band length the tuner may choose (rows per lane group, set as
+    the tuning cache applies it) against the oracle, up to the benchmark's
+    256 generations per launch."""
+    ens, cells = _ensemble()
+    ens.band = band
+    assert ens.band == band
+    ens.upload(cells)
+    ens.step(generations)
+    got = ens.download()
+    want = _oracle_cached(ens, cells, generations, "mixed")
+    for i in range(ens.count):
+        assert np.array_equal(ens.lattice(got, i), ens.lattice(want, i)), \
+            "band %d, lattice %d %s" % (band, i, SIZES[i])
+
+
+def _size_classes(count=4096, base_seed=2041):
+    """One lattice of each of the 25 size classes of the seeded 4096-lattice
+    ensemble (its first member of that class): widths, heights, rules and
+    cells exactly as the full ensemble draws them."""
+    from xentica_gb300.batch import ensemble_seeds
+    widths, heights, rules, dens, seeds = ensemble_seeds(count, base_seed)
+    picks, seen = [], set()
+    for i in range(count):
+        key = (int(widths[i]), int(heights[i]))
+        if key not in seen:
+            seen.add(key)
+            picks.append(i)
+    assert len(picks) == 25
+    cells = np.concatenate([
+        (np.random.RandomState(int(seeds[i])).random_sample(int(widths[i]) * int(heights[i]))
+         < dens[i]).astype(np.uint8) for i in picks])
+    return widths[picks], heights[picks], rules[picks], cells
+
+
+@pytest.mark.parametrize("band", ["tuned", 16])
+def test_benchmark_size_classes_256_generations(band):
+    """The benchmarked configuration: one lattice of every size class of the
+    4096-lattice ensemble (sides 64..1024, their own random rules and
+    densities), 256 generations in one captured launch, at the band the tuner
+    picks for this workload and at 16 rows, lattice by lattice against the
+    oracle."""
+    widths, heights, rules, cells = _size_classes()
+    ens = Ensemble(widths, heights, rules)
+    ens.upload(cells)
+    if band == "tuned":
+        ens.tune(256)
+    else:
+        ens.band = band
+    ens.upload(cells)
+    ens.step(256)
+    got = ens.download()
+    want = _oracle_cached(ens, cells, 256, "classes")
+    for i in range(ens.count):
+        assert np.array_equal(ens.lattice(got, i), ens.lattice(want, i)), \
+            "band %s (%d), lattice %dx%d" % (band, ens.band, widths[i], heights[i])
+    # a second launch from the first one's result: the graph replays
+    ens.step(256)
+    again = ens.download()
+    want2 = _oracle(ens, want, 256)
+    assert np.array_equal(again, want2)
+
+
 def test_plain_run_and_tune_agree():
     ens, cells = _ensemble(3)
     ens.upload(cells)

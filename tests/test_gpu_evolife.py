@@ -8,7 +8,8 @@ import numpy as np
 import pytest
 
 import oracle as O
-from tests.models import EvoLife, BigBangExperiment, CrossbreedingExperiment2, build_from_job
+from tests.models import (EvoLife, BigBangExperiment, CrossbreedingExperiment2,
+                          PrimordialSoupExperiment, build_from_job)
 from tests.test_oracle import crc
 
 pytestmark = pytest.mark.gpu
@@ -77,3 +78,30 @@ def test_long_run_step_transitions():
     _oracle_step(model, fld, col, 2)
     assert np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n])
     assert np.array_equal(model.gpu.arrays.colors.get(), col)
+
+
+def test_uniform_genomes_step_transitions_to_10000():
+    """The benchmarked EvoLife configuration (1920x1080, every cell a uniform
+    random genome, energy and random state): the GPU runs 10 000 generations;
+    at generations drawn from a seeded stream the oracle, started from the GPU
+    state, computes one more generation (cells with their random streams, and
+    colours), compared with the GPU's next generation."""
+    for p in EvoLife.meta.__dict__.values():
+        if hasattr(p, "default"):
+            p.__set__(None, p.default)
+    model = EvoLife(PrimordialSoupExperiment)
+    n = model.cells_num
+    topo = O.Topology(model.size)
+    draws = sorted(np.random.RandomState(2041).randint(1, 10000, 4).tolist()) + [9999]
+    done = 0
+    for g in draws:
+        if g > done:
+            model.gpu.step(g - done)
+            done = g
+        fld = topo.field(model.gpu.arrays.cells.get()[:n], np.uint64)
+        col = model.gpu.arrays.colors.get()
+        model.gpu.step(1)
+        done += 1
+        _oracle_step(model, fld, col, 1)
+        assert np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n]), "generation %d" % g
+        assert np.array_equal(model.gpu.arrays.colors.get(), col), "colours, generation %d" % g

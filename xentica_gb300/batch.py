@@ -175,3 +175,8 @@ class Ensemble:
     def band(self):
         """Rows per lane group of the resident kernel's bands (the tuned choice)."""
         return int(self._lib.xk_batch_band(self._handle))
+
+    @band.setter
+    def band(self, rows_per_band):
+        nat.check(self._lib.xk_batch_set_band(self._handle, int(rows_per_band)),
+                  "xk_batch_set_band")

@@ -375,6 +375,31 @@ class CellularAutomaton(Translator, metaclass=BSCA):
                                   int(self.pos[0]), int(self.pos[1]))
             return img.astype(np.uint8)
 
+    def step_frames(self, nsteps, out=None):
+        """Advance ``nsteps`` generations and render after each one: row ``g``
+        of the result equals what ``step()`` followed by ``render()`` returns
+        after generation ``g + 1`` -- the reference's viewer loop
+        (``base.py:703-753``) in one call, with the frames copied to the host
+        while the next generations run.  ``out`` (optional, uint8,
+        ``nsteps x width * height * 3``) receives them; page-locked memory
+        (``_native.PinnedBuffer``) makes the copies asynchronous.
+
+        :returns: the frames, ``np.uint8`` of shape ``(nsteps, width * height * 3)``.
+        """
+        if self.gpu.arrays.img is None:
+            msg = "Viewport is not set, call set_viewport() before rendering."
+            raise XenticaException(msg)
+        size = self.width * self.height * 3
+        if out is None:
+            out = np.empty((int(nsteps), size), dtype=np.uint8)
+        if self.paused or nsteps <= 0:
+            return out
+        with self._lock:
+            self.gpu.step_frames(int(nsteps), self.width, self.height, int(self.zoom),
+                                 int(self.pos[0]), int(self.pos[1]), out.reshape(-1))
+            self.timestep += int(nsteps)
+        return out.reshape(int(nsteps), size)
+
     def save(self, filename):
         """Save the state (cells, colours, RNG) to ``filename``, in the
         reference's pickle layout (the reference can load it)."""

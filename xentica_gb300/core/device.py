@@ -139,6 +139,30 @@ class GPU:
                   "xk_render")
         return img
 
+    def step_frames(self, nsteps, width, height, zoom, dx, dy, out, on_device=False):
+        """Advance ``nsteps`` generations, rendering a ``width x height``
+        RendererPlain frame (uint8 RGB) after each one into row ``g`` of
+        ``out``: a host array of ``nsteps * width * height * 3`` bytes
+        (page-locked memory lets the copies overlap the next generations), or,
+        with ``on_device``, the device address of a buffer that size."""
+        if not isinstance(self.model.renderer, __import__(
+                "xentica_gb300.core.renderers", fromlist=["RendererPlain"]).RendererPlain):
+            raise XenticaException("only RendererPlain is implemented on the GB300 path")
+        self._ensure()
+        self._bind_params()
+        if on_device:
+            addr = int(out)
+        else:
+            if out.dtype != np.uint8 or not out.flags.c_contiguous or \
+                    out.size != int(nsteps) * width * height * 3:
+                raise XenticaException("frames buffer must be contiguous uint8 of "
+                                       "nsteps * width * height * 3 values")
+            addr = out.ctypes.data
+        nat.check(self._lib.xk_step_frames(self._handle, int(nsteps), width, height, zoom, dx, dy,
+                                           nat.ctypes.c_void_p(addr), int(bool(on_device))),
+                  "xk_step_frames")
+        return self._lib.xk_last_step_ms()
+
     def mass_totals(self, count):
         """Total mass after each generation of the last ``step(count)`` (mass
         transfer models): the conserved quantity."""

@@ -63,6 +63,15 @@ int xk_max_smem_optin()
     return v;
 }
 
+cudaError_t xk_smem_attr_at_least(const void *fn, int bytes)
+{
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, fn);
+    if (e != cudaSuccess) return e;
+    if (a.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 extern "C" int xk_device_info(char *buf, int32_t len)
 {
     int dev = 0;
@@ -86,6 +95,9 @@ static float below_threshold(double p)
     if ((double)t >= p) t = nextafterf(t, -INFINITY);
     return t;
 }
+
+// frames of xk_step_frames in flight between rendering and the host copy
+constexpr int kFrameRing = 4;
 
 struct xk_model {
     xk_desc d;
@@ -124,6 +136,11 @@ struct xk_model {
     int hf = 0;                  // colour is a function of the state alone
     int derived = 0;             // colours currently implied by the state
     int uploaded = 0;
+    // xk_step_frames to host memory: device frame ring and its copy stream
+    uint8_t *ring = nullptr;
+    int64_t ring_cap = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t rendered[kFrameRing] = {}, copied[kFrameRing] = {};
 };
 
 static int64_t cells_of(const xk_desc &d)
@@ -252,6 +269,12 @@ static void free_model(xk_model *m)
     if (m->stage) cudaFree(m->stage);
     if (m->col) cudaFree(m->col);
     if (m->img) cudaFree(m->img);
+    if (m->ring) cudaFree(m->ring);
+    for (int k = 0; k < kFrameRing; ++k) {
+        if (m->rendered[k]) cudaEventDestroy(m->rendered[k]);
+        if (m->copied[k]) cudaEventDestroy(m->copied[k]);
+    }
+    if (m->copy_stream) cudaStreamDestroy(m->copy_stream);
     if (m->d_inst) cudaFree(m->d_inst);
     if (m->ev0) cudaEventDestroy(m->ev0);
     if (m->ev1) cudaEventDestroy(m->ev1);
@@ -584,25 +607,17 @@ static int life_color_step(xk_model *m)
     return XK_OK;
 }
 
-extern "C" int xk_step(xk_model *m, int64_t nsteps)
+// A call of `nsteps` generations in three parts: what must exist before the
+// timed region (totals buffer, materialised colours, the cluster plan), the
+// stream-ordered launches of generations [first, first + count) of the call,
+// and the bookkeeping after the last one.
+static bool colors_free_of(const xk_model *m)
 {
-    XK_REQUIRE(m, XK_ERR_ARG, "xk_step: null model");
-    XK_REQUIRE(nsteps >= 0, XK_ERR_ARG, "xk_step: negative step count");
-    XK_REQUIRE(m->uploaded, XK_ERR_STATE, "xk_step before xk_upload");
-    if (nsteps == 0) return XK_OK;
-    if (m->layout == LAYOUT_VM) {
-        XK_CUDA(cudaEventRecord(m->ev0, m->stream));
-        for (int64_t g = 0; g < nsteps; ++g)
-            for (int w = 0; w < 2; ++w)
-                XK_CUDA(xk_vm_run(m->vm_code[w], m->vm_ncode[w], m->vm_consts[w], m->vm_params,
-                                  m->fld, m->col, m->vg, m->stream));
-        XK_CUDA(cudaEventRecord(m->ev1, m->stream));
-        XK_CUDA(cudaEventSynchronize(m->ev1));
-        float ms = 0.f;
-        XK_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
-        xk_set_last_step_ms(ms);
-        return XK_OK;
-    }
+    return m->hf || m->d.color_kind == XK_COLOR_NONE;
+}
+
+static int step_prepare(xk_model *m, int64_t nsteps)
+{
     if (m->layout == LAYOUT_MASS) {
         if (nsteps > m->totals_cap) {
             if (m->totals) cudaFree(m->totals);
@@ -612,40 +627,10 @@ extern "C" int xk_step(xk_model *m, int64_t nsteps)
             m->totals_cap = nsteps;
         }
         XK_CUDA(cudaMemsetAsync(m->totals, 0, (size_t)nsteps * sizeof(unsigned long long), m->stream));
-        XK_CUDA(cudaEventRecord(m->ev0, m->stream));
-        for (int64_t g = 0; g < nsteps; ++g) {
-            XK_CUDA(xk_mass_step(m->cells32[m->cur], m->cells32[1 - m->cur], m->totals + g, m->d,
-                                 m->mass_small, m->stream));
-            m->cur = 1 - m->cur;
-        }
-        XK_CUDA(cudaEventRecord(m->ev1, m->stream));
-        XK_CUDA(cudaEventSynchronize(m->ev1));
-        float ms = 0.f;
-        XK_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
-        xk_set_last_step_ms(ms);
-        m->totals_count = nsteps;
-        m->proj_valid = 0;
-        if (xk_mass_take_wait_failure()) {
-            xk_set_error("mass-transfer step: a CTA gave up waiting for a tensor copy");
-            return XK_ERR_TIMEOUT;
-        }
         return XK_OK;
     }
-    if (m->layout == LAYOUT_CELLS64) {
-        XK_CUDA(cudaEventRecord(m->ev0, m->stream));
-        for (int64_t g = 0; g < nsteps; ++g) {
-            XK_CUDA(xk_evolife_step(m->cells64[m->cur], m->cells64[1 - m->cur], m->col, m->d,
-                                    m->mut_thresh, m->stream));
-            m->cur = 1 - m->cur;
-        }
-        XK_CUDA(cudaEventRecord(m->ev1, m->stream));
-        XK_CUDA(cudaEventSynchronize(m->ev1));
-        float ms = 0.f;
-        XK_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
-        xk_set_last_step_ms(ms);
-        return XK_OK;
-    }
-    const bool colors_free = m->hf || m->d.color_kind == XK_COLOR_NONE;
+    if (m->layout == LAYOUT_VM || m->layout == LAYOUT_CELLS64) return XK_OK;
+    const bool colors_free = colors_free_of(m);
     if (!colors_free) {
         int rc = materialize_colors(m);
         if (rc != XK_OK) return rc;
@@ -654,11 +639,39 @@ extern "C" int xk_step(xk_model *m, int64_t nsteps)
         int rc = tune_cluster(m);
         if (rc != XK_OK) return rc;
     }
-    XK_CUDA(cudaEventRecord(m->ev0, m->stream));
+    return XK_OK;
+}
+
+static int step_enqueue(xk_model *m, int64_t first, int64_t count)
+{
+    if (m->layout == LAYOUT_VM) {
+        for (int64_t g = 0; g < count; ++g)
+            for (int w = 0; w < 2; ++w)
+                XK_CUDA(xk_vm_run(m->vm_code[w], m->vm_ncode[w], m->vm_consts[w], m->vm_params,
+                                  m->fld, m->col, m->vg, m->stream));
+        return XK_OK;
+    }
+    if (m->layout == LAYOUT_MASS) {
+        for (int64_t g = 0; g < count; ++g) {
+            XK_CUDA(xk_mass_step(m->cells32[m->cur], m->cells32[1 - m->cur], m->totals + first + g,
+                                 m->d, m->mass_small, m->stream));
+            m->cur = 1 - m->cur;
+        }
+        return XK_OK;
+    }
+    if (m->layout == LAYOUT_CELLS64) {
+        for (int64_t g = 0; g < count; ++g) {
+            XK_CUDA(xk_evolife_step(m->cells64[m->cur], m->cells64[1 - m->cur], m->col, m->d,
+                                    m->mut_thresh, m->stream));
+            m->cur = 1 - m->cur;
+        }
+        return XK_OK;
+    }
+    const bool colors_free = colors_free_of(m);
     if (m->layout == LAYOUT_BITS2D && colors_free && m->cl_C) {
         // whole lattice in the shared memory of a cluster; long runs are cut
         // into launches of at most 4096 generations
-        int64_t left = nsteps;
+        int64_t left = count;
         while (left > 0) {
             const int g = (int)(left > 4096 ? 4096 : left);
             XK_CUDA(xk_life_step_cluster(m->bits[m->cur], m->lg, m->rule0, m->rule1, g, m->cl_C, m->cl_R,
@@ -668,7 +681,7 @@ extern "C" int xk_step(xk_model *m, int64_t nsteps)
     } else if (m->layout == LAYOUT_BITS2D && m->resident && colors_free) {
         // whole lattice in shared memory; long runs are cut into launches of
         // at most 4096 generations
-        int64_t left = nsteps;
+        int64_t left = count;
         while (left > 0) {
             const int g = (int)(left > 4096 ? 4096 : left);
             XK_CUDA(xk_life_step_resident(m->d_inst, 1, m->bits[m->cur], 0, g, m->lg.torus,
@@ -678,7 +691,7 @@ extern "C" int xk_step(xk_model *m, int64_t nsteps)
         }
     } else {
         const LifeTable t = xk_life_table(m->rule0, m->rule1);
-        for (int64_t s = 0; s < nsteps; ++s) {
+        for (int64_t s = 0; s < count; ++s) {
             if (m->layout == LAYOUT_BITS2D) {
                 if (m->resident)
                     XK_CUDA(xk_life_step_resident(m->d_inst, 1, m->bits[m->cur], 0, 1, m->lg.torus,
@@ -700,13 +713,140 @@ extern "C" int xk_step(xk_model *m, int64_t nsteps)
             }
         }
     }
+    // history-free colours are implied by the state from here on
+    if (colors_free && m->d.color_kind != XK_COLOR_NONE) m->derived = 1;
+    return XK_OK;
+}
+
+static int step_finish(xk_model *m, int64_t nsteps)
+{
+    if (m->layout == LAYOUT_MASS) {
+        m->totals_count = nsteps;
+        m->proj_valid = 0;
+        if (xk_mass_take_wait_failure()) {
+            xk_set_error("mass-transfer step: a CTA gave up waiting for a tensor copy");
+            return XK_ERR_TIMEOUT;
+        }
+    }
+    return XK_OK;
+}
+
+extern "C" int xk_step(xk_model *m, int64_t nsteps)
+{
+    XK_REQUIRE(m, XK_ERR_ARG, "xk_step: null model");
+    XK_REQUIRE(nsteps >= 0, XK_ERR_ARG, "xk_step: negative step count");
+    XK_REQUIRE(m->uploaded, XK_ERR_STATE, "xk_step before xk_upload");
+    if (nsteps == 0) return XK_OK;
+    int rc = step_prepare(m, nsteps);
+    if (rc != XK_OK) return rc;
+    XK_CUDA(cudaEventRecord(m->ev0, m->stream));
+    rc = step_enqueue(m, 0, nsteps);
+    if (rc != XK_OK) return rc;
     XK_CUDA(cudaEventRecord(m->ev1, m->stream));
     XK_CUDA(cudaEventSynchronize(m->ev1));
     float ms = 0.f;
     XK_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
     xk_set_last_step_ms(ms);
-    if (colors_free && m->d.color_kind != XK_COLOR_NONE) m->derived = 1;
+    return step_finish(m, nsteps);
+}
+
+// RendererPlain of the current state into `img` (int32 or the uint8 frame),
+// stream-ordered on the model's stream
+static int render_enqueue(xk_model *m, void *img, bool bytes, int32_t width, int32_t height,
+                          int32_t zoom, int32_t dx, int32_t dy)
+{
+    if (m->layout == LAYOUT_MASS && m->d.proj_axis0 == 0 && m->d.proj_axis1 == 1 &&
+        m->d.render_smooth == 0) {
+        if (!m->proj_valid) {
+            XK_CUDA(xk_mass_project(m->cells32[m->cur], m->proj, m->d, m->stream));
+            m->proj_valid = 1;
+        }
+        if (bytes)
+            XK_CUDA(xk_mass_render_u8(m->proj, (uint8_t *)img, m->d, width, height, zoom, dx, dy,
+                                      m->stream));
+        else
+            XK_CUDA(xk_mass_render(m->proj, (int32_t *)img, m->d, width, height, zoom, dx, dy,
+                                   m->stream));
+        return XK_OK;
+    }
+    int rc = materialize_colors(m);
+    if (rc != XK_OK) return rc;
+    RenderGeo g;
+    memset(&g, 0, sizeof(g));
+    g.ndim = m->d.ndim;
+    g.a0 = m->d.proj_axis0;
+    g.a1 = m->d.proj_axis1;
+    for (int i = 0; i < m->d.ndim; ++i) g.size[i] = m->d.size[i];
+    g.smooth = m->d.render_smooth;
+    if (bytes)
+        XK_CUDA(xk_render_colors_u8(m->col, (uint8_t *)img, g, width, height, zoom, dx, dy, m->stream));
+    else
+        XK_CUDA(xk_render_colors(m->col, (int32_t *)img, g, width, height, zoom, dx, dy, m->stream));
     return XK_OK;
+}
+
+extern "C" int xk_step_frames(xk_model *m, int64_t nsteps, int32_t width, int32_t height,
+                              int32_t zoom, int32_t dx, int32_t dy, uint8_t *frames,
+                              int32_t frames_on_device)
+{
+    XK_REQUIRE(m && frames, XK_ERR_ARG, "xk_step_frames: null argument");
+    XK_REQUIRE(nsteps >= 0, XK_ERR_ARG, "xk_step_frames: negative step count");
+    XK_REQUIRE(width > 0 && height > 0 && zoom > 0, XK_ERR_ARG,
+               "xk_step_frames: bad viewport %dx%d zoom %d", width, height, zoom);
+    XK_REQUIRE(m->uploaded, XK_ERR_STATE, "xk_step_frames before xk_upload");
+    if (nsteps == 0) return XK_OK;
+    const size_t fb = (size_t)width * height * 3;
+    int rc = step_prepare(m, nsteps);
+    if (rc != XK_OK) return rc;
+    if (!frames_on_device) {
+        // a ring of device frames, each copied to the host on its own stream
+        // while the next generations run
+        if ((int64_t)fb * kFrameRing > m->ring_cap) {
+            if (m->ring) cudaFree(m->ring);
+            m->ring = nullptr;
+            m->ring_cap = 0;
+            XK_CUDA(cudaMalloc(&m->ring, fb * kFrameRing));
+            m->ring_cap = (int64_t)fb * kFrameRing;
+        }
+        if (!m->copy_stream) {
+            XK_CUDA(cudaStreamCreateWithFlags(&m->copy_stream, cudaStreamNonBlocking));
+            for (int k = 0; k < kFrameRing; ++k) {
+                XK_CUDA(cudaEventCreateWithFlags(&m->rendered[k], cudaEventDisableTiming));
+                XK_CUDA(cudaEventCreateWithFlags(&m->copied[k], cudaEventDisableTiming));
+            }
+        }
+    }
+    XK_CUDA(cudaEventRecord(m->ev0, m->stream));
+    for (int64_t g = 0; g < nsteps; ++g) {
+        rc = step_enqueue(m, g, 1);
+        if (rc != XK_OK) return rc;
+        m->proj_valid = 0;
+        if (frames_on_device) {
+            rc = render_enqueue(m, frames + (size_t)g * fb, true, width, height, zoom, dx, dy);
+            if (rc != XK_OK) return rc;
+            continue;
+        }
+        const int k = (int)(g % kFrameRing);
+        uint8_t *slot = m->ring + (size_t)k * fb;
+        if (g >= kFrameRing) XK_CUDA(cudaStreamWaitEvent(m->stream, m->copied[k], 0));
+        rc = render_enqueue(m, slot, true, width, height, zoom, dx, dy);
+        if (rc != XK_OK) return rc;
+        XK_CUDA(cudaEventRecord(m->rendered[k], m->stream));
+        XK_CUDA(cudaStreamWaitEvent(m->copy_stream, m->rendered[k], 0));
+        XK_CUDA(cudaMemcpyAsync(frames + (size_t)g * fb, slot, fb, cudaMemcpyDeviceToHost,
+                                m->copy_stream));
+        XK_CUDA(cudaEventRecord(m->copied[k], m->copy_stream));
+    }
+    if (!frames_on_device) {
+        const int last = (int)((nsteps - 1) % kFrameRing);
+        XK_CUDA(cudaStreamWaitEvent(m->stream, m->copied[last], 0));
+    }
+    XK_CUDA(cudaEventRecord(m->ev1, m->stream));
+    XK_CUDA(cudaEventSynchronize(m->ev1));
+    float ms = 0.f;
+    XK_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+    xk_set_last_step_ms(ms);
+    return step_finish(m, nsteps);
 }
 
 extern "C" int xk_render(xk_model *m, int32_t *host_img, int32_t width, int32_t height,
@@ -722,28 +862,8 @@ extern "C" int xk_render(xk_model *m, int32_t *host_img, int32_t width, int32_t 
         XK_CUDA(cudaMalloc(&m->img, (size_t)npx * 3 * sizeof(int32_t)));
         m->img_cap = npx * 3;
     }
-    if (m->layout == LAYOUT_MASS && m->d.proj_axis0 == 0 && m->d.proj_axis1 == 1 &&
-        m->d.render_smooth == 0) {
-        if (!m->proj_valid) {
-            XK_CUDA(xk_mass_project(m->cells32[m->cur], m->proj, m->d, m->stream));
-            m->proj_valid = 1;
-        }
-        XK_CUDA(xk_mass_render(m->proj, m->img, m->d, width, height, zoom, dx, dy, m->stream));
-        XK_CUDA(cudaMemcpyAsync(host_img, m->img, (size_t)npx * 3 * sizeof(int32_t),
-                                cudaMemcpyDeviceToHost, m->stream));
-        XK_CUDA(cudaStreamSynchronize(m->stream));
-        return XK_OK;
-    }
-    int rc = materialize_colors(m);
+    int rc = render_enqueue(m, m->img, false, width, height, zoom, dx, dy);
     if (rc != XK_OK) return rc;
-    RenderGeo g;
-    memset(&g, 0, sizeof(g));
-    g.ndim = m->d.ndim;
-    g.a0 = m->d.proj_axis0;
-    g.a1 = m->d.proj_axis1;
-    for (int i = 0; i < m->d.ndim; ++i) g.size[i] = m->d.size[i];
-    g.smooth = m->d.render_smooth;
-    XK_CUDA(xk_render_colors(m->col, m->img, g, width, height, zoom, dx, dy, m->stream));
     XK_CUDA(cudaMemcpyAsync(host_img, m->img, (size_t)npx * 3 * sizeof(int32_t),
                             cudaMemcpyDeviceToHost, m->stream));
     XK_CUDA(cudaStreamSynchronize(m->stream));

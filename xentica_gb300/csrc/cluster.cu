@@ -205,7 +205,7 @@ static cudaError_t cluster_attrs(ClusterKernel k, size_t smem)
 {
     cudaError_t e = cudaFuncSetAttribute((const void *)k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute((const void *)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return xk_smem_attr_at_least((const void *)k, (int)smem);
 }
 
 static void cluster_cfg(cudaLaunchConfig_t &cfg, cudaLaunchAttribute &attr, int C, int threads,

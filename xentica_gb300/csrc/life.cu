@@ -471,8 +471,7 @@ static cudaError_t xk_launch_resident(const LifeInst *inst, int ninst, const voi
                                       void *mirror, int generations, uint32_t bfill, unsigned int *bad,
                                       int threads, int smem_bytes, cudaStream_t s)
 {
-    cudaError_t e = cudaFuncSetAttribute(xk_k_life_resident<BYTES, TORUS>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    cudaError_t e = xk_smem_attr_at_least((const void *)xk_k_life_resident<BYTES, TORUS>, smem_bytes);
     if (e != cudaSuccess || ninst <= 0) return e;
     xk_k_life_resident<BYTES, TORUS><<<ninst, threads, smem_bytes, s>>>(inst, in, out, mirror,
                                                                         generations, bfill, bad);
@@ -500,8 +499,7 @@ cudaError_t xk_life_step_resident(const LifeInst *inst, int ninst, void *state, 
 int xk_life_resident_ctas_per_sm(int threads, int smem_bytes)
 {
     int n = 0;
-    if (cudaFuncSetAttribute(xk_k_life_resident<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem_bytes) != cudaSuccess ||
+    if (xk_smem_attr_at_least((const void *)xk_k_life_resident<true, true>, smem_bytes) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, xk_k_life_resident<true, true>, threads,
                                                       smem_bytes) != cudaSuccess) {
         cudaGetLastError();

@@ -731,7 +731,8 @@ __global__ void xk_k_mass_colors(const uint32_t *__restrict__ src, int32_t *__re
 
 // RendererPlain over axes (0, 1) from the column sums: the float sum of a
 // column's colours equals its integer sum, divided by the depth
-__global__ void xk_k_mass_render(const uint32_t *__restrict__ proj, int32_t *__restrict__ img,
+template <typename T>
+__global__ void xk_k_mass_render(const uint32_t *__restrict__ proj, T *__restrict__ img,
                                  MassParams p, int width, int height, int zoom, int dx, int dy)
 {
     const int64_t ip = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -744,7 +745,7 @@ __global__ void xk_k_mass_render(const uint32_t *__restrict__ proj, int32_t *__r
     if (xb < 0) xb = p.H - (-xb % p.H);
     if (xb >= p.H) xb = xb % p.H;
     const float s = (float)proj[(int64_t)xb * p.W + xa];
-    const int v = (int)__fdiv_rn(s, (float)p.D);
+    const T v = (T)(int)__fdiv_rn(s, (float)p.D);
     img[3 * ip] = v;
     img[3 * ip + 1] = v;
     img[3 * ip + 2] = v;
@@ -909,7 +910,17 @@ cudaError_t xk_mass_render(const uint32_t *proj, int32_t *img, const xk_desc &d,
 {
     const MassParams p = mass_params(d);
     const int64_t n = (int64_t)width * height;
-    xk_k_mass_render<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(proj, img, p, width, height, zoom,
-                                                                 dx, dy);
+    xk_k_mass_render<int32_t><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(proj, img, p, width, height,
+                                                                          zoom, dx, dy);
+    return cudaGetLastError();
+}
+
+cudaError_t xk_mass_render_u8(const uint32_t *proj, uint8_t *img, const xk_desc &d, int width,
+                              int height, int zoom, int dx, int dy, cudaStream_t s)
+{
+    const MassParams p = mass_params(d);
+    const int64_t n = (int64_t)width * height;
+    xk_k_mass_render<uint8_t><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(proj, img, p, width, height,
+                                                                          zoom, dx, dy);
     return cudaGetLastError();
 }

@@ -21,14 +21,23 @@
 //     mutex, but the caller must not let two calls' GPU work overlap;
 //   * the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (with that device current); make that first call
-//     before any stream capture.
+//     before any stream capture.  The address is kept per device together
+//     with the identity of the CUDA context it was taken in, and looked up
+//     again when the device's context has changed (after cudaDeviceReset, or
+//     a host framework resetting the primary context, the module is loaded
+//     anew and the old address is stale).
 #include <string.h>
+
+#include <cudaTypedefs.h>   // PFN_cuCtxGetCurrent, PFN_cuCtxGetId
 
 #include <algorithm>
 #include <mutex>
 
 #include "xk_internal.cuh"
 
+// 4096 descriptors of 40 bytes plus the 256-byte flag slot: 164,096 bytes
+// (about 160 KB) on every device that loads the library
+static_assert(sizeof(LifeInst) == 40, "LifeInst layout changed: update the scratch size notes");
 #define XK_NOALLOC_SCRATCH_BYTES (XK_NOALLOC_MAX_LATTICES * sizeof(LifeInst) + 256)
 
 // the only device memory this entry point uses besides the caller's cells:
@@ -40,6 +49,34 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void *g_scratch_addr[kMaxDevices] = {nullptr};
+unsigned long long g_scratch_ctx[kMaxDevices] = {0};   // context id the address belongs to
+
+// identity of the context current on this thread (0 when it cannot be
+// told), through the runtime's driver entry points (no link to libcuda)
+unsigned long long current_context_id()
+{
+    static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+    static PFN_cuCtxGetId_v12000 get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_current = (PFN_cuCtxGetCurrent_v4000)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_id = (PFN_cuCtxGetId_v12000)f;
+        looked_up = true;
+    }
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx ||
+        get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
 // host staging, reused by every call (guarded by g_mu)
 LifeInst g_inst[XK_NOALLOC_MAX_LATTICES];
 int g_order[XK_NOALLOC_MAX_LATTICES];
@@ -63,12 +100,16 @@ extern "C" int xk_batch_step_noalloc(uint8_t *d_cells, int32_t count, const int3
     int dev = 0;
     XK_CUDA(cudaGetDevice(&dev));
     XK_REQUIRE(dev >= 0 && dev < kMaxDevices, XK_ERR_ARG, "device %d out of range", dev);
-    if (!g_scratch_addr[dev]) {
-        // once per device, with that device current: the device address of
-        // the file-scope array (its name is only a host-side stand-in)
+    XK_CUDA(cudaSetDevice(dev));   // makes the device's primary context current
+    const unsigned long long ctx = current_context_id();
+    if (!g_scratch_addr[dev] || ctx == 0 || ctx != g_scratch_ctx[dev]) {
+        // once per device (and per context of it), with that device current:
+        // the device address of the file-scope array (its name is only a
+        // host-side stand-in)
         void *addr = nullptr;
         XK_CUDA(cudaGetSymbolAddress(&addr, g_noalloc_scratch));
         g_scratch_addr[dev] = addr;
+        g_scratch_ctx[dev] = ctx;
     }
     unsigned int *bad = (unsigned int *)g_scratch_addr[dev];
     LifeInst *d_inst = (LifeInst *)((unsigned char *)g_scratch_addr[dev] + 256);

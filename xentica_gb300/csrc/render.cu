@@ -6,10 +6,13 @@
 // on the projection axes (a0, a1), wrapped onto the board with the reference's
 // two-step rule, then sums the colours of every cell along the other axes in
 // float (outer loop = lowest axis), and stores r / num (/ SMOOTH_FACTOR) as an
-// int.  Same operations, same order, same float rounding.
+// int.  Same operations, same order, same float rounding.  The uint8
+// instantiation stores the int's low byte: the frame the reference's render()
+// returns (img.get().astype(np.uint8), base.py:753).
 #include "xk_internal.cuh"
 
-__global__ void xk_k_render(const int32_t *__restrict__ col, int32_t *__restrict__ img,
+template <typename T>
+__global__ void xk_k_render(const int32_t *__restrict__ col, T *__restrict__ img,
                             RenderGeo g, int width, int height, int zoom, int dx, int dy)
 {
     const int64_t ip = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -51,15 +54,25 @@ __global__ void xk_k_render(const int32_t *__restrict__ col, int32_t *__restrict
         vg = __fdiv_rn(vg, sf);
         vb = __fdiv_rn(vb, sf);
     }
-    img[3 * ip] = (int)vr;
-    img[3 * ip + 1] = (int)vg;
-    img[3 * ip + 2] = (int)vb;
+    img[3 * ip] = (T)(int)vr;
+    img[3 * ip + 1] = (T)(int)vg;
+    img[3 * ip + 2] = (T)(int)vb;
 }
 
 cudaError_t xk_render_colors(const int32_t *col, int32_t *img, const RenderGeo &g, int width,
                              int height, int zoom, int dx, int dy, cudaStream_t s)
 {
     const int64_t n = (int64_t)width * height;
-    xk_k_render<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(col, img, g, width, height, zoom, dx, dy);
+    xk_k_render<int32_t><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(col, img, g, width, height,
+                                                                      zoom, dx, dy);
+    return cudaGetLastError();
+}
+
+cudaError_t xk_render_colors_u8(const int32_t *col, uint8_t *img, const RenderGeo &g, int width,
+                                int height, int zoom, int dx, int dy, cudaStream_t s)
+{
+    const int64_t n = (int64_t)width * height;
+    xk_k_render<uint8_t><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(col, img, g, width, height,
+                                                                      zoom, dx, dy);
     return cudaGetLastError();
 }

@@ -103,6 +103,14 @@ struct LifeInst {
 int64_t xk_life_resident_words(int W, int H, int threads);
 // largest dynamic shared memory a CTA may use on this device
 int xk_max_smem_optin();
+// Raise a kernel's cudaFuncAttributeMaxDynamicSharedMemorySize (one value per
+// function and device) to at least `bytes`; never lowers it.  A graph node
+// keeps the shared memory of the launch it captured, and a node launched or
+// replayed later (a profiler replays graph nodes one by one) is checked
+// against the attribute as it is then: had a later, smaller launch lowered
+// the attribute, that node would fail with cudaErrorLaunchFailure or an
+// invalid-argument error.  Kept monotone, every captured node stays valid.
+cudaError_t xk_smem_attr_at_least(const void *fn, int bytes);
 
 // launchers (stream-ordered, no synchronisation)
 cudaError_t xk_life_pack(const void *src, int esz, uint32_t *dst, const LifeGeo &g, cudaStream_t s);
@@ -178,6 +186,10 @@ struct RenderGeo {
 };
 cudaError_t xk_render_colors(const int32_t *col, int32_t *img, const RenderGeo &g, int width,
                              int height, int zoom, int dx, int dy, cudaStream_t s);
+// the same frame as bytes (the int's low byte, as the reference's
+// render() converts it)
+cudaError_t xk_render_colors_u8(const int32_t *col, uint8_t *img, const RenderGeo &g, int width,
+                                int height, int zoom, int dx, int dy, cudaStream_t s);
 
 int xk_sm_count();
 
@@ -257,3 +269,5 @@ cudaError_t xk_mass_project(const uint32_t *src, uint32_t *proj, const xk_desc &
 cudaError_t xk_mass_colors(const uint32_t *src, int32_t *col, const xk_desc &d, cudaStream_t s);
 cudaError_t xk_mass_render(const uint32_t *proj, int32_t *img, const xk_desc &d, int width,
                            int height, int zoom, int dx, int dy, cudaStream_t s);
+cudaError_t xk_mass_render_u8(const uint32_t *proj, uint8_t *img, const xk_desc &d, int width,
+                              int height, int zoom, int dx, int dy, cudaStream_t s);
