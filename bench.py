@@ -298,6 +298,52 @@ def run_reference_arm(args, dist):
     print(json.dumps(line), flush=True)
 
 
+def reference_gpu_sample(ens, cells, generations=2):
+    """The reference's own generated LifelikeCA kernels compiled for sm_103a
+    (``oracle/ref_gpu.py``), launched as the reference's step() does (emit
+    then absorb per lattice per generation, PyCUDA's block and grid) over every
+    lattice of the ensemble for ``generations`` generations after one warm-up
+    generation; their cells are compared with this library's after the same
+    generations.  None when the comparator is not built."""
+    import ctypes
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_gpu
+    path = ref_gpu.available()
+    if not path:
+        return None
+    lib = ctypes.CDLL(path)
+    lib.xkrefg_create.restype = ctypes.c_void_p
+    lib.xkrefg_create.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 4
+    lib.xkrefg_step.restype = ctypes.c_float
+    lib.xkrefg_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.xkrefg_download.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.xkrefg_destroy.argtypes = [ctypes.c_void_p]
+    w = np.ascontiguousarray(ens.widths, dtype=np.int32)
+    h = np.ascontiguousarray(ens.heights, dtype=np.int32)
+    r = np.ascontiguousarray(ens.rules, dtype=np.int32)
+    cells = np.ascontiguousarray(cells, dtype=np.uint8)
+    handle = lib.xkrefg_create(ens.count, w.ctypes.data, h.ctypes.data, r.ctypes.data,
+                               cells.ctypes.data)
+    if not handle:
+        return {"unavailable": "reference kernels missing for a lattice size, or CUDA failed"}
+    lib.xkrefg_step(handle, 1)                       # module load, first launches
+    ms = lib.xkrefg_step(handle, generations)
+    out = np.empty(ens.total_cells, dtype=np.uint8)
+    lib.xkrefg_download(handle, out.ctypes.data)
+    lib.xkrefg_destroy(handle)
+    if ms <= 0:
+        return {"unavailable": "a reference kernel launch failed"}
+    ens.upload(cells)
+    ens.step(1 + generations)
+    exact = bool(np.array_equal(ens.download(), out))
+    return {"value": float(ens.total_cells) * generations / (ms / 1000.0), "unit": "cell-updates/s",
+            "generations": generations, "launches": 2 * ens.count * generations,
+            "bit_exact_vs_ours": exact,
+            "kind": "the reference's generated LifelikeCA emit/absorb kernels (translator "
+                    "output, nvcc -w for sm_103a), one emit and one absorb launch per lattice "
+                    "per generation with PyCUDA's block/grid, launched from a C loop"}
+
+
 def ensemble_parity(ens, widths, heights, G):
     """One lattice of each size class: snapshot, one more step of G
     generations in the timed configuration, the oracle from the snapshot."""
@@ -386,6 +432,9 @@ def run_ours(args, dist):
     pg = args.plain_generations
     plain_ms = ens.step_plain(pg)
     plain_value = float(total) * pg / (plain_ms / 1000.0)
+    ref_gpu = reference_gpu_sample(ens, cells, pg)
+    if ref_gpu and "value" in ref_gpu:
+        ref_gpu["batched_over_reference_gpu"] = value / dist.world / ref_gpu["value"]
     launches = ens.launches(G) * args.steps
     peak, peak_kind = measured_peak()
     mean_ms = statistics.mean(step_ms)
@@ -419,6 +468,7 @@ def run_ours(args, dist):
                     "d2h_bytes_per_step": total, "ms_per_step": e2e_s * 1000 / args.steps},
             "plain": {"value": plain_value, "unit": "cell-updates/s", "generations": pg,
                       "batched_over_plain": value / dist.world / plain_value},
+            "reference_gpu": ref_gpu,
             "seeding": {"device_ms": seed_ms, "host_s": host_seed_s, "bit_exact": seed_exact,
                         "note": "the %d lattices' Bernoulli cells drawn on the device (one "
                                 "MT19937 stream per lattice, NumPy's random_sample) against "

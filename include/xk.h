@@ -207,6 +207,18 @@ int64_t xk_batch_total_cells(const xk_batch *b);
 /* Kernel launches one xk_batch_step makes (one per instance class, plus
  * per-generation launches for instances too large for a CTA). */
 int64_t xk_batch_launches(const xk_batch *b, int32_t generations);
+/* Membership changes between steps.  The reference adds or drops an
+ * instance by creating or discarding a CellularAutomaton
+ * (base.py:591-690); here an ensemble changes in place.  xk_batch_add appends
+ * a lattice (cells one byte each from host_cells, or all 0 when NULL) and
+ * returns its index (>= 0) or a negative status; xk_batch_remove drops
+ * lattice `index` (later lattices move down by one; the last lattice cannot
+ * be removed).  Both keep every other lattice's cells, re-plan the launch
+ * classes and capture a new graph at the next step. */
+int xk_batch_add(xk_batch *b, int32_t width, int32_t height, uint32_t rule,
+                 const uint8_t *host_cells);
+int xk_batch_remove(xk_batch *b, int32_t index);
+int32_t xk_batch_count(const xk_batch *b);
 
 /* Ensemble step that allocates nothing.  No counterpart in the reference.
  * For callers that cannot call cudaMalloc (a host framework owns every

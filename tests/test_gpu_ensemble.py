@@ -249,3 +249,53 @@ def test_end_to_end_rejects_non_binary_cells(form, monkeypatch):
         ens.run(pin_in.array, pin_out.array, 3)
     pin_in.array[3] = 1
     ens.run(pin_in.array, pin_out.array, 3)   # the flag was cleared
+
+
+def test_add_and_remove_between_steps():
+    """Lattices added and removed between steps (xk_batch_add/remove): every
+    lattice keeps its own history, compared with the oracle run for exactly
+    the generations it has been a member."""
+    ens, cells = _ensemble(9)
+    lattices = [ens.lattice(cells, i).copy() for i in range(ens.count)]
+    rules = [int(r) for r in ens.rules]
+    ages = [0] * ens.count
+
+    def check():
+        got = ens.download()
+        for i in range(ens.count):
+            h, w = lattices[i].shape
+            topo = O.Topology((w, h))
+            fld = topo.field(lattices[i].ravel(), np.uint8)
+            O.life_run(topo, fld, np.zeros(topo.cells * 3, np.int32), ages[i],
+                       born=rules[i] & 511, sustain=rules[i] >> 9)
+            assert np.array_equal(ens.lattice(got, i).ravel(), fld[:topo.cells]), \
+                "lattice %d (%dx%d) after %d generations" % (i, w, h, ages[i])
+
+    ens.upload(cells)
+    ens.step(5)
+    ages = [a + 5 for a in ages]
+    rng = np.random.RandomState(4)
+    new = (rng.random_sample((70, 301)) < 0.4).astype(np.uint8)
+    idx = ens.add(301, 70, "B36/S23", new)
+    assert idx == ens.count - 1 == len(SIZES)
+    lattices.append(new)
+    rules.append(int(ens.rules[idx]))
+    ages.append(0)
+    check()
+    ens.step(7)
+    ages = [a + 7 for a in ages]
+    check()
+    for drop in (4, 0):
+        ens.remove(drop)
+        del lattices[drop], rules[drop], ages[drop]
+    assert ens._lib.xk_batch_count(ens._handle) == ens.count == len(SIZES) - 1
+    ens.step(3)
+    ages = [a + 3 for a in ages]
+    check()
+    ens.add(64, 64, 6152)                      # no cells: all dead
+    lattices.append(np.zeros((64, 64), np.uint8))
+    rules.append(6152)
+    ages.append(0)
+    ens.step(2)
+    ages = [a + 2 for a in ages]
+    check()

@@ -101,6 +101,9 @@ SIGNATURES = {
     "xk_batch_run": (_I32, [_P, _P, _P, _I64, _I32]),
     "xk_batch_tune": (_I32, [_P, _I32, ctypes.POINTER(_I32)]),
     "xk_batch_set_band": (_I32, [_P, _I32]),
+    "xk_batch_add": (_I32, [_P, _I32, _I32, _U32, _P]),
+    "xk_batch_remove": (_I32, [_P, _I32]),
+    "xk_batch_count": (_I32, [_P]),
     "xk_batch_band": (_I32, [_P]),
     "xk_batch_total_cells": (_I64, [_P]),
     "xk_batch_launches": (_I64, [_P, _I32]),

@@ -81,10 +81,7 @@ class Ensemble:
         self.rules = np.ascontiguousarray(rules, dtype=np.uint32)
         if not len(self.widths) == len(self.heights) == len(self.rules):
             raise XenticaException("widths, heights and rules differ in length")
-        self.count = len(self.widths)
-        self.sizes = self.widths.astype(np.int64) * self.heights.astype(np.int64)
-        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)[:-1]]).astype(np.int64)
-        self.total_cells = int(self.sizes.sum())
+        self._sync_layout()
         self._lib = nat.load()
         handle = ctypes.c_void_p()
         nat.check(self._lib.xk_batch_create(self.count, nat.ptr(self.widths), nat.ptr(self.heights),
@@ -99,6 +96,41 @@ class Ensemble:
             except Exception:
                 pass
             self._handle = None
+
+    def _sync_layout(self):
+        self.count = len(self.widths)
+        self.sizes = self.widths.astype(np.int64) * self.heights.astype(np.int64)
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)[:-1]]).astype(np.int64)
+        self.total_cells = int(self.sizes.sum())
+
+    def add(self, width, height, rule, cells=None):
+        """Append a lattice (cells: ``height x width`` bytes, 0/1; zeros when
+        omitted) without disturbing the others; returns its index."""
+        rule = LifeLike.golly2int(rule) if isinstance(rule, str) else int(rule)
+        buf = None
+        if cells is not None:
+            buf = np.ascontiguousarray(cells, dtype=np.uint8).ravel()
+            if buf.size != int(width) * int(height):
+                raise XenticaException("expected %d cells, got %d" % (int(width) * int(height),
+                                                                       buf.size))
+        rc = self._lib.xk_batch_add(self._handle, int(width), int(height), rule,
+                                    None if buf is None else nat.ptr(buf))
+        if rc < 0:
+            nat.check(rc, "xk_batch_add")
+        self.widths = np.append(self.widths, np.int32(width))
+        self.heights = np.append(self.heights, np.int32(height))
+        self.rules = np.append(self.rules, np.uint32(rule))
+        self._sync_layout()
+        return int(rc)
+
+    def remove(self, index):
+        """Drop lattice ``index``; the lattices after it move down by one."""
+        index = int(index)
+        nat.check(self._lib.xk_batch_remove(self._handle, index), "xk_batch_remove")
+        self.widths = np.delete(self.widths, index)
+        self.heights = np.delete(self.heights, index)
+        self.rules = np.delete(self.rules, index)
+        self._sync_layout()
 
     def _cells(self, cells):
         cells = np.ascontiguousarray(cells, dtype=np.uint8)

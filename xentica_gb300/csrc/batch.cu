@@ -802,3 +802,98 @@ extern "C" int64_t xk_batch_launches(const xk_batch *b, int32_t generations)
     return (int64_t)b->classes.size() + (int64_t)b->big.size() * generations +
            (int64_t)b->big.size() * (generations & 1);
 }
+
+// ---------------------------------------------------------------------------
+// membership changes: the device state is rebuilt as one buffer in the new
+// order (kept lattices copied device to device), then the classes are
+// re-planned, so the next step captures a new graph
+
+static int rebuild_cells(xk_batch *b, const std::vector<int64_t> &src_off, const std::vector<int64_t> &len,
+                         int64_t new_total)
+{
+    uint8_t *cells = nullptr;
+    XK_CUDA(cudaMalloc(&cells, (size_t)new_total + 16));
+    cudaError_t e = cudaMemsetAsync(cells, 0, (size_t)new_total + 16, b->stream);
+    int64_t at = 0;
+    for (size_t k = 0; k < len.size() && e == cudaSuccess; ++k) {
+        if (src_off[k] >= 0 && len[k] > 0)
+            e = cudaMemcpyAsync(cells + at, b->cells + src_off[k], (size_t)len[k], cudaMemcpyDeviceToDevice,
+                                b->stream);
+        at += len[k];
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) {
+        cudaFree(cells);
+        return xk_cuda_status(e, "rebuilding the ensemble's cells");
+    }
+    cudaFree(b->cells);
+    b->cells = cells;
+    if (b->scratch) cudaFree(b->scratch);   // the plain form's partner, sized anew on use
+    b->scratch = nullptr;
+    return XK_OK;
+}
+
+extern "C" int xk_batch_add(xk_batch *b, int32_t width, int32_t height, uint32_t rule,
+                            const uint8_t *host_cells)
+{
+    XK_REQUIRE(b, XK_ERR_ARG, "xk_batch_add: null batch");
+    XK_REQUIRE(width >= 1 && height >= 1 && (int64_t)width * height <= (1LL << 31), XK_ERR_ARG,
+               "xk_batch_add: size %dx%d", width, height);
+    XK_REQUIRE(rule >> 18 == 0, XK_ERR_ARG, "xk_batch_add: rule %u has bits above 17", rule);
+    XK_CUDA(cudaStreamSynchronize(b->stream));
+    const int64_t n = (int64_t)width * height;
+    std::vector<int64_t> src(b->n + 1), len(b->n + 1);
+    for (int i = 0; i < b->n; ++i) {
+        src[i] = b->off[i];
+        len[i] = (int64_t)b->W[i] * b->H[i];
+    }
+    src[b->n] = -1;          // the new lattice: zeros, then its cells
+    len[b->n] = n;
+    int rc = rebuild_cells(b, src, len, b->total + n);
+    if (rc != XK_OK) return rc;
+    if (host_cells) {
+        XK_CUDA(cudaMemcpyAsync(b->cells + b->total, host_cells, (size_t)n, cudaMemcpyHostToDevice,
+                                b->stream));
+        XK_CUDA(cudaStreamSynchronize(b->stream));
+    }
+    b->W.push_back(width);
+    b->H.push_back(height);
+    b->rule.push_back(rule);
+    b->off.push_back(b->total);
+    b->total += n;
+    b->n += 1;
+    rc = plan_classes(b);
+    return rc == XK_OK ? b->n - 1 : rc;
+}
+
+extern "C" int xk_batch_remove(xk_batch *b, int32_t index)
+{
+    XK_REQUIRE(b, XK_ERR_ARG, "xk_batch_remove: null batch");
+    XK_REQUIRE(index >= 0 && index < b->n, XK_ERR_ARG, "xk_batch_remove: index %d of %d lattices",
+               index, b->n);
+    XK_REQUIRE(b->n > 1, XK_ERR_ARG, "xk_batch_remove: an ensemble keeps at least one lattice");
+    XK_CUDA(cudaStreamSynchronize(b->stream));
+    std::vector<int64_t> src, len;
+    int64_t new_total = 0;
+    for (int i = 0; i < b->n; ++i) {
+        if (i == index) continue;
+        src.push_back(b->off[i]);
+        len.push_back((int64_t)b->W[i] * b->H[i]);
+        new_total += len.back();
+    }
+    int rc = rebuild_cells(b, src, len, new_total);
+    if (rc != XK_OK) return rc;
+    b->W.erase(b->W.begin() + index);
+    b->H.erase(b->H.begin() + index);
+    b->rule.erase(b->rule.begin() + index);
+    b->n -= 1;
+    b->off.assign(b->n, 0);
+    b->total = 0;
+    for (int i = 0; i < b->n; ++i) {
+        b->off[i] = b->total;
+        b->total += (int64_t)b->W[i] * b->H[i];
+    }
+    return plan_classes(b);
+}
+
+extern "C" int32_t xk_batch_count(const xk_batch *b) { return b ? b->n : -1; }

@@ -8,6 +8,7 @@
 #include <mutex>
 #include <new>
 
+#include <cudaTypedefs.h>   // PFN_cuCtxGetCurrent, PFN_cuCtxGetId
 #include <nvtx3/nvToolsExt.h>
 
 #include "xk_internal.cuh"
@@ -61,6 +62,30 @@ int xk_max_smem_optin()
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
     return v;
+}
+
+unsigned long long xk_context_id()
+{
+    static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+    static PFN_cuCtxGetId_v12000 get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_current = (PFN_cuCtxGetCurrent_v4000)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_id = (PFN_cuCtxGetId_v12000)f;
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx ||
+        get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
 }
 
 cudaError_t xk_smem_attr_at_least(const void *fn, int bytes)

@@ -12,9 +12,22 @@
 // x = (x * 58321 + 11113) % 65535 (properties.py:638-660): once for the start
 // gene, then once per gene (twice with mutation).  Floats follow IEEE
 // round-to-nearest with no contraction (__fdiv_rn, __fmul_rn, __fadd_rn).
+//
+// The crossover's draws depend only on the cell's 16-bit random state x0 at
+// the start of the crossover and on the number n of parents: the start gene,
+// and for every gene which parent wins it (and, with mutation, whether it
+// mutates).  So for every (x0, n) the winners are precomputed once per
+// process, on the device, as n "won-gene masks" W_s (bit g of W_s set when
+// gene g is taken from parent slot s), 9.4 MB that stay in L2; a cell's
+// crossover is then OR_s(parent_s & W_s) -- the genes in visiting order,
+// before the max_genes cut -- followed by keeping the first max_genes set
+// genes in visiting order and the mutation flips.  The state after the
+// crossover is one composed affine map of x0.
 #include <string.h>
 
+#include <map>
 #include <mutex>
+#include <utility>
 
 #include "xk_internal.cuh"
 
@@ -25,15 +38,6 @@ __device__ __forceinline__ uint32_t xk_lcg(uint32_t x) { return (x * 58321u + 11
 
 // float -> unsigned int as the GPU converts: truncation, NaN -> 0
 __device__ __forceinline__ uint32_t xk_f2u(float v) { return __float2uint_rz(v); }
-
-// 8 bits -> 8 nibbles (bit g to bit 4g)
-__device__ __forceinline__ uint32_t xk_spread_nibbles(uint32_t b)
-{
-    b = (b | (b << 12)) & 0x000F000Fu;
-    b = (b | (b << 6)) & 0x03030303u;
-    b = (b | (b << 3)) & 0x11111111u;
-    return b;
-}
 
 // bit j of the result = bit (s + j) mod 18 of v (v < 2^18, s < 18), and back
 __device__ __forceinline__ uint32_t xk_rot18(uint32_t v, uint32_t s)
@@ -131,6 +135,8 @@ struct EvoParams {
     uint32_t kmul[9];          // parent draw for 0..8 parents (0: none)
     uint32_t kstart;           // start-gene draw (n = 18)
     uint32_t jump_a, jump_c;   // the crossover's RNG advances as one map x -> (a x + c) % 65535
+    const uint32_t *won;       // won-gene masks: n masks per x0, blocks of 65536 x0 per n
+    const uint32_t *mut;       // mutation flips per x0 (mutation only)
 };
 
 static float evo_u(uint32_t x) { return (float)x / 65535.0f; }
@@ -195,6 +201,105 @@ static void evo_draws(EvoParams &p, float mut_thresh)
     p.mut_x = (int32_t)lo;
 }
 
+// ---------------------------------------------------------------------------
+// crossover tables
+
+struct EvoDraws {
+    uint32_t kmul[9], kstart;
+};
+
+// won-gene masks of every (x0, n): thread t = x0 + 65536 (n - 1) replays the
+// crossover's draws from x0 -- one advance for the start gene, then per
+// visited gene one advance and a parent draw (and one more advance with
+// mutation) -- and writes its n masks at 32768 n (n - 1) + n x0
+__global__ void xk_k_evo_won(uint32_t *__restrict__ won, EvoDraws d, int mutation)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 65536u * 8u) return;
+    const uint32_t x0 = t & 65535u, n = (t >> 16) + 1u;
+    uint32_t w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint32_t x = xk_lcg(x0);
+    const uint32_t start = __umulhi(x, d.kstart) % 8u;
+    for (uint32_t j = 0; j < 18; ++j) {
+        x = xk_lcg(x);
+        const uint32_t win = __umulhi(x, d.kmul[n]);      // < n for every state
+        const uint32_t gene = start + j < 18u ? start + j : start + j - 18u;
+#pragma unroll
+        for (uint32_t s = 0; s < 8; ++s) w[s] |= (uint32_t)(s == win) << gene;
+        if (mutation) x = xk_lcg(x);
+    }
+    uint32_t *o = won + 32768u * n * (n - 1u) + x0 * n;
+#pragma unroll
+    for (uint32_t s = 0; s < 8; ++s)
+        if (s < n) o[s] = w[s];
+}
+
+// mutation flips of every x0 (genes whose second draw is <= mut_x), in
+// gene order
+__global__ void xk_k_evo_mut(uint32_t *__restrict__ mut, int32_t mut_x, uint32_t kstart)
+{
+    const uint32_t x0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x0 >= 65536u) return;
+    uint32_t x = xk_lcg(x0);
+    const uint32_t start = __umulhi(x, kstart) % 8u;
+    uint32_t m = 0;
+    for (uint32_t j = 0; j < 18; ++j) {
+        x = xk_lcg(xk_lcg(x));
+        const uint32_t gene = start + j < 18u ? start + j : start + j - 18u;
+        m |= (uint32_t)((int32_t)x <= mut_x) << gene;
+    }
+    mut[x0] = m;
+}
+
+namespace {
+struct EvoTables {
+    uint32_t *won[2] = {nullptr, nullptr};     // without / with mutation
+    std::map<int32_t, uint32_t *> mut;        // per mut_x
+};
+std::mutex g_evo_tab_mu;
+std::map<std::pair<int, unsigned long long>, EvoTables> g_evo_tabs;   // per device and context
+}  // namespace
+
+// the tables for p's draws, built on first use in this device context (the
+// stream is synchronised once so that every stream may use them)
+static cudaError_t evo_tables(EvoParams &p, cudaStream_t s)
+{
+    std::lock_guard<std::mutex> lk(g_evo_tab_mu);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    EvoTables &t = g_evo_tabs[std::make_pair(dev, xk_context_id())];
+    EvoDraws d;
+    memcpy(d.kmul, p.kmul, sizeof(d.kmul));
+    d.kstart = p.kstart;
+    bool built = false;
+    uint32_t *&won = t.won[p.mutation ? 1 : 0];
+    if (!won) {
+        if ((e = cudaMalloc(&won, 65536u * 36u * sizeof(uint32_t))) != cudaSuccess) {
+            won = nullptr;
+            return e;
+        }
+        xk_k_evo_won<<<65536u * 8u / 256u, 256, 0, s>>>(won, d, p.mutation);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        built = true;
+    }
+    p.won = won;
+    p.mut = nullptr;
+    if (p.mutation) {
+        auto it = t.mut.find(p.mut_x);
+        if (it == t.mut.end()) {
+            uint32_t *m = nullptr;
+            if ((e = cudaMalloc(&m, 65536u * sizeof(uint32_t))) != cudaSuccess) return e;
+            xk_k_evo_mut<<<65536u / 256u, 256, 0, s>>>(m, p.mut_x, p.kstart);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            it = t.mut.emplace(p.mut_x, m).first;
+            built = true;
+        }
+        p.mut = it->second;
+    }
+    return built ? cudaStreamSynchronize(s) : cudaSuccess;
+}
+
 #define XK_EVO_BX 32
 #define XK_EVO_BY 8
 
@@ -202,10 +307,8 @@ __global__ void __launch_bounds__(XK_EVO_BX * XK_EVO_BY)
 xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32_t *__restrict__ col,
              EvoParams p)
 {
-    __shared__ uint32_t gsm[8][XK_EVO_BX * XK_EVO_BY];   // compacted parent genomes
     const int x = blockIdx.x * XK_EVO_BX + threadIdx.x;
     const int y = blockIdx.y * XK_EVO_BY + threadIdx.y;
-    const int tid = threadIdx.y * XK_EVO_BX + threadIdx.x;
     if (x >= p.W || y >= p.H) return;   // no block-wide synchronisation below
     xk_grid_dep_wait();                 // launched as a dependent of the previous generation
     const int xl = x > 0 ? x - 1 : p.W - 1, xr = x < p.W - 1 ? x + 1 : 0;
@@ -228,68 +331,55 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
     uint32_t rule = (uint32_t)((c >> 9) & 262143u);
     uint32_t rng = (uint32_t)((c >> 27) & 65535u);
     const uint32_t is_sustained = ((rule & 261120u) >> (num_neighbors + 9)) & 1u;
-    // num_parents for every birth count 1..8 at once: nibble g counts the
-    // live neighbours whose rule has bit g + 1
-    uint32_t acc = 0;
+    // num_parents for every birth count 1..8 at once, bit-sliced: lane g of
+    // the 4-bit counts (b3 b2 b1 b0) counts the neighbours whose rule has
+    // bit g + 1 (a dead neighbour has rule 0).  Carry-save adder tree over
+    // the eight 8-lane words.
+    uint32_t m[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) acc += xk_spread_nibbles(alive[k] ? ((nr[k] >> 1) & 255u) : 0u);
-    uint32_t num_fit = 0;
-#pragma unroll
-    for (int g = 0; g < 8; ++g) {
-        const uint32_t np = (acc >> (4 * g)) & 15u;
-        const uint32_t fit = np * (uint32_t)(np == (uint32_t)(g + 1));
-        num_fit = num_fit > fit ? num_fit : fit;
-    }
+    for (int k = 0; k < 8; ++k) m[k] = (nr[k] >> 1) & 255u;
+    const uint32_t s0 = m[0] ^ m[1] ^ m[2], c0 = (m[0] & m[1]) | (m[2] & (m[0] ^ m[1]));
+    const uint32_t s1 = m[3] ^ m[4] ^ m[5], c1 = (m[3] & m[4]) | (m[5] & (m[3] ^ m[4]));
+    const uint32_t s2 = m[6] ^ m[7], c2 = m[6] & m[7];
+    const uint32_t b0 = s0 ^ s1 ^ s2, c3 = (s0 & s1) | (s2 & (s0 ^ s1));
+    const uint32_t t0 = c0 ^ c1 ^ c2, d0 = (c0 & c1) | (c2 & (c0 ^ c1));
+    const uint32_t b1 = t0 ^ c3, d1 = t0 & c3;
+    const uint32_t b2 = d0 ^ d1, b3 = d0 & d1;
+    // lane g has a fit when its count equals g + 1 (bit planes of g + 1 per
+    // lane: 0x55, 0x66, 0x78, 0x80); num_fit = the largest such g + 1
+    const uint32_t eq = ~(b0 ^ 0x55u) & ~(b1 ^ 0x66u) & ~(b2 ^ 0x78u) & ~(b3 ^ 0x80u) & 255u;
+    const uint32_t num_fit = 32u - (uint32_t)__clz(eq);
     // parents: rules with the winning birth count, in neighbour order
-    uint32_t n = 0, any = 0;
+    uint32_t pmask = 0, any = 0;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-        const uint32_t genome = nr[k] * (((nr[k] & 510u) >> num_fit) & 1u);
-        n += genome > 0;
-        any |= genome;
+        const uint32_t par = ((nr[k] & 510u) >> num_fit) & 1u;
+        pmask |= par << k;
+        any |= nr[k] * par;
     }
+    const uint32_t n = __popc(pmask);
     const uint32_t old_rule = rule, old_energy = energy;
     // genome_crossover(main, 18, *genomes, max_genes, mutation_prob).  With
     // no parent, every gene is 0 (no winner, and a mutation needs a gene that
     // some parent has): only the RNG advances, by the composed map.
     uint32_t new_genome = 0;
-    if (n == 0) {
-        rng = (p.jump_a * rng + p.jump_c) % 65535u;
-    } else {
-        rng = xk_lcg(rng);
-        const uint32_t start_gene = __umulhi(rng, p.kstart) % 8u;
-        // genes are visited from start_gene, wrapping at 18: the parents and
-        // the mutation mask are rotated so that step j reads bit j (the
-        // unrolled loop then shifts by constants), the result rotated back
-        uint32_t slot = 0;
+    const uint32_t x0 = rng;
+    rng = (p.jump_a * rng + p.jump_c) % 65535u;
+    if (n != 0) {
+        const uint32_t start_gene = __umulhi(xk_lcg(x0), p.kstart) % 8u;
+        const uint32_t *w = p.won + 32768u * n * (n - 1) + x0 * n;
+        uint32_t raw = 0, slot = 0;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const uint32_t genome = nr[k] * (((nr[k] & 510u) >> num_fit) & 1u);
-            if (genome > 0) {
-                gsm[slot][tid] = xk_rot18(genome, start_gene);
-                ++slot;
-            }
-        }
-        const uint32_t any_rot = xk_rot18(any, start_gene);
-        const uint32_t kn = p.kmul[n];
-        uint32_t num_active = 0, rot_genome = 0;
-#pragma unroll
-        for (int j = 0; j < 18; ++j) {
-            rng = xk_lcg(rng);
-            // winner < n for every state: the multiplier reproduces
-            // trunc(RN(u * n)) with u = x / 65535 < 1
-            const uint32_t winner = __umulhi(rng, kn);
-            uint32_t new_gene = (gsm[winner][tid] >> j) & 1u;
-            num_active += new_gene;
-            new_gene *= (uint32_t)(num_active <= p.max_genes);
-            uint32_t mutated = 0;
-            if (p.mutation) {
-                rng = xk_lcg(rng);
-                mutated = (uint32_t)((int32_t)rng <= p.mut_x) & ((any_rot >> j) & 1u);
-            }
-            rot_genome |= (new_gene ^ mutated) << j;
-        }
-        new_genome = xk_unrot18(rot_genome, start_gene);
+        for (int k = 0; k < 8; ++k)
+            if ((pmask >> k) & 1u) raw |= nr[k] & __ldg(w + slot++);
+        // the first max_genes genes taken, in visiting order (from
+        // start_gene, wrapping at 18): keep the lowest set bits of the
+        // rotated word
+        uint32_t rot = xk_rot18(raw, start_gene);
+        for (int e = __popc(rot) - (int)p.max_genes; e > 0; --e)
+            rot &= ~(0x80000000u >> __clz(rot));
+        new_genome = xk_unrot18(rot, start_gene);
+        if (p.mutation) new_genome ^= __ldg(p.mut + x0) & any;
     }
     rule = new_genome + rule * (uint32_t)(new_genome == 0);
     const uint32_t is_live = (uint32_t)(old_energy < 255u) &
@@ -337,6 +427,8 @@ cudaError_t xk_evolife_step(const uint64_t *src, uint64_t *dst, int32_t *col, co
     p.smooth = d.smooth;
     evo_draws(p, mut_thresh);
     evo_jump(p);
+    cudaError_t e = evo_tables(p, s);
+    if (e != cudaSuccess) return e;
     dim3 block(XK_EVO_BX, XK_EVO_BY);
     dim3 grid((p.W + XK_EVO_BX - 1) / XK_EVO_BX, (p.H + XK_EVO_BY - 1) / XK_EVO_BY);
     return xk_launch_pdl(xk_k_evolife, grid, block, 0, s, src, dst, col, p);

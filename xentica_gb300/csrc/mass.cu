@@ -698,18 +698,42 @@ xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict
     }
 }
 
-// column colour sums of a state (pitched rows; the sums are W * H, unpadded);
-// grid: x over a row's cells, y striding over the rows
-__global__ void xk_k_mass_project(const uint32_t *__restrict__ src, uint32_t *__restrict__ proj,
-                                  MassParams p)
+// column colour sums of a state (pitched rows; the sums are W * H, unpadded).
+// A CTA owns 32 columns of one row y: its 8 warps take every 8th plane each
+// (a warp reads 32 consecutive cells of a plane row, 128 bytes), four loads
+// in flight per thread, and the 8 partial sums of a column meet in shared
+// memory.  Integer sums, so the order of the additions does not matter.
+// grid: x over row chunks of 32, y striding over the rows
+#define XK_PROJ_ZS 8
+__global__ void __launch_bounds__(32 * XK_PROJ_ZS)
+xk_k_mass_project(const uint32_t *__restrict__ src, uint32_t *__restrict__ proj, MassParams p)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= p.W) return;
+    __shared__ uint32_t part[XK_PROJ_ZS][33];
+    const int x = blockIdx.x * 32 + threadIdx.x;
     const int64_t plane = (int64_t)p.P * p.H;
     for (int64_t y = blockIdx.y; y < p.H; y += gridDim.y) {
         uint32_t s = 0;
-        for (int z = 0; z < p.D; ++z) s += xk_mass_color(src[(int64_t)z * plane + y * p.P + x]);
-        proj[y * p.W + x] = s;
+        if (x < p.W) {
+            const uint32_t *col = src + y * p.P + x;
+            int z = threadIdx.y;
+            for (; z + 3 * XK_PROJ_ZS < p.D; z += 4 * XK_PROJ_ZS) {
+                const uint32_t a = __ldg(col + (int64_t)z * plane);
+                const uint32_t b = __ldg(col + (int64_t)(z + XK_PROJ_ZS) * plane);
+                const uint32_t c = __ldg(col + (int64_t)(z + 2 * XK_PROJ_ZS) * plane);
+                const uint32_t d = __ldg(col + (int64_t)(z + 3 * XK_PROJ_ZS) * plane);
+                s += xk_mass_color(a) + xk_mass_color(b) + xk_mass_color(c) + xk_mass_color(d);
+            }
+            for (; z < p.D; z += XK_PROJ_ZS) s += xk_mass_color(__ldg(col + (int64_t)z * plane));
+        }
+        part[threadIdx.y][threadIdx.x] = s;
+        __syncthreads();
+        if (threadIdx.y == 0 && x < p.W) {
+            uint32_t t = 0;
+#pragma unroll
+            for (int k = 0; k < XK_PROJ_ZS; ++k) t += part[k][threadIdx.x];
+            proj[y * p.W + x] = t;
+        }
+        __syncthreads();
     }
 }
 
@@ -892,7 +916,8 @@ cudaError_t xk_mass_project(const uint32_t *src, uint32_t *proj, const xk_desc &
 {
     const MassParams p = mass_params(d);
     const unsigned gy = (unsigned)(p.H < 65535 ? p.H : 65535);
-    xk_k_mass_project<<<dim3((unsigned)((p.W + 255) / 256), gy), 256, 0, s>>>(src, proj, p);
+    xk_k_mass_project<<<dim3((unsigned)((p.W + 31) / 32), gy), dim3(32, XK_PROJ_ZS), 0, s>>>(src, proj,
+                                                                                            p);
     return cudaGetLastError();
 }
 

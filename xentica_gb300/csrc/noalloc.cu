@@ -28,8 +28,6 @@
 //     anew and the old address is stale).
 #include <string.h>
 
-#include <cudaTypedefs.h>   // PFN_cuCtxGetCurrent, PFN_cuCtxGetId
-
 #include <algorithm>
 #include <mutex>
 
@@ -50,33 +48,6 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void *g_scratch_addr[kMaxDevices] = {nullptr};
 unsigned long long g_scratch_ctx[kMaxDevices] = {0};   // context id the address belongs to
-
-// identity of the context current on this thread (0 when it cannot be
-// told), through the runtime's driver entry points (no link to libcuda)
-unsigned long long current_context_id()
-{
-    static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
-    static PFN_cuCtxGetId_v12000 get_id = nullptr;
-    static bool looked_up = false;
-    if (!looked_up) {
-        void *f = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) ==
-                cudaSuccess && q == cudaDriverEntryPointSuccess)
-            get_current = (PFN_cuCtxGetCurrent_v4000)f;
-        f = nullptr;
-        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess && q == cudaDriverEntryPointSuccess)
-            get_id = (PFN_cuCtxGetId_v12000)f;
-        looked_up = true;
-    }
-    CUcontext ctx = nullptr;
-    unsigned long long id = 0;
-    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx ||
-        get_id(ctx, &id) != CUDA_SUCCESS)
-        return 0;
-    return id;
-}
 // host staging, reused by every call (guarded by g_mu)
 LifeInst g_inst[XK_NOALLOC_MAX_LATTICES];
 int g_order[XK_NOALLOC_MAX_LATTICES];
@@ -101,7 +72,7 @@ extern "C" int xk_batch_step_noalloc(uint8_t *d_cells, int32_t count, const int3
     XK_CUDA(cudaGetDevice(&dev));
     XK_REQUIRE(dev >= 0 && dev < kMaxDevices, XK_ERR_ARG, "device %d out of range", dev);
     XK_CUDA(cudaSetDevice(dev));   // makes the device's primary context current
-    const unsigned long long ctx = current_context_id();
+    const unsigned long long ctx = xk_context_id();
     if (!g_scratch_addr[dev] || ctx == 0 || ctx != g_scratch_ctx[dev]) {
         // once per device (and per context of it), with that device current:
         // the device address of the file-scope array (its name is only a

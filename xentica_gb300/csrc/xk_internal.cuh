@@ -103,6 +103,10 @@ struct LifeInst {
 int64_t xk_life_resident_words(int W, int H, int threads);
 // largest dynamic shared memory a CTA may use on this device
 int xk_max_smem_optin();
+// identity of the CUDA context current on this thread (unique for the
+// process's lifetime; 0 when it cannot be told): device-side objects cached
+// per context are looked up again after a context reset
+unsigned long long xk_context_id();
 // Raise a kernel's cudaFuncAttributeMaxDynamicSharedMemorySize (one value per
 // function and device) to at least `bytes`; never lowers it.  A graph node
 // keeps the shared memory of the launch it captured, and a node launched or
