@@ -667,7 +667,9 @@ static int step_prepare(xk_model *m, int64_t nsteps)
     return XK_OK;
 }
 
-static int step_enqueue(xk_model *m, int64_t first, int64_t count)
+// frame (EvoLife, count == 1 only): the generation's zoom-1 frame written by
+// the step kernel itself
+static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *frame = nullptr)
 {
     if (m->layout == LAYOUT_VM) {
         for (int64_t g = 0; g < count; ++g)
@@ -687,7 +689,7 @@ static int step_enqueue(xk_model *m, int64_t first, int64_t count)
     if (m->layout == LAYOUT_CELLS64) {
         for (int64_t g = 0; g < count; ++g) {
             XK_CUDA(xk_evolife_step(m->cells64[m->cur], m->cells64[1 - m->cur], m->col, m->d,
-                                    m->mut_thresh, m->stream));
+                                    m->mut_thresh, m->stream, frame, m->d.render_smooth));
             m->cur = 1 - m->cur;
         }
         return XK_OK;
@@ -782,6 +784,13 @@ static int render_enqueue(xk_model *m, void *img, bool bytes, int32_t width, int
 {
     if (m->layout == LAYOUT_MASS && m->d.proj_axis0 == 0 && m->d.proj_axis1 == 1 &&
         m->d.render_smooth == 0) {
+        if (bytes && !m->proj_valid && zoom == 1 && dx == 0 && dy == 0 && width == m->d.size[0] &&
+            height == m->d.size[1]) {
+            // the whole lattice at zoom 1: the projection writes the frame
+            XK_CUDA(xk_mass_project(m->cells32[m->cur], m->proj, m->d, m->stream, (uint8_t *)img));
+            m->proj_valid = 1;
+            return XK_OK;
+        }
         if (!m->proj_valid) {
             XK_CUDA(xk_mass_project(m->cells32[m->cur], m->proj, m->d, m->stream));
             m->proj_valid = 1;
@@ -841,21 +850,25 @@ extern "C" int xk_step_frames(xk_model *m, int64_t nsteps, int32_t width, int32_
             }
         }
     }
+    // EvoLife viewed whole at zoom 1: the step kernel writes the frame
+    const bool fused = m->layout == LAYOUT_CELLS64 && m->d.color_kind != XK_COLOR_NONE &&
+                       m->d.ndim == 2 && m->d.proj_axis0 == 0 && m->d.proj_axis1 == 1 && zoom == 1 &&
+                       dx == 0 && dy == 0 && width == m->d.size[0] && height == m->d.size[1];
     XK_CUDA(cudaEventRecord(m->ev0, m->stream));
     for (int64_t g = 0; g < nsteps; ++g) {
-        rc = step_enqueue(m, g, 1);
+        const int k = (int)(g % kFrameRing);
+        uint8_t *dst = frames_on_device ? frames + (size_t)g * fb : m->ring + (size_t)k * fb;
+        if (!frames_on_device && g >= kFrameRing)
+            XK_CUDA(cudaStreamWaitEvent(m->stream, m->copied[k], 0));
+        rc = step_enqueue(m, g, 1, fused ? dst : nullptr);
         if (rc != XK_OK) return rc;
         m->proj_valid = 0;
-        if (frames_on_device) {
-            rc = render_enqueue(m, frames + (size_t)g * fb, true, width, height, zoom, dx, dy);
+        if (!fused) {
+            rc = render_enqueue(m, dst, true, width, height, zoom, dx, dy);
             if (rc != XK_OK) return rc;
-            continue;
         }
-        const int k = (int)(g % kFrameRing);
-        uint8_t *slot = m->ring + (size_t)k * fb;
-        if (g >= kFrameRing) XK_CUDA(cudaStreamWaitEvent(m->stream, m->copied[k], 0));
-        rc = render_enqueue(m, slot, true, width, height, zoom, dx, dy);
-        if (rc != XK_OK) return rc;
+        if (frames_on_device) continue;
+        uint8_t *slot = dst;
         XK_CUDA(cudaEventRecord(m->rendered[k], m->stream));
         XK_CUDA(cudaStreamWaitEvent(m->copy_stream, m->rendered[k], 0));
         XK_CUDA(cudaMemcpyAsync(frames + (size_t)g * fb, slot, fb, cudaMemcpyDeviceToHost,

@@ -56,12 +56,13 @@ __device__ __forceinline__ int xk_ma_clamp(int v, int old, int fade_in, int fade
     return m > old - fade_out ? m : old - fade_out;
 }
 
-// hsv2rgb(hue, 1, 1) with deferred hue (tools/color.py:8-60) and the energy
-// weighting of EvoLife.color (evolife.py:431-444), modular genome colour
-__device__ __forceinline__ void xk_evo_color_modular(uint32_t rule, uint32_t energy, int *rgb)
+// hsv2rgb(hue, 1, 1) with deferred hue (tools/color.py:8-60) of the modular
+// genome colour's hue (rule >> 1) % 360: the float channels before EvoLife's
+// energy weighting
+__device__ __forceinline__ void xk_evo_hue_rgb(uint32_t hue, float *out)
 {
     float hue_f = 0.0f;
-    hue_f = __fadd_rn(hue_f, __fmul_rn(__fdiv_rn((float)((rule >> 1) % 360u), 360.0f), 6.0f));
+    hue_f = __fadd_rn(hue_f, __fmul_rn(__fdiv_rn((float)hue, 360.0f), 6.0f));
     uint32_t hue_i = 0;
     hue_i += xk_f2u(hue_f);
     hue_f = __fsub_rn(hue_f, (float)hue_i);
@@ -85,10 +86,32 @@ __device__ __forceinline__ void xk_evo_color_modular(uint32_t rule, uint32_t ene
     b = __fadd_rn(b, __fmul_rn((float)(hue_i == 2), grad_t));
     b = __fadd_rn(b, __fmul_rn((float)((hue_i == 3) | (hue_i == 4)), val));
     b = __fadd_rn(b, __fmul_rn((float)(hue_i == 5), grad_q));
+    out[0] = r;
+    out[1] = g;
+    out[2] = b;
+}
+
+// the 360 hues' channels, computed once per device context by the same
+// operations (xk_k_evo_hues) and read per cell
+__global__ void xk_k_evo_hues(float4 *__restrict__ hues)
+{
+    const uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= 360u) return;
+    float c[3];
+    xk_evo_hue_rgb(h, c);
+    hues[h] = make_float4(c[0], c[1], c[2], 0.0f);
+}
+
+// modular genome colour with the energy weighting of EvoLife.color
+// (evolife.py:431-444)
+__device__ __forceinline__ void xk_evo_color_modular(const float4 *__restrict__ hues, uint32_t rule,
+                                                     uint32_t energy, int *rgb)
+{
+    const float4 c = __ldg(hues + (rule >> 1) % 360u);
     const int e = (255 - (int)energy) * ((int)(rule > 0) * (int)(energy < 255));
-    rgb[0] = (int)xk_f2u(__fmul_rn(r, (float)e));
-    rgb[1] = (int)xk_f2u(__fmul_rn(g, (float)e));
-    rgb[2] = (int)xk_f2u(__fmul_rn(b, (float)e));
+    rgb[0] = (int)xk_f2u(__fmul_rn(c.x, (float)e));
+    rgb[1] = (int)xk_f2u(__fmul_rn(c.y, (float)e));
+    rgb[2] = (int)xk_f2u(__fmul_rn(c.z, (float)e));
 }
 
 // GenomeColor.positional (tools/color.py:63-104): double weights added into
@@ -137,6 +160,9 @@ struct EvoParams {
     uint32_t jump_a, jump_c;   // the crossover's RNG advances as one map x -> (a x + c) % 65535
     const uint32_t *won;       // won-gene masks: n masks per x0, blocks of 65536 x0 per n
     const uint32_t *mut;       // mutation flips per x0 (mutation only)
+    const float4 *hues;        // modular colour channels per hue
+    uint8_t *frame;            // null, or the W x H RendererPlain frame (zoom 1, no offset)
+    int32_t frame_smooth;      // its SMOOTH_FACTOR (0: none)
 };
 
 static float evo_u(uint32_t x) { return (float)x / 65535.0f; }
@@ -253,6 +279,7 @@ __global__ void xk_k_evo_mut(uint32_t *__restrict__ mut, int32_t mut_x, uint32_t
 
 namespace {
 struct EvoTables {
+    float4 *hues = nullptr;
     uint32_t *won[2] = {nullptr, nullptr};     // without / with mutation
     std::map<int32_t, uint32_t *> mut;        // per mut_x
 };
@@ -273,6 +300,16 @@ static cudaError_t evo_tables(EvoParams &p, cudaStream_t s)
     memcpy(d.kmul, p.kmul, sizeof(d.kmul));
     d.kstart = p.kstart;
     bool built = false;
+    if (!t.hues) {
+        if ((e = cudaMalloc(&t.hues, 360 * sizeof(float4))) != cudaSuccess) {
+            t.hues = nullptr;
+            return e;
+        }
+        xk_k_evo_hues<<<2, 192, 0, s>>>(t.hues);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        built = true;
+    }
+    p.hues = t.hues;
     uint32_t *&won = t.won[p.mutation ? 1 : 0];
     if (!won) {
         if ((e = cudaMalloc(&won, 65536u * 36u * sizeof(uint32_t))) != cudaSuccess) {
@@ -392,7 +429,7 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
     if (p.color_kind != XK_COLOR_NONE) {
         int rgb[3];
         if (p.positional) xk_evo_color_positional(rule, energy, rgb);
-        else xk_evo_color_modular(rule, energy, rgb);
+        else xk_evo_color_modular(p.hues, rule, energy, rgb);
         if (p.color_kind == XK_COLOR_MOVING_AVERAGE) {
 #pragma unroll
             for (int ch = 0; ch < 3; ++ch)
@@ -401,6 +438,17 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
         col[3 * i] = rgb[0];
         col[3 * i + 1] = rgb[1];
         col[3 * i + 2] = rgb[2];
+        if (p.frame) {
+            // the pixel of this cell as RendererPlain computes it at zoom 1
+            // (render.cu): the colour as a float, / SMOOTH_FACTOR, truncated,
+            // its low byte
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+                float v = (float)rgb[ch];
+                if (p.frame_smooth > 0) v = __fdiv_rn(v, (float)p.frame_smooth);
+                p.frame[3 * i + ch] = (uint8_t)(int)v;
+            }
+        }
     }
     dst[i] = ((uint64_t)energy & 511u) + (((uint64_t)rule & 262143u) << 9) +
              (((uint64_t)rng & 65535u) << 27);
@@ -412,7 +460,7 @@ cudaError_t xk_evolife_set_positional(const double *lut54)
 }
 
 cudaError_t xk_evolife_step(const uint64_t *src, uint64_t *dst, int32_t *col, const xk_desc &d,
-                            float mut_thresh, cudaStream_t s)
+                            float mut_thresh, cudaStream_t s, uint8_t *frame, int frame_smooth)
 {
     EvoParams p;
     p.W = (int32_t)d.size[0];
@@ -425,6 +473,8 @@ cudaError_t xk_evolife_step(const uint64_t *src, uint64_t *dst, int32_t *col, co
     p.fade_in = d.fade_in;
     p.fade_out = d.fade_out;
     p.smooth = d.smooth;
+    p.frame = frame;
+    p.frame_smooth = frame_smooth;
     evo_draws(p, mut_thresh);
     evo_jump(p);
     cudaError_t e = evo_tables(p, s);

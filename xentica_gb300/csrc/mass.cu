@@ -705,8 +705,11 @@ xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict
 // memory.  Integer sums, so the order of the additions does not matter.
 // grid: x over row chunks of 32, y striding over the rows
 #define XK_PROJ_ZS 8
+// frame: null, or the W x H frame of RendererPlain over axes (0, 1) at zoom 1
+// with no offset, written from the column sums as xk_k_mass_render does
 __global__ void __launch_bounds__(32 * XK_PROJ_ZS)
-xk_k_mass_project(const uint32_t *__restrict__ src, uint32_t *__restrict__ proj, MassParams p)
+xk_k_mass_project(const uint32_t *__restrict__ src, uint32_t *__restrict__ proj, MassParams p,
+                  uint8_t *__restrict__ frame)
 {
     __shared__ uint32_t part[XK_PROJ_ZS][33];
     const int x = blockIdx.x * 32 + threadIdx.x;
@@ -732,6 +735,13 @@ xk_k_mass_project(const uint32_t *__restrict__ src, uint32_t *__restrict__ proj,
 #pragma unroll
             for (int k = 0; k < XK_PROJ_ZS; ++k) t += part[k][threadIdx.x];
             proj[y * p.W + x] = t;
+            if (frame) {
+                const uint8_t v = (uint8_t)(int)__fdiv_rn((float)t, (float)p.D);
+                uint8_t *px = frame + 3 * (y * p.W + x);
+                px[0] = v;
+                px[1] = v;
+                px[2] = v;
+            }
         }
         __syncthreads();
     }
@@ -912,12 +922,13 @@ bool xk_mass_take_wait_failure()
     return v != 0;
 }
 
-cudaError_t xk_mass_project(const uint32_t *src, uint32_t *proj, const xk_desc &d, cudaStream_t s)
+cudaError_t xk_mass_project(const uint32_t *src, uint32_t *proj, const xk_desc &d, cudaStream_t s,
+                            uint8_t *frame)
 {
     const MassParams p = mass_params(d);
     const unsigned gy = (unsigned)(p.H < 65535 ? p.H : 65535);
     xk_k_mass_project<<<dim3((unsigned)((p.W + 31) / 32), gy), dim3(32, XK_PROJ_ZS), 0, s>>>(src, proj,
-                                                                                            p);
+                                                                                            p, frame);
     return cudaGetLastError();
 }
 

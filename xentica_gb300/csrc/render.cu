@@ -59,20 +59,62 @@ __global__ void xk_k_render(const int32_t *__restrict__ col, T *__restrict__ img
     img[3 * ip + 2] = (T)(int)vb;
 }
 
+// The same for a 2-D lattice viewed on axes (0, 1), where nothing is
+// projected: one cell per pixel, the sum over projected cells is the cell's
+// colour and the division by their number (1) is exact, as is the division
+// of a coordinate below 2^24 by a zoom of 1, so both are skipped; the rest
+// are the same operations.
+template <typename T>
+__global__ void xk_k_render2d(const int32_t *__restrict__ col, T *__restrict__ img, int w0, int w1,
+                              int smooth, int width, int height, int zoom, int dx, int dy)
+{
+    const int64_t ip = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ip >= (int64_t)width * height) return;
+    const unsigned i = (unsigned)ip;
+    const unsigned px = i % (unsigned)width, py = i / (unsigned)width;
+    int xa, xb;
+    if (zoom == 1) {
+        xa = (int)px + dx;
+        xb = (int)py + dy;
+    } else {
+        xa = (int)(__fdiv_rn((float)px, (float)zoom)) + dx;
+        xb = (int)(__fdiv_rn((float)py, (float)zoom)) + dy;
+    }
+    if (xa < 0) xa = w0 - (-xa % w0);
+    if (xa >= w0) xa = xa % w0;
+    if (xb < 0) xb = w1 - (-xb % w1);
+    if (xb >= w1) xb = xb % w1;
+    const int32_t *c = col + 3 * ((int64_t)xb * w0 + xa);
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+        float v = (float)__ldg(c + ch);
+        if (smooth > 0) v = __fdiv_rn(v, (float)smooth);
+        img[3 * ip + ch] = (T)(int)v;
+    }
+}
+
+template <typename T>
+static cudaError_t render_any(const int32_t *col, T *img, const RenderGeo &g, int width, int height,
+                              int zoom, int dx, int dy, cudaStream_t s)
+{
+    const int64_t n = (int64_t)width * height;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    if (g.ndim == 2 && g.a0 == 0 && g.a1 == 1 && (zoom != 1 || (width <= (1 << 24) && height <= (1 << 24))))
+        xk_k_render2d<T><<<blocks, 256, 0, s>>>(col, img, (int)g.size[0], (int)g.size[1], g.smooth, width,
+                                                height, zoom, dx, dy);
+    else
+        xk_k_render<T><<<blocks, 256, 0, s>>>(col, img, g, width, height, zoom, dx, dy);
+    return cudaGetLastError();
+}
+
 cudaError_t xk_render_colors(const int32_t *col, int32_t *img, const RenderGeo &g, int width,
                              int height, int zoom, int dx, int dy, cudaStream_t s)
 {
-    const int64_t n = (int64_t)width * height;
-    xk_k_render<int32_t><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(col, img, g, width, height,
-                                                                      zoom, dx, dy);
-    return cudaGetLastError();
+    return render_any<int32_t>(col, img, g, width, height, zoom, dx, dy, s);
 }
 
 cudaError_t xk_render_colors_u8(const int32_t *col, uint8_t *img, const RenderGeo &g, int width,
                                 int height, int zoom, int dx, int dy, cudaStream_t s)
 {
-    const int64_t n = (int64_t)width * height;
-    xk_k_render<uint8_t><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(col, img, g, width, height,
-                                                                      zoom, dx, dy);
-    return cudaGetLastError();
+    return render_any<uint8_t>(col, img, g, width, height, zoom, dx, dy, s);
 }

@@ -212,8 +212,12 @@ cudaError_t xk_vm_run(const xk_vm_ins *code, int ncode, const uint64_t *consts,
 
 // EvoLife family (evolife.cu)
 cudaError_t xk_evolife_set_positional(const double *lut54);
+// frame: null, or a W x H uint8 RGB frame written as RendererPlain renders the
+// new colours at zoom 1 with no offset (frame_smooth: its SMOOTH_FACTOR, 0
+// for none)
 cudaError_t xk_evolife_step(const uint64_t *src, uint64_t *dst, int32_t *col, const xk_desc &d,
-                            float mut_thresh, cudaStream_t s);
+                            float mut_thresh, cudaStream_t s, uint8_t *frame = nullptr,
+                            int frame_smooth = 0);
 
 // Programmatic dependent launch for kernels that run once per generation: the
 // launch may begin while the previous kernel in the stream finishes, and the
@@ -269,7 +273,10 @@ cudaError_t xk_mass_sum(const uint32_t *src, int64_t n, unsigned long long *out,
 // true when a mass-transfer CTA gave up waiting for a tensor copy since the
 // last call (the flag is cleared)
 bool xk_mass_take_wait_failure();
-cudaError_t xk_mass_project(const uint32_t *src, uint32_t *proj, const xk_desc &d, cudaStream_t s);
+// column colour sums over z; with `frame`, also the W x H RendererPlain frame
+// over axes (0, 1) at zoom 1, no offset, as uint8 RGB
+cudaError_t xk_mass_project(const uint32_t *src, uint32_t *proj, const xk_desc &d, cudaStream_t s,
+                            uint8_t *frame = nullptr);
 cudaError_t xk_mass_colors(const uint32_t *src, int32_t *col, const xk_desc &d, cudaStream_t s);
 cudaError_t xk_mass_render(const uint32_t *proj, int32_t *img, const xk_desc &d, int width,
                            int height, int zoom, int dx, int dy, cudaStream_t s);
