@@ -1,0 +1,79 @@
+"""GPU parity of the temporally blocked 2-D Life-like kernel (``life_tb.cu``).
+
+Lattices of many shapes -- widths not a multiple of 32, heights below one
+tile, several tiles across and down -- on a torus and with static borders of
+either state, stepped with every depth (generations per launch, forced with
+``XK_TB``) for generation counts that are not multiples of the depth, against
+the oracle; the tuned choice (no override) as well; and large requests of the
+serving loop at its default depth.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from tests.models import GameOfLife, GameOfLifeStatic, GOLExperiment2
+from xentica_gb300 import core
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(64, 64), (70, 9), (100, 75), (1000, 70), (1030, 130), (2049, 131), (97, 600)]
+
+
+def _model(shape, border):
+    if border == "torus":
+        cls = GameOfLife
+    else:
+        state = 1 if border == "static1" else 0
+
+        class Static(GameOfLife):
+            class Topology(GameOfLife.Topology):
+                border = core.StaticBorder(state)
+        cls = Static
+    exp = type("E", (GOLExperiment2, ), {"size": shape, "zoom": 1})
+    return cls(exp)
+
+
+def _run(shape, border, generations, seed):
+    model = _model(shape, border)
+    n = model.cells_num
+    rng = np.random.RandomState(seed)
+    cells = (rng.random_sample(n) < 0.4).astype(np.uint8)
+    model.gpu.load(cells, np.zeros(3 * n, np.int32))
+    model.gpu.step(generations)
+    got = model.gpu.arrays.cells.get()[:n]
+    kw = {} if border == "torus" else {"border": 1 if border == "static1" else 0}
+    topo = O.Topology(shape, **kw)
+    fld = topo.field(cells, np.uint8)
+    O.life_run(topo, fld, np.zeros(3 * n, np.int32), generations)
+    return got, fld[:n]
+
+
+@pytest.mark.parametrize("depth", [2, 3, 5, 8])
+@pytest.mark.parametrize("border", ["torus", "static0", "static1"])
+@pytest.mark.parametrize("shape", SHAPES, ids=["%dx%d" % s for s in SHAPES])
+def test_depth_matches_oracle(shape, border, depth, monkeypatch):
+    monkeypatch.setenv("XK_TB", str(depth))
+    got, want = _run(shape, border, 17, hash((shape, border, depth)) % 1000)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("shape", [(1500, 700), (4000, 300), (100, 75)])
+def test_tuned_choice_matches_oracle(shape):
+    got, want = _run(shape, "torus", 41, 7)
+    assert np.array_equal(got, want)
+
+
+def test_serving_large_requests_at_default_depth():
+    from xentica_gb300 import serve
+    rng = np.random.RandomState(3)
+    shapes = [(700, 1500), (130, 2049), (1100, 300)]
+    rules = [6152, int(rng.randint(0, 2 ** 18)), int(rng.randint(0, 2 ** 18))]
+    with serve.Server(1 << 30, host_bytes=64 << 20, quantum=20) as srv:
+        cells = [(rng.random_sample(s) < 0.35).astype(np.uint8) for s in shapes]
+        hs = [srv.submit("life2d", c, r, 53) for c, r in zip(cells, rules)]
+        for c, r, h, (hh, ww) in zip(cells, rules, hs, shapes):
+            topo = O.Topology((ww, hh))
+            fld = topo.field(c.ravel(), np.uint8)
+            O.life_run(topo, fld, np.zeros(topo.cells * 3, np.int32), 53, born=r & 511,
+                       sustain=r >> 9)
+            assert np.array_equal(h.result(timeout=120).ravel(), fld[:topo.cells])

@@ -150,6 +150,7 @@ struct xk_model {
     LifeInst *d_inst = nullptr;  // the lattice as a one-instance resident batch
     int resident = 0, res_threads = 0, res_smem = 0;
     int cl_tuned = 0, cl_C = 0, cl_R = 0, cl_threads = 0;   // cluster plan (cl_C = 0: none)
+    int tb_T = 0;                // temporally blocked global kernel: generations per launch (0: none)
     uint32_t rule0 = 0, rule1 = 0;
     int32_t lut[6] = {0, 0, 0, 0, 0, 0};
     uint8_t *fld = nullptr;      // interpreter: the reference's N + 1 planes
@@ -226,6 +227,14 @@ static int tune_cluster(xk_model *m)
 {
     m->cl_tuned = 1;
     m->cl_C = 0;
+    m->tb_T = 0;
+    const char *tenv = getenv("XK_TB");
+    if (tenv && tenv[0]) {
+        // a fixed temporal-blocking depth (1: the per-generation kernel)
+        const int T = atoi(tenv);
+        if (T >= 2 && T <= 8 && xk_life_tb_supported(m->lg)) m->tb_T = T;
+        return XK_OK;
+    }
     const char *env = getenv("XK_CLUSTER");
     if (env && env[0]) {
         const int want = atoi(env);
@@ -252,6 +261,38 @@ static int tune_cluster(xk_model *m)
         XK_CUDA(cudaEventSynchronize(m->ev1));
         XK_CUDA(cudaEventElapsedTime(&best, m->ev0, m->ev1));
     }
+    if (xk_life_tb_supported(m->lg)) {
+        // temporal blocking, 2..8 generations per launch, ping-pong through
+        // a temporary partner of the scratch copy
+        uint32_t *tmp = nullptr;
+        XK_CUDA(cudaMalloc(&tmp, bytes));
+        const LifeTable9 t9 = xk_life_table9(m->rule0, m->rule1);
+        cudaError_t e = cudaSuccess;
+        const LifeTable t = xk_life_table(m->rule0, m->rule1);
+        // depth 1: the per-generation kernel, what runs when no plan is kept
+        static const int depths[] = {1, 2, 4, 8};
+        for (int T : depths) {
+            if (T == 1 && m->resident) continue;
+            float ms = 0.f;
+            uint32_t *a = scratch, *b = tmp;
+            e = cudaEventRecord(m->ev0, m->stream);
+            for (int g = 0; g < G && e == cudaSuccess; g += T) {
+                e = T == 1 ? xk_life_step_global(a, b, m->lg, t, m->stream)
+                           : xk_life_step_tb(a, b, m->lg, t9, T, m->stream);
+                std::swap(a, b);
+            }
+            if (e == cudaSuccess) e = cudaEventRecord(m->ev1, m->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(m->ev1);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, m->ev0, m->ev1);
+            if (e != cudaSuccess) break;
+            if (ms < best) {
+                best = ms;
+                m->tb_T = T == 1 ? 0 : T;
+            }
+        }
+        cudaFree(tmp);
+        XK_CUDA(e);
+    }
     static const int cand[] = {16, 8, 4, 2};
     static const int bands[] = {1, 2, 4};
     for (int k = 0; k < 12; ++k) {
@@ -269,6 +310,7 @@ static int tune_cluster(xk_model *m)
             m->cl_C = C;
             m->cl_R = R;
             m->cl_threads = th;
+            m->tb_T = 0;
         }
     }
     return XK_OK;
@@ -704,6 +746,17 @@ static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *fram
             XK_CUDA(xk_life_step_cluster(m->bits[m->cur], m->lg, m->rule0, m->rule1, g, m->cl_C, m->cl_R,
                                          m->cl_threads, m->stream));
             left -= g;
+        }
+    } else if (m->layout == LAYOUT_BITS2D && colors_free && m->tb_T > 1) {
+        // temporal blocking: launches of tb_T generations, the rest in one
+        // shorter launch; ping-pong between the two word buffers
+        const LifeTable9 t9 = xk_life_table9(m->rule0, m->rule1);
+        int64_t left = count;
+        while (left > 0) {
+            const int T = (int)(left >= m->tb_T ? m->tb_T : left);
+            XK_CUDA(xk_life_step_tb(m->bits[m->cur], m->bits[1 - m->cur], m->lg, t9, T, m->stream));
+            m->cur = 1 - m->cur;
+            left -= T;
         }
     } else if (m->layout == LAYOUT_BITS2D && m->resident && colors_free) {
         // whole lattice in shared memory; long runs are cut into launches of

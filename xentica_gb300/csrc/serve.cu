@@ -76,6 +76,8 @@ struct Req {
     LifeGeo lg;                // bit-packed rows (3-D: H * D rows)
     Life3Geo g3;
     LifeTable lt;
+    LifeTable9 lt9;
+    int tb_T = 0;              // global2d: generations per temporally blocked launch (0: one per launch)
     xk_desc md;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};   // full round from buffer 0 / 1
     uint32_t rule0 = 0, rule1 = 0;
@@ -154,6 +156,7 @@ struct xk_server {
     int64_t budget = 0, host_bytes = 0;
     int max_active = 0;
     int64_t quantum = 0;
+    int tb_depth = 8;          // generations per launch of large 2-D requests (XK_SERVE_TB)
     int64_t resident_max = 1 << 18;
     uint8_t *dev_base = nullptr;
     uint8_t *host_base = nullptr;
@@ -273,6 +276,8 @@ static int admit(xk_server *s, Req *q, bool *admitted)
             q->path = PATH_GLOBAL2D;
             q->lg = xk_life_geo(r.size[0], r.size[1], 1, 0);
             q->lt = xk_life_table(q->rule0, q->rule1);
+            q->lt9 = xk_life_table9(q->rule0, q->rule1);
+            q->tb_T = xk_life_tb_supported(q->lg) ? s->tb_depth : 0;
             uint32_t *w0 = (uint32_t *)(base + rnd(q->n + 16));
             XK_CUDA(xk_life_pack(base, 1, w0, q->lg, q->stream));
             s->st.launches++;
@@ -330,6 +335,16 @@ static int enqueue_round(xk_server *s, Req *q, int64_t chunk)
         uint32_t *w[2];
         w[0] = (uint32_t *)(base + rnd(q->n + 16));
         w[1] = (uint32_t *)((uint8_t *)w[0] + rnd((int64_t)q->lg.wpr * q->lg.H * 4));
+        if (q->path == PATH_GLOBAL2D && q->tb_T > 1) {
+            // temporal blocking: tb_T generations per launch
+            for (int64_t g = 0; g < chunk;) {
+                const int T = (int)std::min<int64_t>(q->tb_T, chunk - g);
+                XK_CUDA(xk_life_step_tb(w[q->cur], w[1 - q->cur], q->lg, q->lt9, T, q->stream));
+                q->cur ^= 1;
+                g += T;
+            }
+            return XK_OK;
+        }
         for (int64_t g = 0; g < chunk; ++g) {
             if (q->path == PATH_GLOBAL2D)
                 XK_CUDA(xk_life_step_global(w[q->cur], w[1 - q->cur], q->lg, q->lt, q->stream));
@@ -651,6 +666,10 @@ extern "C" int xk_serve_create(int64_t budget_bytes, int64_t host_bytes, int32_t
     s->host_bytes = host_bytes;
     s->max_active = max_active;
     s->quantum = quantum;
+    if (const char *e = getenv("XK_SERVE_TB")) {
+        const int T = atoi(e);
+        s->tb_depth = T >= 2 && T <= 8 ? T : 0;
+    }
     if (const char *e = getenv("XK_SERVE_RESIDENT_MAX")) s->resident_max = atoll(e);
     cudaError_t e;
     if ((e = cudaGetDevice(&s->device)) != cudaSuccess ||

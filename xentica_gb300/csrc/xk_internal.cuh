@@ -164,6 +164,12 @@ int xk_life_cluster_config(const LifeGeo &g, int C, int band, int *C_out, int *R
 cudaError_t xk_life_step_cluster(uint32_t *bits, const LifeGeo &g, uint32_t rule0, uint32_t rule1,
                                  int generations, int C, int R, int threads, cudaStream_t s);
 
+// T (1..8) generations per launch of a 2-D lattice of any size (W >= 64),
+// tiles with a T-generation halo in shared memory, src -> dst (life_tb.cu)
+int xk_life_tb_supported(const LifeGeo &g);
+cudaError_t xk_life_step_tb(const uint32_t *src, uint32_t *dst, const LifeGeo &g, const LifeTable9 &t,
+                            int T, cudaStream_t s);
+
 // byte-per-cell lattices (N-D, any neighbourhood; and the plain 2-D form)
 struct NdGeo {
     int32_t ndim, nbr, torus;
