@@ -124,6 +124,18 @@ int xk_render(xk_model *m, int32_t *host_img, int32_t width, int32_t height,
 int xk_step_frames(xk_model *m, int64_t nsteps, int32_t width, int32_t height, int32_t zoom,
                    int32_t dx, int32_t dy, uint8_t *frames, int32_t frames_on_device);
 
+/* Launch plan of a 2-D Life-like model whose colours follow from its state:
+ * which kernel family runs its multi-generation steps, chosen by timing on
+ * the first step (or by xk_model_plan before it).  The reference has one
+ * kernel shape for every model (base.py:254-283); these exist so that a host
+ * can cache the choice per device, library build and lattice and re-apply it
+ * without timing.  plan[0]: XK_PLAN_*; CLUSTER: plan[1] = CTAs asked for
+ * (1..16), plan[2] = rows per lane group; TEMPORAL: plan[3] = generations per
+ * launch (2..8).  xk_model_plan gives kind -1 for models without plans. */
+enum { XK_PLAN_GLOBAL = 0, XK_PLAN_RESIDENT = 1, XK_PLAN_CLUSTER = 2, XK_PLAN_TEMPORAL = 3 };
+int xk_model_plan(xk_model *m, int32_t plan[4]);
+int xk_model_set_plan(xk_model *m, const int32_t plan[4]);
+
 /* Mass family: total mass after each of the last xk_step's generations
  * (count = that nsteps); the invariant the configuration checks. */
 int xk_mass_totals(xk_model *m, uint64_t *host_totals, int64_t count);

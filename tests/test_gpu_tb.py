@@ -77,3 +77,56 @@ def test_serving_large_requests_at_default_depth():
             O.life_run(topo, fld, np.zeros(topo.cells * 3, np.int32), 53, born=r & 511,
                        sustain=r >> 9)
             assert np.array_equal(h.result(timeout=120).ravel(), fld[:topo.cells])
+
+
+PLANS = {(512, 512): [[1, 0, 0, 0], [2, 16, 2, 0], [2, 4, 1, 0], [2, 8, 4, 0], [3, 0, 0, 2],
+                      [3, 0, 0, 8]],
+         (2049, 131): [[0, 0, 0, 0], [3, 0, 0, 4], [3, 0, 0, 7]]}
+
+
+@pytest.mark.parametrize("shape", list(PLANS), ids=["%dx%d" % s for s in PLANS])
+def test_every_plan_kind_matches_oracle(shape):
+    """Each launch plan the tuner can choose or the cache can re-apply
+    (xk_model_set_plan): resident CTA, clusters of several sizes and bands,
+    temporal blocking of several depths, the per-generation kernel -- the same
+    cells as the oracle; plans that do not fit the lattice are refused."""
+    import ctypes
+    from xentica_gb300 import _native as nat
+    for plan in PLANS[shape]:
+        model = _model(shape, "torus")
+        n = model.cells_num
+        cells = (np.random.RandomState(sum(plan)).random_sample(n) < 0.4).astype(np.uint8)
+        model.gpu.load(cells, np.zeros(3 * n, np.int32))
+        model.gpu._ensure()
+        model.gpu._planned = True          # no tuning: the plan under test
+        arr = (ctypes.c_int32 * 4)(*plan)
+        nat.check(model.gpu._lib.xk_model_set_plan(model.gpu._handle, arr), "xk_model_set_plan")
+        out = (ctypes.c_int32 * 4)()
+        nat.check(model.gpu._lib.xk_model_plan(model.gpu._handle, out), "xk_model_plan")
+        assert list(out) == plan
+        model.gpu.step(29)
+        topo = O.Topology(shape)
+        fld = topo.field(cells, np.uint8)
+        O.life_run(topo, fld, np.zeros(3 * n, np.int32), 29)
+        assert np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n]), "plan %s" % plan
+    bad = {(512, 512): [[0, 0, 0, 0], [3, 0, 0, 9], [2, 17, 1, 0], [5, 0, 0, 0]],
+           (2049, 131): [[1, 0, 0, 0], [2, 4, 1, 0], [3, 0, 0, 1]]}[shape]
+    model = _model(shape, "torus")
+    model.gpu._ensure()
+    for plan in bad:
+        arr = (ctypes.c_int32 * 4)(*plan)
+        assert model.gpu._lib.xk_model_set_plan(model.gpu._handle, arr) != 0, plan
+
+
+def test_plan_cache_round_trip(monkeypatch, tmp_path):
+    """A model's tuned plan is stored; a second model of the same lattice
+    takes it from the cache and steps to the oracle's cells."""
+    monkeypatch.setenv("XK_TUNE_CACHE", str(tmp_path / "tune.json"))
+    shape = (1500, 700)
+    first = _model(shape, "torus")
+    first.gpu.step(1)
+    import json
+    stored = list(json.loads((tmp_path / "tune.json").read_text()).values())
+    assert stored == [first.gpu.plan]
+    got, want = _run(shape, "torus", 23, 5)
+    assert np.array_equal(got, want)

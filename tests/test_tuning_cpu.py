@@ -125,3 +125,64 @@ def test_unidentifiable_library_tunes_without_cache(monkeypatch, tmp_path):
     lib = FakeLib(best=8)
     assert tuning.tuned_band(lib, None, W, H, 256) == 8
     assert lib.tuned == [256] and not (tmp_path / "t.json").exists()
+
+
+class FakePlanLib(FakeLib):
+    """Records the plan calls a 2-D Life-like model handle would get."""
+
+    def __init__(self, plan=(2, 16, 2, 0), **kw):
+        super().__init__(**kw)
+        self.plan, self.timed, self.applied = list(plan), 0, []
+
+    def xk_model_plan(self, handle, out):
+        self.timed += 1
+        out[:] = self.plan
+        return 0
+
+    def xk_model_set_plan(self, handle, plan):
+        self.applied.append(list(plan))
+        return 0
+
+
+@pytest.mark.parametrize("plan", [(0, 0, 0, 0), (1, 0, 0, 0), (2, 16, 2, 0), (3, 0, 0, 8)],
+                         ids=["global", "resident", "cluster", "temporal"])
+def test_lattice_plan_stored_then_applied(monkeypatch, tmp_path, plan):
+    """Every kind of plan: a miss times (xk_model_plan) and stores it, a hit
+    re-applies it (xk_model_set_plan) without timing, and the key separates
+    sizes, borders, devices and library builds."""
+    monkeypatch.setenv("XK_TUNE_CACHE", str(tmp_path / "t.json"))
+    lib = FakePlanLib(plan=plan)
+    assert tuning.lattice_plan(lib, None, 512, 512, "torus", library="L") == list(plan)
+    assert lib.timed == 1 and lib.applied == []
+    lib.plan = [0, 0, 0, 0]                        # a new timing would disagree
+    assert tuning.lattice_plan(lib, None, 512, 512, "torus", library="L") == list(plan)
+    assert lib.timed == 1 and lib.applied == [list(plan)]
+    for args in [(512, 256, "torus", "L"), (512, 512, "static1", "L"), (512, 512, "torus", "L2")]:
+        assert tuning.lattice_plan(lib, None, args[0], args[1], args[2], library=args[3]) == [0] * 4
+    other = FakePlanLib(device=b"another device", plan=(3, 0, 0, 4))
+    assert tuning.lattice_plan(other, None, 512, 512, "torus", library="L") == [3, 0, 0, 4]
+    assert lib.timed == 4 and other.timed == 1
+
+
+def test_lattice_plan_rejected_or_invalid_entries_retime(monkeypatch, tmp_path):
+    path = tmp_path / "t.json"
+    monkeypatch.setenv("XK_TUNE_CACHE", str(path))
+    key = tuning.lattice_key(FakeLib().device.decode(), "L", 300, 200, "torus")
+    for bad in ([9, 0, 0, 0], [1, 2], "x", [True, 0, 0, 0]):
+        path.write_text(json.dumps({key: bad}))
+        lib = FakePlanLib(plan=(3, 0, 0, 2))
+        assert tuning.lattice_plan(lib, None, 300, 200, "torus", library="L") == [3, 0, 0, 2]
+        assert lib.timed == 1 and lib.applied == []
+    # a stored plan the library refuses (e.g. a size it no longer supports)
+    path.write_text(json.dumps({key: [2, 16, 1, 0]}))
+    lib = FakePlanLib(plan=(1, 0, 0, 0))
+    lib.xk_model_set_plan = lambda handle, plan: -1
+    assert tuning.lattice_plan(lib, None, 300, 200, "torus", library="L") == [1, 0, 0, 0]
+    assert json.loads(path.read_text())[key] == [1, 0, 0, 0]
+
+
+def test_models_without_plans(monkeypatch, tmp_path):
+    monkeypatch.setenv("XK_TUNE_CACHE", str(tmp_path / "t.json"))
+    lib = FakePlanLib(plan=(-1, 0, 0, 0))
+    assert tuning.lattice_plan(lib, None, 50, 30, "torus", library="L") is None
+    assert not (tmp_path / "t.json").exists()

@@ -88,6 +88,8 @@ SIGNATURES = {
     "xk_step": (_I32, [_P, _I64]),
     "xk_render": (_I32, [_P, _P, _I32, _I32, _I32, _I32, _I32]),
     "xk_step_frames": (_I32, [_P, _I64, _I32, _I32, _I32, _I32, _I32, _P, _I32]),
+    "xk_model_plan": (_I32, [_P, _P]),
+    "xk_model_set_plan": (_I32, [_P, _P]),
     "xk_mass_totals": (_I32, [_P, _P, _I64]),
     "xk_sync": (_I32, [_P]),
     "xk_last_step_ms": (ctypes.c_double, []),

@@ -122,10 +122,30 @@ class GPU:
         self._rule = (rule0, rule1, list(lut))
 
     # -- operations used by CellularAutomaton -------------------------------
+    def _plan(self):
+        """Launch plan of a 2-D Life-like lattice: from the tuning cache, or
+        timed and stored there (once per model)."""
+        if getattr(self, "_planned", False):
+            return
+        self._planned = True
+        topo = self.model.topology
+        if topo.dimensions != 2 or not hasattr(self.template, "history_free"):
+            return
+        border = topo.border
+        if isinstance(border, __import__("xentica_gb300.core.topology.border",
+                                         fromlist=["TorusBorder"]).TorusBorder):
+            kind = "torus"
+        else:
+            kind = "static%d" % int(getattr(border, "value", 0) or 0)
+        from xentica_gb300 import tuning
+        self.plan = tuning.lattice_plan(self._lib, self._handle, self.model.size[0],
+                                        self.model.size[1], kind)
+
     def step(self, nsteps=1):
         """Advance ``nsteps`` generations with the current parameter values."""
         self._ensure()
         self._bind_params()
+        self._plan()
         nat.check(self._lib.xk_step(self._handle, int(nsteps)), "xk_step")
 
     def render(self, width, height, zoom, dx, dy):

@@ -150,6 +150,7 @@ struct xk_model {
     LifeInst *d_inst = nullptr;  // the lattice as a one-instance resident batch
     int resident = 0, res_threads = 0, res_smem = 0;
     int cl_tuned = 0, cl_C = 0, cl_R = 0, cl_threads = 0;   // cluster plan (cl_C = 0: none)
+    int cl_want = 0, cl_band = 0;    // the cluster size and band length the plan was made from
     int tb_T = 0;                // temporally blocked global kernel: generations per launch (0: none)
     uint32_t rule0 = 0, rule1 = 0;
     int32_t lut[6] = {0, 0, 0, 0, 0, 0};
@@ -245,6 +246,8 @@ static int tune_cluster(xk_model *m)
             m->cl_C = C;
             m->cl_R = R;
             m->cl_threads = th;
+            m->cl_want = want;
+            m->cl_band = band;
         }
         return XK_OK;
     }
@@ -310,6 +313,8 @@ static int tune_cluster(xk_model *m)
             m->cl_C = C;
             m->cl_R = R;
             m->cl_threads = th;
+            m->cl_want = want;
+            m->cl_band = band;
             m->tb_T = 0;
         }
     }
@@ -610,6 +615,9 @@ extern "C" int xk_upload_colors(xk_model *m, const int32_t *host_col, int64_t nc
 {
     XK_REQUIRE(m && host_col, XK_ERR_ARG, "xk_upload_colors: null argument");
     XK_REQUIRE(ncells == m->n, XK_ERR_ARG, "xk_upload_colors: cell count mismatch");
+    // mass transfer: the colour is a function of the state, recomputed from
+    // it whenever it is read, so uploaded colours would never be seen
+    if (m->layout == LAYOUT_MASS) return XK_OK;
     XK_CUDA(cudaMemcpyAsync(m->col, host_col, (size_t)m->n * 3 * sizeof(int32_t),
                             cudaMemcpyHostToDevice, m->stream));
     XK_CUDA(cudaStreamSynchronize(m->stream));
@@ -828,6 +836,80 @@ extern "C" int xk_step(xk_model *m, int64_t nsteps)
     XK_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
     xk_set_last_step_ms(ms);
     return step_finish(m, nsteps);
+}
+
+// ---------------------------------------------------------------------------
+// launch plans of 2-D Life-like models (the autotuner's choice), for a cache
+
+static bool plan_applies(const xk_model *m)
+{
+    return m->layout == LAYOUT_BITS2D && colors_free_of(m);
+}
+
+extern "C" int xk_model_plan(xk_model *m, int32_t plan[4])
+{
+    XK_REQUIRE(m && plan, XK_ERR_ARG, "xk_model_plan: null argument");
+    XK_REQUIRE(m->uploaded, XK_ERR_STATE, "xk_model_plan before xk_upload");
+    if (!plan_applies(m)) {
+        plan[0] = -1;
+        plan[1] = plan[2] = plan[3] = 0;
+        return XK_OK;
+    }
+    if (!m->cl_tuned) {
+        int rc = tune_cluster(m);
+        if (rc != XK_OK) return rc;
+    }
+    if (m->cl_C) {
+        plan[0] = XK_PLAN_CLUSTER;
+        plan[1] = m->cl_want;
+        plan[2] = m->cl_band;
+        plan[3] = 0;
+    } else if (m->tb_T > 1) {
+        plan[0] = XK_PLAN_TEMPORAL;
+        plan[1] = plan[2] = 0;
+        plan[3] = m->tb_T;
+    } else {
+        plan[0] = m->resident ? XK_PLAN_RESIDENT : XK_PLAN_GLOBAL;
+        plan[1] = plan[2] = plan[3] = 0;
+    }
+    return XK_OK;
+}
+
+extern "C" int xk_model_set_plan(xk_model *m, const int32_t plan[4])
+{
+    XK_REQUIRE(m && plan, XK_ERR_ARG, "xk_model_set_plan: null argument");
+    XK_REQUIRE(plan_applies(m), XK_ERR_STATE,
+               "xk_model_set_plan: only 2-D Life-like models with colours implied by the state "
+               "have launch plans");
+    int C = 0, R = 0, th = 0;
+    switch (plan[0]) {
+    case XK_PLAN_GLOBAL:
+        XK_REQUIRE(!m->resident, XK_ERR_ARG, "xk_model_set_plan: this lattice fits one CTA");
+        break;
+    case XK_PLAN_RESIDENT:
+        XK_REQUIRE(m->resident, XK_ERR_ARG, "xk_model_set_plan: the lattice does not fit one CTA");
+        break;
+    case XK_PLAN_CLUSTER:
+        XK_REQUIRE(plan[1] >= 1 && plan[1] <= 16 && plan[2] >= 1 &&
+                       xk_life_cluster_config(m->lg, plan[1], plan[2], &C, &R, &th),
+                   XK_ERR_ARG, "xk_model_set_plan: no cluster of %d CTAs with bands of %d rows",
+                   plan[1], plan[2]);
+        break;
+    case XK_PLAN_TEMPORAL:
+        XK_REQUIRE(plan[3] >= 2 && plan[3] <= 8 && xk_life_tb_supported(m->lg), XK_ERR_ARG,
+                   "xk_model_set_plan: temporal depth %d (2..8, width >= 64)", plan[3]);
+        break;
+    default:
+        XK_REQUIRE(false, XK_ERR_ARG, "xk_model_set_plan: unknown plan kind %d", plan[0]);
+    }
+    m->cl_tuned = 1;
+    m->cl_C = C;
+    m->cl_R = R;
+    m->cl_threads = th;
+    m->cl_want = plan[0] == XK_PLAN_CLUSTER ? plan[1] : 0;
+    m->cl_band = plan[0] == XK_PLAN_CLUSTER ? plan[2] : 0;
+    m->tb_T = plan[0] == XK_PLAN_TEMPORAL ? plan[3] : 0;
+    return XK_OK;
 }
 
 // RendererPlain of the current state into `img` (int32 or the uint8 frame),

@@ -1,18 +1,31 @@
 """Persistent cache of autotuned launch choices.
 
-The ensemble's autotuner (``xk_batch_tune``) times the resident kernel for
-several band lengths and keeps the fastest.  Its choice depends on the device,
-on the kernels in ``libxk.so`` and on the workload, so a choice is stored in a
-JSON file under a key made of
+Two choices are timed on the device and cached:
+
+* the ensemble's band length (``xk_batch_tune`` times the resident kernel for
+  several band lengths and keeps the fastest), re-applied with
+  ``xk_batch_set_band``;
+* a single 2-D Life-like lattice's launch plan (``xk_model_plan``: the
+  kernel family -- per-generation global kernel, one resident CTA, a
+  thread-block cluster of a size and band length, or temporal blocking of a
+  depth -- timed on the model's first step), re-applied with
+  ``xk_model_set_plan``.
+
+A choice depends on the device, on the kernels in ``libxk.so`` and on the
+workload, so it is stored in a JSON file under a key made of
 
 * the device (``xk_device_info``: name, compute capability, SM count, shared
   memory per block),
 * the library build (SHA-1 of ``libxk.so``; any rebuild with changed kernels
   changes it),
-* the workload (SHA-1 of the lattice sizes and the generations per step),
+* the workload: for an ensemble the SHA-1 of the lattice sizes and the
+  generations per step; for a lattice its size and border (torus, or static
+  with its state).  The rule is not part of the key: every Life-like kernel
+  evaluates the rule through the same multiplexer over a table loaded at run
+  time, so its instruction stream and cost are the same for every rule.
 
-and a later tune of the same workload on the same device and library applies
-it with ``xk_batch_set_band`` instead of timing again.  The file is
+A later tune of the same workload on the same device and library applies the
+stored choice instead of timing again.  The file is
 ``$XK_TUNE_CACHE``, else ``$XDG_CACHE_HOME/xentica_gb300/tune.json`` (default
 ``~/.cache``); ``XK_TUNE_CACHE=off`` disables the cache.  Writes replace the
 file atomically; concurrent writers can lose each other's newest entry, never
@@ -126,3 +139,50 @@ def tuned_band(lib, handle, widths, heights, generations, cache=True, library=No
         except OSError:
             pass   # a read-only cache location only costs the next tuning run
     return int(chosen.value)
+
+
+PLAN_KINDS = {0: "global", 1: "resident", 2: "cluster", 3: "temporal"}
+
+
+def lattice_key(device, library, width, height, border):
+    """Cache key of a 2-D lattice's launch plan; ``border`` is "torus" or
+    "static0" / "static1"."""
+    return "life2d_plan|%s|%s|%dx%d|%s" % (device, library, int(width), int(height), border)
+
+
+def _valid_plan(hit):
+    return (isinstance(hit, list) and len(hit) == 4 and
+            all(isinstance(v, int) and not isinstance(v, bool) for v in hit) and hit[0] in PLAN_KINDS)
+
+
+def lattice_plan(lib, handle, width, height, border, cache=True, library=None):
+    """The launch plan of a 2-D Life-like model: from the cache when present
+    (applied with ``xk_model_set_plan``), else the one ``xk_model_plan``
+    times, stored.  Returns the plan (4 ints) or None for models without
+    plans."""
+    path = cache_path() if cache else None
+    store = key = None
+    if path is not None:
+        try:
+            lib_id = library if library is not None else library_id()
+        except OSError:
+            path = None
+    plan = (ctypes.c_int32 * 4)()
+    if path is not None:
+        key = lattice_key(device_id(lib), lib_id, width, height, border)
+        store = TuneCache(path)
+        hit = store.get(key)
+        if _valid_plan(hit):
+            plan[:] = hit
+            if lib.xk_model_set_plan(handle, plan) == 0:
+                return list(hit)
+    nat.check(lib.xk_model_plan(handle, plan), "xk_model_plan")
+    chosen = [int(v) for v in plan]
+    if chosen[0] < 0:
+        return None
+    if store is not None:
+        try:
+            store.put(key, chosen)
+        except OSError:
+            pass
+    return chosen
