@@ -70,11 +70,12 @@ def parse():
     ap.add_argument("--quantum", type=int, default=128, help="serve: generations per round")
     ap.add_argument("--sweep", default="", help="serve: extra offered loads after the main run, "
                                                 "comma-separated (e.g. 0.3,0.5,0.9)")
-    ap.add_argument("--extras", default="life512,evolife,mass,serve",
+    ap.add_argument("--extras", default="life512,evolife,mass,serve,sands",
                     help="default run: the other configurations measured after the ensemble "
                          "(comma-separated, or 'none')")
     ap.add_argument("--serve-budget-gb", type=int, default=16, help="serve: HBM budget (GiB)")
-    ap.add_argument("--workload", choices=("ensemble", "life512", "evolife", "mass", "serve"),
+    ap.add_argument("--workload", choices=("ensemble", "life512", "evolife", "mass", "serve",
+                                           "sands"),
                     default="ensemble",
                     help="ensemble: the batched Life-like ensemble (default); life512: Conway's "
                          "Life 512x512 torus, 1000 generations per step; evolife: EvoLife "
@@ -490,9 +491,9 @@ def run_ours(args, dist):
         small.cpu_seconds = 4.0
         for name in extras:
             fn = {"life512": life512_line, "evolife": evolife_line, "mass": mass_line,
-                  "serve": serve_line}[name]
+                  "serve": serve_line, "sands": sands_line}[name]
             steps, warmup = {"life512": (10, 3), "evolife": (5, 3), "mass": (5, 3),
-                             "serve": (None, 3)}[name]
+                             "serve": (None, 3), "sands": (10, 3)}[name]
             small.steps, small.warmup = steps, warmup
             if name == "serve" and not small.sweep:
                 small.sweep = "0.3,0.5,0.9"
@@ -911,6 +912,164 @@ def life512_line(args, dist):
     return None
 
 
+def sands_model(template=None):
+    """ShiftingSands as the reference's examples/shifting_sands.py:15-47
+    writes it, on a 1920x1080 torus seeded Bernoulli(0.5); ``template="vm"``
+    builds it on the generic interpreter instead of its fused family."""
+    from xentica_gb300 import core, seeds
+    from xentica_gb300.core import color_effects
+
+    class ShiftingSands(core.CellularAutomaton):
+        state = core.IntegerProperty(max_val=1)
+
+        class Topology:
+            dimensions = 2
+            lattice = core.OrthogonalLattice()
+            neighborhood = core.MooreNeighborhood()
+            border = core.TorusBorder()
+
+        def emit(self):
+            for i, buf in enumerate(self.buffers):
+                if i == 0:
+                    buf.state = self.main.state
+                else:
+                    buf.state = 0
+
+        def absorb(self):
+            new_val = core.IntegerVariable()
+            for i in range(len(self.buffers)):
+                new_val += self.neighbors[i].buffer.state
+            self.main.state = new_val
+
+        @color_effects.MovingAverage
+        def color(self):
+            return (self.main.state * 255, self.main.state * 255, self.main.state * 255)
+
+    class Sands(core.Experiment):
+        word = "SHIFTING SANDS 1920X1080"
+        size = (1920, 1080)
+        zoom = 1
+        pos = [0, 0]
+        seed = seeds.patterns.PrimordialSoup(vals={"state": seeds.random.RandInt(0, 1)})
+
+    old = os.environ.get("XENTICA_GB300_TEMPLATE")
+    if template:
+        os.environ["XENTICA_GB300_TEMPLATE"] = template
+    try:
+        return ShiftingSands(Sands)
+    finally:
+        if template:
+            if old is None:
+                os.environ.pop("XENTICA_GB300_TEMPLATE")
+            else:
+                os.environ["XENTICA_GB300_TEMPLATE"] = old
+
+
+def sands_line(args, dist):
+    """ShiftingSands 1920x1080 torus: the fused shifting family (K steps of
+    1000 generations; on a torus a step is one gather, since every generation
+    moves the states by the same offset), its per-generation kernel (the
+    form a history-dependent colour forces, 100 generations) and the generic
+    interpreter on the same model (100 generations: the reference's two
+    passes over N + 1 planes); final states compared with each other and the
+    oracle."""
+    from xentica_gb300 import build as xk_build
+    from xentica_gb300 import _native as nat
+    xk_build.build()
+    nat.set_device(dist.local)
+    lib = nat.load()
+    fused, vm = sands_model(), sands_model("vm")
+    n = fused.cells_num
+    init = fused.gpu.arrays.cells.get()[:n].copy()
+    colors0 = fused.gpu.arrays.colors.get()
+    gens = 1000
+    for _ in range(args.warmup):
+        fused.gpu.step(gens)
+    clocks = Clocks(dist.local)
+    time.sleep(0.6)
+    dist.barrier()
+    lib.xk_range_push(b"timed")
+    step_ms = []
+    for _ in range(args.steps):
+        fused.gpu.step(gens)
+        step_ms.append(lib.xk_last_step_ms())
+    lib.xk_range_pop()
+    dist.barrier()
+    clk = clocks.stop()
+    dev_s = dist.max(sum(step_ms) / 1000.0)
+    value = float(n) * gens * args.steps * dist.world / dev_s
+    # per generation: one launch each (reference calling pattern, model.step())
+    fused.gpu.load(init, colors0)
+    fused.step()
+    t0 = time.perf_counter()
+    per_gen = 100
+    for _ in range(per_gen):
+        fused.step()
+    fused.gpu.arrays.cells.get()
+    api_s = time.perf_counter() - t0
+    # the interpreter, 100 generations in one call
+    vm.gpu.load(init, colors0)
+    vm.gpu.step(1)
+    vm.gpu.step(per_gen)
+    vm_ms = lib.xk_last_step_ms()
+    fused.gpu.load(init, colors0)
+    fused.gpu.step(1 + per_gen)
+    same = bool(np.array_equal(fused.gpu.arrays.cells.get()[:n], vm.gpu.arrays.cells.get()[:n]))
+    peak, peak_kind = measured_peak()
+    vm_rate = float(n) * per_gen / (vm_ms / 1000.0)
+    line = {"metric": "cell-updates/s (ShiftingSands 1920x1080)", "value": value,
+            "unit": "cell-updates/s", "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_s * 1000 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded Bernoulli(0.5))",
+            "config": {"workload": "ShiftingSands (examples/shifting_sands.py) 1920x1080 torus, "
+                                   "1000 generations per step",
+                       "l2": "2 MB state, L2 resident; no flush"},
+            "api_step_loop": {"value": float(n) * per_gen / api_s, "unit": "cell-updates/s",
+                              "note": "100 calls of model.step(), one generation each"},
+            "interpreter": {"value": vm_rate, "unit": "cell-updates/s", "generations": per_gen,
+                            "bytes_per_cell_update": 2 * 9,
+                            "achieved_gbs": 18.0 * vm_rate / 1e9,
+                            "frac": 18.0 * vm_rate / 1e9 / peak,
+                            "fused_over_interpreter": value / dist.world / vm_rate,
+                            "same_cells_as_fused": same,
+                            "note": "(N + 1) x 2 x S = 18 B per cell-update: the reference's "
+                                    "emit writes 8 buffer planes, absorb reads them and "
+                                    "writes the main plane"},
+            "roofline": {"bound": "hbm", "achieved": 2.0 * value / dist.world / 1e9, "peak": peak,
+                         "unit": "GB/s", "frac": 2.0 * value / dist.world / 1e9 / peak,
+                         "peak_kind": peak_kind, "traffic": None,
+                         "kernel": "xk_k_shift_jump (1000 generations per launch)",
+                         "note": "B_alg = 2 B per cell-update (uint8 read + write); a step "
+                                 "of 1000 generations reads and writes the state once, so "
+                                 "frac is reference-format effective"},
+            "gpu_launches": args.steps, "clocks": clk}
+    if dist.rank == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        topo = O.Topology(fused.size)
+        fld = topo.field(init, np.uint8)
+        col = np.zeros(3 * n, dtype=np.int32)
+        lut = [0, 0, 0] + [255 * v for v in range(1, 9) for _ in range(3)]
+        t0 = time.perf_counter()
+        O.shift_run(topo, fld, col, 1 + per_gen, 8, lut)
+        el = time.perf_counter() - t0
+        line["parity"] = {"generations": 1 + per_gen,
+                          "bit_exact": bool(np.array_equal(fld[:n], fused.gpu.arrays.cells.get()[:n]))}
+        line["cpu_baseline"] = {"value": n * (1 + per_gen) / el, "unit": "cell-updates/s",
+                                "cores": os.cpu_count(), "kind": "port",
+                                "sample": "%d generations of the lattice, oracle (OpenMP)"
+                                          % (1 + per_gen)}
+        return line
+    return None
+
+
+def run_sands(args, dist):
+    line = sands_line(args, dist)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
 def run_life512(args, dist):
     line = life512_line(args, dist)
     if line is not None:
@@ -1098,6 +1257,8 @@ def main():
             run_mass(args, dist)
         elif args.workload == "serve":
             run_serve(args, dist)
+        elif args.workload == "sands":
+            run_sands(args, dist)
         else:
             run_ours(args, dist)
     finally:

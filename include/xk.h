@@ -38,7 +38,10 @@ enum {
     XK_ERR_INVARIANT = -7     /* a conserved quantity changed              */
 };
 
-enum { XK_FAMILY_LIFE = 1, XK_FAMILY_EVOLIFE = 2, XK_FAMILY_MASS = 3, XK_FAMILY_VM = 4 };
+/* XK_FAMILY_SHIFT: ShiftingSands' family (examples/shifting_sands.py:15-47),
+ * a 1-bit state that moves in from neighbour rule0 each generation. */
+enum { XK_FAMILY_LIFE = 1, XK_FAMILY_EVOLIFE = 2, XK_FAMILY_MASS = 3, XK_FAMILY_VM = 4,
+       XK_FAMILY_SHIFT = 5 };
 enum { XK_COLOR_NONE = 0, XK_COLOR_PLAIN = 1, XK_COLOR_MOVING_AVERAGE = 2 };
 
 /* Model descriptor filled by the translator (xentica_gb300/core/templates.py)

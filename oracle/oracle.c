@@ -162,6 +162,38 @@ void xo_life_step(const xo_topo *t, void *fld, int esz, int bits,
 }
 
 /* ------------------------------------------------------------------------ */
+/* ShiftingSands (examples/shifting_sands.py:15-47): a 1-bit ``state``; emit
+ * writes it into one buffer and 0 into the others (the buffer that lands in
+ * plane ``plane0``, 1..N, after the rev_index_map placement), absorb sums the
+ * neighbours' buffers (the off-board container for an off-board neighbour)
+ * into an int, the colour effect sees that int, and the state stores it
+ * masked to 1 bit.  ``lut`` holds the rgb for every sum 0..N. */
+void xo_shift_step(const xo_topo *t, void *fld, int esz, int plane0, int32_t *col,
+                   const xo_color *cc, const int32_t *lut, int threads)
+{
+    const int64_t n = xo_cells(t);
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        uint64_t s = xo_load(fld, esz, i) & 1u;
+        for (int p = 1; p <= t->nbr; ++p) xo_store(fld, esz, i + n * (int64_t)p, p == plane0 ? s : 0u);
+    }
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t x[XO_MAXDIM];
+        xo_coords(t, i, x);
+        int new_val = 0;
+        for (int k = 0; k < t->nbr; ++k) {
+            int64_t j = xo_neighbor(t, x, k);
+            uint64_t v = j < 0 ? t->border_value : xo_load(fld, esz, j + n * (int64_t)(k + 1));
+            new_val += (int)(v & 1u);
+        }
+        const int32_t *rgb = lut + 3 * new_val;
+        xo_color_write(col, i, rgb[0], rgb[1], rgb[2], cc);
+        xo_store(fld, esz, i, (uint64_t)new_val & 1u);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
 /* Mass transfer (3-D von Neumann, StaticBorder(WALL)): the model added for the
  * sand-transfer configuration, written in the reference DSL (see
  * tests/golden/ref_models.py:MassTransfer).  uint32 cell = mass.

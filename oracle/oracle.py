@@ -141,6 +141,21 @@ def life_run(topo, fld, col, steps, born=8, sustain=12, bits=1, color=None,
            ctypes.byref(cc), _ptr(lut6), ctypes.c_int(threads))
 
 
+def shift_run(topo, fld, col, steps, plane0, lut, color=None, threads=None):
+    """Advance a ShiftingSands-style model ``steps`` generations in place:
+    emit writes the state into plane ``plane0`` (1..N) and 0 into the others,
+    absorb sums the neighbours' buffers; ``lut`` is the rgb for every sum
+    0..N before the colour effect."""
+    threads = threads or os.cpu_count()
+    cc = color or _color()
+    lut = np.ascontiguousarray(lut, dtype=np.int32)
+    fn = lib().xo_shift_step
+    fn.restype = None
+    for _ in range(steps):
+        fn(ctypes.byref(topo._c), _ptr(fld), ctypes.c_int(fld.itemsize), ctypes.c_int(plane0),
+           _ptr(col), ctypes.byref(cc), _ptr(lut), ctypes.c_int(threads))
+
+
 def mass_run(topo, fld, col, steps, wall=2 ** 32 - 1, threads=None, totals=None):
     """Advance the mass-transfer model; optionally record the total mass per step."""
     threads = threads or os.cpu_count()

@@ -84,6 +84,25 @@ CASES.update({
                         checkpoints=[1, 30], render={"viewport": [100, 90]}),
 })
 
+SANDS = "examples.shifting_sands"
+CASES.update({
+    "sands_640x360": dict(model=SANDS + ":ShiftingSands", experiment=SANDS + ":ShiftingSandsExperiment",
+                          checkpoints=[1, 7, 100, 1000], render={"viewport": [640, 360]},
+                          exp_overrides={"zoom": 1}),
+    "sands_static_97x61": dict(model=REF_MODELS + ":ShiftingSandsStatic",
+                               experiment=GOL + ":GOLExperiment2",
+                               exp_overrides={"size": [97, 61], "word": "static sands"},
+                               checkpoints=[1, 2, 30, 100]),
+    "sands3d_vn_20x17x9": dict(model=REF_MODELS + ":ShiftingSands3D",
+                               experiment=GOL + ":GOLExperiment2",
+                               exp_overrides={"size": [20, 17, 9], "word": "sands 3d", "zoom": 1},
+                               checkpoints=[1, 5, 64], render={"viewport": [20, 17]}),
+    "sands_fade_80x50": dict(model=REF_MODELS + ":ShiftingSandsFade",
+                             experiment=REF_MODELS + ":FadeExperiment",
+                             exp_overrides={"size": [80, 50], "word": "fading sands"},
+                             checkpoints=[1, 4, 33], render={"viewport": [80, 50]}),
+})
+
 # odd sizes, both borders: pins word-boundary and wrap handling
 for w, h in [(1, 1), (1, 17), (17, 1), (2, 2), (31, 5), (32, 7), (33, 9), (63, 64), (64, 63),
              (65, 3), (100, 100), (1023, 5), (1024, 3), (1025, 4), (2000, 11), (3, 1200)]:

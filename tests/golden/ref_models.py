@@ -134,3 +134,40 @@ class MassExperiment(core.Experiment):
     zoom = 1
     pos = [0, 0]
     seed = _seeds.patterns.PrimordialSoup(vals={"mass": RandPoisson(4)})
+
+
+from examples.shifting_sands import ShiftingSands as _ShiftingSands  # noqa: E402
+
+
+class ShiftingSandsStatic(_ShiftingSands):
+    """ShiftingSands with a static border of dead cells: edge cells lose the
+    state that would wrap in."""
+
+    class Topology(_ShiftingSands.Topology):
+        border = core.StaticBorder(0)
+
+
+class ShiftingSands3D(_ShiftingSands):
+    """ShiftingSands on a 3-D von Neumann torus (emit into buffer 2)."""
+
+    class Topology(_ShiftingSands.Topology):
+        dimensions = 3
+        neighborhood = core.VonNeumannNeighborhood()
+
+    def emit(self):
+        for i, buf in enumerate(self.buffers):
+            if i == 2:
+                buf.state = self.main.state
+            else:
+                buf.state = 0
+
+
+class ShiftingSandsFade(_ShiftingSands):
+    """ShiftingSands with history-dependent colours (FadeExperiment's fades)."""
+
+    @color_effects.MovingAverage
+    def color(self):
+        red = self.main.state * 200
+        green = self.main.state * 100 + 10
+        blue = 250 - self.main.state * 250
+        return (red, green, blue)

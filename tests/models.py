@@ -108,7 +108,8 @@ class DiamoebaExperiment(GOLExperiment):
 
 
 class ShiftingSands(core.CellularAutomaton):
-    """Directional emit: not a Life-like model (no GB300 template yet)."""
+    """Directional emit (examples/shifting_sands.py:15-47): the shifting
+    family's template."""
 
     state = core.IntegerProperty(max_val=1)
 
@@ -197,7 +198,42 @@ class LifelikeFixed(GameOfLife):
         self.main.state = is_born | is_sustain & self.main.state
 
 
+class ShiftingSandsStatic(ShiftingSands):
+    """ShiftingSands with a static border of dead cells."""
+
+    class Topology(ShiftingSands.Topology):
+        border = core.StaticBorder(0)
+
+
+class ShiftingSands3D(ShiftingSands):
+    """ShiftingSands on a 3-D von Neumann torus (emit into buffer 2)."""
+
+    class Topology(ShiftingSands.Topology):
+        dimensions = 3
+        neighborhood = core.VonNeumannNeighborhood()
+
+    def emit(self):
+        for i, buf in enumerate(self.buffers):
+            if i == 2:
+                buf.state = self.main.state
+            else:
+                buf.state = 0
+
+
+class ShiftingSandsFade(ShiftingSands):
+    """ShiftingSands with history-dependent colours."""
+
+    @color_effects.MovingAverage
+    def color(self):
+        red = self.main.state * 200
+        green = self.main.state * 100 + 10
+        blue = 250 - self.main.state * 250
+        return (red, green, blue)
+
+
 MODELS = {
+    "ShiftingSands": ShiftingSands, "ShiftingSandsStatic": ShiftingSandsStatic,
+    "ShiftingSands3D": ShiftingSands3D, "ShiftingSandsFade": ShiftingSandsFade,
     "GameOfLife": GameOfLife, "GameOfLifeStatic": GameOfLifeStatic,
     "GameOfLife6D": GameOfLife6D, "GameOfLifeInt": GameOfLifeInt, "LifelikeCA": LifelikeCA,
     "GameOfLifeFade": GameOfLifeFade, "GameOfLifePlainColor": GameOfLifePlainColor,
@@ -206,6 +242,7 @@ MODELS = {
 EXPERIMENTS = {
     "GOLExperiment": GOLExperiment, "GOLExperiment2": GOLExperiment2,
     "DiamoebaExperiment": DiamoebaExperiment, "FadeExperiment": FadeExperiment,
+    "ShiftingSandsExperiment": ShiftingSandsExperiment,
 }
 
 

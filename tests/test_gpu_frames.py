@@ -4,7 +4,8 @@ then ``render()`` (``xentica/core/base.py:703-753``).
 
 Every frame equals the ``render()`` of a twin model stepped one generation at
 a time, for each kernel family (Life-like with history-free and with fading
-colours, EvoLife, mass transfer, the interpreter) and for host frames
+colours, EvoLife, mass transfer, the shifting family, the interpreter) and
+for host frames
 (page-locked and pageable) and device frames; EvoLife frames are also checked
 against the oracle's render after every generation.
 """
@@ -41,6 +42,15 @@ def _random_evolife(model, seed):
     return cells, colors
 
 
+def _on_interpreter(model_cls, exp):
+    import os
+    os.environ["XENTICA_GB300_TEMPLATE"] = "vm"
+    try:
+        return model_cls(exp)
+    finally:
+        del os.environ["XENTICA_GB300_TEMPLATE"]
+
+
 def _twins(make, viewport, zoom, pos, load=None):
     a, b = make(), make()
     for m in (a, b):
@@ -68,7 +78,9 @@ CASES = {
                 lambda m: _random_evolife(m, 5)),
     "mass": (lambda: MassTransfer(type("E", (MassExperiment, ), {"size": (36, 20, 12)})),
              (36, 20), 1, (0, 0), None),
-    "interpreter": (lambda: ShiftingSands(ShiftingSandsExperiment), (160, 90), 3, (0, 0), None),
+    "shift": (lambda: ShiftingSands(ShiftingSandsExperiment), (160, 90), 3, (0, 0), None),
+    "interpreter": (lambda: _on_interpreter(ShiftingSands, ShiftingSandsExperiment), (160, 90), 3,
+                    (0, 0), None),
 }
 
 

@@ -161,3 +161,18 @@ def test_headless_viewer_frames_vs_oracle(tmp_path):
                     smooth=smooth)
     assert np.array_equal(frames[-1].ravel(), want.astype(np.uint8))
     assert len(os.listdir(str(tmp_path))) == 11
+
+
+def test_shifting_sands_reference_golden():
+    """Reference tests/core/test_base.py:182-189: ShiftingSands (the shifting
+    family's template, every generation of the run in one gather) after 1000
+    steps of model.step() and as one step(1000)."""
+    from tests.models import ShiftingSands, ShiftingSandsExperiment
+    a, b = ShiftingSands(ShiftingSandsExperiment), ShiftingSands(ShiftingSandsExperiment)
+    assert type(a.gpu.template).__name__ == "ShiftTemplate"
+    for _ in range(1000):
+        a.step()
+    b.gpu.step(1000)
+    assert crc(a.gpu.arrays.cells.get()[:a.cells_num]) == 1639048270
+    assert crc(b.gpu.arrays.cells.get()[:b.cells_num]) == 1639048270
+    assert np.array_equal(a.gpu.arrays.colors.get(), b.gpu.arrays.colors.get())

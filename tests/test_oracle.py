@@ -38,6 +38,26 @@ LUTS = {"GameOfLifeFade": (0, 10, 250, 200, 110, 0),
         "GameOfLifePlainColor": (0, 0, 7, 255, 3, 7)}
 
 
+def shift_params(model):
+    """(plane0, lut) of a ShiftingSands-style model for ``oracle.shift_run``:
+    the plane its emit writes the state into, and the colour of every sum
+    0..N of the neighbours' buffers, both from evaluating the traced
+    programs."""
+    from xentica_gb300.core import ir
+    n = len(model.buffers)
+    one = np.array([1], dtype=np.uint64)
+    ev = ir.evaluate(model.programs["emit"], {("main", -1): one}, lanes=1)
+    plane0 = [key[1] for key, v in ev.stores.items() if int(v[0]) & 1]
+    assert len(plane0) == 1
+    lanes = np.arange(n + 1, dtype=np.uint64)
+    inputs = {("main", -1): np.zeros(n + 1, dtype=np.uint64)}
+    for k in range(n):
+        inputs[("nbuf", k)] = (lanes > np.uint64(k)).astype(np.uint64)
+    ev = ir.evaluate(model.programs["absorb"], inputs, lanes=n + 1)
+    rgb = ev.color[0]
+    return plane0[0], [int(rgb[c][v]) for v in range(n + 1) for c in range(3)]
+
+
 def life_params(model):
     tpl = model.gpu.template
     info = tpl.color.extra if tpl.color is not None else {"kind": "none"}
@@ -68,6 +88,15 @@ def test_oracle_reference_goldens(golden, case, steps, expected):
     O.life_run(topo, fld, col, steps, born=tpl.rule0, sustain=tpl.rule1, color=color,
                rule_schedule=schedule)
     assert crc(fld[:topo.cells]) == expected
+
+
+def test_oracle_shifting_sands_golden(golden):
+    # reference tests/core/test_base.py:182-189: ShiftingSands after 1000 steps
+    topo, fld, col, model = oracle_setup(golden["sands_640x360"]["job"])
+    assert crc(fld[:topo.cells]) == golden["sands_640x360"]["init"]
+    plane0, lut = shift_params(model)
+    O.shift_run(topo, fld, col, 1000, plane0, lut, color=life_params(model)[1])
+    assert crc(fld[:topo.cells]) == 1639048270
 
 
 def test_oracle_render_golden(golden):
@@ -101,6 +130,9 @@ def test_oracle_fixtures(golden, case):
     for cp in sorted(int(c) for c in entry["steps"]):
         if type(model).__name__ == "MassTransfer":
             O.mass_run(topo, fld, col, cp - done)
+        elif type(model).__name__.startswith("ShiftingSands"):
+            plane0, lut = shift_params(model)
+            O.shift_run(topo, fld, col, cp - done, plane0, lut, color=color)
         else:
             O.life_run(topo, fld, col, cp - done, born=tpl.rule0, sustain=tpl.rule1, color=color,
                        bits=model.main.properties["state"].bit_width,

@@ -17,6 +17,11 @@ Life-like family (``XK_FAMILY_LIFE``)
     re-extracted whenever their values change (LifelikeCA,
     ``examples/game_of_life.py:183-203``).
 
+Shifting family (``XK_FAMILY_SHIFT``)
+    ShiftingSands: one 1-bit property sent into one buffer and absorbed as the
+    sum of the neighbours' buffers, i.e. moved by one neighbour offset per
+    generation (see :class:`ShiftTemplate`).
+
 EvoLife (``XK_FAMILY_EVOLIFE``) and mass transfer (``XK_FAMILY_MASS``)
     matched statement by statement against the canonical programs of
     ``core/canonical.py``.
@@ -38,7 +43,7 @@ from xentica_gb300.core.topology.lattice import OrthogonalLattice
 from xentica_gb300.core.topology.neighborhood import OrthogonalNeighborhood
 from xentica_gb300.core.renderers import RendererPlain
 
-__all__ = ['match', 'LifeTemplate', 'NoTemplate']
+__all__ = ['match', 'LifeTemplate', 'ShiftTemplate', 'NoTemplate']
 
 MAX_EXHAUSTIVE_NBR = 16
 
@@ -256,6 +261,94 @@ class LifeTemplate:
         return d
 
 
+class ShiftTemplate(LifeTemplate):
+    """ShiftingSands' family (``examples/shifting_sands.py:15-47``): one 1-bit
+    property; emit copies it into exactly one buffer plane and writes 0 into
+    every other; absorb sets it to the sum of the neighbours' buffers.  Which
+    neighbour's plane faces a cell (the one whose state moves in) is read off
+    the evaluated emit: the plane written with the state, p, is the plane a
+    cell reads from neighbour p - 1.  Absorb is evaluated on every
+    combination of the cell's state and its neighbours' buffers and must equal
+    their sum masked to the field; the colour is a function of the new state,
+    as for the Life-like family."""
+
+    family = nat.XK_FAMILY_SHIFT
+
+    def __init__(self, model):
+        props = list(model.main.properties.values())
+        if len(props) != 1 or not isinstance(props[0], IntegerProperty):
+            raise NoTemplate("needs exactly one IntegerProperty")
+        self.model = model
+        self.prop = props[0]
+        self.mask = (1 << self.prop.bit_width) - 1
+        if self.mask != 1:
+            raise NoTemplate("needs a 1-bit property")
+        deltas, torus, border = _topology(model)
+        self.nbr = len(deltas)
+        self.border_state = border & self.mask
+        emit = model.programs["emit"]
+        if not emit.loads() <= {("main", -1)} or emit.params():
+            raise NoTemplate("emit reads more than the cell's state")
+        planes = {("buf", p) for p in range(1, self.nbr + 1)}
+        if _store_keys(emit) != planes:
+            raise NoTemplate("emit must write every buffer")
+        lanes = np.array([0, 1], dtype=np.uint64)
+        ev = ir.evaluate(emit, {("main", -1): lanes}, lanes=2)
+        copies, zeros = [], []
+        for key in sorted(planes):
+            out = ev.stores[key].astype(np.uint64) & np.uint64(self.mask)
+            if np.array_equal(out, lanes):
+                copies.append(key[1])
+            elif not out.any():
+                zeros.append(key[1])
+        if len(copies) != 1 or len(zeros) != self.nbr - 1:
+            raise NoTemplate("emit does not send the state into exactly one buffer")
+        self.i0 = copies[0] - 1
+        if not torus and self.border_state:
+            # edge cells would add the live border once per off-board
+            # neighbour: sums above 1, whose colour no state table gives
+            raise NoTemplate("static border of live cells")
+        absorb = model.programs["absorb"]
+        allowed = {("main", -1)} | {("nbuf", k) for k in range(self.nbr)}
+        if not absorb.loads() <= allowed or absorb.params():
+            raise NoTemplate("absorb reads %s" % sorted(absorb.loads() - allowed))
+        if _store_keys(absorb) != {("main", 0)}:
+            raise NoTemplate("absorb must write only the cell's own main state")
+        self.absorb = absorb
+        self.color = _color_stmt(absorb)
+        if self.color is not None and self.color.extra["kind"] not in ("plain", "moving_average"):
+            raise NoTemplate("custom colour effect")
+        inputs, state, count = self._inputs()
+        ev = ir.evaluate(absorb, inputs, lanes=len(state))
+        new = ev.stores[("main", 0)].astype(np.uint64) & np.uint64(self.mask)
+        if not np.array_equal(new.astype(np.int64), count & self.mask):
+            raise NoTemplate("absorb is not the sum of the neighbours' buffers")
+        # the colour on the inputs that occur: only neighbour i0's buffer can
+        # hold a state, every other buffer a cell reads is 0
+        reach = np.array([0, 1, 2, 3], dtype=np.uint64)
+        rin = {("main", -1): reach & np.uint64(1)}
+        for k in range(self.nbr):
+            rin[("nbuf", k)] = (reach >> np.uint64(1)) if k == self.i0 else np.zeros(4, np.uint64)
+        ev = ir.evaluate(absorb, rin, lanes=4)
+        new = ev.stores[("main", 0)].astype(np.uint64) & np.uint64(self.mask)
+        lut = [0] * 6
+        if ev.color is not None:
+            rgb = ev.color[0]
+            for s in (0, 1):
+                sel = new.astype(np.int64) == s
+                for c in range(3):
+                    vals = np.unique(rgb[c][sel])
+                    if len(vals) > 1:
+                        raise NoTemplate("colour depends on more than the new state")
+                    if len(vals):
+                        lut[3 * s + c] = int(vals[0])
+        self.param_names = []
+        self.rule0, self.rule1, self.lut = self.i0, 0, lut
+
+    def rule_for(self, params):
+        return self.rule0, self.rule1, self.lut
+
+
 class EvoLifeTemplate:
     """EvoLife (``canonical.EvoLifeProgram``): matched by program fingerprint.
 
@@ -406,7 +499,7 @@ class VMTemplate:
         self._bound = vals
 
 
-FAMILIES = (LifeTemplate, EvoLifeTemplate, MassTemplate, VMTemplate)
+FAMILIES = (LifeTemplate, ShiftTemplate, EvoLifeTemplate, MassTemplate, VMTemplate)
 
 
 def match(model):

@@ -390,8 +390,11 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
     const int64_t n = cells_of(d);
     XK_REQUIRE(n <= (1LL << 40), XK_ERR_ARG, "lattice of %lld cells too large", (long long)n);
     XK_REQUIRE(d.family == XK_FAMILY_LIFE || d.family == XK_FAMILY_EVOLIFE ||
-                   d.family == XK_FAMILY_MASS || d.family == XK_FAMILY_VM,
+                   d.family == XK_FAMILY_MASS || d.family == XK_FAMILY_VM || d.family == XK_FAMILY_SHIFT,
                XK_ERR_UNSUPPORTED, "model family %d has no kernel in this library", d.family);
+    if (d.family == XK_FAMILY_SHIFT)
+        XK_REQUIRE(d.rule0 < (uint32_t)d.nbr, XK_ERR_ARG, "shifting family: neighbour %u of %d",
+                   d.rule0, d.nbr);
     if (d.family == XK_FAMILY_MASS)
         XK_REQUIRE(d.ndim == 3 && d.nbr == 6 && !d.torus && d.state_bytes == 4, XK_ERR_ARG,
                    "mass transfer needs a 3-D von Neumann lattice of 32-bit cells with a wall");
@@ -457,7 +460,7 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
             XK_TRY(cudaMemsetAsync(m->cells64[0], 0, (size_t)n * 8, m->stream));
             XK_TRY(xk_evolife_set_positional(d.palette));
             m->mut_thresh = below_threshold(d.mutation_prob);
-        } else if (is_moore2d(d)) {
+        } else if (d.family == XK_FAMILY_LIFE && is_moore2d(d)) {
             m->layout = LAYOUT_BITS2D;
             m->lg = xk_life_geo(d.size[0], d.size[1], d.torus, border_state);
             const size_t words = (size_t)m->lg.H * m->lg.wpr;
@@ -755,6 +758,11 @@ static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *fram
                                          m->cl_threads, m->stream));
             left -= g;
         }
+    } else if (m->d.family == XK_FAMILY_SHIFT && m->d.torus && colors_free) {
+        // every generation moves the states by the same offset: one gather
+        XK_CUDA(xk_shift_jump(m->bytes[m->cur], m->bytes[1 - m->cur], m->ng, (int)m->rule0, count,
+                              m->stream));
+        m->cur = 1 - m->cur;
     } else if (m->layout == LAYOUT_BITS2D && colors_free && m->tb_T > 1) {
         // temporal blocking: launches of tb_T generations, the rest in one
         // shorter launch; ping-pong between the two word buffers
@@ -791,8 +799,12 @@ static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *fram
                     m->cur = 1 - m->cur;
                 }
             } else {
-                XK_CUDA(xk_life_step_nd(m->bytes[m->cur], m->bytes[1 - m->cur], m->ng, m->rule0,
-                                        m->rule1, m->stream));
+                if (m->d.family == XK_FAMILY_SHIFT)
+                    XK_CUDA(xk_shift_step_nd(m->bytes[m->cur], m->bytes[1 - m->cur], m->ng, (int)m->rule0,
+                                             m->stream));
+                else
+                    XK_CUDA(xk_life_step_nd(m->bytes[m->cur], m->bytes[1 - m->cur], m->ng, m->rule0,
+                                            m->rule1, m->stream));
                 m->cur = 1 - m->cur;
             }
             if (!colors_free) {

@@ -365,6 +365,14 @@ static int enqueue_round(xk_server *s, Req *q, int64_t chunk)
     return XK_OK;
 }
 
+// ping-pong flips of a round of `chunk` generations: one per launch (a
+// temporally blocked launch covers up to tb_T generations)
+static int64_t round_flips(const Req *q, int64_t chunk)
+{
+    if (q->path == PATH_GLOBAL2D && q->tb_T > 1) return (chunk + q->tb_T - 1) / q->tb_T;
+    return chunk;
+}
+
 // next round of a request on its own stream; full rounds of requests with at
 // least two of them left are captured once per parity and replayed
 static int launch_round(xk_server *s, Req *q)
@@ -389,12 +397,12 @@ static int launch_round(xk_server *s, Req *q)
     }
     if (full && q->graph[c0]) {
         XK_CUDA(cudaGraphLaunch(q->graph[c0], q->stream));
-        q->cur = c0 ^ (int)(chunk & 1);
+        q->cur = c0 ^ (int)(round_flips(q, chunk) & 1);
     } else {
         int rc = enqueue_round(s, q, chunk);
         if (rc != XK_OK) return rc;
     }
-    s->st.launches += chunk;
+    s->st.launches += round_flips(q, chunk);
     XK_CUDA(cudaEventRecord(q->ev, q->stream));
     q->ev_pending = true;
     q->chunk = chunk;

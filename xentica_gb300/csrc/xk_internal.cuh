@@ -183,6 +183,11 @@ cudaError_t xk_life_step_nd(const uint8_t *src, uint8_t *dst, const NdGeo &g, ui
                             uint32_t rule1, cudaStream_t s);
 cudaError_t xk_life_step_bytes2d(const uint8_t *src, uint8_t *dst, int W, int H,
                                  uint32_t rule0, uint32_t rule1, cudaStream_t s);
+// shifting family (shift.cu): one generation (any topology and border), or
+// `generations` at once on a torus
+cudaError_t xk_shift_step_nd(const uint8_t *src, uint8_t *dst, const NdGeo &g, int i0, cudaStream_t s);
+cudaError_t xk_shift_jump(const uint8_t *src, uint8_t *dst, const NdGeo &g, int i0, int64_t generations,
+                          cudaStream_t s);
 cudaError_t xk_nd_colors(const uint8_t *st, int32_t *col, int64_t n, const int32_t *lut6,
                          int smooth, cudaStream_t s);
 cudaError_t xk_nd_color_step(const uint8_t *st, int32_t *col, int64_t n, const int32_t *lut6,
