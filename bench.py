@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--mass-side", type=int, default=256, help="mass: lattice side (a cube)")
     ap.add_argument("--load", type=float, default=0.7,
                     help="serve: offered load as a fraction of the measured capacity")
+    ap.add_argument("--rate", type=float, default=100.0,
+                    help="serve: also run at this fixed arrival rate (requests/s; 0: no)")
     ap.add_argument("--quantum", type=int, default=128, help="serve: generations per round")
     ap.add_argument("--sweep", default="", help="serve: extra offered loads after the main run, "
                                                 "comma-separated (e.g. 0.3,0.5,0.9)")
@@ -1007,6 +1009,17 @@ def sands_line(args, dist):
         fused.step()
     fused.gpu.arrays.cells.get()
     api_s = time.perf_counter() - t0
+    # the fused kernel one generation per launch (what a history-dependent
+    # colour or a static border needs), 100 generations in one call
+    os.environ["XK_SHIFT_JUMP"] = "0"
+    try:
+        fused.gpu.load(init, colors0)
+        fused.gpu.step(1)
+        fused.gpu.step(per_gen)
+        pg_ms = lib.xk_last_step_ms()
+    finally:
+        del os.environ["XK_SHIFT_JUMP"]
+    pg_rate = float(n) * per_gen / (pg_ms / 1000.0)
     # the interpreter, 100 generations in one call
     vm.gpu.load(init, colors0)
     vm.gpu.step(1)
@@ -1027,11 +1040,16 @@ def sands_line(args, dist):
                        "l2": "2 MB state, L2 resident; no flush"},
             "api_step_loop": {"value": float(n) * per_gen / api_s, "unit": "cell-updates/s",
                               "note": "100 calls of model.step(), one generation each"},
+            "per_generation": {"value": pg_rate, "unit": "cell-updates/s", "generations": per_gen,
+                               "achieved_gbs": 2.0 * pg_rate / 1e9,
+                               "frac": 2.0 * pg_rate / 1e9 / peak,
+                               "note": "xk_k_shift_nd, one launch per generation (XK_SHIFT_JUMP=0)"},
             "interpreter": {"value": vm_rate, "unit": "cell-updates/s", "generations": per_gen,
                             "bytes_per_cell_update": 2 * 9,
                             "achieved_gbs": 18.0 * vm_rate / 1e9,
                             "frac": 18.0 * vm_rate / 1e9 / peak,
                             "fused_over_interpreter": value / dist.world / vm_rate,
+                            "per_generation_over_interpreter": pg_rate / vm_rate,
                             "same_cells_as_fused": same,
                             "note": "(N + 1) x 2 x S = 18 B per cell-update: the reference's "
                                     "emit writes 8 buffer planes, absorb reads them and "
@@ -1110,9 +1128,11 @@ def serve_line(args, dist):
     capacity = sum(work[i] for i in probe) / (time.perf_counter() - t0)
     mean_work = sum(work) / len(work)
 
-    def open_loop(load, seed):
-        """Poisson arrivals offering ``load`` x capacity; returns the stats."""
-        rate = load * capacity / mean_work
+    def open_loop(load, seed, fixed_rate=None):
+        """Poisson arrivals offering ``load`` x capacity (or ``fixed_rate``
+        requests per second); returns the stats."""
+        rate = fixed_rate if fixed_rate else load * capacity / mean_work
+        load = rate * mean_work / capacity
         arrivals = serve.poisson_arrivals(rate, len(specs), seed=seed)
         handles = [None] * len(specs)
         launches0 = srv.stats()["launches"]
@@ -1143,7 +1163,14 @@ def serve_line(args, dist):
         last = max(inf["done_s"] for inf in infos)
         span = dist.max(last - first)
         lat = [inf["done_s"] - inf["submit_s"] for inf in infos]
-        return {"offered_load": load, "rate_per_s": rate,
+        by_kind = {}
+        for k in ("life2d", "life3d", "mass"):
+            idx = [i for i in range(len(specs)) if specs[i]["kind"] == k]
+            if idx:
+                by_kind[k] = {"latency_s": serve.latency_summary([lat[i] for i in idx]),
+                              "slowdown": serve.latency_summary(
+                                  [lat[i] * capacity / work[i] for i in idx])}
+        return {"offered_load": load, "rate_per_s": rate, "by_kind": by_kind,
                 "value": sum(work) * dist.world / span, "span_s": span,
                 "latency_s": serve.latency_summary(lat),
                 "admission_wait_s": serve.latency_summary(
@@ -1168,6 +1195,7 @@ def serve_line(args, dist):
     keep = {}
     sweep = [open_loop(float(v), args.seed + 17 + k)
              for k, v in enumerate(args.sweep.split(",")) if v.strip()] if args.sweep else []
+    fixed = open_loop(None, args.seed + 17, fixed_rate=args.rate) if args.rate > 0 else None
     st = srv.stats()
     srv.close()
     value = main_run["value"]
@@ -1197,8 +1225,11 @@ def serve_line(args, dist):
             "rate_per_s": main_run["rate_per_s"], "offered_load": args.load,
             "capacity_probe": capacity, "latency_s": main_run["latency_s"],
             "admission_wait_s": main_run["admission_wait_s"], "slowdown": main_run["slowdown"],
+            "by_kind": main_run["by_kind"],
             "sweep": [{k: r[k] for k in ("offered_load", "rate_per_s", "value", "latency_s",
                                           "slowdown")} for r in sweep],
+            "fixed_rate": ({k: fixed[k] for k in ("offered_load", "rate_per_s", "value", "latency_s",
+                                                  "slowdown", "by_kind")} if fixed else None),
             "device_bytes_peak": st["device_bytes_peak"],
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d / len(specs),
                     "d2h_bytes_per_step": h2d / len(specs),

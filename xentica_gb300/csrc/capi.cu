@@ -720,6 +720,14 @@ static int step_prepare(xk_model *m, int64_t nsteps)
     return XK_OK;
 }
 
+// XK_SHIFT_JUMP=0 in the environment steps the shifting family one
+// generation per launch even where one gather would do (for comparison)
+static bool shift_jump_enabled()
+{
+    const char *v = getenv("XK_SHIFT_JUMP");
+    return !(v && v[0] == '0');
+}
+
 // frame (EvoLife, count == 1 only): the generation's zoom-1 frame written by
 // the step kernel itself
 static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *frame = nullptr)
@@ -758,7 +766,7 @@ static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *fram
                                          m->cl_threads, m->stream));
             left -= g;
         }
-    } else if (m->d.family == XK_FAMILY_SHIFT && m->d.torus && colors_free) {
+    } else if (m->d.family == XK_FAMILY_SHIFT && m->d.torus && colors_free && shift_jump_enabled()) {
         // every generation moves the states by the same offset: one gather
         XK_CUDA(xk_shift_jump(m->bytes[m->cur], m->bytes[1 - m->cur], m->ng, (int)m->rule0, count,
                               m->stream));
