@@ -133,11 +133,23 @@ int xk_step_frames(xk_model *m, int64_t nsteps, int32_t width, int32_t height, i
  * kernel shape for every model (base.py:254-283); these exist so that a host
  * can cache the choice per device, library build and lattice and re-apply it
  * without timing.  plan[0]: XK_PLAN_*; CLUSTER: plan[1] = CTAs asked for
- * (1..16), plan[2] = rows per lane group; TEMPORAL: plan[3] = generations per
- * launch (2..8).  xk_model_plan gives kind -1 for models without plans. */
+ * (1..16), plan[2] = rows per lane group, plan[3] = 1 when the CTAs wait
+ * only for their two neighbours' rows (mbarriers) instead of a cluster
+ * barrier per generation (bands of 1, 2 or 4 rows); TEMPORAL: plan[3] =
+ * generations per launch (2..8).  xk_model_plan gives kind -1 for models
+ * without plans.  A bounded wait of the neighbour form that gave up makes
+ * the next xk_download return XK_ERR_TIMEOUT. */
 enum { XK_PLAN_GLOBAL = 0, XK_PLAN_RESIDENT = 1, XK_PLAN_CLUSTER = 2, XK_PLAN_TEMPORAL = 3 };
 int xk_model_plan(xk_model *m, int32_t plan[4]);
 int xk_model_set_plan(xk_model *m, const int32_t plan[4]);
+/* Rule form the 2-D Life-like kernels of a model run with its current rule:
+ * 1 (Conway's B3/S23, compiled into the kernels: fewer instructions per
+ * word), 0 (any other rule, read from a table at run time), -1 for models
+ * without 2-D Life-like kernels.  A plan is timed with this form, so a
+ * cache of plans keys on it.  No reference counterpart (the reference
+ * compiles every rule into its generated source, base.py:538-541, or passes
+ * it as a kernel argument, game_of_life.py:183-203). */
+int32_t xk_model_rule_form(const xk_model *m);
 
 /* Mass family: total mass after each of the last xk_step's generations
  * (count = that nsteps); the invariant the configuration checks. */
@@ -212,12 +224,25 @@ int xk_batch_run(xk_batch *b, const uint8_t *host_in, uint8_t *host_out,
  * ensemble needs no host array.  One CTA per instance; last_step_ms is the
  * device time. */
 int xk_batch_seed_bernoulli(xk_batch *b, const uint32_t *seeds, const double *p);
-/* Autotune the batched kernel's block size for this batch (timed on device). */
+/* Autotune the batched kernel's CTA shapes for this batch, timed on the
+ * device over `generations` (the state is restored): one band length (rows
+ * per lane group) for every lattice, then per lattice size (W, H) holding at
+ * least 3 % of the cells a band length of its own where that makes the whole
+ * batch at least 2 % faster (confirmed by repeated timing).
+ * *chosen_rows_per_band is the common band; xk_batch_size_bands reads the
+ * per-size choices. */
 int xk_batch_tune(xk_batch *b, int32_t generations, int32_t *chosen_rows_per_band);
-/* Set the band length (rows per lane group, 1..1024) the tuner would choose,
- * e.g. from a cached tuning result, without timing; and read it back. */
+/* Set the common band length (rows per lane group, 1..1024) the tuner would
+ * choose, e.g. from a cached tuning result, without timing (this clears the
+ * per-size choices); and read it back. */
 int xk_batch_set_band(xk_batch *b, int32_t rows_per_band);
 int32_t xk_batch_band(const xk_batch *b);
+/* Per-size band lengths: `count` triples (W, H, band) replace the per-size
+ * choices (W x H lattices use `band` instead of the common one); and read
+ * them back (returns how many there are, writing at most `capacity`
+ * triples).  No reference counterpart (tuning state). */
+int xk_batch_set_size_bands(xk_batch *b, const int32_t *triples, int32_t count);
+int32_t xk_batch_size_bands(const xk_batch *b, int32_t *triples, int32_t capacity);
 int64_t xk_batch_total_cells(const xk_batch *b);
 /* Kernel launches one xk_batch_step makes (one per instance class, plus
  * per-generation launches for instances too large for a CTA). */
@@ -262,12 +287,16 @@ int xk_batch_step_noalloc(uint8_t *d_cells, int32_t count, const int32_t *width,
  * arena of `host_bytes` (each one allocation at creation), a worker thread and
  * its CUDA streams.  Requests are admitted first come, first served, when their
  * device bytes and result bytes fit and fewer than `max_active` run; each
- * active request advances in rounds of at most `quantum` generations, a new
- * round starting as soon as its previous one finished, so requests admitted
- * while others run share the GPU with them.  2-D lattices that fit one CTA
- * run together, one resident-kernel launch per shape class per round; larger
- * and 3-D lattices run on their own streams.  Results wait in the pinned arena
- * until xk_serve_result collects them.  A request computes exactly what it
+ * active request advances in rounds, a new round starting as soon as its
+ * previous one finished, so requests admitted while others run share the GPU
+ * with them.  Large 2-D, 3-D and mass-transfer lattices run rounds of
+ * `quantum` generations on their own streams.  2-D lattices that fit one CTA
+ * run together, one resident-kernel launch per shape class over its idle
+ * members (up to 4 such rounds of a class in flight), each member running
+ * about quantum x 2^18 cell-generations per round (at least `quantum`
+ * generations).  Kernels of requests with less work (cells x generations)
+ * run at a greater stream priority.  Results wait in the pinned arena until
+ * xk_serve_result collects them.  A request computes exactly what it
  * computes alone. */
 enum { XK_SERVE_LIFE2D = 1, XK_SERVE_LIFE3D_VN = 2, XK_SERVE_MASS3D = 3 };
 enum {

@@ -251,3 +251,129 @@ def run(W, H, C_want, band, gens, torus, border, seed):
 def test_cluster_halo_protocol(W, H, C, band, torus, border):
     got, want = run(W, H, C, band, 3, torus, border, W * 7 + H)
     assert np.array_equal(got, want)
+
+
+# ---------------------------------------------------------------------------
+# The neighbour form (P2P): CTAs wait only for their two neighbours' rows on
+# mbarriers, and run generations at their own pace.  The model below replays
+# that protocol with the CTAs (and the first and last band of each, which are
+# different lanes and wait and send independently) interleaved in a random
+# order, with the hardware's mbarrier semantics (a phase completes after the
+# expected arrivals; a parity wait passes while the barrier's current phase
+# parity differs from the one asked for), and checks that
+#
+# * every phase of every mbarrier completes with exactly 2 wpr arrivals, all
+#   of them for the generation that phase belongs to (none of the next
+#   generation's arrivals is counted early);
+# * a wait passes only once the phase of its own generation has completed,
+#   never two phases later (parity aliasing);
+# * every slot word a band reads was written for the generation reading it,
+#   and no slot word is overwritten before its reader has read it;
+# * every CTA finishes (no wait is left that nothing will satisfy).
+
+class Mbar:
+    def __init__(self, expected):
+        self.expected, self.pending, self.parity, self.done, self.tags = expected, expected, 0, 0, []
+
+    def arrive(self, tag):
+        self.tags.append(tag)
+        self.pending -= 1
+        assert self.pending >= 0
+        if self.pending == 0:
+            assert len(set(self.tags)) == 1, ("arrivals of several generations in one phase", self.tags)
+            self.done += 1
+            self.parity ^= 1
+            self.pending, self.tags = self.expected, []
+
+    def passes(self, parity):
+        return self.parity != parity
+
+
+def run_p2p(C, nb, wpr, gens, seed):
+    rng = np.random.RandomState(seed)
+    bars = [[Mbar(2 * wpr), Mbar(2 * wpr)] for _ in range(C)]
+    # slot [cta][parity][above/below]: (generation tag, read since written)
+    slot = {}
+    agents = []
+    for c in range(C):
+        kinds = [("first", "last")] if nb == 1 else [("first",), ("last",)]
+        for roles in kinds:
+            agents.append(dict(c=c, roles=roles, gen=0, step="top"))
+    up = [c - 1 if c > 0 else C - 1 for c in range(C)]
+    dn = [c + 1 if c + 1 < C else 0 for c in range(C)]
+
+    def send(c, role, g):
+        # rows computed in generation g - 1 (or loaded, g = 0) for generation g
+        par = g & 1
+        tgt, side = (up[c], 1) if role == "first" else (dn[c], 0)
+        key = (tgt, par, side)
+        if key in slot:
+            tag, read = slot[key]
+            assert read, ("slot overwritten before it was read", key, tag, g)
+        slot[key] = (g, False)
+        for _ in range(wpr):
+            bars[tgt][par].arrive(g)
+
+    for c in range(C):                         # publication after the first cluster barrier
+        for role in ("first", "last"):
+            send(c, role, 0)
+    for _ in range(100000):
+        live = [a for a in agents if a["gen"] < gens]
+        if not live:
+            return True
+        ready = []
+        for a in live:
+            g, c = a["gen"], a["c"]
+            if a["step"] == "top":
+                # __syncthreads_or at the top of generation g: released when
+                # every band of the CTA has arrived there
+                if all(b["gen"] == g and b["step"] == "top" for b in agents if b["c"] == c):
+                    ready.append(a)
+            elif a["step"] == "wait":
+                if bars[c][g & 1].passes((g >> 1) & 1):
+                    ready.append(a)
+            else:
+                ready.append(a)
+        assert ready, "deadlock"
+        a = ready[rng.randint(len(ready))]
+        g, c = a["gen"], a["c"]
+        if a["step"] == "top":
+            for b in agents:                   # the barrier releases the whole CTA
+                if b["c"] == c:
+                    b["step"] = "wait"
+        elif a["step"] == "wait":
+            assert bars[c][g & 1].done == (g >> 1) + 1, ("wait passed on another phase", g)
+            a["step"] = "read"
+        elif a["step"] == "read":
+            for role in a["roles"]:
+                key = (c, g & 1, 0 if role == "first" else 1)
+                tag, _ = slot[key]
+                assert tag == g, ("slot of another generation", key, tag, g)
+                slot[key] = (tag, True)
+            a["step"] = "send"
+        else:
+            if g + 1 < gens:                   # the last generation sends nothing
+                for role in a["roles"]:
+                    send(c, role, g + 1)
+            a["gen"], a["step"] = g + 1, "top"
+    raise AssertionError("no progress")
+
+
+@pytest.mark.parametrize("C", [2, 3, 4, 16])
+@pytest.mark.parametrize("nb", [1, 2, 5])
+def test_neighbour_form_protocol(C, nb):
+    for seed in range(12):
+        assert run_p2p(C, nb, wpr=3, gens=9, seed=seed * 31 + C * 7 + nb)
+
+
+def test_neighbour_form_mbarriers_fit_the_allocation():
+    """The two mbarriers sit 8-byte aligned after the slab, halos and slots,
+    inside the shared memory the host sizes."""
+    for W, H, C, band in [(64, 33, 16, 2), (33, 17, 4, 1), (100, 40, 8, 4), (1, 9, 2, 2),
+                          (1024, 1024, 16, 4), (512, 512, 16, 2), (7, 70, 16, 1)]:
+        Cr, R, threads = config(W, H, C, band)
+        wpr = (W + 31) // 32
+        data = cluster_words(wpr, R, threads)
+        total = ((data + 1) & ~1) + 4
+        mbar_word = (data + 1) & ~1
+        assert mbar_word % 2 == 0 and mbar_word >= data and mbar_word + 4 <= total

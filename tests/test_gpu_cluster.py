@@ -27,9 +27,10 @@ pytestmark = pytest.mark.gpu
 SIZES = [(512, 512), (33, 17), (1024, 40), (1, 9), (100, 301), (1000, 700), (32, 2), (7, 1024)]
 
 
-def _run(cls, size, forced, gens, monkeypatch, seed, band=2):
+def _run(cls, size, forced, gens, monkeypatch, seed, band=2, sync="barrier"):
     monkeypatch.setenv("XK_CLUSTER", str(forced))
     monkeypatch.setenv("XK_CLUSTER_BAND", str(band))
+    monkeypatch.setenv("XK_CLUSTER_SYNC", sync)
     exp = type("E", (SoupExperiment, ), {"size": size})
     model = cls(exp)
     n = model.cells_num
@@ -53,10 +54,32 @@ def test_cluster_sizes_vs_oracle(cls, forced, band, monkeypatch):
         assert np.array_equal(got, want), (cls.__name__, size, forced, band)
 
 
+@pytest.mark.parametrize("band", [1, 2, 4])
+@pytest.mark.parametrize("forced", [2, 3, 4, 8, 16])
+@pytest.mark.parametrize("cls", [GameOfLife, GameOfLifeStatic])
+def test_neighbour_sync_vs_oracle(cls, forced, band, monkeypatch):
+    """The neighbour form (each CTA waits on mbarriers for its two
+    neighbours' rows only, CTAs run at their own pace) for every cluster size
+    and band length it has, against the oracle; odd generation counts leave
+    the last generation's slots unsent."""
+    for k, size in enumerate(SIZES):
+        got, want = _run(cls, size, forced, 37 + k % 2, monkeypatch, 10 * forced + k, band, "p2p")
+        assert np.array_equal(got, want), (cls.__name__, size, forced, band)
+
+
+@pytest.mark.parametrize("band", [1, 2, 4])
+def test_neighbour_sync_long_run(band, monkeypatch):
+    """3000 generations in one launch of the neighbour form on 16 CTAs (a
+    race between a slot's reader and its next writer would show here)."""
+    got, want = _run(GameOfLife, (512, 512), 16, 3000, monkeypatch, 5 + band, band, "p2p")
+    assert np.array_equal(got, want)
+
+
 def test_long_run_and_tuner_choice(monkeypatch):
     # 1000 generations (one launch) with the tuner's own choice
     monkeypatch.delenv("XK_CLUSTER", raising=False)
     monkeypatch.delenv("XK_CLUSTER_BAND", raising=False)
+    monkeypatch.delenv("XK_CLUSTER_SYNC", raising=False)
     exp = type("E", (SoupExperiment, ), {"size": (512, 512)})
     model = GameOfLife(exp)
     n = model.cells_num

@@ -81,6 +81,25 @@ def test_every_band_matches_oracle(band, generations):
             "band %d, lattice %d %s" % (band, i, SIZES[i])
 
 
+def test_per_size_bands_match_oracle():
+    """Per-size band lengths (as the tuner's second phase sets them, mixed
+    with a common band) against the oracle; clearing them restores the
+    common band."""
+    ens, cells = _ensemble()
+    ens.band = 8
+    ens.size_bands = [[1024, 1024, 32], [128, 1024, 2], [33, 200, 4], [95, 95, 16], [64, 64, 1]]
+    assert sorted(map(tuple, ens.size_bands)) == sorted(
+        [(1024, 1024, 32), (128, 1024, 2), (33, 200, 4), (95, 95, 16), (64, 64, 1)])
+    ens.upload(cells)
+    ens.step(17)
+    got = ens.download()
+    want = _oracle_cached(ens, cells, 17, "mixed")
+    for i in range(ens.count):
+        assert np.array_equal(ens.lattice(got, i), ens.lattice(want, i)), "lattice %d %s" % (i, SIZES[i])
+    ens.band = 8
+    assert ens.size_bands == []
+
+
 def _size_classes(count=4096, base_seed=2041):
     """One lattice of each of the 25 size classes of the seeded 4096-lattice
     ensemble (its first member of that class): widths, heights, rules and
@@ -148,9 +167,10 @@ def test_plain_run_and_tune_agree():
 
 
 def test_tuning_cache_applies_the_stored_band(monkeypatch, tmp_path):
-    # the first tune times and stores its choice; a second ensemble of the
-    # same sizes takes it from the cache (xk_batch_set_band) and steps to the
-    # same cells as the plain form
+    # the first tune times and stores its choices (the common band and the
+    # per-size ones); a second ensemble of the same sizes takes them from the
+    # cache (xk_batch_set_band, xk_batch_set_size_bands) and steps to the same
+    # cells as the plain form
     monkeypatch.setenv("XK_TUNE_CACHE", str(tmp_path / "tune.json"))
     ens, cells = _ensemble(3)
     ens.upload(cells)
@@ -158,12 +178,14 @@ def test_tuning_cache_applies_the_stored_band(monkeypatch, tmp_path):
     plain = ens.download()
     chosen = ens.tune(9)
     assert ens.band == chosen
-    assert list(json.loads((tmp_path / "tune.json").read_text()).values()) == [chosen]
+    sizes = ens.size_bands
+    assert list(json.loads((tmp_path / "tune.json").read_text()).values()) == \
+        [{"band": chosen, "sizes": sizes}]
     again, _ = _ensemble(3)
     for band in (2, 32):
         nat.check(again._lib.xk_batch_set_band(again._handle, band), "xk_batch_set_band")
         assert again.band == band
-    assert again.tune(9) == chosen and again.band == chosen
+    assert again.tune(9) == chosen and again.band == chosen and again.size_bands == sizes
     again.upload(cells)
     again.step(9)
     assert np.array_equal(again.download(), plain)

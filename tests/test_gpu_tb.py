@@ -11,15 +11,21 @@ import numpy as np
 import pytest
 
 import oracle as O
-from tests.models import GameOfLife, GameOfLifeStatic, GOLExperiment2
+from tests.models import GameOfLife, GameOfLifeStatic, GOLExperiment2, LifelikeFixed
 from xentica_gb300 import core
+from xentica_gb300.tools.rules import LifeLike
 
 pytestmark = pytest.mark.gpu
 
 SHAPES = [(64, 64), (70, 9), (100, 75), (1000, 70), (1030, 130), (2049, 131), (97, 600)]
 
 
-def _model(shape, border):
+def _model(shape, border, rule=None):
+    if rule is not None:
+        # a rule read from a table at run time (Conway's B3/S23 has its own
+        # compiled rule form)
+        exp = type("E", (GOLExperiment2, ), {"size": shape, "zoom": 1, "rule": rule})
+        return LifelikeFixed(exp)
     if border == "torus":
         cls = GameOfLife
     else:
@@ -79,21 +85,25 @@ def test_serving_large_requests_at_default_depth():
             assert np.array_equal(h.result(timeout=120).ravel(), fld[:topo.cells])
 
 
-PLANS = {(512, 512): [[1, 0, 0, 0], [2, 16, 2, 0], [2, 4, 1, 0], [2, 8, 4, 0], [3, 0, 0, 2],
-                      [3, 0, 0, 8]],
+PLANS = {(512, 512): [[1, 0, 0, 0], [2, 16, 2, 0], [2, 4, 1, 0], [2, 8, 4, 0], [2, 16, 2, 1],
+                      [2, 3, 4, 1], [2, 16, 4, 1], [2, 8, 1, 1], [3, 0, 0, 2], [3, 0, 0, 8]],
          (2049, 131): [[0, 0, 0, 0], [3, 0, 0, 4], [3, 0, 0, 7]]}
 
 
+@pytest.mark.parametrize("rule", ["B3/S23", "B35678/S5678", "B36/S23"])
 @pytest.mark.parametrize("shape", list(PLANS), ids=["%dx%d" % s for s in PLANS])
-def test_every_plan_kind_matches_oracle(shape):
+def test_every_plan_kind_matches_oracle(shape, rule):
     """Each launch plan the tuner can choose or the cache can re-apply
     (xk_model_set_plan): resident CTA, clusters of several sizes and bands,
     temporal blocking of several depths, the per-generation kernel -- the same
-    cells as the oracle; plans that do not fit the lattice are refused."""
+    cells as the oracle; plans that do not fit the lattice are refused.
+    Conway's Life (the kernels with B3/S23 compiled in) and two rules read
+    from a table at run time."""
     import ctypes
     from xentica_gb300 import _native as nat
+    code = LifeLike.golly2int(rule)
     for plan in PLANS[shape]:
-        model = _model(shape, "torus")
+        model = _model(shape, "torus") if rule == "B3/S23" else _model(shape, "torus", code)
         n = model.cells_num
         cells = (np.random.RandomState(sum(plan)).random_sample(n) < 0.4).astype(np.uint8)
         model.gpu.load(cells, np.zeros(3 * n, np.int32))
@@ -104,12 +114,14 @@ def test_every_plan_kind_matches_oracle(shape):
         out = (ctypes.c_int32 * 4)()
         nat.check(model.gpu._lib.xk_model_plan(model.gpu._handle, out), "xk_model_plan")
         assert list(out) == plan
+        assert model.gpu._lib.xk_model_rule_form(model.gpu._handle) == (rule == "B3/S23")
         model.gpu.step(29)
         topo = O.Topology(shape)
         fld = topo.field(cells, np.uint8)
-        O.life_run(topo, fld, np.zeros(3 * n, np.int32), 29)
+        O.life_run(topo, fld, np.zeros(3 * n, np.int32), 29, born=code & 511, sustain=code >> 9)
         assert np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n]), "plan %s" % plan
-    bad = {(512, 512): [[0, 0, 0, 0], [3, 0, 0, 9], [2, 17, 1, 0], [5, 0, 0, 0]],
+    bad = {(512, 512): [[0, 0, 0, 0], [3, 0, 0, 9], [2, 17, 1, 0], [5, 0, 0, 0], [2, 16, 2, 2],
+                        [2, 16, 3, 1], [2, 3, 1, 1]],
            (2049, 131): [[1, 0, 0, 0], [2, 4, 1, 0], [3, 0, 0, 1]]}[shape]
     model = _model(shape, "torus")
     model.gpu._ensure()

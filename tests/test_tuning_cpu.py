@@ -13,9 +13,9 @@ from xentica_gb300 import tuning
 class FakeLib:
     """Records the tuning calls a batch handle would get."""
 
-    def __init__(self, device=b"GB300 sm_103 SMs=152 smem_optin=232448", best=16):
-        self.device, self.best = device, best
-        self.tuned, self.set = [], []
+    def __init__(self, device=b"GB300 sm_103 SMs=152 smem_optin=232448", best=16, sizes=()):
+        self.device, self.best, self.sizes = device, best, [list(t) for t in sizes]
+        self.tuned, self.set, self.set_sizes = [], [], []
 
     def xk_device_info(self, buf, n):
         buf.value = self.device[:n - 1]
@@ -28,6 +28,15 @@ class FakeLib:
 
     def xk_batch_set_band(self, handle, rows):
         self.set.append(rows)
+        return 0
+
+    def xk_batch_size_bands(self, handle, buf, capacity):
+        for k, t in enumerate(self.sizes[:capacity]):
+            buf[3 * k:3 * k + 3] = t
+        return len(self.sizes)
+
+    def xk_batch_set_size_bands(self, handle, buf, count):
+        self.set_sizes.append([list(buf[3 * k:3 * k + 3]) for k in range(count)])
         return 0
 
 
@@ -107,7 +116,39 @@ def test_invalid_entries_are_ignored(monkeypatch, tmp_path, bad):
     lib = FakeLib(best=4)
     assert tuning.tuned_band(lib, None, W, H, 256, library="L") == 4
     assert lib.tuned == [256] and lib.set == []
-    assert json.loads(path.read_text())[key] == 4
+    assert json.loads(path.read_text())[key] == {"band": 4, "sizes": []}
+
+
+@pytest.mark.parametrize("bad", [{"band": 0}, {"sizes": []}, {"band": 8, "sizes": [[64, 64]]},
+                                 {"band": 8, "sizes": [[64, 64, 0]]},
+                                 {"band": 8, "sizes": [[64, 64, True]]}, {"band": 8, "sizes": 3}])
+def test_invalid_size_entries_are_ignored(monkeypatch, tmp_path, bad):
+    path = tmp_path / "t.json"
+    monkeypatch.setenv("XK_TUNE_CACHE", str(path))
+    key = tuning.ensemble_key(FakeLib().device.decode(), "L", W, H, 256)
+    path.write_text(json.dumps({key: bad}))
+    lib = FakeLib(best=4)
+    assert tuning.tuned_band(lib, None, W, H, 256, library="L") == 4
+    assert lib.tuned == [256] and lib.set == [] and lib.set_sizes == []
+
+
+def test_per_size_bands_are_stored_and_reapplied(monkeypatch, tmp_path):
+    path = tmp_path / "t.json"
+    monkeypatch.setenv("XK_TUNE_CACHE", str(path))
+    lib = FakeLib(best=16, sizes=[[1024, 512, 32], [128, 256, 4]])
+    assert tuning.tuned_band(lib, None, W, H, 256, library="L") == 16
+    key = tuning.ensemble_key(lib.device.decode(), "L", W, H, 256)
+    assert json.loads(path.read_text())[key] == {"band": 16,
+                                                 "sizes": [[1024, 512, 32], [128, 256, 4]]}
+    again = FakeLib(best=2)                        # would time differently: not asked
+    assert tuning.tuned_band(again, None, W, H, 256, library="L") == 16
+    assert again.tuned == [] and again.set == [16]
+    assert again.set_sizes == [[[1024, 512, 32], [128, 256, 4]]]
+    # the older form without per-size choices still applies
+    path.write_text(json.dumps({key: 8}))
+    old = FakeLib(best=2)
+    assert tuning.tuned_band(old, None, W, H, 256, library="L") == 8
+    assert old.tuned == [] and old.set == [8] and old.set_sizes == []
 
 
 def test_library_id_tracks_the_file(tmp_path):
@@ -130,9 +171,12 @@ def test_unidentifiable_library_tunes_without_cache(monkeypatch, tmp_path):
 class FakePlanLib(FakeLib):
     """Records the plan calls a 2-D Life-like model handle would get."""
 
-    def __init__(self, plan=(2, 16, 2, 0), **kw):
+    def __init__(self, plan=(2, 16, 2, 0), form=0, **kw):
         super().__init__(**kw)
-        self.plan, self.timed, self.applied = list(plan), 0, []
+        self.plan, self.timed, self.applied, self.form = list(plan), 0, [], form
+
+    def xk_model_rule_form(self, handle):
+        return self.form
 
     def xk_model_plan(self, handle, out):
         self.timed += 1
@@ -162,6 +206,22 @@ def test_lattice_plan_stored_then_applied(monkeypatch, tmp_path, plan):
     other = FakePlanLib(device=b"another device", plan=(3, 0, 0, 4))
     assert tuning.lattice_plan(other, None, 512, 512, "torus", library="L") == [3, 0, 0, 4]
     assert lib.timed == 4 and other.timed == 1
+
+
+def test_lattice_plan_keys_on_the_rule_form(monkeypatch, tmp_path):
+    """Conway's rule runs kernels with the rule compiled in: its plan is
+    timed and kept apart from the plan of a rule read from a table."""
+    monkeypatch.setenv("XK_TUNE_CACHE", str(tmp_path / "t.json"))
+    table = FakePlanLib(plan=(2, 16, 2, 0), form=0)
+    assert tuning.lattice_plan(table, None, 512, 512, "torus", library="L") == [2, 16, 2, 0]
+    conway = FakePlanLib(plan=(2, 8, 4, 0), form=1)
+    assert tuning.lattice_plan(conway, None, 512, 512, "torus", library="L") == [2, 8, 4, 0]
+    assert table.timed == 1 and conway.timed == 1
+    again = FakePlanLib(plan=(0, 0, 0, 0), form=1)
+    assert tuning.lattice_plan(again, None, 512, 512, "torus", library="L") == [2, 8, 4, 0]
+    assert again.timed == 0 and again.applied == [[2, 8, 4, 0]]
+    assert tuning.lattice_key("d", "L", 512, 512, "torus", 0) != \
+        tuning.lattice_key("d", "L", 512, 512, "torus", 1)
 
 
 def test_lattice_plan_rejected_or_invalid_entries_retime(monkeypatch, tmp_path):

@@ -107,6 +107,9 @@ SIGNATURES = {
     "xk_batch_remove": (_I32, [_P, _I32]),
     "xk_batch_count": (_I32, [_P]),
     "xk_batch_band": (_I32, [_P]),
+    "xk_model_rule_form": (_I32, [_P]),
+    "xk_batch_set_size_bands": (_I32, [_P, _P, _I32]),
+    "xk_batch_size_bands": (_I32, [_P, _P, _I32]),
     "xk_batch_total_cells": (_I64, [_P]),
     "xk_batch_launches": (_I64, [_P, _I32]),
     "xk_batch_step_noalloc": (_I32, [_P, _I32, _P, _P, _P, _I32, _P]),

@@ -195,7 +195,9 @@ class Ensemble:
         return self._lib.xk_last_step_ms()
 
     def tune(self, generations, cache=True):
-        """Pick the resident kernel's band length by timing; returns it.  With
+        """Pick the resident kernel's band lengths by timing (one for every
+        lattice, then per lattice size where that is faster: :attr:`band`,
+        :attr:`size_bands`); returns the common one.  With
         ``cache`` the choice is kept in the tuning cache
         (:mod:`xentica_gb300.tuning`, keyed by device, library build, lattice
         sizes and ``generations``) and a later tune of the same workload
@@ -212,3 +214,13 @@ class Ensemble:
     def band(self, rows_per_band):
         nat.check(self._lib.xk_batch_set_band(self._handle, int(rows_per_band)),
                   "xk_batch_set_band")
+
+    @property
+    def size_bands(self):
+        """Per-size band lengths ``[[W, H, band], ...]`` overriding :attr:`band`
+        for the lattices of those sizes (the tuner's per-size choices)."""
+        return tuning.size_bands(self._lib, self._handle)
+
+    @size_bands.setter
+    def size_bands(self, triples):
+        tuning.apply_bands(self._lib, self._handle, self.band, [list(t) for t in triples])

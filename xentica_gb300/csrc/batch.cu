@@ -36,6 +36,7 @@ namespace {
 struct Class {
     int threads = 0, smem = 0;
     int first = 0, count = 0;      // range in the sorted instance table
+    int priority = 0;              // launch priority: larger CTAs (longer runs) first
     cudaStream_t stream = nullptr;
 };
 
@@ -55,6 +56,9 @@ struct xk_batch {
     std::vector<Class> classes;
     std::vector<int> big;          // instances run with the plain kernel
     int rows_per_band = 8;
+    // band length of the lattices of one size (W, H), overriding
+    // rows_per_band (the tuner's per-size choices)
+    std::map<std::pair<int, int>, int> size_band;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, fork = nullptr;
     std::vector<cudaEvent_t> joins;
@@ -131,7 +135,14 @@ static void free_batch(xk_batch *b)
 static inline uint32_t rule0_of(uint32_t golly) { return golly & 511u; }
 static inline uint32_t rule1_of(uint32_t golly) { return (golly & 511u) | ((golly >> 9) & 511u); }
 
-// (re)build the class table for the current rows_per_band
+// band length of a W x H lattice: its size's override, else rows_per_band
+static int band_for(const xk_batch *b, int W, int H)
+{
+    auto it = b->size_band.find(std::make_pair(W, H));
+    return it == b->size_band.end() ? b->rows_per_band : it->second;
+}
+
+// (re)build the class table for the current band lengths
 static int plan_classes(xk_batch *b)
 {
     destroy_graphs(b);
@@ -150,7 +161,7 @@ static int plan_classes(xk_batch *b)
     std::vector<Item> items;
     for (int i = 0; i < b->n; ++i) {
         int threads = 0, smem = 0;
-        if (xk_life_resident_config(b->W[i], b->H[i], b->rows_per_band, &threads, &smem))
+        if (xk_life_resident_config(b->W[i], b->H[i], band_for(b, b->W[i], b->H[i]), &threads, &smem))
             items.push_back({i, threads, smem, (int64_t)b->W[i] * b->H[i]});
         else
             b->big.push_back(i);
@@ -190,8 +201,15 @@ static int plan_classes(xk_batch *b)
         in.smem_words = it.smem / 4;
         b->h_inst.push_back(in);
     }
+    // classes come sorted by block size, largest first; their CTAs run longest,
+    // so they get the greater launch priorities and the block scheduler
+    // dispatches them first (longest work first packs the SMs best)
+    int prio_least = 0, prio_greatest = 0;
+    XK_CUDA(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
+    for (size_t k = 0; k < b->classes.size(); ++k)
+        b->classes[k].priority = prio_greatest + std::min<int>((int)k, prio_least - prio_greatest);
     for (auto &c : b->classes) {
-        XK_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+        XK_CUDA(cudaStreamCreateWithPriority(&c.stream, cudaStreamNonBlocking, c.priority));
         cudaEvent_t e;
         XK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         b->joins.push_back(e);
@@ -308,7 +326,7 @@ static int enqueue_batched(xk_batch *b, int generations)
         const Class &c = b->classes[k];
         XK_CUDA(cudaStreamWaitEvent(c.stream, b->fork, 0));
         XK_CUDA(xk_life_step_resident(b->d_inst + c.first, c.count, b->cells, 1, generations, 1, 0u,
-                                      b->bad, c.threads, c.smem, c.stream));
+                                      b->bad, c.threads, c.smem, c.stream, XK_RULE_TABLE, c.priority));
         XK_CUDA(cudaEventRecord(b->joins[k], c.stream));
     }
     for (int i : b->big) {
@@ -360,7 +378,7 @@ static int graph_for(xk_batch *b, int generations, cudaGraphExec_t *exec)
     }
     XK_CUDA(e);
     cudaGraphExec_t g = nullptr;
-    e = cudaGraphInstantiate(&g, graph, 0);
+    e = cudaGraphInstantiate(&g, graph, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(graph);
     XK_CUDA(e);
     b->graphs[generations] = g;
@@ -736,12 +754,15 @@ extern "C" int xk_batch_set_band(xk_batch *b, int32_t rows_per_band)
     XK_REQUIRE(b, XK_ERR_ARG, "xk_batch_set_band: null batch");
     XK_REQUIRE(rows_per_band >= 1 && rows_per_band <= 1024, XK_ERR_ARG,
                "xk_batch_set_band: rows per band must be 1..1024, got %d", (int)rows_per_band);
-    if (rows_per_band == b->rows_per_band) return XK_OK;
+    if (rows_per_band == b->rows_per_band && b->size_band.empty()) return XK_OK;
     const int old = b->rows_per_band;
+    std::map<std::pair<int, int>, int> old_sizes;
+    old_sizes.swap(b->size_band);
     b->rows_per_band = rows_per_band;
     const int rc = plan_classes(b);
     if (rc != XK_OK) {
         b->rows_per_band = old;
+        b->size_band.swap(old_sizes);
         plan_classes(b);
     }
     return rc;
@@ -752,47 +773,171 @@ extern "C" int32_t xk_batch_band(const xk_batch *b)
     return b ? b->rows_per_band : 0;
 }
 
+extern "C" int xk_batch_set_size_bands(xk_batch *b, const int32_t *triples, int32_t count)
+{
+    XK_REQUIRE(b && (triples || count == 0), XK_ERR_ARG, "xk_batch_set_size_bands: null argument");
+    XK_REQUIRE(count >= 0 && count <= 4096, XK_ERR_ARG,
+               "xk_batch_set_size_bands: count %d out of [0, 4096]", (int)count);
+    std::map<std::pair<int, int>, int> sizes;
+    for (int k = 0; k < count; ++k) {
+        const int W = triples[3 * k], H = triples[3 * k + 1], band = triples[3 * k + 2];
+        XK_REQUIRE(W >= 1 && H >= 1 && band >= 1 && band <= 1024, XK_ERR_ARG,
+                   "xk_batch_set_size_bands: entry %d (%d x %d, band %d) out of range", k, W, H, band);
+        sizes[std::make_pair(W, H)] = band;
+    }
+    if (sizes == b->size_band) return XK_OK;
+    sizes.swap(b->size_band);
+    const int rc = plan_classes(b);
+    if (rc != XK_OK) {
+        b->size_band.swap(sizes);
+        plan_classes(b);
+    }
+    return rc;
+}
+
+extern "C" int32_t xk_batch_size_bands(const xk_batch *b, int32_t *triples, int32_t capacity)
+{
+    if (!b) return -1;
+    int32_t k = 0;
+    for (const auto &kv : b->size_band) {
+        if (triples && k < capacity) {
+            triples[3 * k] = kv.first.first;
+            triples[3 * k + 1] = kv.first.second;
+            triples[3 * k + 2] = kv.second;
+        }
+        ++k;
+    }
+    return k;
+}
+
+// device time of one graph launch of the current plan (the graph is built,
+// and run once untimed, first)
+static int time_plan(xk_batch *b, int generations, float *ms)
+{
+    int rc = plan_classes(b);
+    if (rc != XK_OK) return rc;
+    if ((rc = launch_batched(b, generations)) != XK_OK) return rc;
+    XK_CUDA(cudaEventRecord(b->ev0, b->stream));
+    if ((rc = launch_batched(b, generations)) != XK_OK) return rc;
+    XK_CUDA(cudaEventRecord(b->ev1, b->stream));
+    XK_CUDA(cudaEventSynchronize(b->ev1));
+    XK_CUDA(cudaEventElapsedTime(ms, b->ev0, b->ev1));
+    return XK_OK;
+}
+
+// Band lengths by timing the whole batch (on a copy of the state, so tuning
+// never changes the cells).  (1) One band for every lattice: the candidates
+// are timed in turn, three rounds (a clock that changes during tuning then
+// biases no candidate), best of the three per candidate.  (2) Per lattice
+// size, largest shares of the cells first, for every size holding at least 3
+// % of them: each candidate that gives that size another CTA shape is timed
+// (best of two) against the current plan; one that looks at least 3 % faster
+// is timed again, alternating with the current plan three more times, and
+// kept only when its best time stays at least 2 % below the current plan's
+// (a graph launch of the whole batch varies by a few per cent from run to
+// run, so smaller gains are not told apart from noise).
 extern "C" int xk_batch_tune(xk_batch *b, int32_t generations, int32_t *chosen)
 {
     XK_REQUIRE(b && chosen, XK_ERR_ARG, "xk_batch_tune: null argument");
     XK_REQUIRE(generations > 0, XK_ERR_ARG, "xk_batch_tune: generations must be positive");
-    // candidates for the band length; each is timed on a copy of the state so
-    // tuning never changes the batch's cells
     static const int cand[] = {2, 4, 8, 16, 32};
+    const int ncand = (int)(sizeof(cand) / sizeof(cand[0]));
     uint8_t *keep = nullptr;
     XK_CUDA(cudaMalloc(&keep, (size_t)b->total + 16));
     XK_CUDA(cudaMemcpyAsync(keep, b->cells, (size_t)b->total, cudaMemcpyDeviceToDevice, b->stream));
-    float best = 1e30f;
-    int best_rpb = b->rows_per_band;
+    const int old_rpb = b->rows_per_band;
+    std::map<std::pair<int, int>, int> old_sizes;
+    old_sizes.swap(b->size_band);
     int rc = XK_OK;
-    for (int r : cand) {
-        b->rows_per_band = r;
-        if ((rc = plan_classes(b)) != XK_OK) break;
-        // best of three timed launches after one that builds the graph
-        float ms = 1e30f;
-        if ((rc = launch_batched(b, generations)) != XK_OK) break;
-        for (int rep = 0; rep < 3; ++rep) {
+    float best[8];
+    for (int c = 0; c < ncand; ++c) best[c] = 1e30f;
+    for (int round = 0; round < 3 && rc == XK_OK; ++round)
+        for (int c = 0; c < ncand && rc == XK_OK; ++c) {
+            b->rows_per_band = cand[c];
             float t = 0.f;
-            cudaEventRecord(b->ev0, b->stream);
-            if ((rc = launch_batched(b, generations)) != XK_OK) break;
-            cudaEventRecord(b->ev1, b->stream);
-            cudaEventSynchronize(b->ev1);
-            cudaEventElapsedTime(&t, b->ev0, b->ev1);
-            ms = std::min(ms, t);
+            if ((rc = time_plan(b, generations, &t)) == XK_OK) best[c] = std::min(best[c], t);
         }
-        if (rc != XK_OK) break;
-        if (ms < best) {
-            best = ms;
-            best_rpb = r;
+    int bc = 0;
+    for (int c = 1; c < ncand; ++c)
+        if (best[c] < best[bc]) bc = c;
+    b->rows_per_band = cand[bc];
+    if (rc == XK_OK) {
+        std::map<std::pair<int, int>, int64_t> cells;
+        int64_t all = 0;
+        for (int i = 0; i < b->n; ++i) {
+            cells[std::make_pair(b->W[i], b->H[i])] += (int64_t)b->W[i] * b->H[i];
+            all += (int64_t)b->W[i] * b->H[i];
+        }
+        std::vector<std::pair<int64_t, std::pair<int, int>>> order;
+        for (const auto &kv : cells)
+            if (kv.second * 100 >= all * 3) order.push_back(std::make_pair(kv.second, kv.first));
+        std::sort(order.rbegin(), order.rend());
+        for (const auto &o : order) {
+            if (rc != XK_OK) break;
+            const int W = o.second.first, H = o.second.second;
+            int th0 = 0, sm0 = 0;
+            if (!xk_life_resident_config(W, H, band_for(b, W, H), &th0, &sm0)) continue;
+            float cur = 1e30f;
+            for (int rep = 0; rep < 2 && rc == XK_OK; ++rep) {
+                float t = 0.f;
+                if ((rc = time_plan(b, generations, &t)) == XK_OK) cur = std::min(cur, t);
+            }
+            std::vector<int> seen_threads{th0};
+            for (int c = 0; c < ncand && rc == XK_OK; ++c) {
+                int th = 0, sm = 0;
+                if (!xk_life_resident_config(W, H, cand[c], &th, &sm)) continue;
+                if (std::find(seen_threads.begin(), seen_threads.end(), th) != seen_threads.end()) continue;
+                seen_threads.push_back(th);
+                const int before = band_for(b, W, H);
+                const bool had = b->size_band.count(std::make_pair(W, H)) > 0;
+                auto set_trial = [&](bool on) {
+                    if (on) b->size_band[std::make_pair(W, H)] = cand[c];
+                    else if (had) b->size_band[std::make_pair(W, H)] = before;
+                    else b->size_band.erase(std::make_pair(W, H));
+                };
+                set_trial(true);
+                float t = 1e30f;
+                for (int rep = 0; rep < 2 && rc == XK_OK; ++rep) {
+                    float u = 0.f;
+                    if ((rc = time_plan(b, generations, &u)) == XK_OK) t = std::min(t, u);
+                }
+                bool keep = rc == XK_OK && t < cur * 0.97f;
+                if (keep) {
+                    // confirm: the current plan and the trial alternately
+                    float base = cur;
+                    for (int rep = 0; rep < 3 && rc == XK_OK; ++rep) {
+                        float u = 0.f;
+                        set_trial(false);
+                        if ((rc = time_plan(b, generations, &u)) != XK_OK) break;
+                        base = std::min(base, u);
+                        set_trial(true);
+                        if ((rc = time_plan(b, generations, &u)) != XK_OK) break;
+                        t = std::min(t, u);
+                    }
+                    keep = rc == XK_OK && t < base * 0.98f;
+                    cur = keep ? t : base;
+                }
+                if (keep) {
+                    set_trial(true);
+                } else if (had) {
+                    b->size_band[std::make_pair(W, H)] = before;
+                } else {
+                    b->size_band.erase(std::make_pair(W, H));
+                }
+            }
         }
     }
     cudaMemcpyAsync(b->cells, keep, (size_t)b->total, cudaMemcpyDeviceToDevice, b->stream);
     cudaStreamSynchronize(b->stream);
     cudaFree(keep);
-    if (rc != XK_OK) return rc;
-    b->rows_per_band = best_rpb;
+    if (rc != XK_OK) {
+        b->rows_per_band = old_rpb;
+        b->size_band.swap(old_sizes);
+        plan_classes(b);
+        return rc;
+    }
     rc = plan_classes(b);
-    *chosen = best_rpb;
+    *chosen = b->rows_per_band;
     return rc;
 }
 

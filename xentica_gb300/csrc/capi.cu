@@ -5,6 +5,7 @@
 #include <stdarg.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 #include <new>
 
@@ -151,6 +152,7 @@ struct xk_model {
     int resident = 0, res_threads = 0, res_smem = 0;
     int cl_tuned = 0, cl_C = 0, cl_R = 0, cl_threads = 0;   // cluster plan (cl_C = 0: none)
     int cl_want = 0, cl_band = 0;    // the cluster size and band length the plan was made from
+    int cl_p2p = 0;                  // the cluster plan's neighbour form of synchronisation
     int tb_T = 0;                // temporally blocked global kernel: generations per launch (0: none)
     uint32_t rule0 = 0, rule1 = 0;
     int32_t lut[6] = {0, 0, 0, 0, 0, 0};
@@ -228,6 +230,7 @@ static int tune_cluster(xk_model *m)
 {
     m->cl_tuned = 1;
     m->cl_C = 0;
+    m->cl_p2p = 0;
     m->tb_T = 0;
     const char *tenv = getenv("XK_TB");
     if (tenv && tenv[0]) {
@@ -248,6 +251,8 @@ static int tune_cluster(xk_model *m)
             m->cl_threads = th;
             m->cl_want = want;
             m->cl_band = band;
+            const char *senv = getenv("XK_CLUSTER_SYNC");
+            m->cl_p2p = senv && strcmp(senv, "p2p") == 0 && xk_life_cluster_has_p2p(m->lg, R, th);
         }
         return XK_OK;
     }
@@ -255,14 +260,29 @@ static int tune_cluster(xk_model *m)
     uint32_t *scratch = m->bits[1 - m->cur];
     XK_CUDA(cudaMemcpyAsync(scratch, m->bits[m->cur], bytes, cudaMemcpyDeviceToDevice, m->stream));
     const int G = 32;
+    const int rf = xk_rule_form(m->rule0, m->rule1);
+    // device time of `run` (G generations): one untimed run, then the best
+    // of three timed ones
+    auto time_it = [&](auto run, float *best_ms) -> cudaError_t {
+        cudaError_t e = run();
+        *best_ms = 1e30f;
+        for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+            float ms = 0.f;
+            e = cudaEventRecord(m->ev0, m->stream);
+            if (e == cudaSuccess) e = run();
+            if (e == cudaSuccess) e = cudaEventRecord(m->ev1, m->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(m->ev1);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, m->ev0, m->ev1);
+            if (e == cudaSuccess) *best_ms = std::min(*best_ms, ms);
+        }
+        return e;
+    };
     float best = 1e30f;
     if (m->resident) {
-        XK_CUDA(cudaEventRecord(m->ev0, m->stream));
-        XK_CUDA(xk_life_step_resident(m->d_inst, 1, scratch, 0, G, m->lg.torus, m->lg.bfill, nullptr,
-                                      m->res_threads, m->res_smem, m->stream));
-        XK_CUDA(cudaEventRecord(m->ev1, m->stream));
-        XK_CUDA(cudaEventSynchronize(m->ev1));
-        XK_CUDA(cudaEventElapsedTime(&best, m->ev0, m->ev1));
+        XK_CUDA(time_it([&]() {
+            return xk_life_step_resident(m->d_inst, 1, scratch, 0, G, m->lg.torus, m->lg.bfill, nullptr,
+                                         m->res_threads, m->res_smem, m->stream, rf);
+        }, &best));
     }
     if (xk_life_tb_supported(m->lg)) {
         // temporal blocking, 2..8 generations per launch, ping-pong through
@@ -277,16 +297,16 @@ static int tune_cluster(xk_model *m)
         for (int T : depths) {
             if (T == 1 && m->resident) continue;
             float ms = 0.f;
-            uint32_t *a = scratch, *b = tmp;
-            e = cudaEventRecord(m->ev0, m->stream);
-            for (int g = 0; g < G && e == cudaSuccess; g += T) {
-                e = T == 1 ? xk_life_step_global(a, b, m->lg, t, m->stream)
-                           : xk_life_step_tb(a, b, m->lg, t9, T, m->stream);
-                std::swap(a, b);
-            }
-            if (e == cudaSuccess) e = cudaEventRecord(m->ev1, m->stream);
-            if (e == cudaSuccess) e = cudaEventSynchronize(m->ev1);
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, m->ev0, m->ev1);
+            e = time_it([&]() {
+                uint32_t *a = scratch, *b = tmp;
+                cudaError_t r = cudaSuccess;
+                for (int g = 0; g < G && r == cudaSuccess; g += T) {
+                    r = T == 1 ? xk_life_step_global(a, b, m->lg, t, m->stream)
+                               : xk_life_step_tb(a, b, m->lg, t9, T, m->stream);
+                    std::swap(a, b);
+                }
+                return r;
+            }, &ms);
             if (e != cudaSuccess) break;
             if (ms < best) {
                 best = ms;
@@ -296,18 +316,22 @@ static int tune_cluster(xk_model *m)
         cudaFree(tmp);
         XK_CUDA(e);
     }
+    // clusters: sizes, band lengths and both synchronisation forms
     static const int cand[] = {16, 8, 4, 2};
     static const int bands[] = {1, 2, 4};
-    for (int k = 0; k < 12; ++k) {
-        const int want = cand[k / 3], band = bands[k % 3];
+    for (int k = 0; k < 24; ++k) {
+        const int want = cand[k / 6], band = bands[(k / 2) % 3], p2p = k & 1;
         int C = 0, R = 0, th = 0;
         if (!xk_life_cluster_config(m->lg, want, band, &C, &R, &th)) continue;
+        if (p2p && !xk_life_cluster_has_p2p(m->lg, R, th)) continue;
         float ms = 0.f;
-        XK_CUDA(cudaEventRecord(m->ev0, m->stream));
-        XK_CUDA(xk_life_step_cluster(scratch, m->lg, m->rule0, m->rule1, G, C, R, th, m->stream));
-        XK_CUDA(cudaEventRecord(m->ev1, m->stream));
-        XK_CUDA(cudaEventSynchronize(m->ev1));
-        XK_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+        XK_CUDA(time_it([&]() {
+            return xk_life_step_cluster(scratch, m->lg, m->rule0, m->rule1, G, C, R, th, m->stream, p2p);
+        }, &ms));
+        if (xk_cluster_take_wait_failure()) {
+            xk_set_error("cluster step: a CTA gave up waiting for its neighbours' rows");
+            return XK_ERR_TIMEOUT;
+        }
         if (ms < best) {
             best = ms;
             m->cl_C = C;
@@ -315,6 +339,7 @@ static int tune_cluster(xk_model *m)
             m->cl_threads = th;
             m->cl_want = want;
             m->cl_band = band;
+            m->cl_p2p = p2p;
             m->tb_T = 0;
         }
     }
@@ -593,6 +618,13 @@ extern "C" int xk_download(xk_model *m, void *host_main, int64_t ncells)
     XK_CUDA(cudaMemcpyAsync(host_main, m->stage, (size_t)m->n * esz, cudaMemcpyDeviceToHost,
                             m->stream));
     XK_CUDA(cudaStreamSynchronize(m->stream));
+    // the neighbour form of the cluster kernel records bounded waits that
+    // gave up; the steps do not synchronise, so it is checked here
+    if (m->layout == LAYOUT_BITS2D && xk_cluster_take_wait_failure()) {
+        xk_set_error("cluster step: a CTA gave up waiting for its neighbours' rows; the cells are "
+                     "not valid");
+        return XK_ERR_TIMEOUT;
+    }
     return XK_OK;
 }
 
@@ -763,7 +795,7 @@ static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *fram
         while (left > 0) {
             const int g = (int)(left > 4096 ? 4096 : left);
             XK_CUDA(xk_life_step_cluster(m->bits[m->cur], m->lg, m->rule0, m->rule1, g, m->cl_C, m->cl_R,
-                                         m->cl_threads, m->stream));
+                                         m->cl_threads, m->stream, m->cl_p2p));
             left -= g;
         }
     } else if (m->d.family == XK_FAMILY_SHIFT && m->d.torus && colors_free && shift_jump_enabled()) {
@@ -790,7 +822,7 @@ static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *fram
             const int g = (int)(left > 4096 ? 4096 : left);
             XK_CUDA(xk_life_step_resident(m->d_inst, 1, m->bits[m->cur], 0, g, m->lg.torus,
                                           m->lg.bfill, nullptr, m->res_threads, m->res_smem,
-                                          m->stream));
+                                          m->stream, xk_rule_form(m->rule0, m->rule1)));
             left -= g;
         }
     } else {
@@ -800,7 +832,8 @@ static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *fram
                 if (m->resident)
                     XK_CUDA(xk_life_step_resident(m->d_inst, 1, m->bits[m->cur], 0, 1, m->lg.torus,
                                                   m->lg.bfill, nullptr, m->res_threads,
-                                                  m->res_smem, m->stream));
+                                                  m->res_smem, m->stream,
+                                                  xk_rule_form(m->rule0, m->rule1)));
                 else {
                     XK_CUDA(xk_life_step_global(m->bits[m->cur], m->bits[1 - m->cur], m->lg, t,
                                                 m->stream));
@@ -883,7 +916,7 @@ extern "C" int xk_model_plan(xk_model *m, int32_t plan[4])
         plan[0] = XK_PLAN_CLUSTER;
         plan[1] = m->cl_want;
         plan[2] = m->cl_band;
-        plan[3] = 0;
+        plan[3] = m->cl_p2p;
     } else if (m->tb_T > 1) {
         plan[0] = XK_PLAN_TEMPORAL;
         plan[1] = plan[2] = 0;
@@ -893,6 +926,12 @@ extern "C" int xk_model_plan(xk_model *m, int32_t plan[4])
         plan[1] = plan[2] = plan[3] = 0;
     }
     return XK_OK;
+}
+
+extern "C" int32_t xk_model_rule_form(const xk_model *m)
+{
+    if (!m || m->layout != LAYOUT_BITS2D) return -1;
+    return xk_rule_form(m->rule0, m->rule1);
 }
 
 extern "C" int xk_model_set_plan(xk_model *m, const int32_t plan[4])
@@ -914,6 +953,9 @@ extern "C" int xk_model_set_plan(xk_model *m, const int32_t plan[4])
                        xk_life_cluster_config(m->lg, plan[1], plan[2], &C, &R, &th),
                    XK_ERR_ARG, "xk_model_set_plan: no cluster of %d CTAs with bands of %d rows",
                    plan[1], plan[2]);
+        XK_REQUIRE(plan[3] == 0 || (plan[3] == 1 && xk_life_cluster_has_p2p(m->lg, R, th)), XK_ERR_ARG,
+                   "xk_model_set_plan: cluster synchronisation form %d (0, or 1 for bands of 1, 2 "
+                   "or 4 rows)", plan[3]);
         break;
     case XK_PLAN_TEMPORAL:
         XK_REQUIRE(plan[3] >= 2 && plan[3] <= 8 && xk_life_tb_supported(m->lg), XK_ERR_ARG,
@@ -928,6 +970,7 @@ extern "C" int xk_model_set_plan(xk_model *m, const int32_t plan[4])
     m->cl_threads = th;
     m->cl_want = plan[0] == XK_PLAN_CLUSTER ? plan[1] : 0;
     m->cl_band = plan[0] == XK_PLAN_CLUSTER ? plan[2] : 0;
+    m->cl_p2p = plan[0] == XK_PLAN_CLUSTER ? plan[3] : 0;
     m->tb_T = plan[0] == XK_PLAN_TEMPORAL ? plan[3] : 0;
     return XK_OK;
 }

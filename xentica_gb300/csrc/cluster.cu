@@ -15,15 +15,34 @@
 // double-buffered by generation parity: generation g reads the parity-g
 // buffers (all local loads) and, as it computes a band's first and last row,
 // stores them straight from registers into the parity-(g + 1) buffers, last
-// read by generation g - 1.  One cluster barrier starts every generation: it
-// orders the stores of generation g - 1 before the loads of generation g and
-// the loads of generation g - 1 before the stores of generation g (release /
-// acquire at cluster scope; every thread of every CTA arrives once per
-// generation and no CTA leaves the loop early).  It is the hardware cluster
-// barrier, so there is no software spin to bound.  A last barrier after the
-// loop keeps every CTA's shared memory alive until the remote stores of the
-// final generation have landed.  A lane only ever touches its own column word
-// of its own band.
+// read by generation g - 1.  Two ways to order that:
+//
+// * barrier form: one cluster barrier starts every generation; it orders the
+//   stores of generation g - 1 before the loads of generation g and the loads
+//   of generation g - 1 before the stores of generation g (release / acquire
+//   at cluster scope; every thread of every CTA arrives once per generation
+//   and no CTA leaves the loop early).  It is the hardware cluster barrier,
+//   so there is no software spin to bound.
+// * neighbour form (P2P): only the two CTAs a slab exchanges rows with are
+//   waited for.  Each CTA has one mbarrier per slot parity, expecting 2 wpr
+//   arrivals a phase: every lane that stores a row word into a neighbour's
+//   slot then arrives on that neighbour's mbarrier with release semantics at
+//   cluster scope, and the lanes of a slab's first and last band wait
+//   (acquire, cluster scope) on their own mbarrier before reading the slots.
+//   Bands inside the CTA are ordered by one __syncthreads per generation.
+//   The write-after-read order needs nothing more: a lane writes parity
+//   (g + 1) slots of a neighbour only after it has received that
+//   neighbour's generation g - 1 row, which the neighbour sent after reading
+//   the parity (g - 1) = (g + 1) slot; and a phase's arrivals all come
+//   before the next phase's can start.  The last generation sends nothing.
+//   Waits are bounded (1 s): a CTA that gives up sets xk_cluster_wait_failed and
+//   leaves the generation loop (every thread at once, through
+//   __syncthreads_or), its neighbours then give up in turn, and the step
+//   reports XK_ERR_TIMEOUT.
+//
+// A last cluster barrier after the loop keeps every CTA's shared memory alive
+// until the remote stores of the final generation have landed.  A lane only
+// ever touches its own column word of its own band.
 #include <cooperative_groups.h>
 
 #include <string.h>
@@ -34,21 +53,78 @@
 namespace cg = cooperative_groups;
 
 // shared words: slab of the widest CTA (R rows), halos [2][G][2][wpr], slots
-// [2][2][wpr]; the offsets are the same in every CTA of the cluster, which
-// the remote stores rely on
-static inline int64_t cluster_words(int wpr, int R, int threads)
+// [2][2][wpr], then (rounded to 8 bytes) the neighbour form's two mbarriers;
+// the offsets are the same in every CTA of the cluster, which the remote
+// stores and arrivals rely on
+static inline int64_t cluster_data_words(int wpr, int R, int threads)
 {
     const ResidentPlan p = xk_resident_plan(wpr, R, threads);
     return xk_res_lat_words(p) + 4LL * p.G * wpr + 4LL * wpr;
 }
 
+static inline int64_t cluster_words(int wpr, int R, int threads)
+{
+    return ((cluster_data_words(wpr, R, threads) + 1) & ~1LL) + 4;
+}
+
+#define XK_CL_WAIT_NS 1000000000ull   // a CTA gives up after 1 s of waiting (never expected)
+
+// set when a CTA of the neighbour form gave up waiting (never expected)
+__device__ unsigned int xk_cluster_wait_failed;
+
+__device__ __forceinline__ bool xk_cl_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t done;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ uint64_t xk_globaltimer()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// wait for the phase of `parity` to complete; false after XK_CL_WAIT_NS
+__device__ __forceinline__ bool xk_cl_wait(uint32_t bar, uint32_t parity)
+{
+    if (xk_cl_try_wait(bar, parity)) return true;
+    const uint64_t t0 = xk_globaltimer();
+    while (!xk_cl_try_wait(bar, parity))
+        if (xk_globaltimer() - t0 > XK_CL_WAIT_NS) return false;
+    return true;
+}
+
+// arrive on the mbarrier at shared::cluster address `bar` (another CTA's),
+// ordering this thread's earlier stores before it
+__device__ __forceinline__ void xk_cl_arrive_remote(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" : : "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ uint32_t xk_cl_mapa(uint32_t addr, uint32_t rank)
+{
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+    return r;
+}
+
 // TORUS: wrap, else static border; FULLW: torus rows of whole words (each
 // neighbour vector one funnel shift); LB: every band of the widest CTA has
-// exactly LB rows (1, 2 or 4; the row loop is unrolled), 0 for any length
-template <bool TORUS, bool FULLW, int LB>
+// exactly LB rows (1, 2 or 4; the row loop is unrolled), 0 for any length;
+// RF: the rule form (XK_RULE_TABLE: `t`; XK_RULE_CONWAY: B3/S23 compiled in);
+// P2P: the neighbour form of synchronisation instead of the barrier form
+template <bool TORUS, bool FULLW, int LB, int RF, bool P2P>
 __global__ void __launch_bounds__(1024)
-xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t, int generations, int R)
+xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int generations, int R)
 {
+    const auto &t = RuleForm<RF>::make(t9);
     extern __shared__ uint32_t sm[];
     cg::cluster_group cluster = cg::this_cluster();
     const int C = (int)cluster.num_blocks();
@@ -65,6 +141,19 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t, int gene
     uint32_t *slot_up = cluster.map_shared_rank(slot, cu);
     uint32_t *slot_dn = cluster.map_shared_rank(slot, cd);
     const int hwords = 2 * pw.G * wpr;
+    // neighbour form: mbarrier [parity] (8-byte aligned, after the data)
+    const int64_t dwords = xk_res_lat_words(pw) + 4LL * pw.G * wpr + 4LL * wpr;
+    uint64_t *mbar = (uint64_t *)(sm + ((dwords + 1) & ~1LL));
+    const uint32_t mbar0 = (uint32_t)__cvta_generic_to_shared(mbar);
+    if (P2P && threadIdx.x == 0) {
+        for (int q = 0; q < 2; ++q)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" : : "r"(mbar0 + 8u * q), "r"(2 * wpr)
+                         : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" : : : "memory");
+    }
+    // the neighbours' mbarriers [parity] at shared::cluster addresses
+    const uint32_t mb_up = P2P ? xk_cl_mapa(mbar0, (uint32_t)cu) : 0u;
+    const uint32_t mb_dn = P2P ? xk_cl_mapa(mbar0, (uint32_t)cd) : 0u;
 
     for (int w = threadIdx.x; w < Rc * wpr; w += blockDim.x) {
         const int y = w / wpr, jj = w - y * wpr;
@@ -118,25 +207,46 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t, int gene
     // a band's first row goes to its halo and, for the slab's first band, to
     // the CTA above ("row below" slot); its last row likewise downwards
     const bool send_up = active && band == 0, send_dn = active && band == p.nb - 1;
-    auto publish = [&](int npar, int i, uint32_t w) {
+    // `remote`: also store into the neighbours' slots (and, in the neighbour
+    // form, arrive on their parity-npar mbarrier)
+    auto publish = [&](int npar, int i, uint32_t w, bool remote) {
         if (!active) return;
         if (i == 0) {
             halo[npar * hwords + (band * 2 + 0) * wpr + j] = w;
-            if (send_up) slot_up[(npar * 2 + 1) * wpr + j] = w;
+            if (send_up && remote) {
+                slot_up[(npar * 2 + 1) * wpr + j] = w;
+                if (P2P) xk_cl_arrive_remote(mb_up + 8u * (uint32_t)npar);
+            }
         }
         if (i == y1 - 1 - y0) {
             halo[npar * hwords + (band * 2 + 1) * wpr + j] = w;
-            if (send_dn) slot_dn[(npar * 2 + 0) * wpr + j] = w;
+            if (send_dn && remote) {
+                slot_dn[(npar * 2 + 0) * wpr + j] = w;
+                if (P2P) xk_cl_arrive_remote(mb_dn + 8u * (uint32_t)npar);
+            }
         }
     };
 
-    cluster.sync();   // every CTA running (before any remote store) and every slab loaded
-    publish(0, 0, wp[0]);
-    publish(0, y1 - 1 - y0, wp[32 * (y1 - 1 - y0)]);
+    cluster.sync();   // every CTA running (before any remote store), slabs loaded, mbarriers set
+    // each edge row sent once (a one-row band's row is its first and last)
+    publish(0, 0, wp[0], true);
+    if (y1 - 1 - y0 != 0) publish(0, y1 - 1 - y0, wp[32 * (y1 - 1 - y0)], true);
+    bool failed = false;
     for (int gen = 0; gen < generations; ++gen) {
         const int par = gen & 1;
         const uint32_t *hp = halo + par * hwords;
-        cluster.sync();
+        if (P2P) {
+            // bands of this CTA; every thread leaves together after a failure
+            if (__syncthreads_or(failed)) break;
+            if ((first_band || last_band) &&
+                !xk_cl_wait(mbar0 + 8u * (uint32_t)par, (uint32_t)(gen >> 1) & 1u)) {
+                failed = true;
+                atomicOr(&xk_cluster_wait_failed, 1u);
+            }
+        } else {
+            cluster.sync();
+        }
+        const bool remote = gen + 1 < generations || !P2P;
         const uint32_t wu = first_band ? slot[(par * 2 + 0) * wpr + jc] : hp[((bc - 1) * 2 + 1) * wpr + jc];
         const uint32_t wl = last_band ? slot[(par * 2 + 1) * wpr + jc] : hp[((bc + 1) * 2 + 0) * wpr + jc];
         uint32_t su, cu_, sm_, cm_, Cm = wp[0];
@@ -154,7 +264,7 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t, int gene
             if (!FULLW) out &= outmask;
             if (active && y < y1) {
                 wp[32 * i] = out;
-                publish(par ^ 1, i, out);
+                publish(par ^ 1, i, out, remote);
             }
             su = sm_;
             cu_ = cm_;
@@ -180,25 +290,42 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t, int gene
 
 typedef void (*ClusterKernel)(uint32_t *, LifeGeo, LifeTable9, int, int);
 
-template <bool TORUS, bool FULLW>
-static ClusterKernel cluster_kernel_l(int L)
+// the neighbour form has instantiations for bands of 1, 2 and 4 rows
+template <bool TORUS, bool FULLW, int RF>
+static ClusterKernel cluster_kernel_l(int L, bool p2p)
 {
+    if (p2p) {
+        switch (L) {
+        case 1: return xk_k_life_cluster<TORUS, FULLW, 1, RF, true>;
+        case 2: return xk_k_life_cluster<TORUS, FULLW, 2, RF, true>;
+        case 4: return xk_k_life_cluster<TORUS, FULLW, 4, RF, true>;
+        default: return nullptr;
+        }
+    }
     switch (L) {
-    case 1: return xk_k_life_cluster<TORUS, FULLW, 1>;
-    case 2: return xk_k_life_cluster<TORUS, FULLW, 2>;
-    case 4: return xk_k_life_cluster<TORUS, FULLW, 4>;
-    default: return xk_k_life_cluster<TORUS, FULLW, 0>;
+    case 1: return xk_k_life_cluster<TORUS, FULLW, 1, RF, false>;
+    case 2: return xk_k_life_cluster<TORUS, FULLW, 2, RF, false>;
+    case 4: return xk_k_life_cluster<TORUS, FULLW, 4, RF, false>;
+    default: return xk_k_life_cluster<TORUS, FULLW, 0, RF, false>;
     }
 }
 
-// the instantiation for a lattice and launch shape (L: band length of the
-// widest CTA)
-static ClusterKernel cluster_kernel(const LifeGeo &g, int R, int threads)
+template <int RF>
+static ClusterKernel cluster_kernel_rf(const LifeGeo &g, int L, bool p2p)
+{
+    if (!g.torus) return cluster_kernel_l<false, false, RF>(L, p2p);
+    if (g.rlast == 32) return cluster_kernel_l<true, true, RF>(L, p2p);
+    return cluster_kernel_l<true, false, RF>(L, p2p);
+}
+
+// the instantiation for a lattice, launch shape (L: band length of the
+// widest CTA), rule form and synchronisation form (null: none)
+static ClusterKernel cluster_kernel(const LifeGeo &g, int R, int threads, int rf = XK_RULE_TABLE,
+                                    bool p2p = false)
 {
     const int L = xk_resident_plan(g.wpr, R, threads).L;
-    if (!g.torus) return cluster_kernel_l<false, false>(L);
-    if (g.rlast == 32) return cluster_kernel_l<true, true>(L);
-    return cluster_kernel_l<true, false>(L);
+    return rf == XK_RULE_CONWAY ? cluster_kernel_rf<XK_RULE_CONWAY>(g, L, p2p)
+                                : cluster_kernel_rf<XK_RULE_TABLE>(g, L, p2p);
 }
 
 static cudaError_t cluster_attrs(ClusterKernel k, size_t smem)
@@ -222,6 +349,11 @@ static void cluster_cfg(cudaLaunchConfig_t &cfg, cudaLaunchAttribute &attr, int 
     attr.val.clusterDim.z = 1;
     cfg.attrs = &attr;
     cfg.numAttrs = 1;
+}
+
+int xk_rule_form(uint32_t rule0, uint32_t rule1)
+{
+    return rule0 == 8u && rule1 == 12u ? XK_RULE_CONWAY : XK_RULE_TABLE;
 }
 
 LifeTable9 xk_life_table9(uint32_t rule0, uint32_t rule1)
@@ -259,7 +391,13 @@ int xk_life_cluster_config(const LifeGeo &g, int C, int band, int *C_out, int *R
     const size_t smem = 4ull * cluster_words(g.wpr, rows, th);
     if ((int64_t)smem > xk_max_smem_optin()) return 0;
     const ClusterKernel k = cluster_kernel(g, rows, th);
-    if (cluster_attrs(k, smem) != cudaSuccess) {
+    bool attrs_ok = true;
+    for (int rf = XK_RULE_TABLE; rf <= XK_RULE_CONWAY && attrs_ok; ++rf)
+        for (int p2p = 0; p2p < 2 && attrs_ok; ++p2p) {
+            const ClusterKernel kk = cluster_kernel(g, rows, th, rf, p2p != 0);
+            attrs_ok = !kk || cluster_attrs(kk, smem) == cudaSuccess;
+        }
+    if (!attrs_ok) {
         cudaGetLastError();
         return 0;
     }
@@ -278,11 +416,25 @@ int xk_life_cluster_config(const LifeGeo &g, int C, int band, int *C_out, int *R
     return 1;
 }
 
+int xk_life_cluster_has_p2p(const LifeGeo &g, int R, int threads)
+{
+    return cluster_kernel(g, R, threads, XK_RULE_TABLE, true) != nullptr;
+}
+
+bool xk_cluster_take_wait_failure()
+{
+    unsigned int v = 0, z = 0;
+    if (cudaMemcpyFromSymbol(&v, xk_cluster_wait_failed, sizeof(v)) != cudaSuccess) return false;
+    if (v) cudaMemcpyToSymbol(xk_cluster_wait_failed, &z, sizeof(z));
+    return v != 0;
+}
+
 cudaError_t xk_life_step_cluster(uint32_t *bits, const LifeGeo &g, uint32_t rule0, uint32_t rule1,
-                                 int generations, int C, int R, int threads, cudaStream_t s)
+                                 int generations, int C, int R, int threads, cudaStream_t s, int p2p)
 {
     const size_t smem = 4ull * cluster_words(g.wpr, R, threads);
-    const ClusterKernel k = cluster_kernel(g, R, threads);
+    const ClusterKernel k = cluster_kernel(g, R, threads, xk_rule_form(rule0, rule1), p2p != 0);
+    if (!k) return cudaErrorInvalidValue;
     cudaError_t e = cluster_attrs(k, smem);
     if (e != cudaSuccess) return e;
     const LifeTable9 t = xk_life_table9(rule0, rule1);

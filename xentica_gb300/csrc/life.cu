@@ -12,6 +12,8 @@
 // Layout: 32 cells per 32-bit word, LSB = lowest x; a generation is pure
 // bitwise logic -- a carry-save adder network counts the 8 neighbours of 32
 // cells at once and a LOP3 multiplexer tree applies the runtime rule.
+#include <string.h>
+
 #include <type_traits>
 
 #include "xk_internal.cuh"
@@ -193,13 +195,15 @@ int64_t xk_life_resident_words(int W, int H, int threads)
     return xk_res_lat_words(p) + 4LL * p.G * wpr + XK_TAB_WORDS;
 }
 
-template <bool BYTES, bool TORUS>
+template <bool BYTES, bool TORUS, int RF>
 __global__ void __launch_bounds__(1024)
 xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out, void *mirror,
-                   int generations, uint32_t bfill, unsigned int *__restrict__ bad)
+                   int generations, const int32_t *__restrict__ gens, uint32_t bfill,
+                   unsigned int *__restrict__ bad)
 {
     extern __shared__ uint32_t sm[];
     const LifeInst I = insts[blockIdx.x];
+    if (gens) generations = gens[blockIdx.x];         // per-lattice generation counts
     const int wpr = I.wpr, H = I.H, W = I.W;
     const ResidentPlan p = xk_resident_plan(wpr, H, blockDim.x);
     uint32_t *lat = sm;
@@ -291,15 +295,16 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
     const int hdn = bc + 1 < p.nb ? bc + 1 : 0;         // band holding the row below
     const bool full = (H % p.L) == 0;                   // every band has L rows
     __syncthreads();
-    LifeTable9 t;
+    LifeTable9 t9;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-        t.a[q] = tabs[2 * q];
-        t.k[q] = tabs[2 * q + 1];
+        t9.a[q] = tabs[2 * q];
+        t9.k[q] = tabs[2 * q + 1];
     }
-    t.d8 = tabs[16];
-    t.a9 = tabs[17];
-    t.k9 = tabs[18];
+    t9.d8 = tabs[16];
+    t9.a9 = tabs[17];
+    t9.k9 = tabs[18];
+    const auto &t = RuleForm<RF>::make(t9);   // RF != XK_RULE_TABLE: the table is not read
 
     const int hw = 2 * p.G * wpr;                      // halo words per parity
     // a band's first and last row into the halos of parity `par`
@@ -466,24 +471,51 @@ xk_k_life_resident(const LifeInst *__restrict__ insts, const void *in, void *out
     }
 }
 
-template <bool BYTES, bool TORUS>
+template <bool BYTES, bool TORUS, int RF = XK_RULE_TABLE>
 static cudaError_t xk_launch_resident(const LifeInst *inst, int ninst, const void *in, void *out,
                                       void *mirror, int generations, uint32_t bfill, unsigned int *bad,
-                                      int threads, int smem_bytes, cudaStream_t s)
+                                      int threads, int smem_bytes, cudaStream_t s,
+                                      const int32_t *gens = nullptr, int priority = XK_NO_PRIORITY)
 {
-    cudaError_t e = xk_smem_attr_at_least((const void *)xk_k_life_resident<BYTES, TORUS>, smem_bytes);
+    cudaError_t e = xk_smem_attr_at_least((const void *)xk_k_life_resident<BYTES, TORUS, RF>, smem_bytes);
     if (e != cudaSuccess || ninst <= 0) return e;
-    xk_k_life_resident<BYTES, TORUS><<<ninst, threads, smem_bytes, s>>>(inst, in, out, mirror,
-                                                                        generations, bfill, bad);
-    return cudaGetLastError();
+    if (priority == XK_NO_PRIORITY) {
+        xk_k_life_resident<BYTES, TORUS, RF><<<ninst, threads, smem_bytes, s>>>(inst, in, out, mirror,
+                                                                                generations, gens, bfill, bad);
+        return cudaGetLastError();
+    }
+    // a launch priority (kept by a graph instantiated with node priorities)
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cudaLaunchAttribute attr;
+    cfg.gridDim = dim3(ninst);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem_bytes;
+    cfg.stream = s;
+    attr.id = cudaLaunchAttributePriority;
+    attr.val.priority = priority;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, xk_k_life_resident<BYTES, TORUS, RF>, inst, in, out, mirror, generations,
+                              gens, bfill, bad);
 }
 
 // ninst == 0 only sets the kernel's shared-memory attribute (done before a
 // graph capture, where attribute changes are not recorded)
 cudaError_t xk_life_step_resident(const LifeInst *inst, int ninst, void *state, int bytes_io,
                                   int generations, int torus, uint32_t bfill, unsigned int *bad,
-                                  int threads, int smem_bytes, cudaStream_t s)
+                                  int threads, int smem_bytes, cudaStream_t s, int rule_form, int priority)
 {
+    if (bytes_io && torus && priority != XK_NO_PRIORITY)
+        return xk_launch_resident<true, true>(inst, ninst, state, state, nullptr, generations, bfill, bad,
+                                              threads, smem_bytes, s, nullptr, priority);
+    if (!bytes_io && rule_form == XK_RULE_CONWAY)
+        return torus ? xk_launch_resident<false, true, XK_RULE_CONWAY>(inst, ninst, state, state, nullptr,
+                                                                       generations, bfill, bad, threads,
+                                                                       smem_bytes, s)
+                     : xk_launch_resident<false, false, XK_RULE_CONWAY>(inst, ninst, state, state, nullptr,
+                                                                        generations, bfill, bad, threads,
+                                                                        smem_bytes, s);
     if (bytes_io)
         return torus ? xk_launch_resident<true, true>(inst, ninst, state, state, nullptr, generations,
                                                       bfill, bad, threads, smem_bytes, s)
@@ -495,12 +527,20 @@ cudaError_t xk_life_step_resident(const LifeInst *inst, int ninst, void *state, 
                                                     bfill, bad, threads, smem_bytes, s);
 }
 
+cudaError_t xk_life_step_resident_each(const LifeInst *inst, const int32_t *gens, int ninst, void *state,
+                                       unsigned int *bad, int threads, int smem_bytes, cudaStream_t s)
+{
+    return xk_launch_resident<true, true>(inst, ninst, state, state, nullptr, 0, 0u, bad, threads,
+                                          smem_bytes, s, gens);
+}
+
 // CTAs of the one-byte torus resident kernel one SM holds at once
 int xk_life_resident_ctas_per_sm(int threads, int smem_bytes)
 {
     int n = 0;
-    if (xk_smem_attr_at_least((const void *)xk_k_life_resident<true, true>, smem_bytes) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, xk_k_life_resident<true, true>, threads,
+    if (xk_smem_attr_at_least((const void *)xk_k_life_resident<true, true, XK_RULE_TABLE>, smem_bytes) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, xk_k_life_resident<true, true, XK_RULE_TABLE>, threads,
                                                       smem_bytes) != cudaSuccess) {
         cudaGetLastError();
         return 1;

@@ -23,6 +23,8 @@
 // stored.
 //
 // Requires W >= 64 (a 32-cell window wraps at most once).
+#include <string.h>
+
 #include "life_word.cuh"
 
 #define XK_TB_ROWS 64
@@ -53,9 +55,11 @@ __device__ __forceinline__ uint32_t xk_tb_cells32(const uint32_t *__restrict__ r
     return v;
 }
 
+template <int RF>
 __global__ void __launch_bounds__(32 * XK_TB_WARPS)
-xk_k_life_tb(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, TbParams p, LifeTable9 t)
+xk_k_life_tb(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, TbParams p, LifeTable9 t9)
 {
+    const auto &t = RuleForm<RF>::make(t9);
     __shared__ uint32_t tile[2][XK_TB_ROWS][32];
     const LifeGeo &g = p.g;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -163,5 +167,9 @@ cudaError_t xk_life_step_tb(const uint32_t *src, uint32_t *dst, const LifeGeo &g
     p.TH = XK_TB_ROWS - 2 * T;
     const dim3 grid((unsigned)((g.W + 30 * 32 - 1) / (30 * 32)), (unsigned)((g.H + p.TH - 1) / p.TH));
     if (grid.y > 65535u) return cudaErrorInvalidValue;
-    return xk_launch_pdl(xk_k_life_tb, grid, dim3(32 * XK_TB_WARPS), 0, s, src, dst, p, t);
+    // B3/S23 runs the instantiation with the rule compiled in
+    const LifeTable9 conway = xk_life_table9(8u, 12u);
+    if (memcmp(&t, &conway, sizeof(t)) == 0)
+        return xk_launch_pdl(xk_k_life_tb<XK_RULE_CONWAY>, grid, dim3(32 * XK_TB_WARPS), 0, s, src, dst, p, t);
+    return xk_launch_pdl(xk_k_life_tb<XK_RULE_TABLE>, grid, dim3(32 * XK_TB_WARPS), 0, s, src, dst, p, t);
 }

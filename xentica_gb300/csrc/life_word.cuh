@@ -106,21 +106,14 @@ __device__ __forceinline__ uint32_t xk_life_word_fa(uint32_t su, uint32_t cu, ui
     return xk_mux(b3, low, eight);
 }
 
-// Next state of 32 cells from the column sums (s, c) = FA(L, C, R) of the
-// rows above (u), at (m) and below (d) -- the 3 x 3 block including the cell
-// -- and the cells themselves (C).  A row's sums are computed once, when it
-// is the row below, and reused twice; the count n9 = (su + sm + sd) +
-// 2 (cu + cm + cd) <= 9 needs one fewer logic instruction than the
-// neighbour count of xk_life_word_fa, and the rule is indexed by it
-// (LifeTable9).
-__device__ __forceinline__ uint32_t xk_life_word9(uint32_t su, uint32_t cu, uint32_t sm, uint32_t cm,
-                                                  uint32_t sd, uint32_t cd, uint32_t C,
-                                                  const LifeTable9 &t)
+// The rule stage: next state of 32 cells from the bits of the 3 x 3 block
+// count n9 = b0 + 2 b1 + 4 b2 + 8 b3 (the cell included; b3: n9 is 8 or 9,
+// so b1 = b2 = 0) and the cells themselves (C).  A rule loaded at run time
+// (LifeTable9): a multiplexer tree over warp-uniform masks, its first level
+// as integer multiply-adds.
+__device__ __forceinline__ uint32_t xk_rule9(const LifeTable9 &t, uint32_t b0, uint32_t b1, uint32_t b2,
+                                             uint32_t b3, uint32_t C)
 {
-    const uint32_t b0 = xk_lop3_xor3(su, sm, sd), k1 = xk_maj(su, sm, sd);
-    const uint32_t tw = xk_lop3_xor3(cu, cm, cd), k2 = xk_maj(cu, cm, cd);
-    const uint32_t b1 = tw ^ k1, k3 = tw & k1;
-    const uint32_t b2 = k2 ^ k3, b3 = k2 & k3;   // b3: n9 is 8 or 9, so b1 = b2 = 0
     uint32_t m[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) m[q] = xk_imux(b0, t.a[q], t.k[q]);
@@ -133,6 +126,74 @@ __device__ __forceinline__ uint32_t xk_life_word9(uint32_t su, uint32_t cu, uint
     const uint32_t high = xk_mux(C, t.d8, xk_imux(b0, t.a9, t.k9));
     return xk_mux(b3, low, high);
 }
+
+// A rule fixed at compile time: a dead cell is born with k neighbours iff
+// bit k of B is set, a live cell survives with k iff bit k of S is set (the
+// golly int B | S << 9 of LifelikeCA).  The same multiplexer tree written in
+// plain C over compile-time masks: the compiler folds every constant leaf,
+// so Conway's B3/S23 takes about four logic instructions instead of the
+// eighteen of a rule loaded at run time.
+template <uint32_t B, uint32_t S>
+struct FixedRule9 {
+    static constexpr uint32_t born = B, sustain = S;
+};
+
+__device__ __forceinline__ uint32_t xk_cmux(uint32_t sel, uint32_t a, uint32_t b)
+{
+    return (a & ~sel) | (b & sel);
+}
+
+template <uint32_t B, uint32_t S>
+__device__ __forceinline__ uint32_t xk_rule9(const FixedRule9<B, S> &, uint32_t b0, uint32_t b1, uint32_t b2,
+                                             uint32_t b3, uint32_t C)
+{
+    // dead cell: D(n9) = born bit n9; live cell: L(n9) = sustain bit n9 - 1
+    auto D = [](int n) -> uint32_t { return n <= 8 && ((B >> n) & 1u) ? 0xFFFFFFFFu : 0u; };
+    auto L = [](int n) -> uint32_t { return n >= 1 && ((S >> (n - 1)) & 1u) ? 0xFFFFFFFFu : 0u; };
+    uint32_t m[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+        m[q] = q < 4 ? xk_cmux(b0, D(2 * q), D(2 * q + 1)) : xk_cmux(b0, L(2 * (q - 4)), L(2 * (q - 4) + 1));
+    uint32_t n[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) n[q] = xk_cmux(b1, m[2 * q], m[2 * q + 1]);
+    const uint32_t dead = xk_cmux(b2, n[0], n[1]);
+    const uint32_t live = xk_cmux(b2, n[2], n[3]);
+    const uint32_t low = xk_cmux(C, dead, live);
+    const uint32_t high = xk_cmux(C, D(8), xk_cmux(b0, L(8), L(9)));
+    return xk_cmux(b3, low, high);
+}
+
+// Next state of 32 cells from the column sums (s, c) = FA(L, C, R) of the
+// rows above (u), at (m) and below (d) -- the 3 x 3 block including the cell
+// -- and the cells themselves (C).  A row's sums are computed once, when it
+// is the row below, and reused twice; the count n9 = (su + sm + sd) +
+// 2 (cu + cm + cd) <= 9 needs one fewer logic instruction than the
+// neighbour count of xk_life_word_fa, and the rule is indexed by it (a
+// LifeTable9 or a FixedRule9).
+template <class Rule>
+__device__ __forceinline__ uint32_t xk_life_word9(uint32_t su, uint32_t cu, uint32_t sm, uint32_t cm,
+                                                  uint32_t sd, uint32_t cd, uint32_t C, const Rule &t)
+{
+    const uint32_t b0 = xk_lop3_xor3(su, sm, sd), k1 = xk_maj(su, sm, sd);
+    const uint32_t tw = xk_lop3_xor3(cu, cm, cd), k2 = xk_maj(cu, cm, cd);
+    const uint32_t b1 = tw ^ k1, k3 = tw & k1;
+    const uint32_t b2 = k2 ^ k3, b3 = k2 & k3;
+    return xk_rule9(t, b0, b1, b2, b3, C);
+}
+
+// the rule form's rule object (XK_RULE_* in xk_internal.cuh)
+template <int RF>
+struct RuleForm {
+    typedef LifeTable9 type;
+    __device__ static const LifeTable9 &make(const LifeTable9 &t) { return t; }
+};
+
+template <>
+struct RuleForm<XK_RULE_CONWAY> {
+    typedef FixedRule9<8u, 12u> type;
+    __device__ static FixedRule9<8u, 12u> make(const LifeTable9 &) { return FixedRule9<8u, 12u>(); }
+};
 
 // Neighbour vectors of word j of a row, given the row's word and the words
 // left and right of it (already wrapped).  lshift: bit of `left` that is

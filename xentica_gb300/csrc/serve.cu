@@ -9,8 +9,8 @@
 // Execution: a worker thread owns every CUDA call after creation.  Each pass
 // it (1) retires finished work by polling events, (2) admits queued requests
 // first come, first served while their bytes fit and fewer than max_active run,
-// (3) starts the next round (at most `quantum` generations) of every request
-// whose previous round finished, and (4) starts the result copy of requests
+// (3) starts the next round of every request whose previous round finished,
+// and (4) starts the result copy of requests
 // that reached their generation count.  Rounds of different requests are
 // independent, so a request admitted while others run starts computing at
 // once and its kernels overlap theirs on the device.
@@ -18,16 +18,22 @@
 // Paths per request:
 //   resident  2-D Life-like lattices that fit one CTA (and at most
 //             XK_SERVE_RESIDENT_MAX cells): grouped by CTA shape; a group round
-//             is one launch of the resident kernel per distinct round length
-//             over all members (one CTA each), on the group's stream;
+//             is one launch of the resident kernel over the group's idle
+//             members (one CTA each, each with its own generation count, about
+//             quantum x 2^18 cell-generations), in one of XK_SERVE_GROUP_SLOTS
+//             slots, so members admitted while a round runs start at once;
 //   global2d  larger 2-D lattices: packed to 32 cells per word once, one
 //             bit-sliced launch per generation on the request's stream;
 //   life3d    3-D von Neumann Life-like: bit-packed along x like global2d, one
 //             launch per generation;
 //   mass3d    mass transfer: uint32 ping-pong with the per-generation totals
 //             (the fast-only kernel when the submitted total is below 2^30).
-// Full rounds of the per-request paths are captured once as a CUDA graph (per
-// ping-pong parity) and replayed, so a round costs the worker one launch.
+// The other paths run rounds of `quantum` generations.  Full rounds of the
+// per-request paths are captured once as a CUDA graph (per ping-pong parity)
+// and replayed, so a round costs the worker one launch.  Streams carry a
+// priority: resident rounds the device's greatest, other requests one level
+// lower per factor of 4 of work above 2^26 cell-generations, so the block
+// scheduler serves short requests ahead of the kernels of long ones.
 // A request's cells see exactly the arithmetic they see alone: every kernel
 // touches only its own request's range.
 #include <stdlib.h>
@@ -87,14 +93,26 @@ struct Req {
     bool mass_small = false;   // initial total below 2^30
 };
 
-struct Group {
-    int threads = 0, smem = 0;
+// rounds of one resident group that may be in flight at once: a member
+// admitted while earlier members run starts in a free slot at once
+#define XK_SERVE_GROUP_SLOTS 4
+
+// one round of a resident group: its members, their instance records and
+// generation counts (pinned staging, device copy), its stream and event
+struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev = nullptr;
     bool in_flight = false;
     LifeInst *h_inst = nullptr;   // pinned, max_active entries
     LifeInst *d_inst = nullptr;
+    int32_t *h_gens = nullptr;    // pinned, max_active entries
+    int32_t *d_gens = nullptr;
     std::vector<Req *> members;
+};
+
+struct Group {
+    int threads = 0, smem = 0;
+    Slot slot[XK_SERVE_GROUP_SLOTS];
 };
 
 int64_t rnd(int64_t b) { return XkArena::round(b); }
@@ -157,6 +175,8 @@ struct xk_server {
     int max_active = 0;
     int64_t quantum = 0;
     int tb_depth = 8;          // generations per launch of large 2-D requests (XK_SERVE_TB)
+    int64_t round_work = 0;    // cell-generations of a resident member's round (quantum x 2^18)
+    int prio_least = 0, prio_greatest = 0;   // the device's stream priority range
     int64_t resident_max = 1 << 18;
     uint8_t *dev_base = nullptr;
     uint8_t *host_base = nullptr;
@@ -220,15 +240,45 @@ static int group_for(xk_server *s, int threads, int smem)
             s->groups[g].smem = std::max(s->groups[g].smem, smem);
             return (int)g;
         }
-    Group g;
+    s->groups.emplace_back();
+    Group &g = s->groups.back();
     g.threads = threads;
     g.smem = smem;
-    XK_CUDA(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
-    XK_CUDA(cudaEventCreateWithFlags(&g.ev, cudaEventDisableTiming));
-    XK_CUDA(cudaMallocHost(&g.h_inst, sizeof(LifeInst) * s->max_active));
-    XK_CUDA(cudaMalloc(&g.d_inst, sizeof(LifeInst) * s->max_active));
-    s->groups.push_back(g);
+    // resident lattices are the smallest requests: their rounds take the
+    // device's greatest stream priority
+    for (Slot &sl : g.slot) {
+        XK_CUDA(cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking, s->prio_greatest));
+        XK_CUDA(cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming));
+        XK_CUDA(cudaMallocHost(&sl.h_inst, sizeof(LifeInst) * s->max_active));
+        XK_CUDA(cudaMalloc(&sl.d_inst, sizeof(LifeInst) * s->max_active));
+        XK_CUDA(cudaMallocHost(&sl.h_gens, sizeof(int32_t) * s->max_active));
+        XK_CUDA(cudaMalloc(&sl.d_gens, sizeof(int32_t) * s->max_active));
+    }
     return (int)s->groups.size() - 1;
+}
+
+// stream priority of a request: the less work (cell-generations) it asks
+// for, the greater its priority, so that short requests are not queued
+// behind the kernels of long ones; one priority level per factor of 4 of work
+// above 2^26
+static int request_priority(const xk_server *s, const Req *q)
+{
+    const double work = (double)q->n * (double)std::max<int64_t>(1, q->r.generations);
+    const int levels = s->prio_least - s->prio_greatest;
+    int step = 0;
+    for (double w = work; w >= (double)(1LL << 26) && step < levels; w /= 4.0) ++step;
+    return s->prio_greatest + step;
+}
+
+// generations of the next round of a resident member: the round's work is
+// about round_work cell-generations (so small lattices run many generations
+// per round), at least `quantum`, at most what is left
+static int64_t resident_chunk(const xk_server *s, const Req *q)
+{
+    const int64_t left = q->r.generations - q->done;
+    int64_t chunk = std::max<int64_t>(s->quantum, s->round_work / std::max<int64_t>(1, q->n));
+    chunk = std::min<int64_t>(chunk, 1 << 30);
+    return std::min(chunk, left);
 }
 
 static int admit(xk_server *s, Req *q, bool *admitted)
@@ -245,7 +295,7 @@ static int admit(xk_server *s, Req *q, bool *admitted)
     q->host_off = hoff;
     s->st.device_bytes_in_use = s->dev_arena->in_use();
     s->st.device_bytes_peak = std::max(s->st.device_bytes_peak, s->st.device_bytes_in_use);
-    XK_CUDA(cudaStreamCreateWithFlags(&q->stream, cudaStreamNonBlocking));
+    XK_CUDA(cudaStreamCreateWithPriority(&q->stream, cudaStreamNonBlocking, request_priority(s, q)));
     XK_CUDA(cudaEventCreateWithFlags(&q->ev, cudaEventDisableTiming));
     uint8_t *base = s->dev_base + doff;
     const xk_request &r = q->r;
@@ -409,22 +459,28 @@ static int launch_round(xk_server *s, Req *q)
     return XK_OK;
 }
 
-// one round of every idle member of resident group g
+// one round of every idle member of resident group g, in a free slot: one
+// launch over all of them, each member advancing its own generation count
 static int launch_group(xk_server *s, int gi)
 {
     Group &g = s->groups[gi];
-    g.members.clear();
+    Slot *sl = nullptr;
+    for (Slot &c : g.slot)
+        if (!c.in_flight) {
+            sl = &c;
+            break;
+        }
+    if (!sl) return XK_OK;
+    sl->members.clear();
     for (Req *q : s->active)
         if (q->path == PATH_RESIDENT && q->group == gi && !q->ev_pending && !q->in_group &&
             !q->draining && !q->cancel && q->done < q->r.generations)
-            g.members.push_back(q);
-    if (g.members.empty()) return XK_OK;
-    for (Req *q : g.members) q->chunk = std::min(s->quantum, q->r.generations - q->done);
-    std::stable_sort(g.members.begin(), g.members.end(),
-                     [](const Req *a, const Req *b) { return a->chunk > b->chunk; });
-    for (size_t k = 0; k < g.members.size(); ++k) {
-        const Req *q = g.members[k];
-        LifeInst &in = g.h_inst[k];
+            sl->members.push_back(q);
+    if (sl->members.empty()) return XK_OK;
+    for (size_t k = 0; k < sl->members.size(); ++k) {
+        Req *q = sl->members[k];
+        q->chunk = resident_chunk(s, q);
+        LifeInst &in = sl->h_inst[k];
         memset(&in, 0, sizeof(in));
         in.off = q->dev_off;
         in.W = (int32_t)q->r.size[0];
@@ -435,22 +491,19 @@ static int launch_group(xk_server *s, int gi)
         in.rule0 = q->rule0;
         in.rule1 = q->rule1;
         in.smem_words = q->smem / 4;
+        sl->h_gens[k] = (int32_t)q->chunk;
     }
-    XK_CUDA(cudaMemcpyAsync(g.d_inst, g.h_inst, sizeof(LifeInst) * g.members.size(),
-                            cudaMemcpyHostToDevice, g.stream));
-    size_t first = 0;
-    while (first < g.members.size()) {
-        size_t last = first;
-        while (last < g.members.size() && g.members[last]->chunk == g.members[first]->chunk) ++last;
-        XK_CUDA(xk_life_step_resident(g.d_inst + first, (int)(last - first), s->dev_base, 1,
-                                      (int)g.members[first]->chunk, 1, 0u, s->bad, g.threads, g.smem,
-                                      g.stream));
-        s->st.launches++;
-        first = last;
-    }
-    XK_CUDA(cudaEventRecord(g.ev, g.stream));
-    g.in_flight = true;
-    for (Req *q : g.members) q->in_group = true;
+    const size_t n = sl->members.size();
+    XK_CUDA(cudaMemcpyAsync(sl->d_inst, sl->h_inst, sizeof(LifeInst) * n, cudaMemcpyHostToDevice,
+                            sl->stream));
+    XK_CUDA(cudaMemcpyAsync(sl->d_gens, sl->h_gens, sizeof(int32_t) * n, cudaMemcpyHostToDevice,
+                            sl->stream));
+    XK_CUDA(xk_life_step_resident_each(sl->d_inst, sl->d_gens, (int)n, s->dev_base, s->bad, g.threads,
+                                       g.smem, sl->stream));
+    s->st.launches++;
+    XK_CUDA(cudaEventRecord(sl->ev, sl->stream));
+    sl->in_flight = true;
+    for (Req *q : sl->members) q->in_group = true;
     return XK_OK;
 }
 
@@ -514,21 +567,21 @@ static void finish(xk_server *s, Req *q, int status)
 static int worker_pass(xk_server *s, bool *busy)
 {
     // (1) retire
-    for (size_t gi = 0; gi < s->groups.size(); ++gi) {
-        Group &g = s->groups[gi];
-        if (!g.in_flight) continue;
-        cudaError_t e = cudaEventQuery(g.ev);
-        if (e == cudaErrorNotReady) continue;
-        XK_CUDA(e);
-        g.in_flight = false;
-        for (Req *q : g.members) {
-            q->in_group = false;
-            q->done += q->chunk;
-            q->last_chunk = q->chunk;
-            q->chunk = 0;
+    for (Group &g : s->groups)
+        for (Slot &sl : g.slot) {
+            if (!sl.in_flight) continue;
+            cudaError_t e = cudaEventQuery(sl.ev);
+            if (e == cudaErrorNotReady) continue;
+            XK_CUDA(e);
+            sl.in_flight = false;
+            for (Req *q : sl.members) {
+                q->in_group = false;
+                q->done += q->chunk;
+                q->last_chunk = q->chunk;
+                q->chunk = 0;
+            }
+            sl.members.clear();
         }
-        g.members.clear();
-    }
     std::vector<Req *> snapshot = s->active;
     for (Req *q : snapshot) {
         if (q->ev_pending) {
@@ -576,10 +629,10 @@ static int worker_pass(xk_server *s, bool *busy)
         launched = true;
     }
     for (size_t gi = 0; gi < s->groups.size(); ++gi) {
-        if (s->groups[gi].in_flight) continue;
+        const int64_t before = s->st.launches;
         int rc = launch_group(s, (int)gi);
         if (rc != XK_OK) return rc;
-        launched |= s->groups[gi].in_flight;
+        launched |= s->st.launches != before;
     }
     if (launched) s->st.rounds++;
     *busy = !s->active.empty() || !s->pending.empty();
@@ -619,7 +672,8 @@ static void worker_main(xk_server *s)
             s->cv_work.wait(lk, [s] { return s->stop || !s->pending.empty(); });
     }
     for (auto &g : s->groups)
-        if (g.stream) cudaStreamSynchronize(g.stream);
+        for (Slot &sl : g.slot)
+            if (sl.stream) cudaStreamSynchronize(sl.stream);
     for (Req *q : s->active)
         if (q->stream) cudaStreamSynchronize(q->stream);
 }
@@ -639,12 +693,15 @@ extern "C" int xk_serve_request_bytes(const xk_request *req, int64_t *bytes)
 
 static void free_server(xk_server *s)
 {
-    for (auto &g : s->groups) {
-        if (g.stream) cudaStreamDestroy(g.stream);
-        if (g.ev) cudaEventDestroy(g.ev);
-        if (g.h_inst) cudaFreeHost(g.h_inst);
-        if (g.d_inst) cudaFree(g.d_inst);
-    }
+    for (auto &g : s->groups)
+        for (Slot &sl : g.slot) {
+            if (sl.stream) cudaStreamDestroy(sl.stream);
+            if (sl.ev) cudaEventDestroy(sl.ev);
+            if (sl.h_inst) cudaFreeHost(sl.h_inst);
+            if (sl.d_inst) cudaFree(sl.d_inst);
+            if (sl.h_gens) cudaFreeHost(sl.h_gens);
+            if (sl.d_gens) cudaFree(sl.d_gens);
+        }
     for (auto &kv : s->reqs) {
         if (kv.second->stream) cudaStreamDestroy(kv.second->stream);
         if (kv.second->ev) cudaEventDestroy(kv.second->ev);
@@ -674,6 +731,7 @@ extern "C" int xk_serve_create(int64_t budget_bytes, int64_t host_bytes, int32_t
     s->host_bytes = host_bytes;
     s->max_active = max_active;
     s->quantum = quantum;
+    s->round_work = (int64_t)quantum << 18;
     if (const char *e = getenv("XK_SERVE_TB")) {
         const int T = atoi(e);
         s->tb_depth = T >= 2 && T <= 8 ? T : 0;
@@ -681,6 +739,7 @@ extern "C" int xk_serve_create(int64_t budget_bytes, int64_t host_bytes, int32_t
     if (const char *e = getenv("XK_SERVE_RESIDENT_MAX")) s->resident_max = atoll(e);
     cudaError_t e;
     if ((e = cudaGetDevice(&s->device)) != cudaSuccess ||
+        (e = cudaDeviceGetStreamPriorityRange(&s->prio_least, &s->prio_greatest)) != cudaSuccess ||
         (e = cudaMalloc(&s->dev_base, (size_t)budget_bytes)) != cudaSuccess ||
         (e = cudaMallocHost(&s->host_base, (size_t)host_bytes)) != cudaSuccess ||
         (e = cudaMalloc(&s->bad, sizeof(unsigned int))) != cudaSuccess ||

@@ -124,9 +124,19 @@ cudaError_t xk_life_step_global(const uint32_t *src, uint32_t *dst, const LifeGe
 // bytes_io: state is one byte per cell (LifeInst.off in bytes) instead of
 // bit-packed words; `bad` (bytes_io only) is or-ed with 1 if a cell held a
 // value other than 0/1
+// rule_form (bit-packed state only): XK_RULE_CONWAY runs the instantiation
+// with B3/S23 compiled in (every instance's rule must then be B3/S23)
+// priority (one-byte torus state only): the launch's priority attribute
+// (a graph instantiated with cudaGraphInstantiateFlagUseNodePriority keeps it)
+#define XK_NO_PRIORITY (-1000000)
 cudaError_t xk_life_step_resident(const LifeInst *inst, int ninst, void *state, int bytes_io,
                                   int generations, int torus, uint32_t bfill, unsigned int *bad,
-                                  int threads, int smem_bytes, cudaStream_t s);
+                                  int threads, int smem_bytes, cudaStream_t s, int rule_form = 0,
+                                  int priority = XK_NO_PRIORITY);
+// torus, one byte per cell, in place: lattice k advances gens[k]
+// generations (a device array of ninst counts)
+cudaError_t xk_life_step_resident_each(const LifeInst *inst, const int32_t *gens, int ninst, void *state,
+                                       unsigned int *bad, int threads, int smem_bytes, cudaStream_t s);
 // torus, one byte per cell: lattices read from `in`, results written to
 // `out` and, when `mirror` is not null, also to `mirror` (the same offsets);
 // `in` and `out` may be device addresses of mapped host memory
@@ -160,9 +170,23 @@ cudaError_t xk_life_step3d_vn(const uint32_t *src, uint32_t *dst, const Life3Geo
 // cluster of (up to) C CTAs whose lane groups walk bands of about `band` rows
 // fits
 LifeTable9 xk_life_table9(uint32_t rule0, uint32_t rule1);
+// Rule forms of the single-lattice kernels: a rule loaded at run time, or
+// Conway's Life B3/S23 fixed at compile time (the reference's default
+// LifelikeCA rule and its GameOfLife model)
+#define XK_RULE_TABLE 0
+#define XK_RULE_CONWAY 1
+// the rule form a single-lattice kernel compiles for (rule0: dead-cell table,
+// rule1: live-cell table): XK_RULE_CONWAY for B3/S23, else XK_RULE_TABLE
+int xk_rule_form(uint32_t rule0, uint32_t rule1);
 int xk_life_cluster_config(const LifeGeo &g, int C, int band, int *C_out, int *R, int *threads);
+// p2p: the neighbour form of synchronisation (mbarriers of the two
+// neighbouring CTAs) instead of a cluster barrier per generation; it exists
+// for bands of 1, 2 and 4 rows (xk_life_cluster_has_p2p)
 cudaError_t xk_life_step_cluster(uint32_t *bits, const LifeGeo &g, uint32_t rule0, uint32_t rule1,
-                                 int generations, int C, int R, int threads, cudaStream_t s);
+                                 int generations, int C, int R, int threads, cudaStream_t s, int p2p = 0);
+int xk_life_cluster_has_p2p(const LifeGeo &g, int R, int threads);
+// a CTA of the neighbour form gave up waiting since the last call (clears it)
+bool xk_cluster_take_wait_failure();
 
 // T (1..8) generations per launch of a 2-D lattice of any size (W >= 64),
 // tiles with a T-generation halo in shared memory, src -> dst (life_tb.cu)

@@ -4,9 +4,12 @@ The reference has no request loop -- a caller builds one model per lattice
 and steps it (``xentica/core/base.py:591-728``).  :class:`Server` wraps the
 engine's ``xk_serve_*`` C-ABI: a worker thread inside ``libxk`` admits queued
 requests by HBM budget, keeps their state resident on the device and advances
-every active request in rounds of at most ``quantum`` generations, so requests
-admitted while others run overlap with them on the GPU.  Each request computes
-exactly what it computes alone.
+every active request in rounds (``quantum`` generations for large lattices;
+about ``quantum`` x 2^18 cell-generations for 2-D lattices that fit one CTA,
+which run together in one launch per shape class), so requests admitted while
+others run overlap with them on the GPU; requests with less work run at a
+greater stream priority.  Each request computes exactly what it computes
+alone.
 
 Request kinds (cells row-major, axis 0 = x fastest, i.e. NumPy shape
 ``(height, width)`` or ``(depth, height, width)``):
@@ -132,7 +135,8 @@ class Server:
     :param budget_bytes: device arena for request state (HBM budget).
     :param host_bytes: pinned host arena for results (0: min(budget, 8 GiB)).
     :param max_active: requests on the device at once.
-    :param quantum: generations per round.
+    :param quantum: generations per round of a large lattice (small 2-D
+        lattices run about quantum x 2^18 cell-generations per round).
     """
 
     def __init__(self, budget_bytes, host_bytes=0, max_active=1024, quantum=128):

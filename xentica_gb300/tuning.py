@@ -2,9 +2,10 @@
 
 Two choices are timed on the device and cached:
 
-* the ensemble's band length (``xk_batch_tune`` times the resident kernel for
-  several band lengths and keeps the fastest), re-applied with
-  ``xk_batch_set_band``;
+* the ensemble's band lengths (``xk_batch_tune`` times the resident kernel
+  for several band lengths and keeps the fastest, then a band of its own for
+  each lattice size with a large share of the cells where that is faster),
+  re-applied with ``xk_batch_set_band`` and ``xk_batch_set_size_bands``;
 * a single 2-D Life-like lattice's launch plan (``xk_model_plan``: the
   kernel family -- per-generation global kernel, one resident CTA, a
   thread-block cluster of a size and band length, or temporal blocking of a
@@ -19,10 +20,12 @@ workload, so it is stored in a JSON file under a key made of
 * the library build (SHA-1 of ``libxk.so``; any rebuild with changed kernels
   changes it),
 * the workload: for an ensemble the SHA-1 of the lattice sizes and the
-  generations per step; for a lattice its size and border (torus, or static
-  with its state).  The rule is not part of the key: every Life-like kernel
-  evaluates the rule through the same multiplexer over a table loaded at run
-  time, so its instruction stream and cost are the same for every rule.
+  generations per step; for a lattice its size, border (torus, or static
+  with its state) and rule form.  Conway's B3/S23 runs kernels with the
+  rule compiled in (fewer instructions per word, so a different best plan);
+  every other rule is evaluated through the same multiplexer over a table
+  loaded at run time, whose instruction stream and cost are the same for
+  every rule, so the rule itself is not part of the key.
 
 A later tune of the same workload on the same device and library applies the
 stored choice instead of timing again.  The file is
@@ -114,9 +117,44 @@ class TuneCache:
             os.replace(tmp, self.path)
 
 
+def _valid_bands(hit):
+    """A cached ensemble entry: ``{"band": b, "sizes": [[W, H, b], ...]}`` (or
+    a bare band length, the form without per-size choices)."""
+    def band_ok(v):
+        return isinstance(v, int) and not isinstance(v, bool) and 1 <= v <= 1024
+    if band_ok(hit):
+        return True
+    if not (isinstance(hit, dict) and band_ok(hit.get("band"))):
+        return False
+    sizes = hit.get("sizes", [])
+    return isinstance(sizes, list) and all(
+        isinstance(t, list) and len(t) == 3 and all(band_ok(v) for v in t[2:]) and
+        all(isinstance(v, int) and not isinstance(v, bool) and v >= 1 for v in t[:2])
+        for t in sizes)
+
+
+def size_bands(lib, handle):
+    """The per-size band choices of a batch as ``[[W, H, band], ...]``."""
+    n = lib.xk_batch_size_bands(handle, None, 0)
+    if n <= 0:
+        return []
+    buf = (ctypes.c_int32 * (3 * n))()
+    lib.xk_batch_size_bands(handle, buf, n)
+    return [[int(buf[3 * k]), int(buf[3 * k + 1]), int(buf[3 * k + 2])] for k in range(n)]
+
+
+def apply_bands(lib, handle, band, sizes=()):
+    """Set the common band and the per-size choices of a batch."""
+    nat.check(lib.xk_batch_set_band(handle, int(band)), "xk_batch_set_band")
+    if sizes:
+        flat = (ctypes.c_int32 * (3 * len(sizes)))(*[int(v) for t in sizes for v in t])
+        nat.check(lib.xk_batch_set_size_bands(handle, flat, len(sizes)), "xk_batch_set_size_bands")
+
+
 def tuned_band(lib, handle, widths, heights, generations, cache=True, library=None):
-    """Band length for an ensemble: from the cache when present (applied with
-    ``xk_batch_set_band``), else timed by ``xk_batch_tune`` and stored."""
+    """Band lengths for an ensemble: from the cache when present (applied with
+    ``xk_batch_set_band`` and ``xk_batch_set_size_bands``), else timed by
+    ``xk_batch_tune`` and stored.  Returns the common band length."""
     path = cache_path() if cache else None
     store = key = None
     if path is not None:
@@ -128,14 +166,17 @@ def tuned_band(lib, handle, widths, heights, generations, cache=True, library=No
         key = ensemble_key(device_id(lib), lib_id, widths, heights, generations)
         store = TuneCache(path)
         hit = store.get(key)
-        if isinstance(hit, int) and not isinstance(hit, bool) and 1 <= hit <= 1024:
-            nat.check(lib.xk_batch_set_band(handle, hit), "xk_batch_set_band")
+        if _valid_bands(hit):
+            if isinstance(hit, dict):
+                apply_bands(lib, handle, hit["band"], hit.get("sizes", []))
+                return hit["band"]
+            apply_bands(lib, handle, hit)
             return hit
     chosen = ctypes.c_int32()
     nat.check(lib.xk_batch_tune(handle, int(generations), ctypes.byref(chosen)), "xk_batch_tune")
     if store is not None:
         try:
-            store.put(key, int(chosen.value))
+            store.put(key, {"band": int(chosen.value), "sizes": size_bands(lib, handle)})
         except OSError:
             pass   # a read-only cache location only costs the next tuning run
     return int(chosen.value)
@@ -144,10 +185,12 @@ def tuned_band(lib, handle, widths, heights, generations, cache=True, library=No
 PLAN_KINDS = {0: "global", 1: "resident", 2: "cluster", 3: "temporal"}
 
 
-def lattice_key(device, library, width, height, border):
+def lattice_key(device, library, width, height, border, rule_form=0):
     """Cache key of a 2-D lattice's launch plan; ``border`` is "torus" or
-    "static0" / "static1"."""
-    return "life2d_plan|%s|%s|%dx%d|%s" % (device, library, int(width), int(height), border)
+    "static0" / "static1"; ``rule_form`` the kernels' rule form
+    (``xk_model_rule_form``: 1 Conway compiled in, 0 a rule table)."""
+    return "life2d_plan|%s|%s|%dx%d|%s|rule%d" % (device, library, int(width), int(height), border,
+                                                 int(rule_form))
 
 
 def _valid_plan(hit):
@@ -169,7 +212,8 @@ def lattice_plan(lib, handle, width, height, border, cache=True, library=None):
             path = None
     plan = (ctypes.c_int32 * 4)()
     if path is not None:
-        key = lattice_key(device_id(lib), lib_id, width, height, border)
+        form = lib.xk_model_rule_form(handle) if hasattr(lib, "xk_model_rule_form") else 0
+        key = lattice_key(device_id(lib), lib_id, width, height, border, form)
         store = TuneCache(path)
         hit = store.get(key)
         if _valid_plan(hit):
