@@ -535,7 +535,8 @@ def c2_experiment():
 def evolife_line(args, dist):
     """EvoLife 1920x1080 (c2_experiment): K steps of 100 generations, each
     generation followed by a full-frame render (RendererPlain, zoom 1) into a
-    device frame buffer -- the reference's step() + render() pair per frame.
+    device frame buffer -- the reference's step() + render() pair per frame;
+    the step kernel writes that frame itself (one launch per generation).
     e2e: the state and colours loaded from the host, then 100 generations
     with every frame copied to page-locked host memory.  Parity: the oracle
     started from the GPU state after the timed steps, two more generations
@@ -609,12 +610,13 @@ def evolife_line(args, dist):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": committed_traffic("evolife"),
-                         "kernel": "xk_k_evolife + xk_k_render<uint8> per generation",
+                         "kernel": "xk_k_evolife per generation (it also writes the zoom-1 "
+                                   "uint8 frame)",
                          "algorithmic_bytes_per_generation": bytes_per_update * n,
                          "note": "B_alg = 52 B per cell-update (8 B state and 12 B colour read "
                                  "and written, 12 B int3 pixel written); the kernel is bound by "
                                  "integer instruction issue (genome crossover), not by HBM"},
-            "gpu_launches": 2 * gens * args.steps, "clocks": clk}
+            "gpu_launches": gens * args.steps, "clocks": clk}
     if dist.rank == 0:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O
@@ -745,12 +747,13 @@ def mass_line(args, dist):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": committed_traffic("mass_tma") if side == 256 else None,
-                         "kernel": "xk_k_mass_tma + projection + frame per generation",
+                         "kernel": "xk_k_mass_tma + xk_k_mass_project (column sums, writes "
+                                   "the frame) per generation",
                          "algorithmic_bytes_per_generation": bytes_per_update * n,
                          "note": "B_alg = 12 B per cell-update (uint32 read + write, the "
                                  "projection's re-read of the state); traffic: DRAM bytes of "
                                  "one mass-transfer launch (one generation)"},
-            "gpu_launches": 3 * gens * args.steps, "clocks": clk}
+            "gpu_launches": 2 * gens * args.steps, "clocks": clk}
     if dist.rank == 0:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O
@@ -874,13 +877,27 @@ def life512_line(args, dist):
     api_s = time.perf_counter() - t0
     peak, peak_kind = measured_peak()
     achieved = B_ALG * n * gens / (statistics.mean(step_ms) / 1000.0) / 1e9
+    plan = getattr(model.gpu, "plan", None)
+    plan_desc = None
+    if plan:
+        kind = {0: "global", 1: "resident", 2: "cluster", 3: "temporal"}.get(plan[0], str(plan[0]))
+        plan_desc = {"kernel_family": kind}
+        if kind == "cluster":
+            plan_desc.update({"ctas": plan[1], "rows_per_band": plan[2],
+                              "sync": {0: "cluster barrier", 1: "neighbour mbarriers",
+                                       2: "split cluster barrier"}.get(plan[3], plan[3])})
+        elif kind == "temporal":
+            plan_desc["generations_per_launch"] = plan[3]
+        plan_desc["rule_form"] = "B3/S23 compiled in" if nat.load().xk_model_rule_form(
+            model.gpu._handle) == 1 else "rule table"
     line = {"metric": "cell-updates/s (Life 512x512)", "value": value, "unit": "cell-updates/s",
             "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dev_s * 1000 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8",
             "data": "synthetic (seeded Bernoulli(0.5), 64-bit integer seed)",
             "config": {"workload": "Conway's Life B3/S23 512x512 torus, 1000 generations per step",
-                       "l2": "256 KB state, L2 resident; no flush (latency-bound size)"},
+                       "l2": "256 KB state, L2 resident; no flush (latency-bound size)",
+                       "tuned_plan": plan_desc},
             "e2e": {"value": float(n) * gens * args.steps * dist.world / e2e_s,
                     "unit": "cell-updates/s", "h2d_bytes_per_step": n + 12 * n,
                     "d2h_bytes_per_step": n},

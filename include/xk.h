@@ -133,9 +133,11 @@ int xk_step_frames(xk_model *m, int64_t nsteps, int32_t width, int32_t height, i
  * kernel shape for every model (base.py:254-283); these exist so that a host
  * can cache the choice per device, library build and lattice and re-apply it
  * without timing.  plan[0]: XK_PLAN_*; CLUSTER: plan[1] = CTAs asked for
- * (1..16), plan[2] = rows per lane group, plan[3] = 1 when the CTAs wait
- * only for their two neighbours' rows (mbarriers) instead of a cluster
- * barrier per generation (bands of 1, 2 or 4 rows); TEMPORAL: plan[3] =
+ * (1..16), plan[2] = rows per lane group, plan[3] = how the CTAs order
+ * their row exchange each generation: 0 a cluster barrier, 1 each CTA waits
+ * only for its two neighbours' rows (mbarriers; bands of 1, 2 or 4 rows), 2
+ * a cluster barrier whose arrival comes before the bands' inner rows and
+ * whose wait after them (every CTA's bands exactly 4 rows); TEMPORAL: plan[3] =
  * generations per launch (2..8).  xk_model_plan gives kind -1 for models
  * without plans.  A bounded wait of the neighbour form that gave up makes
  * the next xk_download return XK_ERR_TIMEOUT. */

@@ -67,6 +67,20 @@ def test_neighbour_sync_vs_oracle(cls, forced, band, monkeypatch):
         assert np.array_equal(got, want), (cls.__name__, size, forced, band)
 
 
+@pytest.mark.parametrize("size,forced", [((512, 512), 16), ((512, 512), 8), ((1024, 64), 16),
+                                         ((100, 256), 8), ((64, 512), 4), ((1000, 48), 2)])
+@pytest.mark.parametrize("cls", [GameOfLife, GameOfLifeStatic])
+def test_split_sync_vs_oracle(cls, size, forced, monkeypatch):
+    """The split form (the cluster barrier's arrive before the bands' inner
+    rows, its wait after them; bands of exactly 4 rows in every CTA) against
+    the oracle, and over 3000 generations on the C1 lattice."""
+    got, want = _run(cls, size, forced, 41, monkeypatch, 3 * forced, 4, "split")
+    assert np.array_equal(got, want), (cls.__name__, size, forced)
+    if size == (512, 512) and cls is GameOfLife:
+        got, want = _run(cls, size, forced, 3000, monkeypatch, 11, 4, "split")
+        assert np.array_equal(got, want)
+
+
 @pytest.mark.parametrize("band", [1, 2, 4])
 def test_neighbour_sync_long_run(band, monkeypatch):
     """3000 generations in one launch of the neighbour form on 16 CTAs (a

@@ -152,7 +152,7 @@ struct xk_model {
     int resident = 0, res_threads = 0, res_smem = 0;
     int cl_tuned = 0, cl_C = 0, cl_R = 0, cl_threads = 0;   // cluster plan (cl_C = 0: none)
     int cl_want = 0, cl_band = 0;    // the cluster size and band length the plan was made from
-    int cl_p2p = 0;                  // the cluster plan's neighbour form of synchronisation
+    int cl_sync = 0;                 // the cluster plan's synchronisation form (XK_SYNC_*)
     int tb_T = 0;                // temporally blocked global kernel: generations per launch (0: none)
     uint32_t rule0 = 0, rule1 = 0;
     int32_t lut[6] = {0, 0, 0, 0, 0, 0};
@@ -230,7 +230,7 @@ static int tune_cluster(xk_model *m)
 {
     m->cl_tuned = 1;
     m->cl_C = 0;
-    m->cl_p2p = 0;
+    m->cl_sync = 0;
     m->tb_T = 0;
     const char *tenv = getenv("XK_TB");
     if (tenv && tenv[0]) {
@@ -252,7 +252,10 @@ static int tune_cluster(xk_model *m)
             m->cl_want = want;
             m->cl_band = band;
             const char *senv = getenv("XK_CLUSTER_SYNC");
-            m->cl_p2p = senv && strcmp(senv, "p2p") == 0 && xk_life_cluster_has_p2p(m->lg, R, th);
+            const int sync = !senv ? XK_SYNC_BARRIER
+                             : strcmp(senv, "p2p") == 0 ? XK_SYNC_NEIGHBOUR
+                             : strcmp(senv, "split") == 0 ? XK_SYNC_SPLIT : XK_SYNC_BARRIER;
+            m->cl_sync = xk_life_cluster_has_sync(m->lg, C, R, th, sync) ? sync : XK_SYNC_BARRIER;
         }
         return XK_OK;
     }
@@ -316,17 +319,17 @@ static int tune_cluster(xk_model *m)
         cudaFree(tmp);
         XK_CUDA(e);
     }
-    // clusters: sizes, band lengths and both synchronisation forms
+    // clusters: sizes, band lengths and the synchronisation forms
     static const int cand[] = {16, 8, 4, 2};
     static const int bands[] = {1, 2, 4};
-    for (int k = 0; k < 24; ++k) {
-        const int want = cand[k / 6], band = bands[(k / 2) % 3], p2p = k & 1;
+    for (int k = 0; k < 36; ++k) {
+        const int want = cand[k / 9], band = bands[(k / 3) % 3], sync = k % 3;
         int C = 0, R = 0, th = 0;
         if (!xk_life_cluster_config(m->lg, want, band, &C, &R, &th)) continue;
-        if (p2p && !xk_life_cluster_has_p2p(m->lg, R, th)) continue;
+        if (!xk_life_cluster_has_sync(m->lg, C, R, th, sync)) continue;
         float ms = 0.f;
         XK_CUDA(time_it([&]() {
-            return xk_life_step_cluster(scratch, m->lg, m->rule0, m->rule1, G, C, R, th, m->stream, p2p);
+            return xk_life_step_cluster(scratch, m->lg, m->rule0, m->rule1, G, C, R, th, m->stream, sync);
         }, &ms));
         if (xk_cluster_take_wait_failure()) {
             xk_set_error("cluster step: a CTA gave up waiting for its neighbours' rows");
@@ -339,7 +342,7 @@ static int tune_cluster(xk_model *m)
             m->cl_threads = th;
             m->cl_want = want;
             m->cl_band = band;
-            m->cl_p2p = p2p;
+            m->cl_sync = sync;
             m->tb_T = 0;
         }
     }
@@ -795,7 +798,7 @@ static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *fram
         while (left > 0) {
             const int g = (int)(left > 4096 ? 4096 : left);
             XK_CUDA(xk_life_step_cluster(m->bits[m->cur], m->lg, m->rule0, m->rule1, g, m->cl_C, m->cl_R,
-                                         m->cl_threads, m->stream, m->cl_p2p));
+                                         m->cl_threads, m->stream, m->cl_sync));
             left -= g;
         }
     } else if (m->d.family == XK_FAMILY_SHIFT && m->d.torus && colors_free && shift_jump_enabled()) {
@@ -916,7 +919,7 @@ extern "C" int xk_model_plan(xk_model *m, int32_t plan[4])
         plan[0] = XK_PLAN_CLUSTER;
         plan[1] = m->cl_want;
         plan[2] = m->cl_band;
-        plan[3] = m->cl_p2p;
+        plan[3] = m->cl_sync;
     } else if (m->tb_T > 1) {
         plan[0] = XK_PLAN_TEMPORAL;
         plan[1] = plan[2] = 0;
@@ -953,9 +956,10 @@ extern "C" int xk_model_set_plan(xk_model *m, const int32_t plan[4])
                        xk_life_cluster_config(m->lg, plan[1], plan[2], &C, &R, &th),
                    XK_ERR_ARG, "xk_model_set_plan: no cluster of %d CTAs with bands of %d rows",
                    plan[1], plan[2]);
-        XK_REQUIRE(plan[3] == 0 || (plan[3] == 1 && xk_life_cluster_has_p2p(m->lg, R, th)), XK_ERR_ARG,
-                   "xk_model_set_plan: cluster synchronisation form %d (0, or 1 for bands of 1, 2 "
-                   "or 4 rows)", plan[3]);
+        XK_REQUIRE(plan[3] >= XK_SYNC_BARRIER && plan[3] <= XK_SYNC_SPLIT &&
+                       xk_life_cluster_has_sync(m->lg, C, R, th, plan[3]),
+                   XK_ERR_ARG, "xk_model_set_plan: cluster synchronisation form %d does not apply "
+                   "(1: bands of 1, 2 or 4 rows; 2: every CTA's bands 4 rows)", plan[3]);
         break;
     case XK_PLAN_TEMPORAL:
         XK_REQUIRE(plan[3] >= 2 && plan[3] <= 8 && xk_life_tb_supported(m->lg), XK_ERR_ARG,
@@ -970,7 +974,7 @@ extern "C" int xk_model_set_plan(xk_model *m, const int32_t plan[4])
     m->cl_threads = th;
     m->cl_want = plan[0] == XK_PLAN_CLUSTER ? plan[1] : 0;
     m->cl_band = plan[0] == XK_PLAN_CLUSTER ? plan[2] : 0;
-    m->cl_p2p = plan[0] == XK_PLAN_CLUSTER ? plan[3] : 0;
+    m->cl_sync = plan[0] == XK_PLAN_CLUSTER ? plan[3] : 0;
     m->tb_T = plan[0] == XK_PLAN_TEMPORAL ? plan[3] : 0;
     return XK_OK;
 }

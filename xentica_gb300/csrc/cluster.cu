@@ -40,6 +40,16 @@
 //   __syncthreads_or), its neighbours then give up in turn, and the step
 //   reports XK_ERR_TIMEOUT.
 //
+// * split form (bands of exactly 4 rows in every CTA): the barrier form with
+//   the cluster barrier's arrive and wait apart.  A band computes its first
+//   and last row first (from the halos and its own rows, whose old values it
+//   keeps in registers) and publishes them, then arrives; its two inner rows,
+//   which no other band reads, are computed while the barrier completes, and
+//   the wait comes at the top of the next generation.  The ordering argument
+//   is the barrier form's: every halo read of generation g precedes the
+//   arrival of generation g, every halo write of generation g + 1 follows its
+//   wait.
+//
 // A last cluster barrier after the loop keeps every CTA's shared memory alive
 // until the remote stores of the final generation have landed.  A lane only
 // ever touches its own column word of its own band.
@@ -108,6 +118,18 @@ __device__ __forceinline__ void xk_cl_arrive_remote(uint32_t bar)
     asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" : : "r"(bar) : "memory");
 }
 
+// the hardware cluster barrier's two halves (every thread of every CTA
+// alternates them)
+__device__ __forceinline__ void xk_cl_barrier_arrive()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;" : : : "memory");
+}
+
+__device__ __forceinline__ void xk_cl_barrier_wait()
+{
+    asm volatile("barrier.cluster.wait.acquire.aligned;" : : : "memory");
+}
+
 __device__ __forceinline__ uint32_t xk_cl_mapa(uint32_t addr, uint32_t rank)
 {
     uint32_t r;
@@ -119,11 +141,13 @@ __device__ __forceinline__ uint32_t xk_cl_mapa(uint32_t addr, uint32_t rank)
 // neighbour vector one funnel shift); LB: every band of the widest CTA has
 // exactly LB rows (1, 2 or 4; the row loop is unrolled), 0 for any length;
 // RF: the rule form (XK_RULE_TABLE: `t`; XK_RULE_CONWAY: B3/S23 compiled in);
-// P2P: the neighbour form of synchronisation instead of the barrier form
-template <bool TORUS, bool FULLW, int LB, int RF, bool P2P>
+// SYNC: the synchronisation form (XK_SYNC_*)
+template <bool TORUS, bool FULLW, int LB, int RF, int SYNC>
 __global__ void __launch_bounds__(1024)
 xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int generations, int R)
 {
+    constexpr bool P2P = SYNC == XK_SYNC_NEIGHBOUR, SPLIT = SYNC == XK_SYNC_SPLIT;
+    static_assert(!SPLIT || LB == 4, "the split form runs bands of 4 rows");
     const auto &t = RuleForm<RF>::make(t9);
     extern __shared__ uint32_t sm[];
     cg::cluster_group cluster = cg::this_cluster();
@@ -232,6 +256,7 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int gen
     publish(0, 0, wp[0], true);
     if (y1 - 1 - y0 != 0) publish(0, y1 - 1 - y0, wp[32 * (y1 - 1 - y0)], true);
     bool failed = false;
+    if (SPLIT) xk_cl_barrier_arrive();
     for (int gen = 0; gen < generations; ++gen) {
         const int par = gen & 1;
         const uint32_t *hp = halo + par * hwords;
@@ -243,12 +268,52 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int gen
                 failed = true;
                 atomicOr(&xk_cluster_wait_failed, 1u);
             }
+        } else if (SPLIT) {
+            xk_cl_barrier_wait();
         } else {
             cluster.sync();
         }
         const bool remote = gen + 1 < generations || !P2P;
         const uint32_t wu = first_band ? slot[(par * 2 + 0) * wpr + jc] : hp[((bc - 1) * 2 + 1) * wpr + jc];
         const uint32_t wl = last_band ? slot[(par * 2 + 1) * wpr + jc] : hp[((bc + 1) * 2 + 0) * wpr + jc];
+        if (SPLIT) {
+            // every band has 4 rows: the first and last row, then the inner
+            // two after the arrival
+            const uint32_t w0 = wp[0], w1 = wp[32], w2 = wp[64], w3 = wp[96];
+            uint32_t s_u, c_u, s0, c0, s1, c1, s2, c2, s3, c3, s_d, c_d;
+            colsum(wu, s_u, c_u);
+            if (top_off) s_u = c_u = g.bfill;
+            colsum(w0, s0, c0);
+            colsum(w1, s1, c1);
+            colsum(w2, s2, c2);
+            colsum(w3, s3, c3);
+            colsum(wl, s_d, c_d);
+            if (bot_off) s_d = c_d = g.bfill;
+            uint32_t o0 = xk_life_word9(s_u, c_u, s0, c0, s1, c1, w0, t);
+            uint32_t o3 = xk_life_word9(s2, c2, s3, c3, s_d, c_d, w3, t);
+            if (!FULLW) {
+                o0 &= outmask;
+                o3 &= outmask;
+            }
+            if (active) {
+                wp[0] = o0;
+                wp[96] = o3;
+                publish(par ^ 1, 0, o0, true);
+                publish(par ^ 1, 3, o3, true);
+            }
+            xk_cl_barrier_arrive();
+            uint32_t o1 = xk_life_word9(s0, c0, s1, c1, s2, c2, w1, t);
+            uint32_t o2 = xk_life_word9(s1, c1, s2, c2, s3, c3, w2, t);
+            if (!FULLW) {
+                o1 &= outmask;
+                o2 &= outmask;
+            }
+            if (active) {
+                wp[32] = o1;
+                wp[64] = o2;
+            }
+            continue;
+        }
         uint32_t su, cu_, sm_, cm_, Cm = wp[0];
         colsum(wu, su, cu_);
         if (top_off) su = cu_ = g.bfill;
@@ -280,6 +345,7 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int gen
             for (int i = 0; i < p.L; ++i) row(i);
         }
     }
+    if (SPLIT) xk_cl_barrier_wait();   // the phase of the last arrival
     cluster.sync();
     for (int w = threadIdx.x; w < Rc * wpr; w += blockDim.x) {
         const int y = w / wpr, jj = w - y * wpr;
@@ -290,42 +356,44 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int gen
 
 typedef void (*ClusterKernel)(uint32_t *, LifeGeo, LifeTable9, int, int);
 
-// the neighbour form has instantiations for bands of 1, 2 and 4 rows
+// the neighbour form has instantiations for bands of 1, 2 and 4 rows, the
+// split form for bands of 4
 template <bool TORUS, bool FULLW, int RF>
-static ClusterKernel cluster_kernel_l(int L, bool p2p)
+static ClusterKernel cluster_kernel_l(int L, int sync)
 {
-    if (p2p) {
+    if (sync == XK_SYNC_NEIGHBOUR) {
         switch (L) {
-        case 1: return xk_k_life_cluster<TORUS, FULLW, 1, RF, true>;
-        case 2: return xk_k_life_cluster<TORUS, FULLW, 2, RF, true>;
-        case 4: return xk_k_life_cluster<TORUS, FULLW, 4, RF, true>;
+        case 1: return xk_k_life_cluster<TORUS, FULLW, 1, RF, XK_SYNC_NEIGHBOUR>;
+        case 2: return xk_k_life_cluster<TORUS, FULLW, 2, RF, XK_SYNC_NEIGHBOUR>;
+        case 4: return xk_k_life_cluster<TORUS, FULLW, 4, RF, XK_SYNC_NEIGHBOUR>;
         default: return nullptr;
         }
     }
+    if (sync == XK_SYNC_SPLIT) return L == 4 ? xk_k_life_cluster<TORUS, FULLW, 4, RF, XK_SYNC_SPLIT> : nullptr;
     switch (L) {
-    case 1: return xk_k_life_cluster<TORUS, FULLW, 1, RF, false>;
-    case 2: return xk_k_life_cluster<TORUS, FULLW, 2, RF, false>;
-    case 4: return xk_k_life_cluster<TORUS, FULLW, 4, RF, false>;
-    default: return xk_k_life_cluster<TORUS, FULLW, 0, RF, false>;
+    case 1: return xk_k_life_cluster<TORUS, FULLW, 1, RF, XK_SYNC_BARRIER>;
+    case 2: return xk_k_life_cluster<TORUS, FULLW, 2, RF, XK_SYNC_BARRIER>;
+    case 4: return xk_k_life_cluster<TORUS, FULLW, 4, RF, XK_SYNC_BARRIER>;
+    default: return xk_k_life_cluster<TORUS, FULLW, 0, RF, XK_SYNC_BARRIER>;
     }
 }
 
 template <int RF>
-static ClusterKernel cluster_kernel_rf(const LifeGeo &g, int L, bool p2p)
+static ClusterKernel cluster_kernel_rf(const LifeGeo &g, int L, int sync)
 {
-    if (!g.torus) return cluster_kernel_l<false, false, RF>(L, p2p);
-    if (g.rlast == 32) return cluster_kernel_l<true, true, RF>(L, p2p);
-    return cluster_kernel_l<true, false, RF>(L, p2p);
+    if (!g.torus) return cluster_kernel_l<false, false, RF>(L, sync);
+    if (g.rlast == 32) return cluster_kernel_l<true, true, RF>(L, sync);
+    return cluster_kernel_l<true, false, RF>(L, sync);
 }
 
 // the instantiation for a lattice, launch shape (L: band length of the
 // widest CTA), rule form and synchronisation form (null: none)
 static ClusterKernel cluster_kernel(const LifeGeo &g, int R, int threads, int rf = XK_RULE_TABLE,
-                                    bool p2p = false)
+                                    int sync = XK_SYNC_BARRIER)
 {
     const int L = xk_resident_plan(g.wpr, R, threads).L;
-    return rf == XK_RULE_CONWAY ? cluster_kernel_rf<XK_RULE_CONWAY>(g, L, p2p)
-                                : cluster_kernel_rf<XK_RULE_TABLE>(g, L, p2p);
+    return rf == XK_RULE_CONWAY ? cluster_kernel_rf<XK_RULE_CONWAY>(g, L, sync)
+                                : cluster_kernel_rf<XK_RULE_TABLE>(g, L, sync);
 }
 
 static cudaError_t cluster_attrs(ClusterKernel k, size_t smem)
@@ -393,8 +461,8 @@ int xk_life_cluster_config(const LifeGeo &g, int C, int band, int *C_out, int *R
     const ClusterKernel k = cluster_kernel(g, rows, th);
     bool attrs_ok = true;
     for (int rf = XK_RULE_TABLE; rf <= XK_RULE_CONWAY && attrs_ok; ++rf)
-        for (int p2p = 0; p2p < 2 && attrs_ok; ++p2p) {
-            const ClusterKernel kk = cluster_kernel(g, rows, th, rf, p2p != 0);
+        for (int sync = XK_SYNC_BARRIER; sync <= XK_SYNC_SPLIT && attrs_ok; ++sync) {
+            const ClusterKernel kk = cluster_kernel(g, rows, th, rf, sync);
             attrs_ok = !kk || cluster_attrs(kk, smem) == cudaSuccess;
         }
     if (!attrs_ok) {
@@ -416,9 +484,15 @@ int xk_life_cluster_config(const LifeGeo &g, int C, int band, int *C_out, int *R
     return 1;
 }
 
-int xk_life_cluster_has_p2p(const LifeGeo &g, int R, int threads)
+int xk_life_cluster_has_sync(const LifeGeo &g, int C, int R, int threads, int sync)
 {
-    return cluster_kernel(g, R, threads, XK_RULE_TABLE, true) != nullptr;
+    if (sync == XK_SYNC_BARRIER) return 1;
+    if (sync == XK_SYNC_SPLIT) {
+        // every CTA has R rows, cut into bands of exactly 4
+        const ResidentPlan p = xk_resident_plan(g.wpr, R, threads);
+        if ((int64_t)C * R != g.H || p.L != 4 || p.nb * 4 != R) return 0;
+    }
+    return cluster_kernel(g, R, threads, XK_RULE_TABLE, sync) != nullptr;
 }
 
 bool xk_cluster_take_wait_failure()
@@ -430,10 +504,11 @@ bool xk_cluster_take_wait_failure()
 }
 
 cudaError_t xk_life_step_cluster(uint32_t *bits, const LifeGeo &g, uint32_t rule0, uint32_t rule1,
-                                 int generations, int C, int R, int threads, cudaStream_t s, int p2p)
+                                 int generations, int C, int R, int threads, cudaStream_t s, int sync)
 {
     const size_t smem = 4ull * cluster_words(g.wpr, R, threads);
-    const ClusterKernel k = cluster_kernel(g, R, threads, xk_rule_form(rule0, rule1), p2p != 0);
+    if (!xk_life_cluster_has_sync(g, C, R, threads, sync)) return cudaErrorInvalidValue;
+    const ClusterKernel k = cluster_kernel(g, R, threads, xk_rule_form(rule0, rule1), sync);
     if (!k) return cudaErrorInvalidValue;
     cudaError_t e = cluster_attrs(k, smem);
     if (e != cudaSuccess) return e;

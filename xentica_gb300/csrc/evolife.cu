@@ -339,8 +339,15 @@ static cudaError_t evo_tables(EvoParams &p, cudaStream_t s)
 
 #define XK_EVO_BX 32
 #define XK_EVO_BY 8
+#ifndef XK_EVO_MINB
+#define XK_EVO_MINB 8     // CTAs per SM the registers are cut for (32 per thread): latency hiding for
+                          // the crossover's table lookups, which come from L2
+#endif
 
-__global__ void __launch_bounds__(XK_EVO_BX * XK_EVO_BY)
+// MUT: mutation_prob > 0 (the mutation flips, and the union of the parents'
+// genomes they are masked with, exist only then)
+template <bool MUT>
+__global__ void __launch_bounds__(XK_EVO_BX * XK_EVO_BY, XK_EVO_MINB)
 xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32_t *__restrict__ col,
              EvoParams p)
 {
@@ -392,7 +399,7 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
     for (int k = 0; k < 8; ++k) {
         const uint32_t par = ((nr[k] & 510u) >> num_fit) & 1u;
         pmask |= par << k;
-        any |= nr[k] * par;
+        if (MUT) any |= nr[k] * par;
     }
     const uint32_t n = __popc(pmask);
     const uint32_t old_rule = rule, old_energy = energy;
@@ -416,7 +423,7 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
         for (int e = __popc(rot) - (int)p.max_genes; e > 0; --e)
             rot &= ~(0x80000000u >> __clz(rot));
         new_genome = xk_unrot18(rot, start_gene);
-        if (p.mutation) new_genome ^= __ldg(p.mut + x0) & any;
+        if (MUT) new_genome ^= __ldg(p.mut + x0) & any;
     }
     rule = new_genome + rule * (uint32_t)(new_genome == 0);
     const uint32_t is_live = (uint32_t)(old_energy < 255u) &
@@ -481,5 +488,6 @@ cudaError_t xk_evolife_step(const uint64_t *src, uint64_t *dst, int32_t *col, co
     if (e != cudaSuccess) return e;
     dim3 block(XK_EVO_BX, XK_EVO_BY);
     dim3 grid((p.W + XK_EVO_BX - 1) / XK_EVO_BX, (p.H + XK_EVO_BY - 1) / XK_EVO_BY);
-    return xk_launch_pdl(xk_k_evolife, grid, block, 0, s, src, dst, col, p);
+    return p.mutation ? xk_launch_pdl(xk_k_evolife<true>, grid, block, 0, s, src, dst, col, p)
+                      : xk_launch_pdl(xk_k_evolife<false>, grid, block, 0, s, src, dst, col, p);
 }

@@ -107,6 +107,7 @@ struct Slot {
     LifeInst *d_inst = nullptr;
     int32_t *h_gens = nullptr;    // pinned, max_active entries
     int32_t *d_gens = nullptr;
+    bool owned = false;           // arrays allocated for this slot (not carved from the pool)
     std::vector<Req *> members;
 };
 
@@ -177,7 +178,17 @@ struct xk_server {
     int tb_depth = 8;          // generations per launch of large 2-D requests (XK_SERVE_TB)
     int64_t round_work = 0;    // cell-generations of a resident member's round (quantum x 2^18)
     int prio_least = 0, prio_greatest = 0;   // the device's stream priority range
+    // resident-group slot arrays, allocated once at creation (a group created
+    // while requests run then costs no page-locked allocation on the worker):
+    // slot_pool slots of slot_bytes each, pinned and on the device
+    uint8_t *slot_host = nullptr, *slot_dev = nullptr;
+    int slot_pool = 0, slot_used = 0;
+    int64_t slot_bytes = 0;
     int64_t resident_max = 1 << 18;
+    // rows per lane group of resident lattices: 1 gives a lattice as many
+    // threads as a CTA holds, so each generation is as short as it can be (a
+    // request's latency is its generation count times that); XK_SERVE_BAND
+    int resident_band = 1;
     uint8_t *dev_base = nullptr;
     uint8_t *host_base = nullptr;
     unsigned int *bad = nullptr;
@@ -249,8 +260,18 @@ static int group_for(xk_server *s, int threads, int smem)
     for (Slot &sl : g.slot) {
         XK_CUDA(cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking, s->prio_greatest));
         XK_CUDA(cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming));
-        XK_CUDA(cudaMallocHost(&sl.h_inst, sizeof(LifeInst) * s->max_active));
-        XK_CUDA(cudaMalloc(&sl.d_inst, sizeof(LifeInst) * s->max_active));
+        const size_t inst_bytes = sizeof(LifeInst) * s->max_active;
+        if (s->slot_used < s->slot_pool) {
+            const int64_t at = (int64_t)s->slot_used++ * s->slot_bytes;
+            sl.h_inst = (LifeInst *)(s->slot_host + at);
+            sl.d_inst = (LifeInst *)(s->slot_dev + at);
+            sl.h_gens = (int32_t *)(s->slot_host + at + inst_bytes);
+            sl.d_gens = (int32_t *)(s->slot_dev + at + inst_bytes);
+            continue;
+        }
+        sl.owned = true;
+        XK_CUDA(cudaMallocHost(&sl.h_inst, inst_bytes));
+        XK_CUDA(cudaMalloc(&sl.d_inst, inst_bytes));
         XK_CUDA(cudaMallocHost(&sl.h_gens, sizeof(int32_t) * s->max_active));
         XK_CUDA(cudaMalloc(&sl.d_gens, sizeof(int32_t) * s->max_active));
     }
@@ -314,7 +335,8 @@ static int admit(xk_server *s, Req *q, bool *admitted)
         q->rule1 = life2d_rule1(r.rule);
         int threads = 0, smem = 0;
         const bool fits = q->n <= s->resident_max &&
-                          xk_life_resident_config((int)r.size[0], (int)r.size[1], 8, &threads, &smem);
+                          xk_life_resident_config((int)r.size[0], (int)r.size[1], s->resident_band, &threads,
+                                                  &smem);
         if (fits) {
             q->path = PATH_RESIDENT;
             q->threads = threads;
@@ -697,11 +719,14 @@ static void free_server(xk_server *s)
         for (Slot &sl : g.slot) {
             if (sl.stream) cudaStreamDestroy(sl.stream);
             if (sl.ev) cudaEventDestroy(sl.ev);
+            if (!sl.owned) continue;
             if (sl.h_inst) cudaFreeHost(sl.h_inst);
             if (sl.d_inst) cudaFree(sl.d_inst);
             if (sl.h_gens) cudaFreeHost(sl.h_gens);
             if (sl.d_gens) cudaFree(sl.d_gens);
         }
+    if (s->slot_host) cudaFreeHost(s->slot_host);
+    if (s->slot_dev) cudaFree(s->slot_dev);
     for (auto &kv : s->reqs) {
         if (kv.second->stream) cudaStreamDestroy(kv.second->stream);
         if (kv.second->ev) cudaEventDestroy(kv.second->ev);
@@ -737,8 +762,15 @@ extern "C" int xk_serve_create(int64_t budget_bytes, int64_t host_bytes, int32_t
         s->tb_depth = T >= 2 && T <= 8 ? T : 0;
     }
     if (const char *e = getenv("XK_SERVE_RESIDENT_MAX")) s->resident_max = atoll(e);
+    if (const char *e = getenv("XK_SERVE_BAND")) s->resident_band = std::max(1, std::min(1024, atoi(e)));
+    // room for the slots of up to 64 resident groups, at most 64 MB
+    s->slot_bytes = XkArena::round((int64_t)(sizeof(LifeInst) + sizeof(int32_t)) * max_active);
+    s->slot_pool = (int)std::min<int64_t>(64 * XK_SERVE_GROUP_SLOTS, (64LL << 20) / s->slot_bytes);
     cudaError_t e;
     if ((e = cudaGetDevice(&s->device)) != cudaSuccess ||
+        (s->slot_pool > 0 &&
+         ((e = cudaMallocHost(&s->slot_host, (size_t)(s->slot_bytes * s->slot_pool))) != cudaSuccess ||
+          (e = cudaMalloc(&s->slot_dev, (size_t)(s->slot_bytes * s->slot_pool))) != cudaSuccess)) ||
         (e = cudaDeviceGetStreamPriorityRange(&s->prio_least, &s->prio_greatest)) != cudaSuccess ||
         (e = cudaMalloc(&s->dev_base, (size_t)budget_bytes)) != cudaSuccess ||
         (e = cudaMallocHost(&s->host_base, (size_t)host_bytes)) != cudaSuccess ||

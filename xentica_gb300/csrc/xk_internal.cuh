@@ -179,12 +179,17 @@ LifeTable9 xk_life_table9(uint32_t rule0, uint32_t rule1);
 // rule1: live-cell table): XK_RULE_CONWAY for B3/S23, else XK_RULE_TABLE
 int xk_rule_form(uint32_t rule0, uint32_t rule1);
 int xk_life_cluster_config(const LifeGeo &g, int C, int band, int *C_out, int *R, int *threads);
-// p2p: the neighbour form of synchronisation (mbarriers of the two
-// neighbouring CTAs) instead of a cluster barrier per generation; it exists
-// for bands of 1, 2 and 4 rows (xk_life_cluster_has_p2p)
+// sync: how the CTAs of the cluster order their halo exchange every
+// generation -- XK_SYNC_BARRIER a cluster barrier; XK_SYNC_NEIGHBOUR mbarriers
+// of the two neighbouring CTAs only (bands of 1, 2 and 4 rows);
+// XK_SYNC_SPLIT a cluster barrier whose arrive and wait enclose the bands'
+// inner rows (every CTA's bands exactly 4 rows): xk_life_cluster_has_sync
+#define XK_SYNC_BARRIER 0
+#define XK_SYNC_NEIGHBOUR 1
+#define XK_SYNC_SPLIT 2
 cudaError_t xk_life_step_cluster(uint32_t *bits, const LifeGeo &g, uint32_t rule0, uint32_t rule1,
-                                 int generations, int C, int R, int threads, cudaStream_t s, int p2p = 0);
-int xk_life_cluster_has_p2p(const LifeGeo &g, int R, int threads);
+                                 int generations, int C, int R, int threads, cudaStream_t s, int sync = 0);
+int xk_life_cluster_has_sync(const LifeGeo &g, int C, int R, int threads, int sync);
 // a CTA of the neighbour form gave up waiting since the last call (clears it)
 bool xk_cluster_take_wait_failure();
 
