@@ -78,6 +78,15 @@ CASES = {
                 lambda m: _random_evolife(m, 5)),
     "mass": (lambda: MassTransfer(type("E", (MassExperiment, ), {"size": (36, 20, 12)})),
              (36, 20), 1, (0, 0), None),
+    # the whole lattice at zoom 1: the step kernel sums the column colours
+    # itself (one atomic per column and run of planes); an odd width, and a
+    # deep lattice whose columns are cut into many runs
+    "mass-odd": (lambda: MassTransfer(type("E", (MassExperiment, ), {"size": (37, 21, 13)})),
+                 (37, 21), 1, (0, 0), None),
+    "mass-deep": (lambda: MassTransfer(type("E", (MassExperiment, ), {"size": (64, 48, 100)})),
+                  (64, 48), 1, (0, 0), None),
+    "mass-offset": (lambda: MassTransfer(type("E", (MassExperiment, ), {"size": (36, 20, 12)})),
+                    (30, 20), 1, (2, 3), None),
     "shift": (lambda: ShiftingSands(ShiftingSandsExperiment), (160, 90), 3, (0, 0), None),
     "interpreter": (lambda: _on_interpreter(ShiftingSands, ShiftingSandsExperiment), (160, 90), 3,
                     (0, 0), None),

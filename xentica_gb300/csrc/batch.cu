@@ -202,14 +202,18 @@ static int plan_classes(xk_batch *b)
         b->h_inst.push_back(in);
     }
     // classes come sorted by block size, largest first; their CTAs run longest,
-    // so they get the greater launch priorities and the block scheduler
-    // dispatches them first (longest work first packs the SMs best)
+    // so their launches (xk_batch_step, direct or in the graph) carry the
+    // greater priorities and the block scheduler dispatches them first
+    // (longest work first packs the SMs best).  The streams themselves keep
+    // the default priority: the end-to-end schedule (xk_batch_run) launches
+    // the classes that share their SMs on them behind its high-priority
+    // staged groups.
     int prio_least = 0, prio_greatest = 0;
     XK_CUDA(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
     for (size_t k = 0; k < b->classes.size(); ++k)
         b->classes[k].priority = prio_greatest + std::min<int>((int)k, prio_least - prio_greatest);
     for (auto &c : b->classes) {
-        XK_CUDA(cudaStreamCreateWithPriority(&c.stream, cudaStreamNonBlocking, c.priority));
+        XK_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
         cudaEvent_t e;
         XK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         b->joins.push_back(e);

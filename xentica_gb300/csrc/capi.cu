@@ -764,8 +764,10 @@ static bool shift_jump_enabled()
 }
 
 // frame (EvoLife, count == 1 only): the generation's zoom-1 frame written by
-// the step kernel itself
-static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *frame = nullptr)
+// the step kernel itself; proj (mass transfer, count == 1 only): the step
+// kernel also adds the new state's column colour sums into it
+static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *frame = nullptr,
+                        uint32_t *proj = nullptr)
 {
     if (m->layout == LAYOUT_VM) {
         for (int64_t g = 0; g < count; ++g)
@@ -777,7 +779,7 @@ static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *fram
     if (m->layout == LAYOUT_MASS) {
         for (int64_t g = 0; g < count; ++g) {
             XK_CUDA(xk_mass_step(m->cells32[m->cur], m->cells32[1 - m->cur], m->totals + first + g,
-                                 m->d, m->mass_small, m->stream));
+                                 m->d, m->mass_small, m->stream, proj));
             m->cur = 1 - m->cur;
         }
         return XK_OK;
@@ -1056,16 +1058,30 @@ extern "C" int xk_step_frames(xk_model *m, int64_t nsteps, int32_t width, int32_
     const bool fused = m->layout == LAYOUT_CELLS64 && m->d.color_kind != XK_COLOR_NONE &&
                        m->d.ndim == 2 && m->d.proj_axis0 == 0 && m->d.proj_axis1 == 1 && zoom == 1 &&
                        dx == 0 && dy == 0 && width == m->d.size[0] && height == m->d.size[1];
+    // mass transfer viewed whole at zoom 1 along z: the step kernel sums the
+    // column colours as it writes the cells, a small kernel turns them into
+    // the frame (no second pass over the state)
+    const bool mass_fused = m->layout == LAYOUT_MASS && m->d.proj_axis0 == 0 && m->d.proj_axis1 == 1 &&
+                            m->d.render_smooth == 0 && zoom == 1 && dx == 0 && dy == 0 &&
+                            width == m->d.size[0] && height == m->d.size[1] && xk_mass_fuses_projection(m->d);
     XK_CUDA(cudaEventRecord(m->ev0, m->stream));
     for (int64_t g = 0; g < nsteps; ++g) {
         const int k = (int)(g % kFrameRing);
         uint8_t *dst = frames_on_device ? frames + (size_t)g * fb : m->ring + (size_t)k * fb;
         if (!frames_on_device && g >= kFrameRing)
             XK_CUDA(cudaStreamWaitEvent(m->stream, m->copied[k], 0));
-        rc = step_enqueue(m, g, 1, fused ? dst : nullptr);
-        if (rc != XK_OK) return rc;
-        m->proj_valid = 0;
-        if (!fused) {
+        if (mass_fused) {
+            XK_CUDA(cudaMemsetAsync(m->proj, 0, (size_t)m->d.size[0] * m->d.size[1] * 4, m->stream));
+            rc = step_enqueue(m, g, 1, nullptr, m->proj);
+            if (rc != XK_OK) return rc;
+            XK_CUDA(xk_mass_frame(m->proj, dst, m->d, m->stream));
+            m->proj_valid = 1;                     // the sums of the current state
+        } else {
+            rc = step_enqueue(m, g, 1, fused ? dst : nullptr);
+            if (rc != XK_OK) return rc;
+            m->proj_valid = 0;
+        }
+        if (!fused && !mass_fused) {
             rc = render_enqueue(m, dst, true, width, height, zoom, dx, dy);
             if (rc != XK_OK) return rc;
         }

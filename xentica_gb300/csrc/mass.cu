@@ -498,10 +498,18 @@ __device__ __forceinline__ uint4 xk_mt_q4(const uint4 m, bool &big)
     return make_uint4(xk_q_small(m.x), xk_q_small(m.y), xk_q_small(m.z), xk_q_small(m.w));
 }
 
-template <int MINB, bool GENERAL>
+// PROJ: also add the colours of the cells it writes, per column, into
+// proj[y * W + x] (the z-projection RendererPlain renders; proj zeroed
+// before the launch): a thread sums its four columns over its run of planes
+// (two columns per register, 16 bits each: a colour is at most 255 and a run
+// at most 256 planes, which the host checks) and adds each sum with one
+// atomic, so the projection needs no second pass over the state.  Integer
+// sums: the order of the additions does not matter.
+template <int MINB, bool GENERAL, bool PROJ>
 __global__ void __launch_bounds__(32 * XK_MT_BY, MINB)
 xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict__ src,
-              uint32_t *__restrict__ dst, unsigned long long *__restrict__ total, MassParams p, int zc)
+              uint32_t *__restrict__ dst, unsigned long long *__restrict__ total, MassParams p, int zc,
+              uint32_t *__restrict__ proj)
 {
     extern __shared__ __align__(128) uint8_t xk_mt_raw[];
     // tensor copies land on 128-byte boundaries: round the window's start up
@@ -621,6 +629,7 @@ xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict
     // the fast-only form runs when the lattice's whole total is below 2^30,
     // so every partial sum of its cells fits 32 bits
     typename std::conditional<GENERAL, unsigned long long, uint32_t>::type mass_sum = 0;
+    uint32_t cs01 = 0u, cs23 = 0u;                   // PROJ: colour sums, two columns per word
     uint32_t off = in ? (uint32_t)z0 * plane + (uint32_t)y * p.P + x0 : 0u;
     int z = z0;
     // one plane: take plane z + 1 into (mn, qn) and tile qnext, then compute
@@ -673,6 +682,10 @@ xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict
                 mass_sum += (unsigned long long)out[0] + out[1] + (unsigned long long)out[2] + out[3];
             else
                 mass_sum += out[0] + out[1] + out[2] + out[3];
+            if (PROJ) {
+                cs01 += xk_mass_color(out[0]) + (xk_mass_color(out[1]) << 16);
+                cs23 += xk_mass_color(out[2]) + (xk_mass_color(out[3]) << 16);
+            }
         }
         b_prev = b_cur;
         b_cur = b_next;
@@ -687,6 +700,13 @@ xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict
     if (*fail) {
         if (tid == 0) atomicOr(&xk_mass_wait_failed, 1u);
         return;
+    }
+    if (PROJ && in) {
+        uint32_t *pc = proj + (int64_t)y * p.W + x0;
+        const uint32_t csum[4] = {cs01 & 0xFFFFu, cs01 >> 16, cs23 & 0xFFFFu, cs23 >> 16};
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            if (x0 + i < p.W) atomicAdd(pc + i, csum[i]);
     }
     for (int o = 16; o > 0; o >>= 1) mass_sum += __shfl_down_sync(0xFFFFFFFFu, mass_sum, o);
     if (lane == 0) warp_sums[ty] = mass_sum;
@@ -839,8 +859,45 @@ static bool mass_tma_enabled()
     return !(v && !strcmp(v, "rows"));
 }
 
+// the TMA form's grid and planes per CTA for a lattice
+static void mass_tma_shape(const MassParams &p, int *gx, int *gy, int *zc)
+{
+    *gx = (p.W + 127) / 128;
+    *gy = (p.H + XK_MT_BY - 1) / XK_MT_BY;
+    *zc = mass_zchunk(p, *gx, *gy, 1024);
+}
+
+bool xk_mass_fuses_projection(const xk_desc &d)
+{
+    if (!mass_tma_enabled()) return false;
+    int gx, gy, zc;
+    mass_tma_shape(mass_params(d), &gx, &gy, &zc);
+    return zc <= 256;   // the 16-bit column sums of a run of planes
+}
+
+// the zoom-1 frame of the whole lattice from column sums (RendererPlain over
+// axes (0, 1), no smoothing): the float sum of a column's colours equals its
+// integer sum, divided by the depth
+__global__ void xk_k_mass_frame(const uint32_t *__restrict__ proj, uint8_t *__restrict__ frame, MassParams p)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)p.W * p.H) return;
+    const uint8_t v = (uint8_t)(int)__fdiv_rn((float)proj[i], (float)p.D);
+    frame[3 * i] = v;
+    frame[3 * i + 1] = v;
+    frame[3 * i + 2] = v;
+}
+
+cudaError_t xk_mass_frame(const uint32_t *proj, uint8_t *frame, const xk_desc &d, cudaStream_t s)
+{
+    const MassParams p = mass_params(d);
+    const int64_t n = (int64_t)p.W * p.H;
+    xk_k_mass_frame<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(proj, frame, p);
+    return cudaGetLastError();
+}
+
 cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long *total,
-                         const xk_desc &d, bool small, cudaStream_t s)
+                         const xk_desc &d, bool small, cudaStream_t s, uint32_t *proj)
 {
     const MassParams p = mass_params(d);
     const bool vec = p.W % 4 == 0;
@@ -858,8 +915,8 @@ cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long 
                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return cudaErrorInvalidValue;
-        const int gx = (p.W + 127) / 128, gy = (p.H + XK_MT_BY - 1) / XK_MT_BY;
-        const int zc = mass_zchunk(p, gx, gy, 1024);
+        int gx, gy, zc;
+        mass_tma_shape(p, &gx, &gy, &zc);
         dim3 block(32, XK_MT_BY);
         dim3 grid(gx, gy, (p.D + zc - 1) / zc);
         // a lattice whose total mass is below 2^30 keeps every cell below 2^30
@@ -870,10 +927,21 @@ cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long 
         const bool fast = small && !(g && g[0] == '1');
         // programmatic dependent launch: this generation's CTAs may start
         // their set-up while the previous generation's last CTAs run
+        if (proj) {
+            if (zc > 256) return cudaErrorNotSupported;   // the 16-bit column sums would overflow
+            if (fast)
+                return xk_launch_pdl(xk_k_mass_tma<4, false, true>, grid, block, XK_MT_SMEM, s, tm, src, dst, total,
+                                     p, zc, proj);
+            return xk_launch_pdl(xk_k_mass_tma<3, true, true>, grid, block, XK_MT_SMEM, s, tm, src, dst, total, p,
+                                 zc, proj);
+        }
         if (fast)
-            return xk_launch_pdl(xk_k_mass_tma<4, false>, grid, block, XK_MT_SMEM, s, tm, src, dst, total, p, zc);
-        return xk_launch_pdl(xk_k_mass_tma<4, true>, grid, block, XK_MT_SMEM, s, tm, src, dst, total, p, zc);
+            return xk_launch_pdl(xk_k_mass_tma<4, false, false>, grid, block, XK_MT_SMEM, s, tm, src, dst, total, p,
+                                 zc, (uint32_t *)nullptr);
+        return xk_launch_pdl(xk_k_mass_tma<4, true, false>, grid, block, XK_MT_SMEM, s, tm, src, dst, total, p, zc,
+                             (uint32_t *)nullptr);
     }
+    if (proj) return cudaErrorNotSupported;   // the other forms write no projection
     const int cells_x = 32 * (vec ? 4 : 1);
     const int gx = (p.W + cells_x - 1) / cells_x, gy = (p.H + XK_MASS_BY - 1) / XK_MASS_BY;
     const int zc = mass_zchunk(p, gx, gy);
