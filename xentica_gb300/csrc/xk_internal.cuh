@@ -164,6 +164,11 @@ struct Life3Geo {
 };
 cudaError_t xk_life_step3d_vn(const uint32_t *src, uint32_t *dst, const Life3Geo &g,
                               const LifeTable &t, cudaStream_t s);
+// T (1..8) generations per launch on shared-memory tiles (life3d_tb.cu);
+// rows of up to 32 words (W <= 1024)
+int xk_life3d_tb_supported(const Life3Geo &g);
+cudaError_t xk_life_step3d_tb(const uint32_t *src, uint32_t *dst, const Life3Geo &g, const LifeTable &t,
+                              int T, cudaStream_t s);
 
 // one lattice (W <= 1024) on a thread-block cluster of C CTAs, R rows each,
 // in place on its bit-packed words (cluster.cu); config returns 0 when no
@@ -306,8 +311,14 @@ cudaError_t xk_seed_bernoulli(const XkSeedJob *jobs, int count, uint8_t *cells, 
 inline int64_t xk_mass_pitch(int64_t W) { return (W + 3) / 4 * 4; }
 // small: the lattice's total mass is below 2^30 (then every cell stays below
 // it for good), which allows the fast-only kernel
+// proj (only where xk_mass_fuses_projection()): also add the new state's
+// column colour sums into proj (W x H, zeroed by the caller first)
 cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long *total,
-                         const xk_desc &d, bool small, cudaStream_t s);
+                         const xk_desc &d, bool small, cudaStream_t s, uint32_t *proj = nullptr);
+bool xk_mass_fuses_projection(const xk_desc &d);
+// the W x H zoom-1 RendererPlain frame (axes (0, 1), no smoothing) from
+// column colour sums
+cudaError_t xk_mass_frame(const uint32_t *proj, uint8_t *frame, const xk_desc &d, cudaStream_t s);
 // total of n cells into *out (64-bit)
 cudaError_t xk_mass_sum(const uint32_t *src, int64_t n, unsigned long long *out, cudaStream_t s);
 // true when a mass-transfer CTA gave up waiting for a tensor copy since the
