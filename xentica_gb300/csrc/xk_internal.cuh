@@ -164,11 +164,6 @@ struct Life3Geo {
 };
 cudaError_t xk_life_step3d_vn(const uint32_t *src, uint32_t *dst, const Life3Geo &g,
                               const LifeTable &t, cudaStream_t s);
-// T (1..8) generations per launch on shared-memory tiles (life3d_tb.cu);
-// rows of up to 32 words (W <= 1024)
-int xk_life3d_tb_supported(const Life3Geo &g);
-cudaError_t xk_life_step3d_tb(const uint32_t *src, uint32_t *dst, const Life3Geo &g, const LifeTable &t,
-                              int T, cudaStream_t s);
 
 // one lattice (W <= 1024) on a thread-block cluster of C CTAs, R rows each,
 // in place on its bit-packed words (cluster.cu); config returns 0 when no
