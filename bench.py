@@ -273,8 +273,20 @@ def cpu_sample(widths, heights, rules, cells, offsets, seconds, threads):
 def run_reference_arm(args, dist):
     if dist.rank != 0:
         return
-    from xentica_gb300.batch import ensemble_workload
-    widths, heights, rules, dens, cells = ensemble_workload(min(args.instances, 64), args.seed)
+    # one lattice of every size class of the --instances workload (its first
+    # member of the class), cells exactly as the whole workload draws them
+    from xentica_gb300.batch import ensemble_seeds
+    all_w, all_h, all_r, all_d, all_s = ensemble_seeds(args.instances, args.seed)
+    seen, picks = set(), []
+    for i in range(args.instances):
+        key = (int(all_w[i]), int(all_h[i]))
+        if key not in seen:
+            seen.add(key)
+            picks.append(i)
+    widths, heights, rules = all_w[picks], all_h[picks], all_r[picks]
+    cells = np.concatenate([
+        (np.random.RandomState(int(all_s[i])).random_sample(int(all_w[i]) * int(all_h[i]))
+         < all_d[i]).astype(np.uint8) for i in picks])
     offsets = np.concatenate([[0], np.cumsum(widths.astype(np.int64) * heights)[:-1]])
     threads = os.cpu_count()
     per_step = max(2.0, args.cpu_seconds / max(1, args.steps))
@@ -289,7 +301,9 @@ def run_reference_arm(args, dist):
             "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * statistics.median(r["seconds"] for r in results),
             "ms_per_step_note": "one step is a bounded sample of the workload (one lattice "
-                                "of each size class for a fixed time), not the whole ensemble",
+                                "of each of its %d size classes for a fixed time, each class "
+                                "weighted once rather than by its share of the ensemble), not "
+                                "the whole ensemble" % len(picks),
             "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded)",
             "config": {"workload": "ensemble: LifelikeCA lattices, sides {64..1024}^2, "
