@@ -296,8 +296,8 @@ int xk_batch_step_noalloc(uint8_t *d_cells, int32_t count, const int32_t *width,
  * run together, one resident-kernel launch per shape class over its idle
  * members (up to 4 such rounds of a class in flight), each member running
  * about quantum x 2^18 cell-generations per round (at least `quantum`
- * generations).  Kernels of requests with less work (cells x generations)
- * run at a greater stream priority.  Results wait in the pinned arena until
+ * generations, at most 65536).  Kernels of requests with less work (cells x
+ * generations) run at a greater stream priority.  Results wait in the pinned arena until
  * xk_serve_result collects them.  A request computes exactly what it
  * computes alone. */
 enum { XK_SERVE_LIFE2D = 1, XK_SERVE_LIFE3D_VN = 2, XK_SERVE_MASS3D = 3 };

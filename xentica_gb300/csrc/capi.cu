@@ -139,6 +139,7 @@ struct xk_model {
     float mut_thresh = 0.f;
     uint32_t *cells32[2] = {nullptr, nullptr};  // mass transfer: reference layout, ping-pong
     uint32_t *proj = nullptr;                   // mass: colour sum of every (x, y) column
+    uint32_t *proj2 = nullptr;                  // mass: the second buffer of xk_step_frames
     int proj_valid = 0;
     unsigned long long *totals = nullptr;       // mass: total after each generation
     int64_t totals_cap = 0, totals_count = 0;
@@ -365,6 +366,7 @@ static void free_model(xk_model *m)
     if (m->fld) cudaFree(m->fld);
     if (m->vm_params) cudaFree(m->vm_params);
     if (m->proj) cudaFree(m->proj);
+    if (m->proj2) cudaFree(m->proj2);
     if (m->totals) cudaFree(m->totals);
     if (m->stage) cudaFree(m->stage);
     if (m->col) cudaFree(m->col);
@@ -765,9 +767,10 @@ static bool shift_jump_enabled()
 
 // frame (EvoLife, count == 1 only): the generation's zoom-1 frame written by
 // the step kernel itself; proj (mass transfer, count == 1 only): the step
-// kernel also adds the new state's column colour sums into it
+// kernel also adds the new state's column colour sums into it, and with
+// frame_prev writes the previous generation's frame from proj_prev
 static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *frame = nullptr,
-                        uint32_t *proj = nullptr)
+                        uint32_t *proj = nullptr, uint32_t *proj_prev = nullptr, uint8_t *frame_prev = nullptr)
 {
     if (m->layout == LAYOUT_VM) {
         for (int64_t g = 0; g < count; ++g)
@@ -779,7 +782,7 @@ static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *fram
     if (m->layout == LAYOUT_MASS) {
         for (int64_t g = 0; g < count; ++g) {
             XK_CUDA(xk_mass_step(m->cells32[m->cur], m->cells32[1 - m->cur], m->totals + first + g,
-                                 m->d, m->mass_small, m->stream, proj));
+                                 m->d, m->mass_small, m->stream, proj, proj_prev, frame_prev));
             m->cur = 1 - m->cur;
         }
         return XK_OK;
@@ -1023,6 +1026,57 @@ static int render_enqueue(xk_model *m, void *img, bool bytes, int32_t width, int
     return XK_OK;
 }
 
+// The mass-transfer frames of xk_step_frames at zoom 1: generation g adds its
+// column colour sums into one of two buffers (zero on entry) and writes
+// generation g - 1's frame from the other, zeroing it, so no launch comes
+// between two generations; the last frame comes from a small kernel after
+// the loop.  Host frames go through the device ring as in xk_step_frames.
+static int mass_frames_enqueue(xk_model *m, int64_t nsteps, uint8_t *frames, bool on_device, size_t fb)
+{
+    const size_t pbytes = (size_t)m->d.size[0] * m->d.size[1] * 4;
+    if (!m->proj2) XK_CUDA(cudaMalloc(&m->proj2, pbytes));
+    uint32_t *P[2] = {m->proj, m->proj2};
+    XK_CUDA(cudaMemsetAsync(P[0], 0, pbytes, m->stream));
+    XK_CUDA(cudaMemsetAsync(P[1], 0, pbytes, m->stream));
+    auto slot = [&](int64_t g) {
+        return on_device ? frames + (size_t)g * fb : m->ring + (size_t)(g % kFrameRing) * fb;
+    };
+    // frame g is about to be written: its ring slot's previous copy must be done
+    auto claim = [&](int64_t g) -> int {
+        if (!on_device && g >= kFrameRing)
+            XK_CUDA(cudaStreamWaitEvent(m->stream, m->copied[g % kFrameRing], 0));
+        return XK_OK;
+    };
+    // frame g is complete: copy it out
+    auto release = [&](int64_t g) -> int {
+        if (on_device) return XK_OK;
+        const int k = (int)(g % kFrameRing);
+        XK_CUDA(cudaEventRecord(m->rendered[k], m->stream));
+        XK_CUDA(cudaStreamWaitEvent(m->copy_stream, m->rendered[k], 0));
+        XK_CUDA(cudaMemcpyAsync(frames + (size_t)g * fb, slot(g), fb, cudaMemcpyDeviceToHost, m->copy_stream));
+        XK_CUDA(cudaEventRecord(m->copied[k], m->copy_stream));
+        return XK_OK;
+    };
+    for (int64_t g = 0; g < nsteps; ++g) {
+        if (g > 0) {
+            int rc = claim(g - 1);
+            if (rc != XK_OK) return rc;
+        }
+        int rc = step_enqueue(m, g, 1, nullptr, P[g & 1], P[(g + 1) & 1], g > 0 ? slot(g - 1) : nullptr);
+        if (rc != XK_OK) return rc;
+        if (g > 0 && (rc = release(g - 1)) != XK_OK) return rc;
+    }
+    int rc = claim(nsteps - 1);
+    if (rc != XK_OK) return rc;
+    uint32_t *last = P[(nsteps - 1) & 1];
+    XK_CUDA(xk_mass_frame(last, slot(nsteps - 1), m->d, m->stream));
+    if ((rc = release(nsteps - 1)) != XK_OK) return rc;
+    // m->proj holds the current state's column sums from here on
+    if (last != m->proj) std::swap(m->proj, m->proj2);
+    m->proj_valid = 1;
+    return XK_OK;
+}
+
 extern "C" int xk_step_frames(xk_model *m, int64_t nsteps, int32_t width, int32_t height,
                               int32_t zoom, int32_t dx, int32_t dy, uint8_t *frames,
                               int32_t frames_on_device)
@@ -1059,29 +1113,24 @@ extern "C" int xk_step_frames(xk_model *m, int64_t nsteps, int32_t width, int32_
                        m->d.ndim == 2 && m->d.proj_axis0 == 0 && m->d.proj_axis1 == 1 && zoom == 1 &&
                        dx == 0 && dy == 0 && width == m->d.size[0] && height == m->d.size[1];
     // mass transfer viewed whole at zoom 1 along z: the step kernel sums the
-    // column colours as it writes the cells, a small kernel turns them into
-    // the frame (no second pass over the state)
+    // column colours as it writes the cells (no second pass over the state)
     const bool mass_fused = m->layout == LAYOUT_MASS && m->d.proj_axis0 == 0 && m->d.proj_axis1 == 1 &&
                             m->d.render_smooth == 0 && zoom == 1 && dx == 0 && dy == 0 &&
                             width == m->d.size[0] && height == m->d.size[1] && xk_mass_fuses_projection(m->d);
     XK_CUDA(cudaEventRecord(m->ev0, m->stream));
-    for (int64_t g = 0; g < nsteps; ++g) {
+    if (mass_fused) {
+        rc = mass_frames_enqueue(m, nsteps, frames, frames_on_device != 0, fb);
+        if (rc != XK_OK) return rc;
+    }
+    for (int64_t g = 0; g < nsteps && !mass_fused; ++g) {
         const int k = (int)(g % kFrameRing);
         uint8_t *dst = frames_on_device ? frames + (size_t)g * fb : m->ring + (size_t)k * fb;
         if (!frames_on_device && g >= kFrameRing)
             XK_CUDA(cudaStreamWaitEvent(m->stream, m->copied[k], 0));
-        if (mass_fused) {
-            XK_CUDA(cudaMemsetAsync(m->proj, 0, (size_t)m->d.size[0] * m->d.size[1] * 4, m->stream));
-            rc = step_enqueue(m, g, 1, nullptr, m->proj);
-            if (rc != XK_OK) return rc;
-            XK_CUDA(xk_mass_frame(m->proj, dst, m->d, m->stream));
-            m->proj_valid = 1;                     // the sums of the current state
-        } else {
-            rc = step_enqueue(m, g, 1, fused ? dst : nullptr);
-            if (rc != XK_OK) return rc;
-            m->proj_valid = 0;
-        }
-        if (!fused && !mass_fused) {
+        rc = step_enqueue(m, g, 1, fused ? dst : nullptr);
+        if (rc != XK_OK) return rc;
+        m->proj_valid = 0;
+        if (!fused) {
             rc = render_enqueue(m, dst, true, width, height, zoom, dx, dy);
             if (rc != XK_OK) return rc;
         }

@@ -359,15 +359,16 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
     const int yu = y > 0 ? y - 1 : p.H - 1, yd = y < p.H - 1 ? y + 1 : 0;
     const int nxs[8] = {xl, xl, xl, x, x, xr, xr, xr};
     const int nys[8] = {yu, y, yd, yu, yd, yu, y, yd};
-    uint32_t nr[8], alive[8];
+    // a neighbour's energy (bits 0-8) and rule (bits 9-26) are both in the
+    // low 32-bit half of its cell: only that half is read
+    const uint32_t *src_lo = reinterpret_cast<const uint32_t *>(src);
+    uint32_t nr[8], nlo[8];
     uint32_t num_neighbors = 0;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-        const uint64_t v = __ldg(src + (int64_t)nys[k] * p.W + nxs[k]);
-        const uint32_t ne = (uint32_t)(v & 511u);
-        nr[k] = (uint32_t)((v >> 9) & 262143u);
-        alive[k] = (ne + nr[k]) != 0u;              // xmath.min(1, e + r)
-        num_neighbors += alive[k];
+        nlo[k] = __ldg(src_lo + 2 * ((int64_t)nys[k] * p.W + nxs[k]));
+        nr[k] = (nlo[k] >> 9) & 262143u;
+        num_neighbors += (nlo[k] & 0x7FFFFFFu) != 0u;   // xmath.min(1, e + r): e + r != 0
     }
     const int64_t i = (int64_t)y * p.W + x;
     const uint64_t c = src[i];
@@ -381,7 +382,7 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
     // the eight 8-lane words.
     uint32_t m[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) m[k] = (nr[k] >> 1) & 255u;
+    for (int k = 0; k < 8; ++k) m[k] = (nlo[k] >> 10) & 255u;
     const uint32_t s0 = m[0] ^ m[1] ^ m[2], c0 = (m[0] & m[1]) | (m[2] & (m[0] ^ m[1]));
     const uint32_t s1 = m[3] ^ m[4] ^ m[5], c1 = (m[3] & m[4]) | (m[5] & (m[3] ^ m[4]));
     const uint32_t s2 = m[6] ^ m[7], c2 = m[6] & m[7];
@@ -448,12 +449,22 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
         if (p.frame) {
             // the pixel of this cell as RendererPlain computes it at zoom 1
             // (render.cu): the colour as a float, / SMOOTH_FACTOR, truncated,
-            // its low byte
+            // its low byte.  Below 2^24 in magnitude int -> float -> int is
+            // exact, and so is a division by 1: with SMOOTH_FACTOR 1 (or none)
+            // such a pixel is the colour's low byte
 #pragma unroll
             for (int ch = 0; ch < 3; ++ch) {
-                float v = (float)rgb[ch];
-                if (p.frame_smooth > 0) v = __fdiv_rn(v, (float)p.frame_smooth);
-                p.frame[3 * i + ch] = (uint8_t)(int)v;
+                const int c = rgb[ch];
+                const bool small = (uint32_t)(c + (1 << 24)) < (1u << 25);
+                uint8_t px;
+                if (p.frame_smooth <= 1 && small) {
+                    px = (uint8_t)c;
+                } else {
+                    float v = (float)c;
+                    if (p.frame_smooth > 0) v = __fdiv_rn(v, (float)p.frame_smooth);
+                    px = (uint8_t)(int)v;
+                }
+                p.frame[3 * i + ch] = px;
             }
         }
     }

@@ -505,11 +505,19 @@ __device__ __forceinline__ uint4 xk_mt_q4(const uint4 m, bool &big)
 // at most 256 planes, which the host checks) and adds each sum with one
 // atomic, so the projection needs no second pass over the state.  Integer
 // sums: the order of the additions does not matter.
+//
+// With PROJ, the launch can also finish the previous generation's frame:
+// proj_prev holds that generation's column sums (its launch has completed
+// when this one passes its dependency wait), and the CTAs of the first run
+// of planes turn each of their columns into the frame_prev pixel, as
+// RendererPlain renders it at zoom 1, and zero the column for the generation
+// after this one (the sums alternate between two buffers).  So a frame every
+// generation adds no launch between two generations.
 template <int MINB, bool GENERAL, bool PROJ>
 __global__ void __launch_bounds__(32 * XK_MT_BY, MINB)
 xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict__ src,
               uint32_t *__restrict__ dst, unsigned long long *__restrict__ total, MassParams p, int zc,
-              uint32_t *__restrict__ proj)
+              uint32_t *__restrict__ proj, uint32_t *__restrict__ proj_prev, uint8_t *__restrict__ frame_prev)
 {
     extern __shared__ __align__(128) uint8_t xk_mt_raw[];
     // tensor copies land on 128-byte boundaries: round the window's start up
@@ -546,6 +554,21 @@ xk_k_mass_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict
     if (tid == 0)
         for (int k = 0; k < XK_MT_STAGES && k < nplanes; ++k)
             xk_mt_issue(&tm, stage0 + k * XK_MT_STAGE_STRIDE, bar0 + 8 * k, x_lo, y_lo, z0 - 1 + k);
+    if (PROJ && frame_prev && blockIdx.z == 0 && in) {
+        // the previous generation's frame from its column sums (this
+        // thread's four columns), and those sums zeroed for the next one
+        const int64_t c0 = (int64_t)y * p.W + x0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            if (x0 + i < p.W) {
+                const uint8_t v = (uint8_t)(int)__fdiv_rn((float)proj_prev[c0 + i], (float)p.D);
+                uint8_t *px = frame_prev + 3 * (c0 + i);
+                px[0] = v;
+                px[1] = v;
+                px[2] = v;
+                proj_prev[c0 + i] = 0u;
+            }
+    }
     __syncthreads();
 
     // own cells of a stage (row ty + 1, columns 4 + 4 lane ..); the halo
@@ -897,7 +920,8 @@ cudaError_t xk_mass_frame(const uint32_t *proj, uint8_t *frame, const xk_desc &d
 }
 
 cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long *total,
-                         const xk_desc &d, bool small, cudaStream_t s, uint32_t *proj)
+                         const xk_desc &d, bool small, cudaStream_t s, uint32_t *proj, uint32_t *proj_prev,
+                         uint8_t *frame_prev)
 {
     const MassParams p = mass_params(d);
     const bool vec = p.W % 4 == 0;
@@ -931,15 +955,17 @@ cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long 
             if (zc > 256) return cudaErrorNotSupported;   // the 16-bit column sums would overflow
             if (fast)
                 return xk_launch_pdl(xk_k_mass_tma<4, false, true>, grid, block, XK_MT_SMEM, s, tm, src, dst, total,
-                                     p, zc, proj);
+                                     p, zc, proj, proj_prev, frame_prev);
             return xk_launch_pdl(xk_k_mass_tma<3, true, true>, grid, block, XK_MT_SMEM, s, tm, src, dst, total, p,
-                                 zc, proj);
+                                 zc, proj, proj_prev, frame_prev);
         }
+        uint32_t *const none = nullptr;
+        uint8_t *const no_frame = nullptr;
         if (fast)
             return xk_launch_pdl(xk_k_mass_tma<4, false, false>, grid, block, XK_MT_SMEM, s, tm, src, dst, total, p,
-                                 zc, (uint32_t *)nullptr);
+                                 zc, none, none, no_frame);
         return xk_launch_pdl(xk_k_mass_tma<4, true, false>, grid, block, XK_MT_SMEM, s, tm, src, dst, total, p, zc,
-                             (uint32_t *)nullptr);
+                             none, none, no_frame);
     }
     if (proj) return cudaErrorNotSupported;   // the other forms write no projection
     const int cells_x = 32 * (vec ? 4 : 1);

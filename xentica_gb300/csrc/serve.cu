@@ -293,12 +293,14 @@ static int request_priority(const xk_server *s, const Req *q)
 
 // generations of the next round of a resident member: the round's work is
 // about round_work cell-generations (so small lattices run many generations
-// per round), at least `quantum`, at most what is left
+// per round), at least `quantum`, at most 65536 generations (a round of the
+// tiniest lattice stays a few milliseconds, so cancellation and the other
+// members of its slot are not held up) and at most what is left
 static int64_t resident_chunk(const xk_server *s, const Req *q)
 {
     const int64_t left = q->r.generations - q->done;
     int64_t chunk = std::max<int64_t>(s->quantum, s->round_work / std::max<int64_t>(1, q->n));
-    chunk = std::min<int64_t>(chunk, 1 << 30);
+    chunk = std::min<int64_t>(chunk, std::max<int64_t>(s->quantum, 1 << 16));
     return std::min(chunk, left);
 }
 

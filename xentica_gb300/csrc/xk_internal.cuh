@@ -307,9 +307,12 @@ inline int64_t xk_mass_pitch(int64_t W) { return (W + 3) / 4 * 4; }
 // small: the lattice's total mass is below 2^30 (then every cell stays below
 // it for good), which allows the fast-only kernel
 // proj (only where xk_mass_fuses_projection()): also add the new state's
-// column colour sums into proj (W x H, zeroed by the caller first)
+// column colour sums into proj (W x H, zero on entry); with frame_prev, also
+// write the zoom-1 frame of the previous generation from its sums proj_prev
+// and zero proj_prev
 cudaError_t xk_mass_step(const uint32_t *src, uint32_t *dst, unsigned long long *total,
-                         const xk_desc &d, bool small, cudaStream_t s, uint32_t *proj = nullptr);
+                         const xk_desc &d, bool small, cudaStream_t s, uint32_t *proj = nullptr,
+                         uint32_t *proj_prev = nullptr, uint8_t *frame_prev = nullptr);
 bool xk_mass_fuses_projection(const xk_desc &d);
 // the W x H zoom-1 RendererPlain frame (axes (0, 1), no smoothing) from
 // column colour sums
