@@ -764,13 +764,14 @@ def mass_line(args, dist):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": committed_traffic("mass_tma") if side == 256 else None,
-                         "kernel": "xk_k_mass_tma + xk_k_mass_project (column sums, writes "
-                                   "the frame) per generation",
+                         "kernel": "xk_k_mass_tma per generation (it also sums the column "
+                                   "colours and writes the previous generation's frame)",
                          "algorithmic_bytes_per_generation": bytes_per_update * n,
-                         "note": "B_alg = 12 B per cell-update (uint32 read + write, the "
-                                 "projection's re-read of the state); traffic: DRAM bytes of "
-                                 "one mass-transfer launch (one generation)"},
-            "gpu_launches": 2 * gens * args.steps, "clocks": clk}
+                         "note": "B_alg = 12 B per cell-update (uint32 read + write, and the "
+                                 "projection's read of the state, which the step kernel now "
+                                 "does on the cells it writes); traffic: DRAM bytes of one "
+                                 "mass-transfer launch (one generation)"},
+            "gpu_launches": (gens + 1) * args.steps, "clocks": clk}
     if dist.rank == 0:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O
