@@ -106,9 +106,13 @@ int xk_life_set_rule(xk_model *m, uint32_t rule0, uint32_t rule1, const int32_t 
 int xk_set_color_mode(xk_model *m, int32_t history_free);
 
 /* Replaces CellularAutomaton.step (base.py:703-728): nsteps generations of
- * emit + absorb + colour, fused.  XK_ERR_TIMEOUT: a mass-transfer kernel gave
- * up waiting for one of its tensor copies (a bounded wait; the state is then
- * unspecified). */
+ * emit + absorb + colour, fused.  Returns once the work is queued on the
+ * model's stream, as the reference's step() returns after its asynchronous
+ * launches (mass-transfer steps wait, to read their kernels' give-up flag);
+ * xk_download, xk_sync and xk_last_step_ms wait for it, and errors of the
+ * queued work are reported there.  XK_ERR_TIMEOUT: a mass-transfer kernel
+ * gave up waiting for one of its tensor copies (a bounded wait; the state is
+ * then unspecified). */
 int xk_step(xk_model *m, int64_t nsteps);
 
 /* Replaces CellularAutomaton.render (base.py:730-753): width*height*3 int32. */
@@ -184,7 +188,7 @@ int xk_vm_set_params(xk_model *m, const uint64_t *values, int32_t count);
 int xk_sync(xk_model *m);
 
 /* Device time of the last xk_step / batch step, in milliseconds (CUDA events
- * on the launching stream). */
+ * on the launching stream); after an xk_step it waits for that step. */
 double xk_last_step_ms(void);
 
 /* ------------------------------------------------------------------------ */

@@ -35,15 +35,41 @@ int xk_cuda_status(cudaError_t err, const char *what)
     return err == cudaErrorMemoryAllocation ? XK_ERR_OOM : XK_ERR_CUDA;
 }
 
+// the model whose last xk_step returned without waiting for the device: its
+// step's time is read from its events when asked for
+static xk_model *g_pending_model = nullptr;
+static float pending_step_ms(xk_model *m);
+
 void xk_set_last_step_ms(double ms)
 {
     std::lock_guard<std::mutex> lk(g_ms_mu);
     g_last_ms = ms;
+    g_pending_model = nullptr;
+}
+
+static void set_pending_step(xk_model *m)
+{
+    std::lock_guard<std::mutex> lk(g_ms_mu);
+    g_pending_model = m;
+}
+
+// a model going away: its pending step time is resolved first
+static void settle_pending_step(xk_model *m)
+{
+    std::lock_guard<std::mutex> lk(g_ms_mu);
+    if (g_pending_model == m) {
+        g_last_ms = pending_step_ms(m);
+        g_pending_model = nullptr;
+    }
 }
 
 extern "C" double xk_last_step_ms(void)
 {
     std::lock_guard<std::mutex> lk(g_ms_mu);
+    if (g_pending_model) {
+        g_last_ms = pending_step_ms(g_pending_model);
+        g_pending_model = nullptr;
+    }
     return g_last_ms;
 }
 
@@ -533,6 +559,7 @@ fail:
 
 extern "C" void xk_model_destroy(xk_model *m)
 {
+    if (m) settle_pending_step(m);
     if (m && m->stream) cudaStreamSynchronize(m->stream);
     free_model(m);
 }
@@ -880,6 +907,17 @@ static int step_finish(xk_model *m, int64_t nsteps)
     return XK_OK;
 }
 
+// device time between a model's step events (waits for the step)
+static float pending_step_ms(xk_model *m)
+{
+    float ms = 0.f;
+    if (cudaEventSynchronize(m->ev1) != cudaSuccess || cudaEventElapsedTime(&ms, m->ev0, m->ev1) != cudaSuccess) {
+        cudaGetLastError();
+        return 0.f;
+    }
+    return ms;
+}
+
 extern "C" int xk_step(xk_model *m, int64_t nsteps)
 {
     XK_REQUIRE(m, XK_ERR_ARG, "xk_step: null model");
@@ -892,10 +930,17 @@ extern "C" int xk_step(xk_model *m, int64_t nsteps)
     rc = step_enqueue(m, 0, nsteps);
     if (rc != XK_OK) return rc;
     XK_CUDA(cudaEventRecord(m->ev1, m->stream));
-    XK_CUDA(cudaEventSynchronize(m->ev1));
-    float ms = 0.f;
-    XK_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
-    xk_set_last_step_ms(ms);
+    if (m->layout == LAYOUT_MASS) {
+        // the mass kernels' give-up flag is read after the step
+        XK_CUDA(cudaEventSynchronize(m->ev1));
+        float ms = 0.f;
+        XK_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+        xk_set_last_step_ms(ms);
+    } else {
+        // returns once the work is queued, as the reference's step() does
+        // (its launches are asynchronous); xk_last_step_ms waits for it
+        set_pending_step(m);
+    }
     return step_finish(m, nsteps);
 }
 
