@@ -2,7 +2,7 @@
 
 ``XK_CLUSTER=n`` makes a model's multi-generation steps run on a cluster of
 (up to) n CTAs, whatever the tuner would pick, and ``XK_CLUSTER_BAND=b`` sets
-the rows each lane group walks (b = 1 .. 4, and 5 for bands that do not
+the rows each lane group walks (b = 1 .. 4 or 8, and 5 for bands that do not
 divide a CTA's rows); every lattice is compared cell by cell with the oracle,
 torus and static border (value 1), widths around the word size and up to
 1024, heights from a few rows to more than one CTA holds.
@@ -67,17 +67,18 @@ def test_neighbour_sync_vs_oracle(cls, forced, band, monkeypatch):
         assert np.array_equal(got, want), (cls.__name__, size, forced, band)
 
 
+@pytest.mark.parametrize("band", [4, 8])
 @pytest.mark.parametrize("size,forced", [((512, 512), 16), ((512, 512), 8), ((1024, 64), 16),
                                          ((100, 256), 8), ((64, 512), 4), ((1000, 48), 2)])
 @pytest.mark.parametrize("cls", [GameOfLife, GameOfLifeStatic])
-def test_split_sync_vs_oracle(cls, size, forced, monkeypatch):
+def test_split_sync_vs_oracle(cls, size, forced, band, monkeypatch):
     """The split form (the cluster barrier's arrive before the bands' inner
-    rows, its wait after them; bands of exactly 4 rows in every CTA) against
-    the oracle, and over 3000 generations on the C1 lattice."""
-    got, want = _run(cls, size, forced, 41, monkeypatch, 3 * forced, 4, "split")
-    assert np.array_equal(got, want), (cls.__name__, size, forced)
+    rows, its wait after them; bands of exactly 4 or 8 rows in every CTA)
+    against the oracle, and over 3000 generations on the 512 x 512 torus."""
+    got, want = _run(cls, size, forced, 41, monkeypatch, 3 * forced + band, band, "split")
+    assert np.array_equal(got, want), (cls.__name__, size, forced, band)
     if size == (512, 512) and cls is GameOfLife:
-        got, want = _run(cls, size, forced, 3000, monkeypatch, 11, 4, "split")
+        got, want = _run(cls, size, forced, 3000, monkeypatch, 11 + band, band, "split")
         assert np.array_equal(got, want)
 
 

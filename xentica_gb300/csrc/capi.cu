@@ -348,9 +348,9 @@ static int tune_cluster(xk_model *m)
     }
     // clusters: sizes, band lengths and the synchronisation forms
     static const int cand[] = {16, 8, 4, 2};
-    static const int bands[] = {1, 2, 4};
-    for (int k = 0; k < 36; ++k) {
-        const int want = cand[k / 9], band = bands[(k / 3) % 3], sync = k % 3;
+    static const int bands[] = {1, 2, 4, 8};
+    for (int k = 0; k < 48; ++k) {
+        const int want = cand[k / 12], band = bands[(k / 3) % 4], sync = k % 3;
         int C = 0, R = 0, th = 0;
         if (!xk_life_cluster_config(m->lg, want, band, &C, &R, &th)) continue;
         if (!xk_life_cluster_has_sync(m->lg, C, R, th, sync)) continue;

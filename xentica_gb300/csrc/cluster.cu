@@ -139,7 +139,7 @@ __device__ __forceinline__ uint32_t xk_cl_mapa(uint32_t addr, uint32_t rank)
 
 // TORUS: wrap, else static border; FULLW: torus rows of whole words (each
 // neighbour vector one funnel shift); LB: every band of the widest CTA has
-// exactly LB rows (1, 2 or 4; the row loop is unrolled), 0 for any length;
+// exactly LB rows (1, 2, 4 or 8; the row loop is unrolled), 0 for any length;
 // RF: the rule form (XK_RULE_TABLE: `t`; XK_RULE_CONWAY: B3/S23 compiled in);
 // SYNC: the synchronisation form (XK_SYNC_*)
 template <bool TORUS, bool FULLW, int LB, int RF, int SYNC>
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(1024)
 xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int generations, int R)
 {
     constexpr bool P2P = SYNC == XK_SYNC_NEIGHBOUR, SPLIT = SYNC == XK_SYNC_SPLIT;
-    static_assert(!SPLIT || LB == 4, "the split form runs bands of 4 rows");
+    static_assert(!SPLIT || LB == 4 || LB == 8, "the split form runs bands of 4 or 8 rows");
     const auto &t = RuleForm<RF>::make(t9);
     extern __shared__ uint32_t sm[];
     cg::cluster_group cluster = cg::this_cluster();
@@ -276,41 +276,37 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int gen
         const bool remote = gen + 1 < generations || !P2P;
         const uint32_t wu = first_band ? slot[(par * 2 + 0) * wpr + jc] : hp[((bc - 1) * 2 + 1) * wpr + jc];
         const uint32_t wl = last_band ? slot[(par * 2 + 1) * wpr + jc] : hp[((bc + 1) * 2 + 0) * wpr + jc];
-        if (SPLIT) {
-            // every band has 4 rows: the first and last row, then the inner
-            // two after the arrival
-            const uint32_t w0 = wp[0], w1 = wp[32], w2 = wp[64], w3 = wp[96];
-            uint32_t s_u, c_u, s0, c0, s1, c1, s2, c2, s3, c3, s_d, c_d;
+        if constexpr (SPLIT) {
+            // every band has LB rows: the first and last row, then the inner
+            // ones after the arrival (the old rows' column sums in registers)
+            uint32_t w[LB], s[LB], cy[LB];
+            uint32_t s_u, c_u, s_d, c_d;
+#pragma unroll
+            for (int i = 0; i < LB; ++i) w[i] = wp[32 * i];
             colsum(wu, s_u, c_u);
             if (top_off) s_u = c_u = g.bfill;
-            colsum(w0, s0, c0);
-            colsum(w1, s1, c1);
-            colsum(w2, s2, c2);
-            colsum(w3, s3, c3);
+#pragma unroll
+            for (int i = 0; i < LB; ++i) colsum(w[i], s[i], cy[i]);
             colsum(wl, s_d, c_d);
             if (bot_off) s_d = c_d = g.bfill;
-            uint32_t o0 = xk_life_word9(s_u, c_u, s0, c0, s1, c1, w0, t);
-            uint32_t o3 = xk_life_word9(s2, c2, s3, c3, s_d, c_d, w3, t);
+            uint32_t o0 = xk_life_word9(s_u, c_u, s[0], cy[0], s[1], cy[1], w[0], t);
+            uint32_t oL = xk_life_word9(s[LB - 2], cy[LB - 2], s[LB - 1], cy[LB - 1], s_d, c_d, w[LB - 1], t);
             if (!FULLW) {
                 o0 &= outmask;
-                o3 &= outmask;
+                oL &= outmask;
             }
             if (active) {
                 wp[0] = o0;
-                wp[96] = o3;
+                wp[32 * (LB - 1)] = oL;
                 publish(par ^ 1, 0, o0, true);
-                publish(par ^ 1, 3, o3, true);
+                publish(par ^ 1, LB - 1, oL, true);
             }
             xk_cl_barrier_arrive();
-            uint32_t o1 = xk_life_word9(s0, c0, s1, c1, s2, c2, w1, t);
-            uint32_t o2 = xk_life_word9(s1, c1, s2, c2, s3, c3, w2, t);
-            if (!FULLW) {
-                o1 &= outmask;
-                o2 &= outmask;
-            }
-            if (active) {
-                wp[32] = o1;
-                wp[64] = o2;
+#pragma unroll
+            for (int i = 1; i < LB - 1; ++i) {
+                uint32_t o = xk_life_word9(s[i - 1], cy[i - 1], s[i], cy[i], s[i + 1], cy[i + 1], w[i], t);
+                if (!FULLW) o &= outmask;
+                if (active) wp[32 * i] = o;
             }
             continue;
         }
@@ -357,7 +353,7 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int gen
 typedef void (*ClusterKernel)(uint32_t *, LifeGeo, LifeTable9, int, int);
 
 // the neighbour form has instantiations for bands of 1, 2 and 4 rows, the
-// split form for bands of 4
+// split form for bands of 4 and 8
 template <bool TORUS, bool FULLW, int RF>
 static ClusterKernel cluster_kernel_l(int L, int sync)
 {
@@ -369,11 +365,16 @@ static ClusterKernel cluster_kernel_l(int L, int sync)
         default: return nullptr;
         }
     }
-    if (sync == XK_SYNC_SPLIT) return L == 4 ? xk_k_life_cluster<TORUS, FULLW, 4, RF, XK_SYNC_SPLIT> : nullptr;
+    if (sync == XK_SYNC_SPLIT) {
+        if (L == 4) return xk_k_life_cluster<TORUS, FULLW, 4, RF, XK_SYNC_SPLIT>;
+        if (L == 8) return xk_k_life_cluster<TORUS, FULLW, 8, RF, XK_SYNC_SPLIT>;
+        return nullptr;
+    }
     switch (L) {
     case 1: return xk_k_life_cluster<TORUS, FULLW, 1, RF, XK_SYNC_BARRIER>;
     case 2: return xk_k_life_cluster<TORUS, FULLW, 2, RF, XK_SYNC_BARRIER>;
     case 4: return xk_k_life_cluster<TORUS, FULLW, 4, RF, XK_SYNC_BARRIER>;
+    case 8: return xk_k_life_cluster<TORUS, FULLW, 8, RF, XK_SYNC_BARRIER>;
     default: return xk_k_life_cluster<TORUS, FULLW, 0, RF, XK_SYNC_BARRIER>;
     }
 }
@@ -488,9 +489,9 @@ int xk_life_cluster_has_sync(const LifeGeo &g, int C, int R, int threads, int sy
 {
     if (sync == XK_SYNC_BARRIER) return 1;
     if (sync == XK_SYNC_SPLIT) {
-        // every CTA has R rows, cut into bands of exactly 4
+        // every CTA has R rows, cut into bands of exactly 4 or 8
         const ResidentPlan p = xk_resident_plan(g.wpr, R, threads);
-        if ((int64_t)C * R != g.H || p.L != 4 || p.nb * 4 != R) return 0;
+        if ((int64_t)C * R != g.H || (p.L != 4 && p.L != 8) || p.nb * p.L != R) return 0;
     }
     return cluster_kernel(g, R, threads, XK_RULE_TABLE, sync) != nullptr;
 }
