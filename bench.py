@@ -907,7 +907,9 @@ def life512_line(args, dist):
         if kind == "cluster":
             plan_desc.update({"ctas": plan[1], "rows_per_band": plan[2],
                               "sync": {0: "cluster barrier", 1: "neighbour mbarriers",
-                                       2: "split cluster barrier"}.get(plan[3], plan[3])})
+                                       2: "split cluster barrier",
+                                       3: "asynchronous remote stores counted on neighbour "
+                                          "mbarriers"}.get(plan[3], plan[3])})
         elif kind == "temporal":
             plan_desc["generations_per_launch"] = plan[3]
         plan_desc["rule_form"] = "B3/S23 compiled in" if nat.load().xk_model_rule_form(

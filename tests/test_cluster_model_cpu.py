@@ -377,3 +377,136 @@ def test_neighbour_form_mbarriers_fit_the_allocation():
         total = ((data + 1) & ~1) + 4
         mbar_word = (data + 1) & ~1
         assert mbar_word % 2 == 0 and mbar_word >= data and mbar_word + 4 <= total
+
+
+# ---------------------------------------------------------------------------
+# The async form: the neighbour form's order of waits and sends, but each row
+# word travels as an asynchronous remote store that lands some time later and
+# then counts 4 bytes (here: one word) of the transaction count of the
+# receiver's mbarrier of that parity.  The receiving CTA's thread 0 (a lane of
+# its first band) arms that mbarrier once per phase, at the top of the
+# generation that reads it, with one arrival expecting the 2 wpr words.  The
+# model delivers the stores in flight in a random order, interleaved with the
+# bands' steps, and checks that
+#
+# * a phase completes only with its arming and all 2 wpr words of its own
+#   generation (a word that lands before the arming waits for it; none of the
+#   next generation's words is counted early);
+# * a wait passes only on the phase of its own generation;
+# * a store never lands on a slot word its reader has not read yet, and every
+#   slot word a band reads was written for the generation reading it;
+# * nothing is left in flight when every CTA has finished.
+
+class TxBar:
+    def __init__(self, words):
+        self.words, self.pending, self.tx, self.parity, self.done, self.tags = words, 1, 0, 0, 0, []
+
+    def _check(self):
+        if self.pending == 0 and self.tx == 0:
+            assert len(set(self.tags)) == 1, ("several generations in one phase", self.tags)
+            self.done += 1
+            self.parity ^= 1
+            self.pending, self.tags = 1, []
+
+    def arm(self, gen):
+        assert self.pending == 1, "armed twice in one phase"
+        self.pending = 0
+        self.tx += self.words
+        self.tags.append(gen)
+        self._check()
+
+    def complete(self, gen):
+        self.tx -= 1
+        self.tags.append(gen)
+        self._check()
+
+    def passes(self, parity):
+        return self.parity != parity
+
+
+def run_async(C, nb, wpr, gens, seed):
+    rng = np.random.RandomState(seed)
+    bars = [[TxBar(2 * wpr), TxBar(2 * wpr)] for _ in range(C)]
+    slot = {}              # (cta, parity, side, word) -> (generation tag, read since written)
+    flight = []            # stores issued, not yet landed
+    agents = []
+    for c in range(C):
+        kinds = [("first", "last")] if nb == 1 else [("first",), ("last",)]
+        for roles in kinds:
+            agents.append(dict(c=c, roles=roles, gen=0, step="arm" if "first" in roles else "top"))
+    up = [c - 1 if c > 0 else C - 1 for c in range(C)]
+    dn = [c + 1 if c + 1 < C else 0 for c in range(C)]
+
+    def send(c, role, g):
+        tgt, side = (up[c], 1) if role == "first" else (dn[c], 0)
+        for j in range(wpr):
+            flight.append((tgt, g & 1, side, j, g))
+
+    def land(k):
+        tgt, par, side, j, g = flight.pop(k)
+        key = (tgt, par, side, j)
+        if key in slot:
+            tag, read = slot[key]
+            assert read, ("store landed on a slot word not yet read", key, tag, g)
+        slot[key] = (g, False)
+        bars[tgt][par].complete(g)
+
+    for c in range(C):
+        for role in ("first", "last"):
+            send(c, role, 0)
+    for _ in range(200000):
+        live = [a for a in agents if a["gen"] < gens]
+        if not live:
+            assert not flight, "stores still in flight at the end"
+            return True
+        ready = []
+        for a in live:
+            g, c = a["gen"], a["c"]
+            if a["step"] == "top":
+                if all(b["gen"] == g and b["step"] == "top" for b in agents if b["c"] == c):
+                    ready.append(a)
+            elif a["step"] == "wait":
+                if bars[c][g & 1].passes((g >> 1) & 1):
+                    ready.append(a)
+            else:
+                ready.append(a)
+        choices = len(ready) + len(flight)
+        assert choices, "deadlock"
+        k = rng.randint(choices)
+        if k >= len(ready):
+            land(k - len(ready))
+            continue
+        a = ready[k]
+        g, c = a["gen"], a["c"]
+        if a["step"] == "arm":
+            bars[c][g & 1].arm(g)
+            a["step"] = "top"
+        elif a["step"] == "top":
+            for b in agents:
+                if b["c"] == c:
+                    b["step"] = "wait"
+        elif a["step"] == "wait":
+            assert bars[c][g & 1].done == (g >> 1) + 1, ("wait passed on another phase", g)
+            a["step"] = "read"
+        elif a["step"] == "read":
+            for role in a["roles"]:
+                for j in range(wpr):
+                    key = (c, g & 1, 0 if role == "first" else 1, j)
+                    tag, _ = slot[key]
+                    assert tag == g, ("slot of another generation", key, tag, g)
+                    slot[key] = (tag, True)
+            a["step"] = "send"
+        else:
+            if g + 1 < gens:
+                for role in a["roles"]:
+                    send(c, role, g + 1)
+            a["gen"] = g + 1
+            a["step"] = "arm" if "first" in a["roles"] else "top"
+    raise AssertionError("no progress")
+
+
+@pytest.mark.parametrize("C", [2, 3, 4, 16])
+@pytest.mark.parametrize("nb", [1, 2, 5])
+def test_async_form_protocol(C, nb):
+    for seed in range(12):
+        assert run_async(C, nb, wpr=3, gens=9, seed=seed * 37 + C * 5 + nb)

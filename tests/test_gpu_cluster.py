@@ -82,6 +82,31 @@ def test_split_sync_vs_oracle(cls, size, forced, band, monkeypatch):
         assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("band", [1, 2, 4, 8])
+@pytest.mark.parametrize("forced", [2, 3, 4, 8, 16])
+@pytest.mark.parametrize("cls", [GameOfLife, GameOfLifeStatic])
+def test_async_sync_vs_oracle(cls, forced, band, monkeypatch):
+    """The async form (rows sent by asynchronous remote stores, each counted
+    in bytes on the receiving CTA's mbarrier, which that CTA arms once per
+    phase) for every cluster size and band length, against the oracle; bands
+    of 4 or 8 rows only where every CTA's bands have that length, the cluster
+    barrier elsewhere; odd generation counts leave the last generation's
+    rows unsent."""
+    for k, size in enumerate(SIZES):
+        got, want = _run(cls, size, forced, 37 + k % 2, monkeypatch, 10 * forced + k + band, band,
+                         "async")
+        assert np.array_equal(got, want), (cls.__name__, size, forced, band)
+
+
+@pytest.mark.parametrize("band", [1, 2, 4, 8])
+def test_async_sync_long_run(band, monkeypatch):
+    """3000 generations in one launch of the async form on 16 CTAs (a store
+    landing in the wrong phase, or overwriting a slot before it was read,
+    would show here)."""
+    got, want = _run(GameOfLife, (512, 512), 16, 3000, monkeypatch, 21 + band, band, "async")
+    assert np.array_equal(got, want)
+
+
 @pytest.mark.parametrize("band", [1, 2, 4])
 def test_neighbour_sync_long_run(band, monkeypatch):
     """3000 generations in one launch of the neighbour form on 16 CTAs (a

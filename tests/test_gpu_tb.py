@@ -87,7 +87,8 @@ def test_serving_large_requests_at_default_depth():
 
 PLANS = {(512, 512): [[1, 0, 0, 0], [2, 16, 2, 0], [2, 4, 1, 0], [2, 8, 4, 0], [2, 16, 2, 1],
                       [2, 3, 4, 1], [2, 16, 4, 1], [2, 8, 1, 1], [2, 16, 4, 2], [2, 8, 4, 2],
-                      [2, 16, 8, 0], [2, 16, 8, 2], [2, 8, 8, 2], [3, 0, 0, 2], [3, 0, 0, 8]],
+                      [2, 16, 8, 0], [2, 16, 8, 2], [2, 8, 8, 2], [2, 16, 1, 3], [2, 4, 2, 3],
+                      [2, 16, 4, 3], [2, 8, 8, 3], [3, 0, 0, 2], [3, 0, 0, 8]],
          (2049, 131): [[0, 0, 0, 0], [3, 0, 0, 4], [3, 0, 0, 7]]}
 
 
@@ -122,8 +123,8 @@ def test_every_plan_kind_matches_oracle(shape, rule):
         O.life_run(topo, fld, np.zeros(3 * n, np.int32), 29, born=code & 511, sustain=code >> 9)
         assert np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n]), "plan %s" % plan
     bad = {(512, 512): [[0, 0, 0, 0], [3, 0, 0, 9], [2, 17, 1, 0], [5, 0, 0, 0], [2, 16, 2, 2],
-                        [2, 16, 3, 1], [2, 3, 1, 1], [2, 3, 4, 2], [2, 16, 4, 3], [2, 16, 8, 1],
-                        [2, 3, 8, 2]],
+                        [2, 16, 3, 1], [2, 3, 1, 1], [2, 3, 4, 2], [2, 16, 4, 4], [2, 16, 8, 1],
+                        [2, 3, 8, 2], [2, 3, 4, 3], [2, 16, 3, 3]],
            (2049, 131): [[1, 0, 0, 0], [2, 4, 1, 0], [3, 0, 0, 1]]}[shape]
     model = _model(shape, "torus")
     model.gpu._ensure()

@@ -281,7 +281,8 @@ static int tune_cluster(xk_model *m)
             const char *senv = getenv("XK_CLUSTER_SYNC");
             const int sync = !senv ? XK_SYNC_BARRIER
                              : strcmp(senv, "p2p") == 0 ? XK_SYNC_NEIGHBOUR
-                             : strcmp(senv, "split") == 0 ? XK_SYNC_SPLIT : XK_SYNC_BARRIER;
+                             : strcmp(senv, "split") == 0 ? XK_SYNC_SPLIT
+                             : strcmp(senv, "async") == 0 ? XK_SYNC_ASYNC : XK_SYNC_BARRIER;
             m->cl_sync = xk_life_cluster_has_sync(m->lg, C, R, th, sync) ? sync : XK_SYNC_BARRIER;
         }
         return XK_OK;
@@ -349,8 +350,8 @@ static int tune_cluster(xk_model *m)
     // clusters: sizes, band lengths and the synchronisation forms
     static const int cand[] = {16, 8, 4, 2};
     static const int bands[] = {1, 2, 4, 8};
-    for (int k = 0; k < 48; ++k) {
-        const int want = cand[k / 12], band = bands[(k / 3) % 4], sync = k % 3;
+    for (int k = 0; k < 64; ++k) {
+        const int want = cand[k / 16], band = bands[(k / 4) % 4], sync = k % 4;
         int C = 0, R = 0, th = 0;
         if (!xk_life_cluster_config(m->lg, want, band, &C, &R, &th)) continue;
         if (!xk_life_cluster_has_sync(m->lg, C, R, th, sync)) continue;
@@ -1006,10 +1007,11 @@ extern "C" int xk_model_set_plan(xk_model *m, const int32_t plan[4])
                        xk_life_cluster_config(m->lg, plan[1], plan[2], &C, &R, &th),
                    XK_ERR_ARG, "xk_model_set_plan: no cluster of %d CTAs with bands of %d rows",
                    plan[1], plan[2]);
-        XK_REQUIRE(plan[3] >= XK_SYNC_BARRIER && plan[3] <= XK_SYNC_SPLIT &&
+        XK_REQUIRE(plan[3] >= XK_SYNC_BARRIER && plan[3] <= XK_SYNC_ASYNC &&
                        xk_life_cluster_has_sync(m->lg, C, R, th, plan[3]),
                    XK_ERR_ARG, "xk_model_set_plan: cluster synchronisation form %d does not apply "
-                   "(1: bands of 1, 2 or 4 rows; 2: every CTA's bands 4 rows)", plan[3]);
+                   "(1: bands of 1, 2 or 4 rows; 2: every CTA's bands 4 or 8 rows; 3: bands of "
+                   "1 or 2 rows, or every CTA's bands 4 or 8 rows)", plan[3]);
         break;
     case XK_PLAN_TEMPORAL:
         XK_REQUIRE(plan[3] >= 2 && plan[3] <= 8 && xk_life_tb_supported(m->lg), XK_ERR_ARG,

@@ -40,7 +40,16 @@
 //   __syncthreads_or), its neighbours then give up in turn, and the step
 //   reports XK_ERR_TIMEOUT.
 //
-// * split form (bands of exactly 4 rows in every CTA): the barrier form with
+// * async form: the neighbour form's protocol, with each row word sent by an
+//   asynchronous remote store (st.async) that completes 4 bytes of a
+//   transaction count on the neighbour's mbarrier of that parity; the
+//   receiving CTA's thread 0 arms its own mbarrier once per phase (one
+//   arrival expecting the 8 wpr bytes of the two rows), so no release fence
+//   per sending lane.  A store may land before the arming: the phase still
+//   needs the arrival.  Bands of 4 or 8 rows compute their first and last row
+//   before the inner ones, so the rows leave early.
+//
+// * split form (bands of exactly 4 or 8 rows in every CTA): the barrier form with
 //   the cluster barrier's arrive and wait apart.  A band computes its first
 //   and last row first (from the halos and its own rows, whose old values it
 //   keeps in registers) and publishes them, then arrives; its two inner rows,
@@ -51,7 +60,9 @@
 //   wait.
 //
 // A last cluster barrier after the loop keeps every CTA's shared memory alive
-// until the remote stores of the final generation have landed.  A lane only
+// until the remote stores of the final generation have landed (the mbarrier
+// forms send nothing in the final generation, and every earlier row is
+// waited for by its receiver).  A lane only
 // ever touches its own column word of its own band.
 #include <cooperative_groups.h>
 
@@ -118,6 +129,21 @@ __device__ __forceinline__ void xk_cl_arrive_remote(uint32_t bar)
     asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" : : "r"(bar) : "memory");
 }
 
+// store v at shared::cluster address `addr` (another CTA's) asynchronously;
+// its completion counts 4 bytes on the mbarrier at shared::cluster address
+// `bar` of the same CTA
+__device__ __forceinline__ void xk_cl_st_async(uint32_t addr, uint32_t v, uint32_t bar)
+{
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.u32 [%0], %1, [%2];"
+                 : : "r"(addr), "r"(v), "r"(bar) : "memory");
+}
+
+// this CTA's arrival on its own mbarrier, expecting `bytes` of transactions
+__device__ __forceinline__ void xk_cl_arm(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" : : "r"(bar), "r"(bytes) : "memory");
+}
+
 // the hardware cluster barrier's two halves (every thread of every CTA
 // alternates them)
 __device__ __forceinline__ void xk_cl_barrier_arrive()
@@ -146,8 +172,11 @@ template <bool TORUS, bool FULLW, int LB, int RF, int SYNC>
 __global__ void __launch_bounds__(1024)
 xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int generations, int R)
 {
-    constexpr bool P2P = SYNC == XK_SYNC_NEIGHBOUR, SPLIT = SYNC == XK_SYNC_SPLIT;
+    constexpr bool ASYNC = SYNC == XK_SYNC_ASYNC, SPLIT = SYNC == XK_SYNC_SPLIT;
+    constexpr bool P2P = SYNC == XK_SYNC_NEIGHBOUR || ASYNC;     // mbarrier waits
+    constexpr bool EDGE_FIRST = SPLIT || (ASYNC && LB >= 4);      // edge rows, then the inner ones
     static_assert(!SPLIT || LB == 4 || LB == 8, "the split form runs bands of 4 or 8 rows");
+    static_assert(!ASYNC || LB > 0, "the async form runs bands of a fixed length");
     const auto &t = RuleForm<RF>::make(t9);
     extern __shared__ uint32_t sm[];
     cg::cluster_group cluster = cg::this_cluster();
@@ -170,14 +199,20 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int gen
     uint64_t *mbar = (uint64_t *)(sm + ((dwords + 1) & ~1LL));
     const uint32_t mbar0 = (uint32_t)__cvta_generic_to_shared(mbar);
     if (P2P && threadIdx.x == 0) {
+        // neighbour form: the 2 wpr sending lanes arrive; async form: this
+        // CTA's arming is the one arrival, the stores count bytes
         for (int q = 0; q < 2; ++q)
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" : : "r"(mbar0 + 8u * q), "r"(2 * wpr)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" : : "r"(mbar0 + 8u * q), "r"(ASYNC ? 1 : 2 * wpr)
                          : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" : : : "memory");
     }
     // the neighbours' mbarriers [parity] at shared::cluster addresses
     const uint32_t mb_up = P2P ? xk_cl_mapa(mbar0, (uint32_t)cu) : 0u;
     const uint32_t mb_dn = P2P ? xk_cl_mapa(mbar0, (uint32_t)cd) : 0u;
+    // async form: the neighbours' slots at shared::cluster addresses
+    const uint32_t slot0 = (uint32_t)__cvta_generic_to_shared(slot);
+    const uint32_t sa_up = ASYNC ? xk_cl_mapa(slot0, (uint32_t)cu) : 0u;
+    const uint32_t sa_dn = ASYNC ? xk_cl_mapa(slot0, (uint32_t)cd) : 0u;
 
     for (int w = threadIdx.x; w < Rc * wpr; w += blockDim.x) {
         const int y = w / wpr, jj = w - y * wpr;
@@ -238,29 +273,42 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int gen
         if (i == 0) {
             halo[npar * hwords + (band * 2 + 0) * wpr + j] = w;
             if (send_up && remote) {
-                slot_up[(npar * 2 + 1) * wpr + j] = w;
-                if (P2P) xk_cl_arrive_remote(mb_up + 8u * (uint32_t)npar);
+                if (ASYNC) {
+                    xk_cl_st_async(sa_up + 4u * (uint32_t)((npar * 2 + 1) * wpr + j), w, mb_up + 8u * (uint32_t)npar);
+                } else {
+                    slot_up[(npar * 2 + 1) * wpr + j] = w;
+                    if (P2P) xk_cl_arrive_remote(mb_up + 8u * (uint32_t)npar);
+                }
             }
         }
         if (i == y1 - 1 - y0) {
             halo[npar * hwords + (band * 2 + 1) * wpr + j] = w;
             if (send_dn && remote) {
-                slot_dn[(npar * 2 + 0) * wpr + j] = w;
-                if (P2P) xk_cl_arrive_remote(mb_dn + 8u * (uint32_t)npar);
+                if (ASYNC) {
+                    xk_cl_st_async(sa_dn + 4u * (uint32_t)((npar * 2 + 0) * wpr + j), w, mb_dn + 8u * (uint32_t)npar);
+                } else {
+                    slot_dn[(npar * 2 + 0) * wpr + j] = w;
+                    if (P2P) xk_cl_arrive_remote(mb_dn + 8u * (uint32_t)npar);
+                }
             }
         }
     };
 
     cluster.sync();   // every CTA running (before any remote store), slabs loaded, mbarriers set
-    // each edge row sent once (a one-row band's row is its first and last)
-    publish(0, 0, wp[0], true);
-    if (y1 - 1 - y0 != 0) publish(0, y1 - 1 - y0, wp[32 * (y1 - 1 - y0)], true);
+    // each edge row sent once (a one-row band's row is its first and last);
+    // nothing when no generation will read them
+    if (generations > 0) {
+        publish(0, 0, wp[0], true);
+        if (y1 - 1 - y0 != 0) publish(0, y1 - 1 - y0, wp[32 * (y1 - 1 - y0)], true);
+    }
     bool failed = false;
     if (SPLIT) xk_cl_barrier_arrive();
     for (int gen = 0; gen < generations; ++gen) {
         const int par = gen & 1;
         const uint32_t *hp = halo + par * hwords;
         if (P2P) {
+            // async form: one arrival per phase, expecting the two rows
+            if (ASYNC && threadIdx.x == 0) xk_cl_arm(mbar0 + 8u * (uint32_t)par, 8u * (uint32_t)wpr);
             // bands of this CTA; every thread leaves together after a failure
             if (__syncthreads_or(failed)) break;
             if ((first_band || last_band) &&
@@ -276,9 +324,10 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int gen
         const bool remote = gen + 1 < generations || !P2P;
         const uint32_t wu = first_band ? slot[(par * 2 + 0) * wpr + jc] : hp[((bc - 1) * 2 + 1) * wpr + jc];
         const uint32_t wl = last_band ? slot[(par * 2 + 1) * wpr + jc] : hp[((bc + 1) * 2 + 0) * wpr + jc];
-        if constexpr (SPLIT) {
+        if constexpr (EDGE_FIRST) {
             // every band has LB rows: the first and last row, then the inner
-            // ones after the arrival (the old rows' column sums in registers)
+            // ones after the arrival (split form) or the sends (async form),
+            // the old rows' column sums in registers
             uint32_t w[LB], s[LB], cy[LB];
             uint32_t s_u, c_u, s_d, c_d;
 #pragma unroll
@@ -298,10 +347,10 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int gen
             if (active) {
                 wp[0] = o0;
                 wp[32 * (LB - 1)] = oL;
-                publish(par ^ 1, 0, o0, true);
-                publish(par ^ 1, LB - 1, oL, true);
+                publish(par ^ 1, 0, o0, remote);
+                publish(par ^ 1, LB - 1, oL, remote);
             }
-            xk_cl_barrier_arrive();
+            if (SPLIT) xk_cl_barrier_arrive();
 #pragma unroll
             for (int i = 1; i < LB - 1; ++i) {
                 uint32_t o = xk_life_word9(s[i - 1], cy[i - 1], s[i], cy[i], s[i + 1], cy[i + 1], w[i], t);
@@ -353,7 +402,7 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int gen
 typedef void (*ClusterKernel)(uint32_t *, LifeGeo, LifeTable9, int, int);
 
 // the neighbour form has instantiations for bands of 1, 2 and 4 rows, the
-// split form for bands of 4 and 8
+// split form for bands of 4 and 8, the async form for 1, 2, 4 and 8
 template <bool TORUS, bool FULLW, int RF>
 static ClusterKernel cluster_kernel_l(int L, int sync)
 {
@@ -369,6 +418,15 @@ static ClusterKernel cluster_kernel_l(int L, int sync)
         if (L == 4) return xk_k_life_cluster<TORUS, FULLW, 4, RF, XK_SYNC_SPLIT>;
         if (L == 8) return xk_k_life_cluster<TORUS, FULLW, 8, RF, XK_SYNC_SPLIT>;
         return nullptr;
+    }
+    if (sync == XK_SYNC_ASYNC) {
+        switch (L) {
+        case 1: return xk_k_life_cluster<TORUS, FULLW, 1, RF, XK_SYNC_ASYNC>;
+        case 2: return xk_k_life_cluster<TORUS, FULLW, 2, RF, XK_SYNC_ASYNC>;
+        case 4: return xk_k_life_cluster<TORUS, FULLW, 4, RF, XK_SYNC_ASYNC>;
+        case 8: return xk_k_life_cluster<TORUS, FULLW, 8, RF, XK_SYNC_ASYNC>;
+        default: return nullptr;
+        }
     }
     switch (L) {
     case 1: return xk_k_life_cluster<TORUS, FULLW, 1, RF, XK_SYNC_BARRIER>;
@@ -462,7 +520,7 @@ int xk_life_cluster_config(const LifeGeo &g, int C, int band, int *C_out, int *R
     const ClusterKernel k = cluster_kernel(g, rows, th);
     bool attrs_ok = true;
     for (int rf = XK_RULE_TABLE; rf <= XK_RULE_CONWAY && attrs_ok; ++rf)
-        for (int sync = XK_SYNC_BARRIER; sync <= XK_SYNC_SPLIT && attrs_ok; ++sync) {
+        for (int sync = XK_SYNC_BARRIER; sync <= XK_SYNC_ASYNC && attrs_ok; ++sync) {
             const ClusterKernel kk = cluster_kernel(g, rows, th, rf, sync);
             attrs_ok = !kk || cluster_attrs(kk, smem) == cudaSuccess;
         }
@@ -488,9 +546,10 @@ int xk_life_cluster_config(const LifeGeo &g, int C, int band, int *C_out, int *R
 int xk_life_cluster_has_sync(const LifeGeo &g, int C, int R, int threads, int sync)
 {
     if (sync == XK_SYNC_BARRIER) return 1;
-    if (sync == XK_SYNC_SPLIT) {
-        // every CTA has R rows, cut into bands of exactly 4 or 8
-        const ResidentPlan p = xk_resident_plan(g.wpr, R, threads);
+    const ResidentPlan p = xk_resident_plan(g.wpr, R, threads);
+    if (sync == XK_SYNC_SPLIT || (sync == XK_SYNC_ASYNC && p.L >= 4)) {
+        // every CTA has R rows, cut into bands of exactly 4 or 8 (the edge
+        // rows computed first)
         if ((int64_t)C * R != g.H || (p.L != 4 && p.L != 8) || p.nb * p.L != R) return 0;
     }
     return cluster_kernel(g, R, threads, XK_RULE_TABLE, sync) != nullptr;

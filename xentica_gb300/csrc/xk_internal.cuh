@@ -183,10 +183,14 @@ int xk_life_cluster_config(const LifeGeo &g, int C, int band, int *C_out, int *R
 // generation -- XK_SYNC_BARRIER a cluster barrier; XK_SYNC_NEIGHBOUR mbarriers
 // of the two neighbouring CTAs only (bands of 1, 2 and 4 rows);
 // XK_SYNC_SPLIT a cluster barrier whose arrive and wait enclose the bands'
-// inner rows (every CTA's bands exactly 4 rows): xk_life_cluster_has_sync
+// inner rows (every CTA's bands exactly 4 or 8 rows); XK_SYNC_ASYNC the
+// neighbour form with the rows sent by asynchronous remote stores that
+// complete a transaction count on the receiver's mbarrier (bands of 1, 2, 4
+// or 8 rows): xk_life_cluster_has_sync
 #define XK_SYNC_BARRIER 0
 #define XK_SYNC_NEIGHBOUR 1
 #define XK_SYNC_SPLIT 2
+#define XK_SYNC_ASYNC 3
 cudaError_t xk_life_step_cluster(uint32_t *bits, const LifeGeo &g, uint32_t rule0, uint32_t rule1,
                                  int generations, int C, int R, int threads, cudaStream_t s, int sync = 0);
 int xk_life_cluster_has_sync(const LifeGeo &g, int C, int R, int threads, int sync);
