@@ -143,8 +143,8 @@ int xk_step_frames(xk_model *m, int64_t nsteps, int32_t width, int32_t height, i
  * a cluster barrier whose arrival comes before the bands' inner rows and
  * whose wait after them (every CTA's bands exactly 4 or 8 rows), 3 as 1 with
  * the rows sent by asynchronous remote stores counted in bytes on the
- * receiver's mbarrier (bands of 1 or 2 rows, or every CTA's bands exactly 4
- * or 8 rows); TEMPORAL: plan[3] =
+ * receiver's mbarrier (bands of 1 row, or every CTA's bands exactly 2, 4 or
+ * 8 rows); TEMPORAL: plan[3] =
  * generations per launch (2..8).  xk_model_plan gives kind -1 for models
  * without plans.  A bounded wait of the neighbour or async form that gave up makes
  * the next xk_download return XK_ERR_TIMEOUT. */

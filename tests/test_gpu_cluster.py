@@ -89,9 +89,9 @@ def test_async_sync_vs_oracle(cls, forced, band, monkeypatch):
     """The async form (rows sent by asynchronous remote stores, each counted
     in bytes on the receiving CTA's mbarrier, which that CTA arms once per
     phase) for every cluster size and band length, against the oracle; bands
-    of 4 or 8 rows only where every CTA's bands have that length, the cluster
-    barrier elsewhere; odd generation counts leave the last generation's
-    rows unsent."""
+    of 2, 4 or 8 rows only where every CTA's bands have that length, the
+    cluster barrier elsewhere; odd generation counts leave the last
+    generation's rows unsent."""
     for k, size in enumerate(SIZES):
         got, want = _run(cls, size, forced, 37 + k % 2, monkeypatch, 10 * forced + k + band, band,
                          "async")

@@ -124,7 +124,7 @@ def test_every_plan_kind_matches_oracle(shape, rule):
         assert np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n]), "plan %s" % plan
     bad = {(512, 512): [[0, 0, 0, 0], [3, 0, 0, 9], [2, 17, 1, 0], [5, 0, 0, 0], [2, 16, 2, 2],
                         [2, 16, 3, 1], [2, 3, 1, 1], [2, 3, 4, 2], [2, 16, 4, 4], [2, 16, 8, 1],
-                        [2, 3, 8, 2], [2, 3, 4, 3], [2, 16, 3, 3]],
+                        [2, 3, 8, 2], [2, 3, 4, 3], [2, 3, 2, 3], [2, 16, 3, 3]],
            (2049, 131): [[1, 0, 0, 0], [2, 4, 1, 0], [3, 0, 0, 1]]}[shape]
     model = _model(shape, "torus")
     model.gpu._ensure()

@@ -1011,7 +1011,7 @@ extern "C" int xk_model_set_plan(xk_model *m, const int32_t plan[4])
                        xk_life_cluster_has_sync(m->lg, C, R, th, plan[3]),
                    XK_ERR_ARG, "xk_model_set_plan: cluster synchronisation form %d does not apply "
                    "(1: bands of 1, 2 or 4 rows; 2: every CTA's bands 4 or 8 rows; 3: bands of "
-                   "1 or 2 rows, or every CTA's bands 4 or 8 rows)", plan[3]);
+                   "1 row, or every CTA's bands 2, 4 or 8 rows)", plan[3]);
         break;
     case XK_PLAN_TEMPORAL:
         XK_REQUIRE(plan[3] >= 2 && plan[3] <= 8 && xk_life_tb_supported(m->lg), XK_ERR_ARG,

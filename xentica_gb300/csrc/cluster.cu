@@ -46,8 +46,9 @@
 //   receiving CTA's thread 0 arms its own mbarrier once per phase (one
 //   arrival expecting the 8 wpr bytes of the two rows), so no release fence
 //   per sending lane.  A store may land before the arming: the phase still
-//   needs the arrival.  Bands of 4 or 8 rows compute their first and last row
-//   before the inner ones, so the rows leave early.
+//   needs the arrival.  Bands of 2, 4 or 8 rows (the same length in every
+//   CTA) compute their first and last row before the inner ones, so the rows
+//   leave early.
 //
 // * split form (bands of exactly 4 or 8 rows in every CTA): the barrier form with
 //   the cluster barrier's arrive and wait apart.  A band computes its first
@@ -174,7 +175,7 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int gen
 {
     constexpr bool ASYNC = SYNC == XK_SYNC_ASYNC, SPLIT = SYNC == XK_SYNC_SPLIT;
     constexpr bool P2P = SYNC == XK_SYNC_NEIGHBOUR || ASYNC;     // mbarrier waits
-    constexpr bool EDGE_FIRST = SPLIT || (ASYNC && LB >= 4);      // edge rows, then the inner ones
+    constexpr bool EDGE_FIRST = SPLIT || (ASYNC && LB >= 2);      // edge rows, then the inner ones
     static_assert(!SPLIT || LB == 4 || LB == 8, "the split form runs bands of 4 or 8 rows");
     static_assert(!ASYNC || LB > 0, "the async form runs bands of a fixed length");
     const auto &t = RuleForm<RF>::make(t9);
@@ -268,30 +269,33 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int gen
     const bool send_up = active && band == 0, send_dn = active && band == p.nb - 1;
     // `remote`: also store into the neighbours' slots (and, in the neighbour
     // form, arrive on their parity-npar mbarrier)
+    // (active lanes) a band's first row, and its last row
+    auto publish_first = [&](int npar, uint32_t w, bool remote) {
+        halo[npar * hwords + (band * 2 + 0) * wpr + j] = w;
+        if (send_up && remote) {
+            if (ASYNC) {
+                xk_cl_st_async(sa_up + 4u * (uint32_t)((npar * 2 + 1) * wpr + j), w, mb_up + 8u * (uint32_t)npar);
+            } else {
+                slot_up[(npar * 2 + 1) * wpr + j] = w;
+                if (P2P) xk_cl_arrive_remote(mb_up + 8u * (uint32_t)npar);
+            }
+        }
+    };
+    auto publish_last = [&](int npar, uint32_t w, bool remote) {
+        halo[npar * hwords + (band * 2 + 1) * wpr + j] = w;
+        if (send_dn && remote) {
+            if (ASYNC) {
+                xk_cl_st_async(sa_dn + 4u * (uint32_t)((npar * 2 + 0) * wpr + j), w, mb_dn + 8u * (uint32_t)npar);
+            } else {
+                slot_dn[(npar * 2 + 0) * wpr + j] = w;
+                if (P2P) xk_cl_arrive_remote(mb_dn + 8u * (uint32_t)npar);
+            }
+        }
+    };
     auto publish = [&](int npar, int i, uint32_t w, bool remote) {
         if (!active) return;
-        if (i == 0) {
-            halo[npar * hwords + (band * 2 + 0) * wpr + j] = w;
-            if (send_up && remote) {
-                if (ASYNC) {
-                    xk_cl_st_async(sa_up + 4u * (uint32_t)((npar * 2 + 1) * wpr + j), w, mb_up + 8u * (uint32_t)npar);
-                } else {
-                    slot_up[(npar * 2 + 1) * wpr + j] = w;
-                    if (P2P) xk_cl_arrive_remote(mb_up + 8u * (uint32_t)npar);
-                }
-            }
-        }
-        if (i == y1 - 1 - y0) {
-            halo[npar * hwords + (band * 2 + 1) * wpr + j] = w;
-            if (send_dn && remote) {
-                if (ASYNC) {
-                    xk_cl_st_async(sa_dn + 4u * (uint32_t)((npar * 2 + 0) * wpr + j), w, mb_dn + 8u * (uint32_t)npar);
-                } else {
-                    slot_dn[(npar * 2 + 0) * wpr + j] = w;
-                    if (P2P) xk_cl_arrive_remote(mb_dn + 8u * (uint32_t)npar);
-                }
-            }
-        }
+        if (i == 0) publish_first(npar, w, remote);
+        if (i == y1 - 1 - y0) publish_last(npar, w, remote);
     };
 
     cluster.sync();   // every CTA running (before any remote store), slabs loaded, mbarriers set
@@ -347,8 +351,8 @@ xk_k_life_cluster(uint32_t *__restrict__ bits, LifeGeo g, LifeTable9 t9, int gen
             if (active) {
                 wp[0] = o0;
                 wp[32 * (LB - 1)] = oL;
-                publish(par ^ 1, 0, o0, remote);
-                publish(par ^ 1, LB - 1, oL, remote);
+                publish_first(par ^ 1, o0, remote);
+                publish_last(par ^ 1, oL, remote);
             }
             if (SPLIT) xk_cl_barrier_arrive();
 #pragma unroll
@@ -547,10 +551,14 @@ int xk_life_cluster_has_sync(const LifeGeo &g, int C, int R, int threads, int sy
 {
     if (sync == XK_SYNC_BARRIER) return 1;
     const ResidentPlan p = xk_resident_plan(g.wpr, R, threads);
-    if (sync == XK_SYNC_SPLIT || (sync == XK_SYNC_ASYNC && p.L >= 4)) {
-        // every CTA has R rows, cut into bands of exactly 4 or 8 (the edge
-        // rows computed first)
+    if (sync == XK_SYNC_SPLIT) {
+        // every CTA has R rows, cut into bands of exactly 4 or 8
         if ((int64_t)C * R != g.H || (p.L != 4 && p.L != 8) || p.nb * p.L != R) return 0;
+    }
+    if (sync == XK_SYNC_ASYNC && p.L >= 2) {
+        // the edge rows computed first: every CTA has R rows, cut into bands
+        // of exactly 2, 4 or 8
+        if ((int64_t)C * R != g.H || (p.L != 2 && p.L != 4 && p.L != 8) || p.nb * p.L != R) return 0;
     }
     return cluster_kernel(g, R, threads, XK_RULE_TABLE, sync) != nullptr;
 }

@@ -185,8 +185,8 @@ int xk_life_cluster_config(const LifeGeo &g, int C, int band, int *C_out, int *R
 // XK_SYNC_SPLIT a cluster barrier whose arrive and wait enclose the bands'
 // inner rows (every CTA's bands exactly 4 or 8 rows); XK_SYNC_ASYNC the
 // neighbour form with the rows sent by asynchronous remote stores that
-// complete a transaction count on the receiver's mbarrier (bands of 1, 2, 4
-// or 8 rows): xk_life_cluster_has_sync
+// complete a transaction count on the receiver's mbarrier (bands of 1 row, or
+// every CTA's bands exactly 2, 4 or 8 rows): xk_life_cluster_has_sync
 #define XK_SYNC_BARRIER 0
 #define XK_SYNC_NEIGHBOUR 1
 #define XK_SYNC_SPLIT 2
