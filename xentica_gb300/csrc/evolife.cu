@@ -394,13 +394,22 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
     // lane: 0x55, 0x66, 0x78, 0x80); num_fit = the largest such g + 1
     const uint32_t eq = ~(b0 ^ 0x55u) & ~(b1 ^ 0x66u) & ~(b2 ^ 0x78u) & ~(b3 ^ 0x80u) & 255u;
     const uint32_t num_fit = 32u - (uint32_t)__clz(eq);
-    // parents: rules with the winning birth count, in neighbour order
+    // parents: rules with the winning birth count, in neighbour order.  The
+    // neighbours' birth bytes packed four to a word; bit num_fit - 1 of
+    // each byte gathered into a nibble by one multiply (the products of the
+    // four bits land on bits 24..27 without carries)
     uint32_t pmask = 0, any = 0;
+    if (num_fit != 0) {
+        const uint32_t f = num_fit - 1u;
+        const uint32_t M0 = __byte_perm(__byte_perm(m[0], m[1], 0x0040), __byte_perm(m[2], m[3], 0x0040), 0x5410);
+        const uint32_t M1 = __byte_perm(__byte_perm(m[4], m[5], 0x0040), __byte_perm(m[6], m[7], 0x0040), 0x5410);
+        const uint32_t lo = (((M0 >> f) & 0x01010101u) * 0x01020408u) >> 24;
+        const uint32_t hi = (((M1 >> f) & 0x01010101u) * 0x01020408u) >> 24;
+        pmask = lo | (hi << 4);
+    }
+    if (MUT) {
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const uint32_t par = ((nr[k] & 510u) >> num_fit) & 1u;
-        pmask |= par << k;
-        if (MUT) any |= nr[k] * par;
+        for (int k = 0; k < 8; ++k) any |= nr[k] * ((pmask >> k) & 1u);
     }
     const uint32_t n = __popc(pmask);
     const uint32_t old_rule = rule, old_energy = energy;
@@ -426,14 +435,14 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
         new_genome = xk_unrot18(rot, start_gene);
         if (MUT) new_genome ^= __ldg(p.mut + x0) & any;
     }
-    rule = new_genome + rule * (uint32_t)(new_genome == 0);
-    const uint32_t is_live = (uint32_t)(old_energy < 255u) &
-                             ((uint32_t)((old_energy + old_rule) == 0u) | is_sustained);
-    const uint32_t new_energy = old_energy + p.death_speed * (uint32_t)((old_energy + old_rule) != 0u);
-    energy = (uint16_t)(new_energy * (uint32_t)(rule == old_rule));
-    rule = old_rule * (uint32_t)(rule == old_rule) + rule * (uint32_t)(rule != old_rule);
-    energy = (uint16_t)(energy * is_live);
-    rule *= is_live;
+    // the reference's selections by multiplication, as selects (the same
+    // integers): a new genome replaces the rule and resets the energy, a
+    // cell that does not live keeps neither
+    rule = new_genome != 0 ? new_genome : rule;
+    const bool is_live = old_energy < 255u && ((old_energy + old_rule) == 0u || is_sustained != 0u);
+    const uint32_t new_energy = old_energy + ((old_energy + old_rule) != 0u ? p.death_speed : 0u);
+    energy = rule == old_rule && is_live ? (uint16_t)new_energy : 0u;
+    rule = is_live ? rule : 0u;
     if (p.color_kind != XK_COLOR_NONE) {
         int rgb[3];
         if (p.positional) xk_evo_color_positional(rule, energy, rgb);
@@ -452,10 +461,11 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
             // its low byte.  Below 2^24 in magnitude int -> float -> int is
             // exact, and so is a division by 1: with SMOOTH_FACTOR 1 (or none)
             // such a pixel is the colour's low byte
+            const bool small = (((uint32_t)rgb[0] + (1u << 24)) | ((uint32_t)rgb[1] + (1u << 24)) |
+                                ((uint32_t)rgb[2] + (1u << 24))) < (1u << 25);   // all three
 #pragma unroll
             for (int ch = 0; ch < 3; ++ch) {
                 const int c = rgb[ch];
-                const bool small = (uint32_t)(c + (1 << 24)) < (1u << 25);
                 uint8_t px;
                 if (p.frame_smooth <= 1 && small) {
                     px = (uint8_t)c;
@@ -468,8 +478,9 @@ xk_k_evolife(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
             }
         }
     }
-    dst[i] = ((uint64_t)energy & 511u) + (((uint64_t)rule & 262143u) << 9) +
-             (((uint64_t)rng & 65535u) << 27);
+    // energy | rule << 9 | rng << 27 (fields masked, so + and | agree) as two halves
+    const uint32_t rn = rng & 65535u;
+    reinterpret_cast<uint2 *>(dst)[i] = make_uint2((energy & 511u) | ((rule & 262143u) << 9) | (rn << 27), rn >> 5);
 }
 
 cudaError_t xk_evolife_set_positional(const double *lut54)
