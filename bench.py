@@ -734,7 +734,7 @@ def mass_line(args, dist):
     clk = clocks.stop()
     dev_s = dist.max(sum(step_ms) / 1000.0)
     value = float(n) * gens * args.steps * dist.world / dev_s
-    # e2e: host masses and colours in, 100 generations, every frame to pinned host memory
+    # e2e: host masses in, 100 generations, every frame to pinned host memory
     host = nat.PinnedBuffer(gens * fb)
     colors0 = model.gpu.arrays.colors.get()
     e2e = []
@@ -761,11 +761,11 @@ def mass_line(args, dist):
                            4 * n / 2 ** 20, " close to L2 size" if side == 256 else "")},
             "mass_conserved": conserved,
             "e2e": {"value": float(n) * gens * args.steps * dist.world / e2e_s,
-                    "unit": "cell-updates/s", "h2d_bytes_per_step": 4 * n + 12 * n,
+                    "unit": "cell-updates/s", "h2d_bytes_per_step": 4 * n,
                     "d2h_bytes_per_step": gens * fb,
-                    "note": "masses and colours loaded from the host (load(cells, colors), "
-                            "as the reference's load replaces both), every frame copied to "
-                            "page-locked host memory"},
+                    "note": "masses loaded from the host (load(cells, colors): this model's "
+                            "colours are a function of its state, so the library keeps none "
+                            "and copies none), every frame copied to page-locked host memory"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": committed_traffic("mass_tma") if side == 256 else None,
