@@ -39,9 +39,13 @@ enum {
 };
 
 /* XK_FAMILY_SHIFT: ShiftingSands' family (examples/shifting_sands.py:15-47),
- * a 1-bit state that moves in from neighbour rule0 each generation. */
+ * a 1-bit state that moves in from neighbour rule0 each generation.
+ * XK_FAMILY_LIFECOLOR: Conway's Life whose cells carry three 8-bit colour
+ * channels inherited from their neighbours (GameOfLifeColor,
+ * examples/game_of_life.py:112-159): a 2-D Moore lattice of uint32 cells,
+ * torus or static border, MovingAverage colours or none. */
 enum { XK_FAMILY_LIFE = 1, XK_FAMILY_EVOLIFE = 2, XK_FAMILY_MASS = 3, XK_FAMILY_VM = 4,
-       XK_FAMILY_SHIFT = 5 };
+       XK_FAMILY_SHIFT = 5, XK_FAMILY_LIFECOLOR = 6 };
 enum { XK_COLOR_NONE = 0, XK_COLOR_PLAIN = 1, XK_COLOR_MOVING_AVERAGE = 2 };
 
 /* Model descriptor filled by the translator (xentica_gb300/core/templates.py)

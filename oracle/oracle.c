@@ -194,6 +194,47 @@ void xo_shift_step(const xo_topo *t, void *fld, int esz, int plane0, int32_t *co
 }
 
 /* ------------------------------------------------------------------------ */
+/* GameOfLifeColor (examples/game_of_life.py:112-159): a uint32 cell packs
+ * state (1 bit) | red << 1 | green << 9 | blue << 17, LSB first in
+ * declaration order (properties.py:496-541).  emit copies every field into
+ * every buffer (:125-131); absorb runs GameOfLife's absorb (:55-70) on the
+ * states, then each channel becomes the sum over the neighbours' buffers of
+ * (channel + 1) in an unsigned int, times the new state, stored into its
+ * 8-bit field (:133-151); the colour (MovingAverage, :153-159) is state *
+ * channel per channel.  An off-board neighbour reads as the whole border
+ * container. */
+void xo_lifecolor_step(const xo_topo *t, uint32_t *fld, int32_t *col, const xo_color *cc, int threads)
+{
+    const int64_t n = xo_cells(t);
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        const uint32_t v = fld[i];
+        const uint32_t packed = (v & 1u) + (((v >> 1) & 255u) << 1) + (((v >> 9) & 255u) << 9) +
+                                (((v >> 17) & 255u) << 17);
+        for (int k = 0; k < t->nbr; ++k) fld[i + n * (int64_t)(t->rev[k] + 1)] = packed;
+    }
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t x[XO_MAXDIM];
+        xo_coords(t, i, x);
+        uint32_t alive = 0, rs = 0, gs = 0, bs = 0;
+        for (int k = 0; k < t->nbr; ++k) {
+            int64_t j = xo_neighbor(t, x, k);
+            uint32_t v = j < 0 ? (uint32_t)t->border_value : fld[j + n * (int64_t)(k + 1)];
+            alive += v & 1u;
+            rs += ((v >> 1) & 255u) + 1u;
+            gs += ((v >> 9) & 255u) + 1u;
+            bs += ((v >> 17) & 255u) + 1u;
+        }
+        const uint32_t s = fld[i] & 1u;
+        const uint32_t ns = ((8u >> alive) & 1u) | (((12u >> alive) & 1u) & s);
+        const uint32_t r = (uint8_t)(rs * ns), g = (uint8_t)(gs * ns), b = (uint8_t)(bs * ns);
+        xo_color_write(col, i, (int)(ns * r), (int)(ns * g), (int)(ns * b), cc);
+        fld[i] = (ns & 1u) + ((r & 255u) << 1) + ((g & 255u) << 9) + ((b & 255u) << 17);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
 /* Mass transfer (3-D von Neumann, StaticBorder(WALL)): the model added for the
  * sand-transfer configuration, written in the reference DSL (see
  * tests/golden/ref_models.py:MassTransfer).  uint32 cell = mass.

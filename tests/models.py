@@ -86,6 +86,82 @@ class LifelikeCA(GameOfLife):
         super().step()
 
 
+class GameOfLifeColor(GameOfLife):
+    """Life whose live cells carry three colour channels, each the sum over
+    the neighbours of (channel + 1) (examples/game_of_life.py:112-159)."""
+
+    state = core.IntegerProperty(max_val=1)
+    red = core.IntegerProperty(max_val=255)
+    green = core.IntegerProperty(max_val=255)
+    blue = core.IntegerProperty(max_val=255)
+
+    def emit(self):
+        for buf in self.buffers:
+            buf.state = self.main.state
+            buf.red = self.main.red
+            buf.green = self.main.green
+            buf.blue = self.main.blue
+
+    def absorb(self):
+        GameOfLife.absorb(self)
+        red_sum = core.IntegerVariable()
+        green_sum = core.IntegerVariable()
+        blue_sum = core.IntegerVariable()
+        for i in range(len(self.buffers)):
+            red_sum += self.neighbors[i].buffer.red + 1
+            green_sum += self.neighbors[i].buffer.green + 1
+            blue_sum += self.neighbors[i].buffer.blue + 1
+        self.main.red = red_sum * self.main.state
+        self.main.green = green_sum * self.main.state
+        self.main.blue = blue_sum * self.main.state
+
+    @color_effects.MovingAverage
+    def color(self):
+        red = self.main.state * self.main.red
+        green = self.main.state * self.main.green
+        blue = self.main.state * self.main.blue
+        return (red, green, blue)
+
+
+class GameOfLifeColorStatic(GameOfLifeColor):
+    """The same on a lattice surrounded by one fixed container value (a live
+    cell with colour channels 1, 2 and 3)."""
+
+    class Topology(GameOfLife.Topology):
+        border = core.StaticBorder(1 | 1 << 1 | 2 << 9 | 3 << 17)
+
+
+class GameOfLifeColorPlus2(GameOfLifeColor):
+    """Not the colour-Life program (each neighbour adds channel + 2): runs on
+    the interpreter."""
+
+    def absorb(self):
+        GameOfLife.absorb(self)
+        red_sum = core.IntegerVariable()
+        green_sum = core.IntegerVariable()
+        blue_sum = core.IntegerVariable()
+        for i in range(len(self.buffers)):
+            red_sum += self.neighbors[i].buffer.red + 2
+            green_sum += self.neighbors[i].buffer.green + 1
+            blue_sum += self.neighbors[i].buffer.blue + 1
+        self.main.red = red_sum * self.main.state
+        self.main.green = green_sum * self.main.state
+        self.main.blue = blue_sum * self.main.state
+
+
+class GOLColorExperiment(core.Experiment):
+    word = "XENTICA IN COLOR"
+    size = (96, 64)
+    zoom = 1
+    pos = [0, 0]
+    fade_in = 255
+    fade_out = 10
+    smooth_factor = 1
+    seed = seeds.patterns.PrimordialSoup(vals={
+        "state": seeds.random.RandInt(0, 1), "red": seeds.random.RandInt(0, 255),
+        "green": seeds.random.RandInt(0, 255), "blue": seeds.random.RandInt(0, 255)})
+
+
 class GOLExperiment(core.Experiment):
     word = "OBEY XENTICA"
     size = (640, 360, )

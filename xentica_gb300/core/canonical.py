@@ -163,3 +163,53 @@ class MassTransferProgram(core.CellularAutomaton):
     def color(self):
         v = xmath.min(self.main.mass * 32, 255)
         return (v, v, v)
+
+
+class LifeColorProgram(core.CellularAutomaton):
+    """Conway's Life whose live cells carry a colour: each 8-bit channel of
+    a cell becomes the sum over its eight neighbours of (channel + 1), kept
+    only while the cell lives (the reference's GameOfLifeColor,
+    ``examples/game_of_life.py:112-159``; the statement order fixes the
+    traced program the matcher compares with)."""
+
+    state = core.IntegerProperty(max_val=1)
+    red = core.IntegerProperty(max_val=255)
+    green = core.IntegerProperty(max_val=255)
+    blue = core.IntegerProperty(max_val=255)
+
+    class Topology:
+        dimensions = 2
+        lattice = core.OrthogonalLattice()
+        neighborhood = core.MooreNeighborhood()
+        border = core.TorusBorder()
+
+    def emit(self):
+        for buf in self.buffers:
+            buf.state = self.main.state
+            buf.red = self.main.red
+            buf.green = self.main.green
+            buf.blue = self.main.blue
+
+    def absorb(self):
+        alive = core.IntegerVariable()
+        for k in range(len(self.buffers)):
+            alive += self.neighbors[k].buffer.state
+        self.main.state = (8 >> alive) & 1 | (12 >> alive) & 1 & self.main.state
+        # (each accumulator bound to its own local name: a variable's C name
+        # is the Python name it is used under)
+        acc_r = core.IntegerVariable()
+        acc_g = core.IntegerVariable()
+        acc_b = core.IntegerVariable()
+        for k in range(len(self.buffers)):
+            nbr = self.neighbors[k].buffer
+            acc_r += nbr.red + 1
+            acc_g += nbr.green + 1
+            acc_b += nbr.blue + 1
+        self.main.red = acc_r * self.main.state
+        self.main.green = acc_g * self.main.state
+        self.main.blue = acc_b * self.main.state
+
+    @color_effects.MovingAverage
+    def color(self):
+        return (self.main.state * self.main.red, self.main.state * self.main.green,
+                self.main.state * self.main.blue)

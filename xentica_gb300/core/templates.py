@@ -22,7 +22,8 @@ Shifting family (``XK_FAMILY_SHIFT``)
     sum of the neighbours' buffers, i.e. moved by one neighbour offset per
     generation (see :class:`ShiftTemplate`).
 
-EvoLife (``XK_FAMILY_EVOLIFE``) and mass transfer (``XK_FAMILY_MASS``)
+EvoLife (``XK_FAMILY_EVOLIFE``), mass transfer (``XK_FAMILY_MASS``), colour Life
+(``XK_FAMILY_LIFECOLOR``)
     matched statement by statement against the canonical programs of
     ``core/canonical.py``.
 
@@ -43,7 +44,7 @@ from xentica_gb300.core.topology.lattice import OrthogonalLattice
 from xentica_gb300.core.topology.neighborhood import OrthogonalNeighborhood
 from xentica_gb300.core.renderers import RendererPlain
 
-__all__ = ['match', 'LifeTemplate', 'ShiftTemplate', 'NoTemplate']
+__all__ = ['match', 'LifeTemplate', 'ShiftTemplate', 'LifeColorTemplate', 'NoTemplate']
 
 MAX_EXHAUSTIVE_NBR = 16
 
@@ -432,6 +433,42 @@ class MassTemplate:
         return d
 
 
+class LifeColorTemplate:
+    """Conway's Life whose cells carry three 8-bit colour channels inherited
+    from their neighbours (``canonical.LifeColorProgram``: the reference's
+    GameOfLifeColor, ``examples/game_of_life.py:112-159``), matched by
+    program fingerprint; a 2-D Moore lattice, torus or static border (the
+    border is not part of the traced programs), MovingAverage colours with
+    the model's fades."""
+
+    family = nat.XK_FAMILY_LIFECOLOR
+
+    def __init__(self, model):
+        from xentica_gb300.core import canonical
+        props = list(model.main.properties.values())
+        if [type(p).__name__ for p in props] != ["IntegerProperty"] * 4 or \
+                [p.bit_width for p in props] != [1, 8, 8, 8]:
+            raise NoTemplate("not one 1-bit and three 8-bit integer properties")
+        deltas, torus, border = _topology(model)
+        if model.topology.dimensions != 2 or len(deltas) != 8:
+            raise NoTemplate("colour Life kernel is 2-D Moore")
+        attrs = {name: model.__dict__[name] for name in ("fade_in", "fade_out", "smooth_factor")
+                 if name in model.__dict__}
+        programs = canonical.trace(canonical.LifeColorProgram, model.size, {}, attrs)
+        for key in ("emit", "absorb"):
+            if ir.fingerprint(programs[key]) != ir.fingerprint(model.programs[key]):
+                raise NoTemplate("%s differs from the colour Life program" % key)
+        self.model = model
+        self.color = _color_stmt(model.programs["absorb"])
+
+    def descriptor(self):
+        d = _base_desc(self.model, self.family)
+        info = self.color.extra
+        d.color_kind = nat.XK_COLOR_MOVING_AVERAGE
+        d.fade_in, d.fade_out, d.smooth = info["fade_in"], info["fade_out"], info["smooth"]
+        return d
+
+
 class VMTemplate:
     """Any other traced model: its emit and absorb programs, compiled to
     register bytecode (``core/vm.py``), run on the generic interpreter kernel
@@ -499,7 +536,7 @@ class VMTemplate:
         self._bound = vals
 
 
-FAMILIES = (LifeTemplate, ShiftTemplate, EvoLifeTemplate, MassTemplate, VMTemplate)
+FAMILIES = (LifeTemplate, ShiftTemplate, EvoLifeTemplate, MassTemplate, LifeColorTemplate, VMTemplate)
 
 
 def match(model):

@@ -138,7 +138,7 @@ extern "C" int xk_device_info(char *buf, int32_t len)
 // ---------------------------------------------------------------------------
 // model object
 
-enum { LAYOUT_BITS2D = 1, LAYOUT_BYTES = 2, LAYOUT_CELLS64 = 3, LAYOUT_MASS = 4, LAYOUT_VM = 5 };
+enum { LAYOUT_BITS2D = 1, LAYOUT_BYTES = 2, LAYOUT_CELLS64 = 3, LAYOUT_MASS = 4, LAYOUT_VM = 5, LAYOUT_LCOLOR = 6 };
 
 // largest float t with (double)u < p  <=>  u <= t for every float u
 static float below_threshold(double p)
@@ -163,7 +163,7 @@ struct xk_model {
     uint8_t *bytes[2] = {nullptr, nullptr};
     uint64_t *cells64[2] = {nullptr, nullptr};  // EvoLife: reference layout, ping-pong
     float mut_thresh = 0.f;
-    uint32_t *cells32[2] = {nullptr, nullptr};  // mass transfer: reference layout, ping-pong
+    uint32_t *cells32[2] = {nullptr, nullptr};  // mass transfer, colour Life: reference layout, ping-pong
     uint32_t *proj = nullptr;                   // mass: colour sum of every (x, y) column
     uint32_t *proj2 = nullptr;                  // mass: the second buffer of xk_step_frames
     int proj_valid = 0;
@@ -447,8 +447,14 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
     const int64_t n = cells_of(d);
     XK_REQUIRE(n <= (1LL << 40), XK_ERR_ARG, "lattice of %lld cells too large", (long long)n);
     XK_REQUIRE(d.family == XK_FAMILY_LIFE || d.family == XK_FAMILY_EVOLIFE ||
-                   d.family == XK_FAMILY_MASS || d.family == XK_FAMILY_VM || d.family == XK_FAMILY_SHIFT,
+                   d.family == XK_FAMILY_MASS || d.family == XK_FAMILY_VM || d.family == XK_FAMILY_SHIFT ||
+                   d.family == XK_FAMILY_LIFECOLOR,
                XK_ERR_UNSUPPORTED, "model family %d has no kernel in this library", d.family);
+    if (d.family == XK_FAMILY_LIFECOLOR)
+        XK_REQUIRE(is_moore2d(d) && d.state_bytes == 4 &&
+                       (d.color_kind == XK_COLOR_NONE || d.color_kind == XK_COLOR_MOVING_AVERAGE),
+                   XK_ERR_ARG, "colour Life needs a 2-D Moore lattice of 32-bit cells and MovingAverage "
+                   "colours (or none)");
     if (d.family == XK_FAMILY_SHIFT)
         XK_REQUIRE(d.rule0 < (uint32_t)d.nbr, XK_ERR_ARG, "shifting family: neighbour %u of %d",
                    d.rule0, d.nbr);
@@ -510,6 +516,11 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
             XK_TRY(cudaMemsetAsync(m->cells32[0], 0, bytes, m->stream));
             XK_TRY(cudaMemsetAsync(m->cells32[1], 0, bytes, m->stream));
             XK_TRY(cudaMalloc(&m->proj, (size_t)d.size[0] * d.size[1] * 4));
+        } else if (d.family == XK_FAMILY_LIFECOLOR) {
+            m->layout = LAYOUT_LCOLOR;
+            XK_TRY(cudaMalloc(&m->cells32[0], (size_t)n * 4));
+            XK_TRY(cudaMalloc(&m->cells32[1], (size_t)n * 4));
+            XK_TRY(cudaMemsetAsync(m->cells32[0], 0, (size_t)n * 4, m->stream));
         } else if (d.family == XK_FAMILY_EVOLIFE) {
             m->layout = LAYOUT_CELLS64;
             XK_TRY(cudaMalloc(&m->cells64[0], (size_t)n * 8));
@@ -540,7 +551,8 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
             XK_TRY(cudaMalloc(&m->bytes[1], bytes));
             XK_TRY(cudaMemsetAsync(m->bytes[0], 0, bytes, m->stream));
         }
-        if (m->layout != LAYOUT_CELLS64 && m->layout != LAYOUT_MASS && m->layout != LAYOUT_VM)
+        if (m->layout != LAYOUT_CELLS64 && m->layout != LAYOUT_MASS && m->layout != LAYOUT_VM &&
+            m->layout != LAYOUT_LCOLOR)
             XK_TRY(cudaMalloc(&m->stage, (size_t)n * d.state_bytes + 16));
         XK_TRY(cudaMalloc(&m->col, (size_t)n * 3 * sizeof(int32_t)));
         XK_TRY(cudaMemsetAsync(m->col, 0, (size_t)n * 3 * sizeof(int32_t), m->stream));
@@ -571,8 +583,9 @@ extern "C" int xk_upload(xk_model *m, const void *host_main, int64_t ncells)
     XK_REQUIRE(ncells == m->n, XK_ERR_ARG, "xk_upload: %lld cells given, model has %lld",
                (long long)ncells, (long long)m->n);
     const int esz = m->d.state_bytes;
-    if (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_MASS || m->layout == LAYOUT_VM) {
-        void *dst = m->layout == LAYOUT_MASS ? (void *)m->cells32[m->cur]
+    if (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_MASS || m->layout == LAYOUT_VM ||
+        m->layout == LAYOUT_LCOLOR) {
+        void *dst = m->layout == LAYOUT_MASS || m->layout == LAYOUT_LCOLOR ? (void *)m->cells32[m->cur]
                     : m->layout == LAYOUT_VM ? (void *)m->fld : (void *)m->cells64[m->cur];
         if (m->layout == LAYOUT_MASS) {
             // W cells per row into rows of the pitch; the padding keeps its 0s
@@ -628,8 +641,9 @@ extern "C" int xk_download(xk_model *m, void *host_main, int64_t ncells)
     XK_REQUIRE(ncells == m->n, XK_ERR_ARG, "xk_download: %lld cells given, model has %lld",
                (long long)ncells, (long long)m->n);
     const int esz = m->d.state_bytes;
-    if (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_MASS || m->layout == LAYOUT_VM) {
-        const void *src = m->layout == LAYOUT_MASS ? (const void *)m->cells32[m->cur]
+    if (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_MASS || m->layout == LAYOUT_VM ||
+        m->layout == LAYOUT_LCOLOR) {
+        const void *src = m->layout == LAYOUT_MASS || m->layout == LAYOUT_LCOLOR ? (const void *)m->cells32[m->cur]
                           : m->layout == LAYOUT_VM ? (const void *)m->fld
                                                    : (const void *)m->cells64[m->cur];
         if (m->layout == LAYOUT_MASS) {
@@ -664,7 +678,7 @@ extern "C" int xk_download(xk_model *m, void *host_main, int64_t ncells)
 // write the colours implied by the state into m->col
 static int materialize_colors(xk_model *m)
 {
-    if (m->layout == LAYOUT_VM) return XK_OK;   // absorb writes the colours
+    if (m->layout == LAYOUT_VM || m->layout == LAYOUT_LCOLOR) return XK_OK;   // the steps write the colours
     if (m->layout == LAYOUT_MASS) {
         XK_CUDA(xk_mass_colors(m->cells32[m->cur], m->col, m->d, m->stream));
         return XK_OK;
@@ -772,7 +786,7 @@ static int step_prepare(xk_model *m, int64_t nsteps)
         XK_CUDA(cudaMemsetAsync(m->totals, 0, (size_t)nsteps * sizeof(unsigned long long), m->stream));
         return XK_OK;
     }
-    if (m->layout == LAYOUT_VM || m->layout == LAYOUT_CELLS64) return XK_OK;
+    if (m->layout == LAYOUT_VM || m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_LCOLOR) return XK_OK;
     const bool colors_free = colors_free_of(m);
     if (!colors_free) {
         int rc = materialize_colors(m);
@@ -819,6 +833,14 @@ static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *fram
         for (int64_t g = 0; g < count; ++g) {
             XK_CUDA(xk_evolife_step(m->cells64[m->cur], m->cells64[1 - m->cur], m->col, m->d,
                                     m->mut_thresh, m->stream, frame, m->d.render_smooth));
+            m->cur = 1 - m->cur;
+        }
+        return XK_OK;
+    }
+    if (m->layout == LAYOUT_LCOLOR) {
+        for (int64_t g = 0; g < count; ++g) {
+            XK_CUDA(xk_lifecolor_step(m->cells32[m->cur], m->cells32[1 - m->cur], m->col, m->d, m->stream,
+                                      frame, m->d.render_smooth));
             m->cur = 1 - m->cur;
         }
         return XK_OK;
@@ -1155,8 +1177,9 @@ extern "C" int xk_step_frames(xk_model *m, int64_t nsteps, int32_t width, int32_
             }
         }
     }
-    // EvoLife viewed whole at zoom 1: the step kernel writes the frame
-    const bool fused = m->layout == LAYOUT_CELLS64 && m->d.color_kind != XK_COLOR_NONE &&
+    // EvoLife or colour Life viewed whole at zoom 1: the step kernel writes the frame
+    const bool fused = (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_LCOLOR) &&
+                       m->d.color_kind != XK_COLOR_NONE &&
                        m->d.ndim == 2 && m->d.proj_axis0 == 0 && m->d.proj_axis1 == 1 && zoom == 1 &&
                        dx == 0 && dy == 0 && width == m->d.size[0] && height == m->d.size[1];
     // mass transfer viewed whole at zoom 1 along z: the step kernel sums the

@@ -263,6 +263,11 @@ cudaError_t xk_evolife_step(const uint64_t *src, uint64_t *dst, int32_t *col, co
                             float mut_thresh, cudaStream_t s, uint8_t *frame = nullptr,
                             int frame_smooth = 0);
 
+// Life with inherited colour channels (lifecolor.cu): one generation, the
+// colours updated, and (frame) the zoom-1 frame as for EvoLife
+cudaError_t xk_lifecolor_step(const uint32_t *src, uint32_t *dst, int32_t *col, const xk_desc &d,
+                              cudaStream_t s, uint8_t *frame = nullptr, int frame_smooth = 0);
+
 // Programmatic dependent launch for kernels that run once per generation: the
 // launch may begin while the previous kernel in the stream finishes, and the
 // kernel calls xk_grid_dep_wait() before its first global-memory access
