@@ -2,7 +2,8 @@
 
 The stored programs of ``tests/golden/vm_examples.npz`` (see
 ``test_vm_examples_cpu``) run through the C-ABI, bit-exact against the
-checksums of the reference's own generated kernels."""
+checksums of the reference's own generated kernels, as stored and
+optimised."""
 import binascii
 import ctypes
 
@@ -15,9 +16,15 @@ from tests.test_vm_examples_cpu import _cases, load_case
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("optimised", [False, True])
 @pytest.mark.parametrize("name", _cases())
-def test_reference_example_on_the_interpreter(name):
+def test_reference_example_on_the_interpreter(name, optimised):
+    """As stored, and after the compiler's straight-line optimisation (the
+    form models compile to)."""
     desc, programs, c = load_case(name)
+    if optimised:
+        from xentica_gb300.core import vm
+        programs = [vm.optimize(code, consts) for code, consts, _ in programs]
     lib = nat.load()
     h = ctypes.c_void_p()
     nat.check(lib.xk_model_create(ctypes.byref(desc), ctypes.byref(h)), "xk_model_create")

@@ -44,3 +44,25 @@ def test_archive_replays_on_the_cpu_executor():
         vm_cpu.replay(desc, programs, c["params"], fld, col, int(c["steps"]))
         assert binascii.crc32(fld[:n].tobytes()) == int(c["cells_crc"]), name
         assert binascii.crc32(col.tobytes()) == int(c["colors_crc"]), name
+
+
+def test_optimised_archive_replays_on_the_cpu_executor():
+    """The stored bytecode after the compiler's straight-line optimisation
+    (value numbering, constant conversions folded, dead values dropped,
+    registers re-allocated): fewer instructions, the same checksums."""
+    from tests import vm_cpu
+    from xentica_gb300.core import vm
+    for name in _cases():
+        desc, programs, c = load_case(name)
+        opt = []
+        for code, consts, nregs in programs:
+            o_code, o_consts, o_nregs = vm.optimize(code, consts)
+            assert len(o_code) <= len(code) and o_nregs <= max(nregs, 1)
+            opt.append((o_code, o_consts, o_nregs))
+        n = c["init"].size
+        fld = np.zeros(n * (desc.nbr + 1) + 1, dtype=c["init"].dtype)
+        fld[:n] = c["init"]
+        col = c["init_col"].copy()
+        vm_cpu.replay(desc, opt, c["params"], fld, col, int(c["steps"]))
+        assert binascii.crc32(fld[:n].tobytes()) == int(c["cells_crc"]), name
+        assert binascii.crc32(col.tobytes()) == int(c["colors_crc"]), name

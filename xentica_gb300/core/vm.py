@@ -20,7 +20,7 @@ import numpy as np
 from xentica_gb300.core import ir
 from xentica_gb300.core.exceptions import XenticaException
 
-__all__ = ['compile_program', 'VmProgram', 'TYPE_CODES', 'type_code', 'pack_value']
+__all__ = ['compile_program', 'optimize', 'VmProgram', 'TYPE_CODES', 'type_code', 'pack_value']
 
 # type codes shared with csrc/vm.cu
 TYPE_CODES = {"bool": 0, "unsigned char": 1, "unsigned short": 2, "int": 3, "unsigned int": 4,
@@ -265,6 +265,135 @@ class _Compiler:
             raise XenticaException("interpreter: statement %s" % st.op)
 
 
+# -- optimisation -----------------------------------------------------------
+# The compiler above emits one instruction per C operation and conversion, a
+# move per assignment and a constant load per literal; the traced programs
+# unpack and repack every field of every buffer.  The programs are straight
+# lines (no branches), so every register value can be numbered: each
+# instruction result becomes a value, a move only renames one, equal pure
+# operations on equal values (constant loads included) share one value, an
+# integer conversion of a constant becomes a constant, values nothing stored
+# or coloured depends on are dropped, and registers are allocated again over
+# the live ranges that remain.  Loads are shared only up to the next store.
+
+_BINARY = set(range(OP["+"], OP["!="] + 1))
+_SIDE = {OP["store"], OP["color"]}
+_CODE_TYPES = {v: k for k, v in TYPE_CODES.items()}
+_INT_CODES = {TYPE_CODES[n] for n in ("bool", "unsigned char", "unsigned short", "int", "unsigned int",
+                                      "long", "unsigned long")}
+
+
+def _reg_fields(op):
+    """The instruction fields that name registers (the others are immediates)."""
+    if op in _BINARY:
+        return ("a", "b")
+    if op in (OP["sel"], OP["color"]):
+        return ("a", "b", "c")
+    if op in (OP["const"], OP["param"], OP["load"]):
+        return ()
+    return ("a", )    # mov, cvt, neg, ~, abs, f2i, i2f, popc, exp, store
+
+
+def _image_value(image, code):
+    """The integer a register image of integer type ``code`` holds."""
+    image = int(image)
+    if code in (TYPE_CODES["int"], TYPE_CODES["long"]) and image >> 63:
+        return image - (1 << 64)
+    return image
+
+
+def optimize(code, consts):
+    """Straight-line value numbering, constant conversion folding, dead-value
+    removal and register re-allocation of compiled instructions; returns
+    ``(code, consts, nregs)`` computing the same stores and colours."""
+    consts = [int(c) for c in consts]
+    const_slot = {}
+    for slot, c in enumerate(consts):
+        const_slot.setdefault(c, slot)
+    nodes = []            # (op, ty, arg values, immediates)
+    cur = {}              # register -> value it holds
+    table = {}            # (op, ty, args, immediates) -> value
+    load_keys = []
+    for ins in code:
+        op, ty = int(ins["op"]), int(ins["ty"])
+        fields = _reg_fields(op)
+        args = tuple(cur[int(ins[f])] for f in fields)
+        imm = tuple(int(ins[f]) if f not in fields else -1 for f in ("a", "b", "c"))
+        if op == OP["mov"]:
+            cur[int(ins["dst"])] = args[0]
+            continue
+        if op in _SIDE:
+            nodes.append((op, ty, args, imm))
+            if op == OP["store"]:
+                for k in load_keys:
+                    table.pop(k, None)
+                load_keys = []
+            continue
+        if op == OP["cvt"]:
+            src = nodes[args[0]]
+            frm = imm[1]
+            if frm == ty:
+                cur[int(ins["dst"])] = args[0]
+                continue
+            if src[0] == OP["const"] and frm in _INT_CODES and ty in _INT_CODES:
+                value = _image_value(consts[src[3][0]], frm)
+                image = pack_value(value, ir.ctype_of(_CODE_TYPES[ty]))
+                if image not in const_slot:
+                    const_slot[image] = len(consts)
+                    consts.append(image)
+                op, args, imm = OP["const"], (), (const_slot[image], -1, -1)
+        if op == OP["const"]:
+            imm = (const_slot.get(consts[imm[0]], imm[0]), -1, -1)
+        key = (op, ty, args, imm)
+        vid = table.get(key)
+        if vid is None:
+            vid = len(nodes)
+            nodes.append(key)
+            table[key] = vid
+            if op == OP["load"]:
+                load_keys.append(key)
+        cur[int(ins["dst"])] = vid
+    # values the stores and colours depend on
+    live = [False] * len(nodes)
+    stack = [i for i, n in enumerate(nodes) if n[0] in _SIDE]
+    while stack:
+        i = stack.pop()
+        if live[i]:
+            continue
+        live[i] = True
+        stack.extend(nodes[i][2])
+    last = {}
+    for i, n in enumerate(nodes):
+        if live[i]:
+            for a in n[2]:
+                last[a] = i
+    reg_of, free, nregs, out = {}, [], 0, []
+    for i, (op, ty, args, imm) in enumerate(nodes):
+        if not live[i]:
+            continue
+        regs = [reg_of[a] for a in args]
+        for a in set(args):
+            if last[a] == i:
+                free.append(reg_of[a])
+        dst = 0
+        if op not in _SIDE:
+            if free:
+                dst = free.pop()
+            else:
+                dst, nregs = nregs, nregs + 1
+            reg_of[i] = dst
+        fields = _reg_fields(op)
+        vals = {"a": 0, "b": 0, "c": 0}
+        it = iter(regs)
+        for k, f in enumerate(("a", "b", "c")):
+            vals[f] = next(it) if f in fields else max(imm[k], 0)
+        out.append((op, ty, dst, vals["a"], vals["b"], vals["c"], 0))
+    if nregs > MAX_REGS:
+        raise XenticaException("model needs more than %d interpreter registers" % MAX_REGS)
+    code = np.array(out, dtype=INS_DTYPE) if out else np.zeros(0, dtype=INS_DTYPE)
+    return code, np.array(consts or [0], dtype=np.uint64), max(nregs, 1)
+
+
 def compile_program(program, params=None):
     """Compile a traced :class:`ir.Program` into a :class:`VmProgram`.
 
@@ -277,4 +406,5 @@ def compile_program(program, params=None):
         comp.stmt(st)
     code = np.array(comp.code, dtype=INS_DTYPE) if comp.code else np.zeros(0, dtype=INS_DTYPE)
     consts = np.array(comp.consts, dtype=np.uint64) if comp.consts else np.zeros(1, dtype=np.uint64)
-    return VmProgram(code, consts, max(comp.nregs, 1), comp.params, comp.colors)
+    code, consts, nregs = optimize(code, consts)
+    return VmProgram(code, consts, nregs, comp.params, comp.colors)
