@@ -26,11 +26,11 @@ Reported (one JSON line on rank 0):
           launch), EvoLife 1920x1080 with a rendered frame every generation,
           mass transfer 256^3 with a projection frame and the total checked
           every generation, the serving loop (Poisson arrivals, p50/p99
-          latency, a sweep of offered loads), ShiftingSands and GameOfLifeColor
-          1920x1080 with a frame every generation.  ``--extras none`` leaves
-          them out.
+          latency, a sweep of offered loads), ShiftingSands, GameOfLifeColor
+          1920x1080 with a frame every generation and NoiseTV 1920x1080.
+          ``--extras none`` leaves them out.
 
-``--workload life512 | evolife | mass | serve | sands | lifecolor`` prints one of the extras as
+``--workload life512 | evolife | mass | serve | sands | lifecolor | noise`` prints one of the extras as
 its own line (with the given ``--steps``/``--warmup``).  ``--impl reference``
 times the reference's own kernels (its translator's LifelikeCA source compiled
 for the CPU, ``oracle/_ref``) on the host cores instead, with the same metric.
@@ -74,12 +74,12 @@ def parse():
     ap.add_argument("--quantum", type=int, default=128, help="serve: generations per round")
     ap.add_argument("--sweep", default="", help="serve: extra offered loads after the main run, "
                                                 "comma-separated (e.g. 0.3,0.5,0.9)")
-    ap.add_argument("--extras", default="life512,evolife,mass,serve,sands,lifecolor",
+    ap.add_argument("--extras", default="life512,evolife,mass,serve,sands,lifecolor,noise",
                     help="default run: the other configurations measured after the ensemble "
                          "(comma-separated, or 'none')")
     ap.add_argument("--serve-budget-gb", type=int, default=16, help="serve: HBM budget (GiB)")
     ap.add_argument("--workload", choices=("ensemble", "life512", "evolife", "mass", "serve",
-                                           "sands", "lifecolor"),
+                                           "sands", "lifecolor", "noise"),
                     default="ensemble",
                     help="ensemble: the batched Life-like ensemble (default); life512: Conway's "
                          "Life 512x512 torus, 1000 generations per step; evolife: EvoLife "
@@ -512,9 +512,11 @@ def run_ours(args, dist):
         small.cpu_seconds = 4.0
         for name in extras:
             fn = {"life512": life512_line, "evolife": evolife_line, "mass": mass_line,
-                  "serve": serve_line, "sands": sands_line, "lifecolor": lifecolor_line}[name]
+                  "serve": serve_line, "sands": sands_line, "lifecolor": lifecolor_line,
+                  "noise": noise_line}[name]
             steps, warmup = {"life512": (10, 3), "evolife": (100, 3), "mass": (5, 3),
-                             "serve": (None, 3), "sands": (10, 3), "lifecolor": (10, 3)}[name]
+                             "serve": (None, 3), "sands": (10, 3), "lifecolor": (10, 3),
+                             "noise": (5, 3)}[name]
             small.steps, small.warmup = steps, warmup
             if name == "serve" and not small.sweep:
                 small.sweep = "0.3,0.5,0.9"
@@ -821,6 +823,126 @@ def lifecolor_line(args, dist):
                                           "render, oracle (OpenMP)"}
         return line
     return None
+
+
+def noise_line(args, dist):
+    """NoiseTV 1920x1080 (examples/noisetv.py:13-31): K steps of 1000
+    generations (cells are independent, so one launch runs up to 1024
+    generations of a cell in registers), and the viewer's form, 100
+    generations each with its zoom-1 frame; the same model on the generic
+    interpreter beside it; parity: the oracle from the GPU state, 1000 more
+    generations and two with frames."""
+    from xentica_gb300 import build as xk_build
+    from xentica_gb300 import _native as nat
+    from xentica_gb300 import core, seeds
+    from xentica_gb300.core import canonical
+    import torch
+    xk_build.build()
+    nat.set_device(dist.local)
+    lib = nat.load()
+
+    class Noise1080(core.Experiment):
+        word = "PSHSHSHSH! 1920X1080"
+        size = (1920, 1080)
+        zoom = 1
+        pos = [0, 0]
+        seed = seeds.patterns.PrimordialSoup(vals={"rng": seeds.random.RandInt(0, 2 ** 16 - 1)})
+
+    model = canonical.NoiseProgram(Noise1080)
+    assert type(model.gpu.template).__name__ == "NoiseTemplate"
+    W, H = model.size
+    n = model.cells_num
+    gens = 1000
+    for _ in range(args.warmup):
+        model.gpu.step(gens)
+    clocks = Clocks(dist.local)
+    time.sleep(0.6)
+    dist.barrier()
+    lib.xk_range_push(b"timed")
+    step_ms = []
+    for _ in range(args.steps):
+        model.gpu.step(gens)
+        step_ms.append(lib.xk_last_step_ms())
+    lib.xk_range_pop()
+    dist.barrier()
+    clk = clocks.stop()
+    dev_s = dist.max(sum(step_ms) / 1000.0)
+    value = float(n) * gens * args.steps * dist.world / dev_s
+    # the viewer's form: 100 generations, each with its frame (one launch each)
+    model.set_viewport((W, H))
+    fb = W * H * 3
+    frames_dev = torch.empty(100 * fb, dtype=torch.uint8, device="cuda:%d" % dist.local)
+    model.gpu.step_frames(100, W, H, 1, 0, 0, frames_dev.data_ptr(), on_device=True)
+    frame_ms = model.gpu.step_frames(100, W, H, 1, 0, 0, frames_dev.data_ptr(), on_device=True)
+    cells = model.gpu.arrays.cells.get()[:n].copy()
+    colors = model.gpu.arrays.colors.get()
+    os.environ["XENTICA_GB300_TEMPLATE"] = "vm"
+    try:
+        vm_model = canonical.NoiseProgram(Noise1080)
+    finally:
+        del os.environ["XENTICA_GB300_TEMPLATE"]
+    vm_model.gpu.load(cells, colors)
+    vm_model.gpu.step(10)
+    vm_model.gpu.step(100)
+    vm_ms = lib.xk_last_step_ms()
+    del vm_model
+    peak, peak_kind = measured_peak()
+    bytes_per_update = 2 * 2 + 12 * 2        # uint16 state r+w, int3 colour r+w
+    achieved = bytes_per_update * n * gens / (statistics.mean(step_ms) / 1000.0) / 1e9
+    line = {"metric": "cell-updates/s (NoiseTV)", "value": value, "unit": "cell-updates/s",
+            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dev_s * 1000 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u16", "data": "synthetic (seeded PrimordialSoup: uniform "
+                                                           "random states)",
+            "config": {"workload": "NoiseTV 1920x1080, MovingAverage colours, 1000 generations "
+                                   "per step (up to 1024 per launch)",
+                       "l2": "state + colours (29 MB) fit in L2"},
+            "frames": {"value": float(n) * 100 / (frame_ms / 1000.0), "unit": "cell-updates/s",
+                       "note": "100 generations, each with its 1920x1080 uint8 frame written by the "
+                               "step kernel (one launch per generation)"},
+            "interpreter": {"value": float(n) * 100 / (vm_ms / 1000.0), "unit": "cell-updates/s",
+                            "note": "the same model on the generic interpreter, 100 generations"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "kernel": "xk_k_noise, up to 1024 generations per launch",
+                         "note": "B_alg = 28 B per cell-update (uint16 state and int3 colour read and "
+                                 "written); a launch reads and writes each cell once for up to 1024 "
+                                 "generations, so frac > 1 is reference-format effective"},
+            "gpu_launches": args.steps * ((gens + 1023) // 1024), "clocks": clk}
+    if dist.rank == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        topo = O.Topology(model.size)
+        fld = topo.field(cells, np.uint16)
+        col = colors.copy()
+        d = model.gpu.template.descriptor()
+        cc = O._color(True, d.fade_in, d.fade_out, d.smooth)
+        model.gpu.load(cells, colors)
+        model.gpu.step(gens)
+        t0 = time.perf_counter()
+        O.noise_run(topo, fld, col, gens, color=cc)
+        el = time.perf_counter() - t0
+        exact = bool(np.array_equal(model.gpu.arrays.cells.get()[:n], fld[:n])) and \
+            bool(np.array_equal(model.gpu.arrays.colors.get(), col))
+        got = model.step_frames(2)
+        for g in range(2):
+            O.noise_run(topo, fld, col, 1, color=cc)
+            img = O.render(topo, col, W, H, smooth=d.render_smooth).astype(np.uint8)
+            exact &= bool(np.array_equal(got[g], img))
+        line["parity"] = {"checked_generations": gens + 2, "bit_exact": exact,
+                          "note": "oracle from the GPU state: 1000 generations, then two with "
+                                  "frames"}
+        line["cpu_baseline"] = {"value": n * gens / el, "unit": "cell-updates/s",
+                                "cores": os.cpu_count(), "kind": "port",
+                                "sample": "1000 generations of the full lattice, oracle (OpenMP)"}
+        return line
+    return None
+
+
+def run_noise(args, dist):
+    line = noise_line(args, dist)
+    if line is not None:
+        print(json.dumps(line), flush=True)
 
 
 def run_lifecolor(args, dist):
@@ -1490,6 +1612,8 @@ def main():
             run_sands(args, dist)
         elif args.workload == "lifecolor":
             run_lifecolor(args, dist)
+        elif args.workload == "noise":
+            run_noise(args, dist)
         else:
             run_ours(args, dist)
     finally:

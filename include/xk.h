@@ -43,9 +43,11 @@ enum {
  * XK_FAMILY_LIFECOLOR: Conway's Life whose cells carry three 8-bit colour
  * channels inherited from their neighbours (GameOfLifeColor,
  * examples/game_of_life.py:112-159): a 2-D Moore lattice of uint32 cells,
- * torus or static border, MovingAverage colours or none. */
+ * torus or static border, MovingAverage colours or none.
+ * XK_FAMILY_NOISE: per-cell noise (NoiseTV, examples/noisetv.py:13-31), one
+ * 16-bit RandomProperty per cell advanced twice a generation, any lattice. */
 enum { XK_FAMILY_LIFE = 1, XK_FAMILY_EVOLIFE = 2, XK_FAMILY_MASS = 3, XK_FAMILY_VM = 4,
-       XK_FAMILY_SHIFT = 5, XK_FAMILY_LIFECOLOR = 6 };
+       XK_FAMILY_SHIFT = 5, XK_FAMILY_LIFECOLOR = 6, XK_FAMILY_NOISE = 7 };
 enum { XK_COLOR_NONE = 0, XK_COLOR_PLAIN = 1, XK_COLOR_MOVING_AVERAGE = 2 };
 
 /* Model descriptor filled by the translator (xentica_gb300/core/templates.py)

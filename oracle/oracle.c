@@ -436,6 +436,26 @@ void xo_evolife_step(const xo_topo *t, uint64_t *fld, int32_t *col,
 }
 
 /* ------------------------------------------------------------------------ */
+/* NoiseTV (examples/noisetv.py:13-31): a uint16 cell holding one
+ * RandomProperty; emit does nothing; absorb reads main.rng (one advance of
+ * x = (x * 58321 + 11113) % 65535, properties.py:638-660) and the colour
+ * reads its uniform (a second advance), (unsigned)((float)x / 65535 * 255)
+ * on every channel; the cell stores x after both.  No neighbour is read. */
+void xo_noise_step(const xo_topo *t, uint16_t *fld, int32_t *col, const xo_color *cc, int threads)
+{
+    const int64_t n = xo_cells(t);
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        uint32_t x = fld[i];
+        x = xo_lcg(xo_lcg(x));
+        const float u = (float)x / 65535.0f;
+        const int v = (int)(unsigned int)(u * 255.0f);
+        xo_color_write(col, i, v, v, v, cc);
+        fld[i] = (uint16_t)x;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
 /* RendererPlain.render_code (renderers.py:220-270): pixel i of a width x
  * height viewport; axes (a0, a1) are projected, every other axis is summed
  * in nested-loop order (outer loop = lowest axis index). */

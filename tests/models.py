@@ -149,6 +149,50 @@ class GameOfLifeColorPlus2(GameOfLifeColor):
         self.main.blue = blue_sum * self.main.state
 
 
+class NoiseTV(core.CellularAutomaton):
+    """Per-cell pseudo-random noise (examples/noisetv.py:13-31)."""
+
+    rng = core.RandomProperty()
+
+    class Topology:
+        dimensions = 2
+        lattice = core.OrthogonalLattice()
+        neighborhood = core.MooreNeighborhood()
+        border = core.TorusBorder()
+
+    def emit(self):
+        """Nothing is sent."""
+
+    def absorb(self):
+        return self.main.rng
+
+    @color_effects.MovingAverage
+    def color(self):
+        val = xmath.int(self.main.rng.uniform * 255)
+        return (val, val, val)
+
+
+class NoiseTV3D(NoiseTV):
+    """The same noise on a 3-D von Neumann lattice with a static border."""
+
+    class Topology:
+        dimensions = 3
+        lattice = core.OrthogonalLattice()
+        neighborhood = core.VonNeumannNeighborhood()
+        border = core.StaticBorder(7)
+
+
+class NoiseExperiment(core.Experiment):
+    word = "PSHSHSHSH!"
+    size = (64, 48)
+    zoom = 1
+    pos = [0, 0]
+    fade_in = 40
+    fade_out = 25
+    smooth_factor = 1
+    seed = seeds.patterns.PrimordialSoup(vals={"rng": seeds.random.RandInt(0, 2 ** 16 - 1)})
+
+
 class GOLColorExperiment(core.Experiment):
     word = "XENTICA IN COLOR"
     size = (96, 64)

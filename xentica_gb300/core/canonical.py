@@ -213,3 +213,29 @@ class LifeColorProgram(core.CellularAutomaton):
     def color(self):
         return (self.main.state * self.main.red, self.main.state * self.main.green,
                 self.main.state * self.main.blue)
+
+
+class NoiseProgram(core.CellularAutomaton):
+    """Per-cell noise (the reference's NoiseTV, ``examples/noisetv.py:13-31``):
+    no buffer is written; each generation reads the cell's RandomProperty
+    once in absorb and once more for the colour's uniform draw, each read
+    one advance of its stream."""
+
+    rng = core.RandomProperty()
+
+    class Topology:
+        dimensions = 2
+        lattice = core.OrthogonalLattice()
+        neighborhood = core.MooreNeighborhood()
+        border = core.TorusBorder()
+
+    def emit(self):
+        """Nothing: a cell depends on no neighbour."""
+
+    def absorb(self):
+        return self.main.rng      # the read advances the stream
+
+    @color_effects.MovingAverage
+    def color(self):
+        grey = xmath.int(self.main.rng.uniform * 255)
+        return (grey, grey, grey)

@@ -23,7 +23,7 @@ Shifting family (``XK_FAMILY_SHIFT``)
     generation (see :class:`ShiftTemplate`).
 
 EvoLife (``XK_FAMILY_EVOLIFE``), mass transfer (``XK_FAMILY_MASS``), colour Life
-(``XK_FAMILY_LIFECOLOR``)
+(``XK_FAMILY_LIFECOLOR``) and noise (``XK_FAMILY_NOISE``)
     matched statement by statement against the canonical programs of
     ``core/canonical.py``.
 
@@ -44,7 +44,7 @@ from xentica_gb300.core.topology.lattice import OrthogonalLattice
 from xentica_gb300.core.topology.neighborhood import OrthogonalNeighborhood
 from xentica_gb300.core.renderers import RendererPlain
 
-__all__ = ['match', 'LifeTemplate', 'ShiftTemplate', 'LifeColorTemplate', 'NoTemplate']
+__all__ = ['match', 'LifeTemplate', 'ShiftTemplate', 'LifeColorTemplate', 'NoiseTemplate', 'NoTemplate']
 
 MAX_EXHAUSTIVE_NBR = 16
 
@@ -469,6 +469,37 @@ class LifeColorTemplate:
         return d
 
 
+class NoiseTemplate:
+    """Per-cell noise (``canonical.NoiseProgram``: the reference's NoiseTV,
+    ``examples/noisetv.py:13-31``), matched by program fingerprint: one
+    16-bit RandomProperty, nothing emitted, any lattice and border (no cell
+    reads another), MovingAverage colours with the model's fades."""
+
+    family = nat.XK_FAMILY_NOISE
+
+    def __init__(self, model):
+        from xentica_gb300.core import canonical
+        props = list(model.main.properties.values())
+        if [type(p).__name__ for p in props] != ["RandomProperty"]:
+            raise NoTemplate("not one RandomProperty")
+        _topology(model)
+        attrs = {name: model.__dict__[name] for name in ("fade_in", "fade_out", "smooth_factor")
+                 if name in model.__dict__}
+        programs = canonical.trace(canonical.NoiseProgram, model.size, {}, attrs)
+        for key in ("emit", "absorb"):
+            if ir.fingerprint(programs[key]) != ir.fingerprint(model.programs[key]):
+                raise NoTemplate("%s differs from the noise program" % key)
+        self.model = model
+        self.color = _color_stmt(model.programs["absorb"])
+
+    def descriptor(self):
+        d = _base_desc(self.model, self.family)
+        info = self.color.extra
+        d.color_kind = nat.XK_COLOR_MOVING_AVERAGE
+        d.fade_in, d.fade_out, d.smooth = info["fade_in"], info["fade_out"], info["smooth"]
+        return d
+
+
 class VMTemplate:
     """Any other traced model: its emit and absorb programs, compiled to
     register bytecode (``core/vm.py``), run on the generic interpreter kernel
@@ -536,7 +567,8 @@ class VMTemplate:
         self._bound = vals
 
 
-FAMILIES = (LifeTemplate, ShiftTemplate, EvoLifeTemplate, MassTemplate, LifeColorTemplate, VMTemplate)
+FAMILIES = (LifeTemplate, ShiftTemplate, EvoLifeTemplate, MassTemplate, LifeColorTemplate, NoiseTemplate,
+            VMTemplate)
 
 
 def match(model):

@@ -138,7 +138,8 @@ extern "C" int xk_device_info(char *buf, int32_t len)
 // ---------------------------------------------------------------------------
 // model object
 
-enum { LAYOUT_BITS2D = 1, LAYOUT_BYTES = 2, LAYOUT_CELLS64 = 3, LAYOUT_MASS = 4, LAYOUT_VM = 5, LAYOUT_LCOLOR = 6 };
+enum { LAYOUT_BITS2D = 1, LAYOUT_BYTES = 2, LAYOUT_CELLS64 = 3, LAYOUT_MASS = 4, LAYOUT_VM = 5, LAYOUT_LCOLOR = 6,
+       LAYOUT_NOISE = 7 };
 
 // largest float t with (double)u < p  <=>  u <= t for every float u
 static float below_threshold(double p)
@@ -164,6 +165,7 @@ struct xk_model {
     uint64_t *cells64[2] = {nullptr, nullptr};  // EvoLife: reference layout, ping-pong
     float mut_thresh = 0.f;
     uint32_t *cells32[2] = {nullptr, nullptr};  // mass transfer, colour Life: reference layout, ping-pong
+    uint16_t *cells16 = nullptr;                // noise: reference layout, updated in place
     uint32_t *proj = nullptr;                   // mass: colour sum of every (x, y) column
     uint32_t *proj2 = nullptr;                  // mass: the second buffer of xk_step_frames
     int proj_valid = 0;
@@ -385,6 +387,7 @@ static void free_model(xk_model *m)
         if (m->bytes[i]) cudaFree(m->bytes[i]);
         if (m->cells64[i]) cudaFree(m->cells64[i]);
         if (m->cells32[i]) cudaFree(m->cells32[i]);
+        if (i == 0 && m->cells16) cudaFree(m->cells16);
     }
     for (int i = 0; i < 2; ++i) {
         if (m->vm_code[i]) cudaFree(m->vm_code[i]);
@@ -448,8 +451,12 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
     XK_REQUIRE(n <= (1LL << 40), XK_ERR_ARG, "lattice of %lld cells too large", (long long)n);
     XK_REQUIRE(d.family == XK_FAMILY_LIFE || d.family == XK_FAMILY_EVOLIFE ||
                    d.family == XK_FAMILY_MASS || d.family == XK_FAMILY_VM || d.family == XK_FAMILY_SHIFT ||
-                   d.family == XK_FAMILY_LIFECOLOR,
+                   d.family == XK_FAMILY_LIFECOLOR || d.family == XK_FAMILY_NOISE,
                XK_ERR_UNSUPPORTED, "model family %d has no kernel in this library", d.family);
+    if (d.family == XK_FAMILY_NOISE)
+        XK_REQUIRE(d.state_bytes == 2 &&
+                       (d.color_kind == XK_COLOR_NONE || d.color_kind == XK_COLOR_MOVING_AVERAGE),
+                   XK_ERR_ARG, "noise needs 16-bit cells and MovingAverage colours (or none)");
     if (d.family == XK_FAMILY_LIFECOLOR)
         XK_REQUIRE(is_moore2d(d) && d.state_bytes == 4 &&
                        (d.color_kind == XK_COLOR_NONE || d.color_kind == XK_COLOR_MOVING_AVERAGE),
@@ -516,6 +523,10 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
             XK_TRY(cudaMemsetAsync(m->cells32[0], 0, bytes, m->stream));
             XK_TRY(cudaMemsetAsync(m->cells32[1], 0, bytes, m->stream));
             XK_TRY(cudaMalloc(&m->proj, (size_t)d.size[0] * d.size[1] * 4));
+        } else if (d.family == XK_FAMILY_NOISE) {
+            m->layout = LAYOUT_NOISE;
+            XK_TRY(cudaMalloc(&m->cells16, (size_t)n * 2));
+            XK_TRY(cudaMemsetAsync(m->cells16, 0, (size_t)n * 2, m->stream));
         } else if (d.family == XK_FAMILY_LIFECOLOR) {
             m->layout = LAYOUT_LCOLOR;
             XK_TRY(cudaMalloc(&m->cells32[0], (size_t)n * 4));
@@ -552,7 +563,7 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
             XK_TRY(cudaMemsetAsync(m->bytes[0], 0, bytes, m->stream));
         }
         if (m->layout != LAYOUT_CELLS64 && m->layout != LAYOUT_MASS && m->layout != LAYOUT_VM &&
-            m->layout != LAYOUT_LCOLOR)
+            m->layout != LAYOUT_LCOLOR && m->layout != LAYOUT_NOISE)
             XK_TRY(cudaMalloc(&m->stage, (size_t)n * d.state_bytes + 16));
         XK_TRY(cudaMalloc(&m->col, (size_t)n * 3 * sizeof(int32_t)));
         XK_TRY(cudaMemsetAsync(m->col, 0, (size_t)n * 3 * sizeof(int32_t), m->stream));
@@ -584,8 +595,9 @@ extern "C" int xk_upload(xk_model *m, const void *host_main, int64_t ncells)
                (long long)ncells, (long long)m->n);
     const int esz = m->d.state_bytes;
     if (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_MASS || m->layout == LAYOUT_VM ||
-        m->layout == LAYOUT_LCOLOR) {
+        m->layout == LAYOUT_LCOLOR || m->layout == LAYOUT_NOISE) {
         void *dst = m->layout == LAYOUT_MASS || m->layout == LAYOUT_LCOLOR ? (void *)m->cells32[m->cur]
+                    : m->layout == LAYOUT_NOISE ? (void *)m->cells16
                     : m->layout == LAYOUT_VM ? (void *)m->fld : (void *)m->cells64[m->cur];
         if (m->layout == LAYOUT_MASS) {
             // W cells per row into rows of the pitch; the padding keeps its 0s
@@ -642,8 +654,9 @@ extern "C" int xk_download(xk_model *m, void *host_main, int64_t ncells)
                (long long)ncells, (long long)m->n);
     const int esz = m->d.state_bytes;
     if (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_MASS || m->layout == LAYOUT_VM ||
-        m->layout == LAYOUT_LCOLOR) {
+        m->layout == LAYOUT_LCOLOR || m->layout == LAYOUT_NOISE) {
         const void *src = m->layout == LAYOUT_MASS || m->layout == LAYOUT_LCOLOR ? (const void *)m->cells32[m->cur]
+                          : m->layout == LAYOUT_NOISE ? (const void *)m->cells16
                           : m->layout == LAYOUT_VM ? (const void *)m->fld
                                                    : (const void *)m->cells64[m->cur];
         if (m->layout == LAYOUT_MASS) {
@@ -678,7 +691,8 @@ extern "C" int xk_download(xk_model *m, void *host_main, int64_t ncells)
 // write the colours implied by the state into m->col
 static int materialize_colors(xk_model *m)
 {
-    if (m->layout == LAYOUT_VM || m->layout == LAYOUT_LCOLOR) return XK_OK;   // the steps write the colours
+    if (m->layout == LAYOUT_VM || m->layout == LAYOUT_LCOLOR || m->layout == LAYOUT_NOISE)
+        return XK_OK;   // the steps write the colours
     if (m->layout == LAYOUT_MASS) {
         XK_CUDA(xk_mass_colors(m->cells32[m->cur], m->col, m->d, m->stream));
         return XK_OK;
@@ -786,7 +800,9 @@ static int step_prepare(xk_model *m, int64_t nsteps)
         XK_CUDA(cudaMemsetAsync(m->totals, 0, (size_t)nsteps * sizeof(unsigned long long), m->stream));
         return XK_OK;
     }
-    if (m->layout == LAYOUT_VM || m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_LCOLOR) return XK_OK;
+    if (m->layout == LAYOUT_VM || m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_LCOLOR ||
+        m->layout == LAYOUT_NOISE)
+        return XK_OK;
     const bool colors_free = colors_free_of(m);
     if (!colors_free) {
         int rc = materialize_colors(m);
@@ -834,6 +850,15 @@ static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *fram
             XK_CUDA(xk_evolife_step(m->cells64[m->cur], m->cells64[1 - m->cur], m->col, m->d,
                                     m->mut_thresh, m->stream, frame, m->d.render_smooth));
             m->cur = 1 - m->cur;
+        }
+        return XK_OK;
+    }
+    if (m->layout == LAYOUT_NOISE) {
+        // cells are independent: up to 1024 generations per launch (one with a frame)
+        for (int64_t g = 0; g < count;) {
+            const int gens = frame ? 1 : (int)std::min<int64_t>(1024, count - g);
+            XK_CUDA(xk_noise_step(m->cells16, m->col, m->d, m->n, gens, m->stream, frame, m->d.render_smooth));
+            g += gens;
         }
         return XK_OK;
     }
@@ -1178,7 +1203,7 @@ extern "C" int xk_step_frames(xk_model *m, int64_t nsteps, int32_t width, int32_
         }
     }
     // EvoLife or colour Life viewed whole at zoom 1: the step kernel writes the frame
-    const bool fused = (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_LCOLOR) &&
+    const bool fused = (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_LCOLOR || m->layout == LAYOUT_NOISE) &&
                        m->d.color_kind != XK_COLOR_NONE &&
                        m->d.ndim == 2 && m->d.proj_axis0 == 0 && m->d.proj_axis1 == 1 && zoom == 1 &&
                        dx == 0 && dy == 0 && width == m->d.size[0] && height == m->d.size[1];
