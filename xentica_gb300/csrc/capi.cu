@@ -387,8 +387,8 @@ static void free_model(xk_model *m)
         if (m->bytes[i]) cudaFree(m->bytes[i]);
         if (m->cells64[i]) cudaFree(m->cells64[i]);
         if (m->cells32[i]) cudaFree(m->cells32[i]);
-        if (i == 0 && m->cells16) cudaFree(m->cells16);
     }
+    if (m->cells16) cudaFree(m->cells16);
     for (int i = 0; i < 2; ++i) {
         if (m->vm_code[i]) cudaFree(m->vm_code[i]);
         if (m->vm_consts[i]) cudaFree(m->vm_consts[i]);
