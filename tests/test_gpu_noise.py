@@ -45,7 +45,8 @@ def test_random_states_vs_oracle(cls, size):
     assert type(model.gpu.template).__name__ == "NoiseTemplate"
     n = model.cells_num
     rng = np.random.RandomState(n)
-    cells = rng.randint(0, 65535, n).astype(np.uint16)          # 65534 included
+    cells = rng.randint(0, 65536, n).astype(np.uint16)          # 65535 (the seed's maximum) included
+    cells[:3] = 65535
     colors = rng.randint(-600, 600, 3 * n).astype(np.int32)
     model.gpu.load(cells, colors)
     topo = O.Topology(size, "moore" if len(size) == 2 else "von_neumann", None if len(size) == 2 else 7)
