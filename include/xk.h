@@ -98,6 +98,10 @@ int xk_download(xk_model *m, void *host_main, int64_t ncells);
 
 /* Replaces gpu.arrays.colors (int3 per cell, base.py:558, :659). */
 int xk_upload_colors(xk_model *m, const int32_t *host_col, int64_t ncells);
+/* Smallest and largest value of the last xk_upload_colors (out[0], out[1];
+ * 0, 0 before any): what a host needs to decide xk_set_color_mode without a
+ * pass of its own over the colours. */
+int xk_colors_range(const xk_model *m, int32_t out[2]);
 int xk_download_colors(xk_model *m, int32_t *host_col, int64_t ncells);
 
 /* Interactive rule of the Life-like family: the values the reference passes

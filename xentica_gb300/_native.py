@@ -84,6 +84,7 @@ SIGNATURES = {
     "xk_upload": (_I32, [_P, _P, _I64]),
     "xk_download": (_I32, [_P, _P, _I64]),
     "xk_upload_colors": (_I32, [_P, _P, _I64]),
+    "xk_colors_range": (_I32, [_P, _P]),
     "xk_download_colors": (_I32, [_P, _P, _I64]),
     "xk_life_set_rule": (_I32, [_P, _U32, _U32, _P]),
     "xk_set_color_mode": (_I32, [_P, _I32]),

@@ -90,7 +90,9 @@ class GPU:
         nat.check(self._lib.xk_upload_colors(self._handle, nat.ptr(colors), self.cells_num),
                   "xk_upload_colors")
         if hasattr(self.template, "history_free") and colors.size:
-            hf = self.template.history_free(self._rule[2], (int(colors.min()), int(colors.max())))
+            rng = (nat.ctypes.c_int32 * 2)()
+            nat.check(self._lib.xk_colors_range(self._handle, rng), "xk_colors_range")
+            hf = self.template.history_free(self._rule[2], (int(rng[0]), int(rng[1])))
             nat.check(self._lib.xk_set_color_mode(self._handle, int(hf)), "xk_set_color_mode")
 
     def __del__(self):

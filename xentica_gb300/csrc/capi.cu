@@ -166,6 +166,8 @@ struct xk_model {
     float mut_thresh = 0.f;
     uint32_t *cells32[2] = {nullptr, nullptr};  // mass transfer, colour Life: reference layout, ping-pong
     uint16_t *cells16 = nullptr;                // noise: reference layout, updated in place
+    int *col_range_d = nullptr;                 // device scratch of xk_upload_colors' range
+    int32_t col_range[2] = {0, 0};              // smallest and largest colour value of the last upload
     uint32_t *proj = nullptr;                   // mass: colour sum of every (x, y) column
     uint32_t *proj2 = nullptr;                  // mass: the second buffer of xk_step_frames
     int proj_valid = 0;
@@ -389,6 +391,7 @@ static void free_model(xk_model *m)
         if (m->cells32[i]) cudaFree(m->cells32[i]);
     }
     if (m->cells16) cudaFree(m->cells16);
+    if (m->col_range_d) cudaFree(m->col_range_d);
     for (int i = 0; i < 2; ++i) {
         if (m->vm_code[i]) cudaFree(m->vm_code[i]);
         if (m->vm_consts[i]) cudaFree(m->vm_consts[i]);
@@ -716,8 +719,21 @@ extern "C" int xk_upload_colors(xk_model *m, const int32_t *host_col, int64_t nc
     if (m->layout == LAYOUT_MASS) return XK_OK;
     XK_CUDA(cudaMemcpyAsync(m->col, host_col, (size_t)m->n * 3 * sizeof(int32_t),
                             cudaMemcpyHostToDevice, m->stream));
+    // the range of the uploaded values, for the host's colour bookkeeping
+    // (xk_colors_range), reduced on the device while the copy is fresh
+    if (!m->col_range_d) XK_CUDA(cudaMalloc(&m->col_range_d, 2 * sizeof(int)));
+    XK_CUDA(xk_colors_minmax(m->col, m->n * 3, m->col_range_d, m->stream));
+    XK_CUDA(cudaMemcpyAsync(m->col_range, m->col_range_d, 2 * sizeof(int), cudaMemcpyDeviceToHost, m->stream));
     XK_CUDA(cudaStreamSynchronize(m->stream));
     m->derived = 0;
+    return XK_OK;
+}
+
+extern "C" int xk_colors_range(const xk_model *m, int32_t out[2])
+{
+    XK_REQUIRE(m && out, XK_ERR_ARG, "xk_colors_range: null argument");
+    out[0] = m->col_range[0];
+    out[1] = m->col_range[1];
     return XK_OK;
 }
 

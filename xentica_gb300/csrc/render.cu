@@ -9,6 +9,8 @@
 // int.  Same operations, same order, same float rounding.  The uint8
 // instantiation stores the int's low byte: the frame the reference's render()
 // returns (img.get().astype(np.uint8), base.py:753).
+#include <climits>
+
 #include "xk_internal.cuh"
 
 template <typename T>
@@ -117,4 +119,34 @@ cudaError_t xk_render_colors_u8(const int32_t *col, uint8_t *img, const RenderGe
                                 int height, int zoom, int dx, int dy, cudaStream_t s)
 {
     return render_any<uint8_t>(col, img, g, width, height, zoom, dx, dy, s);
+}
+
+// smallest and largest of `count` colour values (out[0], out[1]), for the
+// colour bookkeeping after an upload
+__global__ void xk_k_colors_range(const int32_t *__restrict__ col, int64_t count, int *__restrict__ out)
+{
+    int lo = INT_MAX, hi = INT_MIN;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int v = col[i];
+        lo = v < lo ? v : lo;
+        hi = v > hi ? v : hi;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_down_sync(0xFFFFFFFFu, lo, o));
+        hi = max(hi, __shfl_down_sync(0xFFFFFFFFu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(out, lo);
+        atomicMax(out + 1, hi);
+    }
+}
+
+cudaError_t xk_colors_minmax(const int32_t *col, int64_t count, int *out, cudaStream_t s)
+{
+    const int init[2] = {INT_MAX, INT_MIN};
+    cudaError_t e = cudaMemcpyAsync(out, init, sizeof(init), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    xk_k_colors_range<<<304, 256, 0, s>>>(col, count, out);
+    return cudaGetLastError();
 }

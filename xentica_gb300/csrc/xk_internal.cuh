@@ -232,6 +232,9 @@ struct RenderGeo {
     int64_t size[XK_MAXDIM];
     int32_t smooth;             // 0: no SMOOTH_FACTOR division
 };
+// smallest and largest of `count` colour values into the device ints out[0],
+// out[1] (render.cu)
+cudaError_t xk_colors_minmax(const int32_t *col, int64_t count, int *out, cudaStream_t s);
 cudaError_t xk_render_colors(const int32_t *col, int32_t *img, const RenderGeo &g, int width,
                              int height, int zoom, int dx, int dy, cudaStream_t s);
 // the same frame as bytes (the int's low byte, as the reference's
