@@ -220,10 +220,11 @@ class GPU:
 
     def load(self, cells, colors):
         """Replace state and colours (reference ``save()`` layout accepted)."""
-        cells = np.asarray(cells)[:self.cells_num].astype(self.dtype)
+        cells = np.asarray(cells)[:self.cells_num].astype(self.dtype, copy=False)   # no host copy when typed
         colors = np.asarray(colors, dtype=np.int32)
         if self._handle is None:
-            self._host_cells = np.ascontiguousarray(cells)
-            self._host_colors = np.ascontiguousarray(colors)
+            # kept until the device model exists: copies, not views of the caller's arrays
+            self._host_cells = np.array(cells, copy=True, order="C")
+            self._host_colors = np.array(colors, copy=True, order="C")
             return
         self._upload(cells, colors)
