@@ -33,6 +33,9 @@ struct LColorParams {
 #define XK_LC_BX 32
 #define XK_LC_BY 8
 
+// TORUS: every neighbour on the lattice (wrapped), else off-board ones read
+// the border container
+template <bool TORUS>
 __global__ void __launch_bounds__(XK_LC_BX * XK_LC_BY)
 xk_k_lifecolor(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, int32_t *__restrict__ col,
                LColorParams p)
@@ -51,7 +54,7 @@ xk_k_lifecolor(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, int
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
             if (a == 1 && b == 1) continue;
-            const bool on = p.torus || (yon[a] && xon[b]);
+            const bool on = TORUS || (yon[a] && xon[b]);
             const uint32_t w = on ? __ldg(src + (int64_t)nys[a] * p.W + nxs[b]) : p.border;
             alive += w & 1u;
             rb += (w >> 1) & 0x00FF00FFu;
@@ -114,5 +117,6 @@ cudaError_t xk_lifecolor_step(const uint32_t *src, uint32_t *dst, int32_t *col, 
     p.frame_smooth = frame_smooth;
     dim3 block(XK_LC_BX, XK_LC_BY);
     dim3 grid((p.W + XK_LC_BX - 1) / XK_LC_BX, (p.H + XK_LC_BY - 1) / XK_LC_BY);
-    return xk_launch_pdl(xk_k_lifecolor, grid, block, 0, s, src, dst, col, p);
+    return p.torus ? xk_launch_pdl(xk_k_lifecolor<true>, grid, block, 0, s, src, dst, col, p)
+                   : xk_launch_pdl(xk_k_lifecolor<false>, grid, block, 0, s, src, dst, col, p);
 }
