@@ -31,6 +31,7 @@
 #include <cuda.h>          // CUtensorMap and its enums (types only; no driver link)
 #include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
 
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -883,11 +884,15 @@ static bool mass_tma_enabled()
 }
 
 // the TMA form's grid and planes per CTA for a lattice
+// runs of at least 4 planes (a run loads 2 halo planes and sets up its ring
+// once): with a frame every generation 64^3 46 -> 62 G, 96^3 154 -> 180 G,
+// 128^3 237 -> 301 G cell-updates/s against the 1024-CTA target alone
 static void mass_tma_shape(const MassParams &p, int *gx, int *gy, int *zc)
 {
     *gx = (p.W + 127) / 128;
     *gy = (p.H + XK_MT_BY - 1) / XK_MT_BY;
     *zc = mass_zchunk(p, *gx, *gy, 1024);
+    if (!getenv("XK_MASS_ZC")) *zc = std::max(*zc, std::min(4, p.D));
 }
 
 bool xk_mass_fuses_projection(const xk_desc &d)
