@@ -272,9 +272,12 @@ class _Compiler:
 # lines (no branches), so every register value can be numbered: each
 # instruction result becomes a value, a move only renames one, equal pure
 # operations on equal values (constant loads included) share one value, an
-# integer conversion of a constant becomes a constant, values nothing stored
-# or coloured depends on are dropped, and registers are allocated again over
-# the live ranges that remain.  Loads are shared only up to the next store.
+# integer conversion or integer arithmetic of constants becomes a constant
+# (with the kernel's semantics: wrap-around, truncating division, division
+# by zero giving 0, shift counts modulo the width), integer identities (x + 0,
+# x * 1, x | 0, x * 0, ...) fold, values nothing stored or coloured depends on
+# are dropped, and registers are allocated again over the live ranges that
+# remain.  Loads are shared only up to the next store.
 
 _BINARY = set(range(OP["+"], OP["!="] + 1))
 _SIDE = {OP["store"], OP["color"]}
@@ -300,6 +303,46 @@ def _image_value(image, code):
     if code in (TYPE_CODES["int"], TYPE_CODES["long"]) and image >> 63:
         return image - (1 << 64)
     return image
+
+
+# the integer types binary instructions compute in, with their widths
+_ARITH_BITS = {TYPE_CODES["int"]: 32, TYPE_CODES["unsigned int"]: 32, TYPE_CODES["long"]: 64,
+               TYPE_CODES["unsigned long"]: 64}
+
+
+def _fold_binary(op, code, x, y):
+    """The register image ``csrc/vm.cu`` computes for integer operation ``op``
+    of type ``code`` on the values ``x`` and ``y``, or None."""
+    bits = _ARITH_BITS[code]
+    if op == OP["+"]:
+        v = x + y
+    elif op == OP["-"]:
+        v = x - y
+    elif op == OP["*"]:
+        v = x * y
+    elif op in (OP["/"], OP["%"]):
+        if y == 0:
+            v = 0
+        else:
+            q = abs(x) // abs(y)
+            q = -q if (x < 0) != (y < 0) else q
+            v = q if op == OP["/"] else x - q * y
+    elif op == OP["&"]:
+        v = x & y
+    elif op == OP["|"]:
+        v = x | y
+    elif op == OP["^"]:
+        v = x ^ y
+    elif op == OP["<<"]:
+        v = x << (y & (bits - 1))
+    elif op == OP[">>"]:
+        v = x >> (y & (bits - 1))
+    elif OP["<"] <= op <= OP["!="]:
+        return int({OP["<"]: x < y, OP["<="]: x <= y, OP[">"]: x > y, OP[">="]: x >= y,
+                    OP["=="]: x == y, OP["!="]: x != y}[op])
+    else:
+        return None
+    return pack_value(v, ir.ctype_of(_CODE_TYPES[code]))
 
 
 def optimize(code, consts):
@@ -342,6 +385,25 @@ def optimize(code, consts):
                     const_slot[image] = len(consts)
                     consts.append(image)
                 op, args, imm = OP["const"], (), (const_slot[image], -1, -1)
+        if op in _BINARY and ty in _ARITH_BITS:
+            na, nb = nodes[args[0]], nodes[args[1]]
+            ca = _image_value(consts[na[3][0]], ty) if na[0] == OP["const"] else None
+            cb = _image_value(consts[nb[3][0]], ty) if nb[0] == OP["const"] else None
+            folded = None
+            if ca is not None and cb is not None:
+                folded = _fold_binary(op, ty, ca, cb)
+            elif cb == 0 and op in (OP["+"], OP["-"], OP["|"], OP["^"], OP["<<"], OP[">>"]) or \
+                    cb == 1 and op in (OP["*"], OP["/"]) or ca == 0 and op in (OP["+"], OP["|"], OP["^"]) or \
+                    ca == 1 and op == OP["*"]:
+                cur[int(ins["dst"])] = args[0] if cb is not None else args[1]
+                continue
+            elif (ca == 0 or cb == 0) and op in (OP["*"], OP["&"]):
+                folded = 0
+            if folded is not None:
+                if folded not in const_slot:
+                    const_slot[folded] = len(consts)
+                    consts.append(folded)
+                op, args, imm = OP["const"], (), (const_slot[folded], -1, -1)
         if op == OP["const"]:
             imm = (const_slot.get(consts[imm[0]], imm[0]), -1, -1)
         key = (op, ty, args, imm)
