@@ -85,8 +85,11 @@ def _int_div(x, y, mod, signed):
     zero = y == 0
     ys = np.where(zero, 1, y).astype(y.dtype)
     if signed:
-        q = np.abs(x.astype(np.int64)) // np.abs(ys.astype(np.int64))
-        q = np.where((x < 0) ^ (ys < 0), -q, q).astype(x.dtype)
+        # floor quotient turned toward zero (an absolute value of the most
+        # negative integer would overflow)
+        q = np.floor_divide(x, ys)
+        r = x - q * ys
+        q = np.where((r != 0) & ((x < 0) ^ (ys < 0)), q + 1, q).astype(x.dtype)
     else:
         q = x // ys
     r = (x - q * ys).astype(x.dtype)
