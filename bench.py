@@ -790,7 +790,8 @@ def lifecolor_line(args, dist):
                                     "emit and absorb passes over 8 buffer planes), 10 "
                                     "generations with their frames"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": committed_traffic("lifecolor"),
                          "kernel": "xk_k_lifecolor per generation (it also writes the zoom-1 "
                                    "uint8 frame)",
                          "algorithmic_bytes_per_generation": bytes_per_update * n,
@@ -903,7 +904,8 @@ def noise_line(args, dist):
             "interpreter": {"value": float(n) * 100 / (vm_ms / 1000.0), "unit": "cell-updates/s",
                             "note": "the same model on the generic interpreter, 100 generations"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": committed_traffic("noise"),
                          "kernel": "xk_k_noise, up to 1024 generations per launch",
                          "note": "B_alg = 28 B per cell-update (uint16 state and int3 colour read and "
                                  "written); a launch reads and writes each cell once for up to 1024 "
