@@ -27,10 +27,11 @@ Reported (one JSON line on rank 0):
           mass transfer 256^3 with a projection frame and the total checked
           every generation, the serving loop (Poisson arrivals, p50/p99
           latency, a sweep of offered loads), ShiftingSands, GameOfLifeColor
-          1920x1080 with a frame every generation and NoiseTV 1920x1080.
+          1920x1080 with a frame every generation, NoiseTV 1920x1080 and
+          GraviCowboys 1920x1080 with a frame every generation.
           ``--extras none`` leaves them out.
 
-``--workload life512 | evolife | mass | serve | sands | lifecolor | noise`` prints one of the extras as
+``--workload life512 | evolife | mass | serve | sands | lifecolor | noise | gravity`` prints one of the extras as
 its own line (with the given ``--steps``/``--warmup``).  ``--impl reference``
 times the reference's own kernels (its translator's LifelikeCA source compiled
 for the CPU, ``oracle/_ref``) on the host cores instead, with the same metric.
@@ -74,12 +75,12 @@ def parse():
     ap.add_argument("--quantum", type=int, default=128, help="serve: generations per round")
     ap.add_argument("--sweep", default="", help="serve: extra offered loads after the main run, "
                                                 "comma-separated (e.g. 0.3,0.5,0.9)")
-    ap.add_argument("--extras", default="life512,evolife,mass,serve,sands,lifecolor,noise",
+    ap.add_argument("--extras", default="life512,evolife,mass,serve,sands,lifecolor,noise,gravity",
                     help="default run: the other configurations measured after the ensemble "
                          "(comma-separated, or 'none')")
     ap.add_argument("--serve-budget-gb", type=int, default=16, help="serve: HBM budget (GiB)")
     ap.add_argument("--workload", choices=("ensemble", "life512", "evolife", "mass", "serve",
-                                           "sands", "lifecolor", "noise"),
+                                           "sands", "lifecolor", "noise", "gravity"),
                     default="ensemble",
                     help="ensemble: the batched Life-like ensemble (default); life512: Conway's "
                          "Life 512x512 torus, 1000 generations per step; evolife: EvoLife "
@@ -513,10 +514,10 @@ def run_ours(args, dist):
         for name in extras:
             fn = {"life512": life512_line, "evolife": evolife_line, "mass": mass_line,
                   "serve": serve_line, "sands": sands_line, "lifecolor": lifecolor_line,
-                  "noise": noise_line}[name]
+                  "noise": noise_line, "gravity": gravity_line}[name]
             steps, warmup = {"life512": (10, 3), "evolife": (100, 3), "mass": (5, 3),
                              "serve": (None, 3), "sands": (10, 3), "lifecolor": (10, 3),
-                             "noise": (5, 3)}[name]
+                             "noise": (5, 3), "gravity": (10, 3)}[name]
             small.steps, small.warmup = steps, warmup
             if name == "serve" and not small.sweep:
                 small.sweep = "0.3,0.5,0.9"
@@ -611,7 +612,7 @@ def evolife_line(args, dist):
     generations_done = gens * (1 + args.warmup + args.steps)
     peak, peak_kind = measured_peak()
     mean_ms = statistics.mean(step_ms)
-    bytes_per_update = 8 * 2 + 12 * 2 + 12   # uint64 state r+w, int3 colour r+w, int3 pixel
+    bytes_per_update = 8 * 2 + 12 * 2 + 3    # uint64 state r+w, int3 colour r+w, uint8 RGB pixel
     achieved = bytes_per_update * n * gens / (mean_ms / 1000.0) / 1e9
     line = {"metric": "cell-updates/s (EvoLife, frame every generation)", "value": value,
             "unit": "cell-updates/s", "n_gpus": dist.world, "steps": args.steps,
@@ -638,8 +639,8 @@ def evolife_line(args, dist):
                          "kernel": "xk_k_evolife per generation (it also writes the zoom-1 "
                                    "uint8 frame)",
                          "algorithmic_bytes_per_generation": bytes_per_update * n,
-                         "note": "B_alg = 52 B per cell-update (8 B state and 12 B colour read "
-                                 "and written, 12 B int3 pixel written); the kernel is bound by "
+                         "note": "B_alg = 43 B per cell-update (8 B state and 12 B colour read "
+                                 "and written, 3 B uint8 RGB pixel written); the kernel is bound by "
                                  "integer instruction issue (genome crossover), not by HBM"},
             "gpu_launches": gens * args.steps, "clocks": clk}
     if dist.rank == 0:
@@ -768,7 +769,7 @@ def lifecolor_line(args, dist):
     del vm_model
     peak, peak_kind = measured_peak()
     mean_ms = statistics.mean(step_ms)
-    bytes_per_update = 4 * 2 + 12 * 2 + 12   # uint32 state r+w, int3 colour r+w, int3 pixel
+    bytes_per_update = 4 * 2 + 12 * 2 + 3    # uint32 state r+w, int3 colour r+w, uint8 RGB pixel
     achieved = bytes_per_update * n * gens / (mean_ms / 1000.0) / 1e9
     line = {"metric": "cell-updates/s (GameOfLifeColor, frame every generation)", "value": value,
             "unit": "cell-updates/s", "n_gpus": dist.world, "steps": args.steps,
@@ -795,8 +796,8 @@ def lifecolor_line(args, dist):
                          "kernel": "xk_k_lifecolor per generation (it also writes the zoom-1 "
                                    "uint8 frame)",
                          "algorithmic_bytes_per_generation": bytes_per_update * n,
-                         "note": "B_alg = 44 B per cell-update (4 B state and 12 B colour read "
-                                 "and written, 12 B int3 pixel written)"},
+                         "note": "B_alg = 35 B per cell-update (4 B state and 12 B colour read "
+                                 "and written, 3 B uint8 RGB pixel written)"},
             "gpu_launches": gens * args.steps, "clocks": clk}
     if dist.rank == 0:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -824,6 +825,152 @@ def lifecolor_line(args, dist):
                                           "render, oracle (OpenMP)"}
         return line
     return None
+
+
+def gravity_experiment():
+    """GraviCowboys (examples/gravicowboys.py:20-71) on a 1920x1080 torus,
+    every cell seeded as GraviCowboysExperiment seeds its patches (energy 0
+    or 1, gravity 0), with the reference's MovingAverage fades."""
+    from xentica_gb300 import core, seeds
+    from xentica_gb300.seeds.random import RandInt
+
+    class GraviSoup(core.Experiment):
+        word = "LET IT GROOVE 1920X1080"
+        size = (1920, 1080)
+        zoom = 1
+        pos = [0, 0]
+        seed = seeds.patterns.PrimordialSoup(vals={"energy": RandInt(0, 1) * 1, "gravity": 0})
+    return GraviSoup
+
+
+def gravity_line(args, dist):
+    """GraviCowboys 1920x1080: K steps of 100 generations, each generation
+    with its zoom-1 frame written by the step kernel into a device buffer; the
+    same model on the generic interpreter timed beside it; e2e with every
+    frame copied to page-locked host memory; parity: the oracle from the GPU
+    state after the timed steps, two more generations (cells, colours,
+    frames)."""
+    from xentica_gb300 import build as xk_build
+    from xentica_gb300 import _native as nat
+    from xentica_gb300.core import canonical
+    import torch
+    xk_build.build()
+    nat.set_device(dist.local)
+    lib = nat.load()
+    exp = gravity_experiment()
+    model = canonical.GravityProgram(exp)
+    assert type(model.gpu.template).__name__ == "GravityTemplate"
+    W, H = model.size
+    model.set_viewport((W, H))
+    n = model.cells_num
+    gens = 100
+    fb = W * H * 3
+    dev_frames = torch.empty(gens * fb, dtype=torch.uint8, device="cuda:%d" % dist.local)
+
+    def step_device():
+        return model.gpu.step_frames(gens, W, H, 1, 0, 0, dev_frames.data_ptr(), on_device=True)
+
+    step_device()
+    for _ in range(args.warmup):
+        step_device()
+    clocks = Clocks(dist.local)
+    time.sleep(0.6)
+    dist.barrier()
+    lib.xk_range_push(b"timed")
+    step_ms = [step_device() for _ in range(args.steps)]
+    lib.xk_range_pop()
+    dist.barrier()
+    clk = clocks.stop()
+    dev_s = dist.max(sum(step_ms) / 1000.0)
+    value = float(n) * gens * args.steps * dist.world / dev_s
+    cells = model.gpu.arrays.cells.get()[:n].copy()
+    colors = model.gpu.arrays.colors.get()
+    host = nat.PinnedBuffer(gens * fb)
+    frames = host.array.reshape(gens, fb)
+    e2e = []
+    e2e_steps = min(args.steps, 5)
+    for _ in range(e2e_steps):
+        t0 = time.perf_counter()
+        model.gpu.load(cells, colors)
+        model.gpu.step_frames(gens, W, H, 1, 0, 0, frames.reshape(-1))
+        e2e.append(time.perf_counter() - t0)
+    e2e_s = dist.max(sum(e2e))
+    host.release()
+    os.environ["XENTICA_GB300_TEMPLATE"] = "vm"
+    try:
+        vm_model = canonical.GravityProgram(exp)
+    finally:
+        del os.environ["XENTICA_GB300_TEMPLATE"]
+    vm_model.set_viewport((W, H))
+    vm_model.gpu.load(cells, colors)
+    vm_frames = torch.empty(10 * fb, dtype=torch.uint8, device="cuda:%d" % dist.local)
+    vm_model.gpu.step_frames(10, W, H, 1, 0, 0, vm_frames.data_ptr(), on_device=True)
+    vm_ms = vm_model.gpu.step_frames(10, W, H, 1, 0, 0, vm_frames.data_ptr(), on_device=True)
+    del vm_model
+    peak, peak_kind = measured_peak()
+    mean_ms = statistics.mean(step_ms)
+    bytes_per_update = 8 * 2 + 12 * 2 + 3    # uint64 state r+w, int3 colour r+w, uint8 RGB pixel
+    achieved = bytes_per_update * n * gens / (mean_ms / 1000.0) / 1e9
+    line = {"metric": "cell-updates/s (GraviCowboys, frame every generation)", "value": value,
+            "unit": "cell-updates/s", "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_s * 1000 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64+f32",
+            "data": "synthetic (seeded PrimordialSoup: energy 0 or 1, gravity 0)",
+            "config": {"workload": "GraviCowboys 1920x1080 torus, MovingAverage(255, 255), 100 "
+                                   "generations per step, each followed by a 1920x1080 "
+                                   "RendererPlain frame (uint8 RGB)",
+                       "l2": "state + colours (41 MB) fit in L2; frames (622 MB per step) "
+                             "stream to HBM"},
+            "e2e": {"value": float(n) * gens * e2e_steps * dist.world / e2e_s,
+                    "unit": "cell-updates/s", "h2d_bytes_per_step": n * 8 + n * 12,
+                    "d2h_bytes_per_step": gens * fb,
+                    "note": "state and colours loaded from the host, every frame copied to "
+                            "page-locked host memory"},
+            "interpreter": {"value": float(n) * 10 / (vm_ms / 1000.0), "unit": "cell-updates/s",
+                            "note": "the same model on the generic interpreter (the reference's "
+                                    "emit and absorb passes over 8 buffer planes), 10 "
+                                    "generations with their frames"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": committed_traffic("gravity"),
+                         "kernel": "xk_k_gravity per generation (it also writes the zoom-1 "
+                                   "uint8 frame)",
+                         "algorithmic_bytes_per_generation": bytes_per_update * n,
+                         "note": "B_alg = 43 B per cell-update (8 B state and 12 B colour read "
+                                 "and written, 3 B uint8 RGB pixel written)"},
+            "gpu_launches": gens * args.steps, "clocks": clk}
+    if dist.rank == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        topo = O.Topology(model.size)
+        fld = topo.field(model.gpu.arrays.cells.get()[:n], np.uint64)
+        col = model.gpu.arrays.colors.get()
+        got = model.step_frames(2)
+        gpu_cells = model.gpu.arrays.cells.get()[:n]
+        gpu_col = model.gpu.arrays.colors.get()
+        exact, el = True, 0.0
+        for g in range(2):
+            t0 = time.perf_counter()
+            O.gravity_run(topo, fld, col, 1, color=O._color(True, 255, 255, 1))
+            img = O.render(topo, col, W, H, smooth=1).astype(np.uint8)
+            el += time.perf_counter() - t0
+            exact &= bool(np.array_equal(got[g], img))
+        exact &= bool(np.array_equal(gpu_cells, fld[:n])) and bool(np.array_equal(gpu_col, col))
+        line["parity"] = {"checked_generations": 2, "bit_exact": exact,
+                          "note": "oracle started from the GPU state after the timed and "
+                                  "end-to-end steps: cells, colours and both frames"}
+        line["cpu_baseline"] = {"value": n * 2 / el, "unit": "cell-updates/s",
+                                "cores": os.cpu_count(), "kind": "port",
+                                "sample": "2 generations of the full lattice, each with its "
+                                          "render, oracle (OpenMP)"}
+        return line
+    return None
+
+
+def run_gravity(args, dist):
+    line = gravity_line(args, dist)
+    if line is not None:
+        print(json.dumps(line), flush=True)
 
 
 def noise_line(args, dist):
@@ -1616,6 +1763,8 @@ def main():
             run_lifecolor(args, dist)
         elif args.workload == "noise":
             run_noise(args, dist)
+        elif args.workload == "gravity":
+            run_gravity(args, dist)
         else:
             run_ours(args, dist)
     finally:

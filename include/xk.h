@@ -45,9 +45,13 @@ enum {
  * examples/game_of_life.py:112-159): a 2-D Moore lattice of uint32 cells,
  * torus or static border, MovingAverage colours or none.
  * XK_FAMILY_NOISE: per-cell noise (NoiseTV, examples/noisetv.py:13-31), one
- * 16-bit RandomProperty per cell advanced twice a generation, any lattice. */
+ * 16-bit RandomProperty per cell advanced twice a generation, any lattice.
+ * XK_FAMILY_GRAVITY: energy flowing down a gravity field (GraviCowboys,
+ * examples/gravicowboys.py:20-71): a 2-D Moore lattice of uint64 cells
+ * (energy 12 bits | new_energy 12 bits | float gravity), torus or static
+ * border, MovingAverage colours or none. */
 enum { XK_FAMILY_LIFE = 1, XK_FAMILY_EVOLIFE = 2, XK_FAMILY_MASS = 3, XK_FAMILY_VM = 4,
-       XK_FAMILY_SHIFT = 5, XK_FAMILY_LIFECOLOR = 6, XK_FAMILY_NOISE = 7 };
+       XK_FAMILY_SHIFT = 5, XK_FAMILY_LIFECOLOR = 6, XK_FAMILY_NOISE = 7, XK_FAMILY_GRAVITY = 8 };
 enum { XK_COLOR_NONE = 0, XK_COLOR_PLAIN = 1, XK_COLOR_MOVING_AVERAGE = 2 };
 
 /* Model descriptor filled by the translator (xentica_gb300/core/templates.py)

@@ -456,6 +456,92 @@ void xo_noise_step(const xo_topo *t, uint16_t *fld, int32_t *col, const xo_color
 }
 
 /* ------------------------------------------------------------------------ */
+/* GraviCowboys (examples/gravicowboys.py): a uint64 cell packs energy (12
+ * bits) | new_energy << 12 | gravity (float bits) << 24.  emit: new_energy =
+ * energy; the smallest of the neighbours' gravities (a < b ? a : b in
+ * neighbour order, then 0.0f + it); for each buffer k in order one unit goes
+ * to neighbour k when its gravity equals that smallest and
+ * (unsigned)(energy - sent) > 0; every buffer carries gravity + energy (a
+ * float sum); new_energy -= sent, stored to the cell.  absorb: energy =
+ * new_energy + the units received (16-bit), gravity = (the float sum of the
+ * buffers' gravities in neighbour order) / 8.008 in double, rounded to float;
+ * colour (MovingAverage) energy * 255 and (unsigned)(gravity * 108) twice.
+ * An off-board neighbour reads as the whole border container. */
+static inline float xo_bits_f(uint32_t b) { float f; memcpy(&f, &b, 4); return f; }
+static inline uint32_t xo_f_bits(float f) { uint32_t b; memcpy(&b, &f, 4); return b; }
+
+/* float -> unsigned int as the GPU converts: truncation, NaN and negatives -> 0 */
+static inline uint32_t xo_f2u_sat(float f)
+{
+    if (!(f > 0.0f)) return 0u;
+    if (f >= 4294967296.0f) return 0xFFFFFFFFu;
+    return (uint32_t)f;
+}
+
+void xo_gravity_step(const xo_topo *t, uint64_t *fld, int32_t *col, const xo_color *cc, int threads)
+{
+    const int64_t n = xo_cells(t);
+    uint64_t *mains = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)n);
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t x[XO_MAXDIM];
+        xo_coords(t, i, x);
+        const uint64_t v = fld[i];
+        const uint32_t energy = (uint32_t)(v & 4095u);
+        const float g = xo_bits_f((uint32_t)(v >> 24));
+        uint16_t newe = (uint16_t)(1u * energy);
+        float gk[64];
+        for (int k = 0; k < t->nbr; ++k) {
+            int64_t j = xo_neighbor(t, x, k);
+            const uint64_t w = j < 0 ? t->border_value : fld[j];
+            gk[k] = xo_bits_f((uint32_t)(w >> 24));
+        }
+        float m = gk[0];
+        for (int k = 1; k < t->nbr; ++k) m = m < gk[k] ? m : gk[k];
+        const float lowest = 0.0f + m;
+        uint32_t sent = 0;
+        for (int k = 0; k < t->nbr; ++k) {
+            const uint32_t towards = lowest == gk[k];
+            const uint32_t left = (uint32_t)(energy - sent) > 0u;
+            const uint32_t unit = towards * left * 1u;
+            sent += unit;
+            const uint64_t gb = xo_f_bits(g + (float)energy);
+            fld[i + n * (int64_t)(t->rev[k] + 1)] = ((uint64_t)(unit & 4095u)) + (gb << 24);
+        }
+        newe = (uint16_t)((uint32_t)newe - sent);
+        mains[i] = (v & 4095u) + ((uint64_t)(newe & 4095u) << 12) + (v & ~0xFFFFFFull);
+    }
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int64_t i = 0; i < n; ++i) fld[i] = mains[i];
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t x[XO_MAXDIM];
+        xo_coords(t, i, x);
+        uint32_t received = 0;
+        float field = 0.0f;
+        for (int k = 0; k < t->nbr; ++k) {
+            int64_t j = xo_neighbor(t, x, k);
+            const uint64_t w = j < 0 ? t->border_value : fld[j + n * (int64_t)(k + 1)];
+            received += (uint32_t)(w & 4095u);
+        }
+        for (int k = 0; k < t->nbr; ++k) {
+            int64_t j = xo_neighbor(t, x, k);
+            const uint64_t w = j < 0 ? t->border_value : fld[j + n * (int64_t)(k + 1)];
+            field += xo_bits_f((uint32_t)(w >> 24));
+        }
+        const uint64_t v = fld[i];
+        const uint32_t newe = (uint32_t)((v >> 12) & 4095u);
+        const uint16_t energy = (uint16_t)(newe + received);
+        const float g = (float)((double)field / 8.008);
+        const int r = (int)energy * 255;
+        const int gg = (int)xo_f2u_sat(g * 108.0f);
+        xo_color_write(col, i, r, gg, gg, cc);
+        fld[i] = ((uint64_t)(energy & 4095u)) + ((uint64_t)newe << 12) + ((uint64_t)xo_f_bits(g) << 24);
+    }
+    free(mains);
+}
+
+/* ------------------------------------------------------------------------ */
 /* RendererPlain.render_code (renderers.py:220-270): pixel i of a width x
  * height viewport; axes (a0, a1) are projected, every other axis is summed
  * in nested-loop order (outer loop = lowest axis index). */

@@ -156,6 +156,17 @@ def shift_run(topo, fld, col, steps, plane0, lut, color=None, threads=None):
            _ptr(col), ctypes.byref(cc), _ptr(lut), ctypes.c_int(threads))
 
 
+def gravity_run(topo, fld, col, steps, color=None, threads=None):
+    """Advance a GraviCowboys model (uint64 ``fld``) ``steps`` generations in
+    place (``oracle.c``: ``xo_gravity_step``)."""
+    threads = threads or os.cpu_count()
+    cc = color or _color()
+    fn = lib().xo_gravity_step
+    fn.restype = None
+    for _ in range(steps):
+        fn(ctypes.byref(topo._c), _ptr(fld), _ptr(col), ctypes.byref(cc), ctypes.c_int(threads))
+
+
 def noise_run(topo, fld, col, steps, color=None, threads=None):
     """Advance a NoiseTV model (uint16 ``fld``) ``steps`` generations in place
     (``oracle.c``: ``xo_noise_step``)."""

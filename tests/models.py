@@ -182,6 +182,85 @@ class NoiseTV3D(NoiseTV):
         border = core.StaticBorder(7)
 
 
+class GraviCowboys(core.CellularAutomaton):
+    """Energy units rolling down a gravity field that the energy itself
+    raises (examples/gravicowboys.py:20-71)."""
+
+    energy = core.IntegerProperty(max_val=2 ** 12 - 1)
+    new_energy = core.IntegerProperty(max_val=2 ** 12 - 1)
+    gravity = core.FloatProperty()
+
+    class Topology:
+        dimensions = 2
+        lattice = core.OrthogonalLattice()
+        neighborhood = core.MooreNeighborhood()
+        border = core.TorusBorder()
+
+    def emit(self):
+        self.main.new_energy = 1 * self.main.energy
+        max_gravity = core.FloatVariable()
+        max_gravity += xmath.min(*[nbr.main.gravity for nbr in self.neighbors])
+        energy_passed = core.IntegerVariable()
+        energy_passed *= 0
+        denergy = core.IntegerVariable()
+        for i, buf in enumerate(self.buffers):
+            fit_dir = max_gravity == self.neighbors[i].main.gravity
+            has_energy = (self.main.energy - energy_passed) > 0
+            denergy *= 0
+            denergy += fit_dir * has_energy * 1
+            energy_passed += denergy
+            buf.energy = denergy
+            buf.gravity = self.main.gravity + self.main.energy
+        self.main.new_energy -= energy_passed
+
+    def absorb(self):
+        energy_passed = core.IntegerVariable()
+        for i in range(len(self.buffers)):
+            energy_passed += self.neighbors[i].buffer.energy
+        self.main.energy = self.main.new_energy + energy_passed
+        new_gravity = core.FloatVariable()
+        for i in range(len(self.buffers)):
+            new_gravity += self.neighbors[i].buffer.gravity
+        self.main.gravity = new_gravity / (len(self.buffers) * 1.001)
+
+    @color_effects.MovingAverage
+    def color(self):
+        red = self.main.energy * 255
+        green = xmath.int(self.main.gravity * 108)
+        blue = xmath.int(self.main.gravity * 108)
+        return (red, green, blue)
+
+
+class GraviCowboysStatic(GraviCowboys):
+    """The same inside a fixed border container: energy 3 at gravity 0.5."""
+
+    class Topology(GraviCowboys.Topology):
+        border = core.StaticBorder(3 | 0x3F000000 << 24)
+
+
+class GraviCowboysHalf(GraviCowboys):
+    """Not the GraviCowboys program (gravity averaged over 4.004): runs on the
+    interpreter."""
+
+    def absorb(self):
+        energy_passed = core.IntegerVariable()
+        for i in range(len(self.buffers)):
+            energy_passed += self.neighbors[i].buffer.energy
+        self.main.energy = self.main.new_energy + energy_passed
+        new_gravity = core.FloatVariable()
+        for i in range(len(self.buffers)):
+            new_gravity += self.neighbors[i].buffer.gravity
+        self.main.gravity = new_gravity / (len(self.buffers) * 0.5005)
+
+
+class GraviExperiment(core.Experiment):
+    word = "LET IT GROOVE"
+    size = (64, 48)
+    zoom = 1
+    pos = [0, 0]
+    seed = seeds.patterns.PrimordialSoup(vals={"energy": seeds.random.RandInt(0, 1) * 1, "gravity": 0})
+
+
 class NoiseExperiment(core.Experiment):
     word = "PSHSHSHSH!"
     size = (64, 48)

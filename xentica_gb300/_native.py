@@ -19,6 +19,7 @@ XK_MAXNBR = 32
 XK_FAMILY_LIFE, XK_FAMILY_EVOLIFE, XK_FAMILY_MASS, XK_FAMILY_VM, XK_FAMILY_SHIFT = 1, 2, 3, 4, 5
 XK_FAMILY_LIFECOLOR = 6
 XK_FAMILY_NOISE = 7
+XK_FAMILY_GRAVITY = 8
 XK_COLOR_NONE, XK_COLOR_PLAIN, XK_COLOR_MOVING_AVERAGE = 0, 1, 2
 
 _I32, _U32, _I64, _U64 = ctypes.c_int32, ctypes.c_uint32, ctypes.c_int64, ctypes.c_uint64

@@ -239,3 +239,54 @@ class NoiseProgram(core.CellularAutomaton):
     def color(self):
         grey = xmath.int(self.main.rng.uniform * 255)
         return (grey, grey, grey)
+
+
+class GravityProgram(core.CellularAutomaton):
+    """Energy drifting down a diffusing field (the reference's GraviCowboys,
+    ``examples/gravicowboys.py``): a cell sends one unit of its energy to
+    each neighbour, in neighbour order and while it has energy left, whose
+    field value equals the smallest around it; every buffer carries the
+    cell's field plus its energy, and the new field is the neighbours' sum
+    divided by 8.008.  The statement order fixes the float rounding."""
+
+    energy = core.IntegerProperty(max_val=2 ** 12 - 1)
+    new_energy = core.IntegerProperty(max_val=2 ** 12 - 1)
+    gravity = core.FloatProperty()
+
+    class Topology:
+        dimensions = 2
+        lattice = core.OrthogonalLattice()
+        neighborhood = core.MooreNeighborhood()
+        border = core.TorusBorder()
+
+    def emit(self):
+        self.main.new_energy = 1 * self.main.energy
+        lowest = core.FloatVariable()
+        lowest += xmath.min(*[nbr.main.gravity for nbr in self.neighbors])
+        sent = core.IntegerVariable()
+        sent *= 0
+        unit = core.IntegerVariable()
+        for k, buf in enumerate(self.buffers):
+            towards = lowest == self.neighbors[k].main.gravity
+            left = (self.main.energy - sent) > 0
+            unit *= 0
+            unit += towards * left * 1
+            sent += unit
+            buf.energy = unit
+            buf.gravity = self.main.gravity + self.main.energy
+        self.main.new_energy -= sent
+
+    def absorb(self):
+        received = core.IntegerVariable()
+        for k in range(len(self.buffers)):
+            received += self.neighbors[k].buffer.energy
+        self.main.energy = self.main.new_energy + received
+        field = core.FloatVariable()
+        for k in range(len(self.buffers)):
+            field += self.neighbors[k].buffer.gravity
+        self.main.gravity = field / (len(self.buffers) * 1.001)
+
+    @color_effects.MovingAverage
+    def color(self):
+        return (self.main.energy * 255, xmath.int(self.main.gravity * 108),
+                xmath.int(self.main.gravity * 108))

@@ -500,6 +500,42 @@ class NoiseTemplate:
         return d
 
 
+class GravityTemplate:
+    """Energy flowing down a gravity field (``canonical.GravityProgram``: the
+    reference's GraviCowboys, ``examples/gravicowboys.py:20-71``), matched by
+    program fingerprint: two 12-bit integer properties and a float, a 2-D
+    Moore lattice in the reference's neighbour order, torus or static border,
+    MovingAverage colours with the model's fades."""
+
+    family = nat.XK_FAMILY_GRAVITY
+    MOORE = [(-1, -1), (-1, 0), (-1, 1), (0, -1), (0, 1), (1, -1), (1, 0), (1, 1)]
+
+    def __init__(self, model):
+        from xentica_gb300.core import canonical
+        props = list(model.main.properties.values())
+        if [type(p).__name__ for p in props] != ["IntegerProperty", "IntegerProperty", "FloatProperty"] or \
+                [p.bit_width for p in props] != [12, 12, 32]:
+            raise NoTemplate("not two 12-bit integer properties and a float")
+        deltas, torus, border = _topology(model)
+        if model.topology.dimensions != 2 or [tuple(d) for d in deltas] != self.MOORE:
+            raise NoTemplate("GraviCowboys kernel is 2-D Moore")
+        attrs = {name: model.__dict__[name] for name in ("fade_in", "fade_out", "smooth_factor")
+                 if name in model.__dict__}
+        programs = canonical.trace(canonical.GravityProgram, model.size, {}, attrs)
+        for key in ("emit", "absorb"):
+            if ir.fingerprint(programs[key]) != ir.fingerprint(model.programs[key]):
+                raise NoTemplate("%s differs from the GraviCowboys program" % key)
+        self.model = model
+        self.color = _color_stmt(model.programs["absorb"])
+
+    def descriptor(self):
+        d = _base_desc(self.model, self.family)
+        info = self.color.extra
+        d.color_kind = nat.XK_COLOR_MOVING_AVERAGE
+        d.fade_in, d.fade_out, d.smooth = info["fade_in"], info["fade_out"], info["smooth"]
+        return d
+
+
 class VMTemplate:
     """Any other traced model: its emit and absorb programs, compiled to
     register bytecode (``core/vm.py``), run on the generic interpreter kernel
@@ -568,7 +604,7 @@ class VMTemplate:
 
 
 FAMILIES = (LifeTemplate, ShiftTemplate, EvoLifeTemplate, MassTemplate, LifeColorTemplate, NoiseTemplate,
-            VMTemplate)
+            GravityTemplate, VMTemplate)
 
 
 def match(model):

@@ -139,7 +139,7 @@ extern "C" int xk_device_info(char *buf, int32_t len)
 // model object
 
 enum { LAYOUT_BITS2D = 1, LAYOUT_BYTES = 2, LAYOUT_CELLS64 = 3, LAYOUT_MASS = 4, LAYOUT_VM = 5, LAYOUT_LCOLOR = 6,
-       LAYOUT_NOISE = 7 };
+       LAYOUT_NOISE = 7, LAYOUT_GRAVITY = 8 };
 
 // largest float t with (double)u < p  <=>  u <= t for every float u
 static float below_threshold(double p)
@@ -162,7 +162,7 @@ struct xk_model {
     NdGeo ng;
     uint32_t *bits[2] = {nullptr, nullptr};
     uint8_t *bytes[2] = {nullptr, nullptr};
-    uint64_t *cells64[2] = {nullptr, nullptr};  // EvoLife: reference layout, ping-pong
+    uint64_t *cells64[2] = {nullptr, nullptr};  // EvoLife, GraviCowboys: reference layout, ping-pong
     float mut_thresh = 0.f;
     uint32_t *cells32[2] = {nullptr, nullptr};  // mass transfer, colour Life: reference layout, ping-pong
     uint16_t *cells16 = nullptr;                // noise: reference layout, updated in place
@@ -454,7 +454,8 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
     XK_REQUIRE(n <= (1LL << 40), XK_ERR_ARG, "lattice of %lld cells too large", (long long)n);
     XK_REQUIRE(d.family == XK_FAMILY_LIFE || d.family == XK_FAMILY_EVOLIFE ||
                    d.family == XK_FAMILY_MASS || d.family == XK_FAMILY_VM || d.family == XK_FAMILY_SHIFT ||
-                   d.family == XK_FAMILY_LIFECOLOR || d.family == XK_FAMILY_NOISE,
+                   d.family == XK_FAMILY_LIFECOLOR || d.family == XK_FAMILY_NOISE ||
+                   d.family == XK_FAMILY_GRAVITY,
                XK_ERR_UNSUPPORTED, "model family %d has no kernel in this library", d.family);
     if (d.family == XK_FAMILY_NOISE)
         XK_REQUIRE(d.state_bytes == 2 &&
@@ -464,6 +465,11 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
         XK_REQUIRE(is_moore2d(d) && d.state_bytes == 4 &&
                        (d.color_kind == XK_COLOR_NONE || d.color_kind == XK_COLOR_MOVING_AVERAGE),
                    XK_ERR_ARG, "colour Life needs a 2-D Moore lattice of 32-bit cells and MovingAverage "
+                   "colours (or none)");
+    if (d.family == XK_FAMILY_GRAVITY)
+        XK_REQUIRE(is_moore2d(d) && d.state_bytes == 8 &&
+                       (d.color_kind == XK_COLOR_NONE || d.color_kind == XK_COLOR_MOVING_AVERAGE),
+                   XK_ERR_ARG, "GraviCowboys needs a 2-D Moore lattice of 64-bit cells and MovingAverage "
                    "colours (or none)");
     if (d.family == XK_FAMILY_SHIFT)
         XK_REQUIRE(d.rule0 < (uint32_t)d.nbr, XK_ERR_ARG, "shifting family: neighbour %u of %d",
@@ -535,6 +541,11 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
             XK_TRY(cudaMalloc(&m->cells32[0], (size_t)n * 4));
             XK_TRY(cudaMalloc(&m->cells32[1], (size_t)n * 4));
             XK_TRY(cudaMemsetAsync(m->cells32[0], 0, (size_t)n * 4, m->stream));
+        } else if (d.family == XK_FAMILY_GRAVITY) {
+            m->layout = LAYOUT_GRAVITY;
+            XK_TRY(cudaMalloc(&m->cells64[0], (size_t)n * 8));
+            XK_TRY(cudaMalloc(&m->cells64[1], (size_t)n * 8));
+            XK_TRY(cudaMemsetAsync(m->cells64[0], 0, (size_t)n * 8, m->stream));
         } else if (d.family == XK_FAMILY_EVOLIFE) {
             m->layout = LAYOUT_CELLS64;
             XK_TRY(cudaMalloc(&m->cells64[0], (size_t)n * 8));
@@ -566,7 +577,7 @@ extern "C" int xk_model_create(const xk_desc *desc, xk_model **out)
             XK_TRY(cudaMemsetAsync(m->bytes[0], 0, bytes, m->stream));
         }
         if (m->layout != LAYOUT_CELLS64 && m->layout != LAYOUT_MASS && m->layout != LAYOUT_VM &&
-            m->layout != LAYOUT_LCOLOR && m->layout != LAYOUT_NOISE)
+            m->layout != LAYOUT_LCOLOR && m->layout != LAYOUT_NOISE && m->layout != LAYOUT_GRAVITY)
             XK_TRY(cudaMalloc(&m->stage, (size_t)n * d.state_bytes + 16));
         XK_TRY(cudaMalloc(&m->col, (size_t)n * 3 * sizeof(int32_t)));
         XK_TRY(cudaMemsetAsync(m->col, 0, (size_t)n * 3 * sizeof(int32_t), m->stream));
@@ -598,7 +609,7 @@ extern "C" int xk_upload(xk_model *m, const void *host_main, int64_t ncells)
                (long long)ncells, (long long)m->n);
     const int esz = m->d.state_bytes;
     if (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_MASS || m->layout == LAYOUT_VM ||
-        m->layout == LAYOUT_LCOLOR || m->layout == LAYOUT_NOISE) {
+        m->layout == LAYOUT_LCOLOR || m->layout == LAYOUT_NOISE || m->layout == LAYOUT_GRAVITY) {
         void *dst = m->layout == LAYOUT_MASS || m->layout == LAYOUT_LCOLOR ? (void *)m->cells32[m->cur]
                     : m->layout == LAYOUT_NOISE ? (void *)m->cells16
                     : m->layout == LAYOUT_VM ? (void *)m->fld : (void *)m->cells64[m->cur];
@@ -657,7 +668,7 @@ extern "C" int xk_download(xk_model *m, void *host_main, int64_t ncells)
                (long long)ncells, (long long)m->n);
     const int esz = m->d.state_bytes;
     if (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_MASS || m->layout == LAYOUT_VM ||
-        m->layout == LAYOUT_LCOLOR || m->layout == LAYOUT_NOISE) {
+        m->layout == LAYOUT_LCOLOR || m->layout == LAYOUT_NOISE || m->layout == LAYOUT_GRAVITY) {
         const void *src = m->layout == LAYOUT_MASS || m->layout == LAYOUT_LCOLOR ? (const void *)m->cells32[m->cur]
                           : m->layout == LAYOUT_NOISE ? (const void *)m->cells16
                           : m->layout == LAYOUT_VM ? (const void *)m->fld
@@ -694,7 +705,8 @@ extern "C" int xk_download(xk_model *m, void *host_main, int64_t ncells)
 // write the colours implied by the state into m->col
 static int materialize_colors(xk_model *m)
 {
-    if (m->layout == LAYOUT_VM || m->layout == LAYOUT_LCOLOR || m->layout == LAYOUT_NOISE)
+    if (m->layout == LAYOUT_VM || m->layout == LAYOUT_LCOLOR || m->layout == LAYOUT_NOISE ||
+        m->layout == LAYOUT_GRAVITY)
         return XK_OK;   // the steps write the colours
     if (m->layout == LAYOUT_MASS) {
         XK_CUDA(xk_mass_colors(m->cells32[m->cur], m->col, m->d, m->stream));
@@ -817,7 +829,7 @@ static int step_prepare(xk_model *m, int64_t nsteps)
         return XK_OK;
     }
     if (m->layout == LAYOUT_VM || m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_LCOLOR ||
-        m->layout == LAYOUT_NOISE)
+        m->layout == LAYOUT_NOISE || m->layout == LAYOUT_GRAVITY)
         return XK_OK;
     const bool colors_free = colors_free_of(m);
     if (!colors_free) {
@@ -875,6 +887,14 @@ static int step_enqueue(xk_model *m, int64_t first, int64_t count, uint8_t *fram
             const int gens = frame ? 1 : (int)std::min<int64_t>(1024, count - g);
             XK_CUDA(xk_noise_step(m->cells16, m->col, m->d, m->n, gens, m->stream, frame, m->d.render_smooth));
             g += gens;
+        }
+        return XK_OK;
+    }
+    if (m->layout == LAYOUT_GRAVITY) {
+        for (int64_t g = 0; g < count; ++g) {
+            XK_CUDA(xk_gravity_step(m->cells64[m->cur], m->cells64[1 - m->cur], m->col, m->d, m->stream,
+                                    frame, m->d.render_smooth));
+            m->cur = 1 - m->cur;
         }
         return XK_OK;
     }
@@ -1219,7 +1239,8 @@ extern "C" int xk_step_frames(xk_model *m, int64_t nsteps, int32_t width, int32_
         }
     }
     // EvoLife or colour Life viewed whole at zoom 1: the step kernel writes the frame
-    const bool fused = (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_LCOLOR || m->layout == LAYOUT_NOISE) &&
+    const bool fused = (m->layout == LAYOUT_CELLS64 || m->layout == LAYOUT_LCOLOR || m->layout == LAYOUT_NOISE ||
+                        m->layout == LAYOUT_GRAVITY) &&
                        m->d.color_kind != XK_COLOR_NONE &&
                        m->d.ndim == 2 && m->d.proj_axis0 == 0 && m->d.proj_axis1 == 1 && zoom == 1 &&
                        dx == 0 && dy == 0 && width == m->d.size[0] && height == m->d.size[1];

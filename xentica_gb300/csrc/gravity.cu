@@ -1,0 +1,191 @@
+// Energy flowing down a gravity field (the reference's GraviCowboys,
+// examples/gravicowboys.py:20-71) for sm_103a.
+//
+// A cell is a uint64 packed LSB first in declaration order
+// (properties.py:496-541): energy (12 bits) | new_energy << 12 | gravity
+// (float bits) << 24.  One generation, per cell, in the reference's
+// arithmetic (its emit and absorb as traced):
+//   emit    lowest = 0 + min over the neighbours' gravities (a < b ? a : b, in
+//           neighbour order); for buffer k in order, one unit goes to
+//           neighbour k when its gravity equals lowest and energy - sent > 0
+//           (unsigned); every buffer carries gravity + energy (float);
+//           new_energy = energy - sent
+//   absorb  energy = (uint16)(new_energy + the units sent towards the cell),
+//           gravity = (float)((double)(the float sum of the buffers'
+//           gravities in neighbour order) / 8.008)
+// and the colour (MovingAverage, color_effects.py:106-130) energy * 255,
+// (unsigned)(gravity * 108) twice.  An off-board neighbour of a static border
+// reads as the whole border container (border.py:144-151).
+//
+// One launch per generation: a block loads its 32 x 8 cells with a halo of
+// two into shared memory, runs emit on the tile and a halo of one (what a
+// neighbour sends is a bit of an 8-bit mask, its new energy and the one
+// float every buffer carries), then absorb on the tile.  A cell's state is
+// read and written once per generation; the reference's nine containers per
+// cell never exist.
+#include "xk_internal.cuh"
+
+struct GravParams {
+    int32_t W, H;
+    uint64_t border;            // off-board container (static border)
+    int32_t color_kind;         // XK_COLOR_*
+    int32_t fade_in, fade_out, smooth;
+    uint8_t *frame;             // null, or the W x H RendererPlain frame (zoom 1, no offset)
+    int32_t frame_smooth;       // its SMOOTH_FACTOR (0: none)
+};
+
+#define XK_GC_TX 32
+#define XK_GC_TY 8
+
+// the Moore deltas in the reference's order (x, y): (-1,-1) (-1,0) (-1,1)
+// (0,-1) (0,1) (1,-1) (1,0) (1,1); neighbour 7 - k points back along k
+__device__ __forceinline__ int xk_gc_dx(int k) { return k < 3 ? -1 : k < 5 ? 0 : 1; }
+__device__ __forceinline__ int xk_gc_dy(int k) { return (k == 0 || k == 3 || k == 5) ? -1 : (k == 1 || k == 6) ? 0 : 1; }
+
+__device__ __forceinline__ float xk_gc_grav(uint64_t c) { return __uint_as_float((uint32_t)(c >> 24)); }
+
+// (float)((double)f / 8.008), correctly rounded: the quotient by Markstein's
+// method (q0 = f * RN(1/8.008), remainder by an exact fma, one corrected
+// product; correctly rounded when the reciprocal is and q0 is within an ulp;
+// checked equal to the division for every finite non-zero float), a zero
+// keeps its sign, non-finite values go through the division itself
+__device__ __forceinline__ float xk_gc_mean(float f)
+{
+    constexpr double c = 8.008, r = 1.0 / 8.008;
+    const double x = (double)f;
+    if (f == 0.0f) return f;
+    if (!isfinite(f)) return __double2float_rn(__ddiv_rn(x, c));
+    const double q0 = __dmul_rn(x, r);
+    const double rem = __fma_rn(-q0, c, x);
+    return __double2float_rn(__fma_rn(rem, r, q0));
+}
+
+// emit of the cell at tile position (y, x): bit k of the mask = the unit sent
+// to neighbour k, new_energy << 8, the buffers' gravity << 32
+__device__ __forceinline__ uint64_t xk_gc_emit(const uint64_t (*S)[XK_GC_TX + 4], int y, int x)
+{
+    const uint64_t c = S[y][x];
+    const uint32_t energy = (uint32_t)c & 4095u;
+    float gk[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) gk[k] = xk_gc_grav(S[y + xk_gc_dy(k)][x + xk_gc_dx(k)]);
+    float m = gk[0];
+#pragma unroll
+    for (int k = 1; k < 8; ++k) m = m < gk[k] ? m : gk[k];
+    const float lowest = __fadd_rn(0.0f, m);
+    uint32_t sent = 0, mask = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint32_t unit = (lowest == gk[k]) & (energy - sent > 0u);
+        sent += unit;
+        mask |= unit << k;
+    }
+    const float gsend = __fadd_rn(xk_gc_grav(c), (float)energy);
+    return (uint64_t)mask | (uint64_t)((energy - sent) & 4095u) << 8 | (uint64_t)__float_as_uint(gsend) << 32;
+}
+
+template <bool TORUS>
+__global__ void __launch_bounds__(XK_GC_TX * XK_GC_TY)
+xk_k_gravity(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32_t *__restrict__ col,
+             GravParams p)
+{
+    __shared__ uint64_t S[XK_GC_TY + 4][XK_GC_TX + 4];   // cells, halo of two
+    __shared__ uint64_t X[XK_GC_TY + 2][XK_GC_TX + 2];   // emitted, halo of one
+    const int tid = threadIdx.y * XK_GC_TX + threadIdx.x;
+    const int x0 = blockIdx.x * XK_GC_TX, y0 = blockIdx.y * XK_GC_TY;
+    xk_grid_dep_wait();                 // launched as a dependent of the previous generation
+    for (int e = tid; e < (XK_GC_TY + 4) * (XK_GC_TX + 4); e += XK_GC_TX * XK_GC_TY) {
+        const int sy = e / (XK_GC_TX + 4), sx = e % (XK_GC_TX + 4);
+        int gx = x0 + sx - 2, gy = y0 + sy - 2;
+        uint64_t v;
+        if (TORUS) {
+            if ((unsigned)gx >= (unsigned)p.W) { gx %= p.W; if (gx < 0) gx += p.W; }
+            if ((unsigned)gy >= (unsigned)p.H) { gy %= p.H; if (gy < 0) gy += p.H; }
+            v = __ldg(src + (int64_t)gy * p.W + gx);
+        } else {
+            v = (gx >= 0 && gx < p.W && gy >= 0 && gy < p.H) ? __ldg(src + (int64_t)gy * p.W + gx) : p.border;
+        }
+        S[sy][sx] = v;
+    }
+    __syncthreads();
+    for (int e = tid; e < (XK_GC_TY + 2) * (XK_GC_TX + 2); e += XK_GC_TX * XK_GC_TY) {
+        const int ey = e / (XK_GC_TX + 2), ex = e % (XK_GC_TX + 2);
+        X[ey][ex] = xk_gc_emit(S, ey + 1, ex + 1);   // off-board positions are never read
+    }
+    __syncthreads();
+    const int gx = x0 + threadIdx.x, gy = y0 + threadIdx.y;
+    if (gx >= p.W || gy >= p.H) return;
+    const int ty = threadIdx.y + 1, tx = threadIdx.x + 1;
+    uint32_t received = 0;
+    float gk[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int dx = xk_gc_dx(k), dy = xk_gc_dy(k);
+        const bool on = TORUS || ((unsigned)(gx + dx) < (unsigned)p.W && (unsigned)(gy + dy) < (unsigned)p.H);
+        if (on) {
+            const uint64_t w = X[ty + dy][tx + dx];
+            received += (uint32_t)(w >> (7 - k)) & 1u;
+            gk[k] = __uint_as_float((uint32_t)(w >> 32));
+        } else {
+            received += (uint32_t)p.border & 4095u;
+            gk[k] = xk_gc_grav(p.border);
+        }
+    }
+    float field = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) field = __fadd_rn(field, gk[k]);
+    const uint32_t newe = (uint32_t)(X[ty][tx] >> 8) & 4095u;
+    const uint32_t energy = (newe + received) & 0xFFFFu;
+    const float g = xk_gc_mean(field);
+    const int64_t i = (int64_t)gy * p.W + gx;
+    dst[i] = (uint64_t)(energy & 4095u) | (uint64_t)newe << 12 | (uint64_t)__float_as_uint(g) << 24;
+    if (p.color_kind == XK_COLOR_NONE) return;
+    const int gg = (int)__float2uint_rz(__fmul_rn(g, 108.0f));
+    int rgb[3] = {(int)energy * 255 * p.smooth, gg * p.smooth, gg * p.smooth};
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+        const int old = col[3 * i + ch];
+        const int m = rgb[ch] < old + p.fade_in ? rgb[ch] : old + p.fade_in;
+        rgb[ch] = m > old - p.fade_out ? m : old - p.fade_out;
+    }
+    col[3 * i] = rgb[0];
+    col[3 * i + 1] = rgb[1];
+    col[3 * i + 2] = rgb[2];
+    if (p.frame) {
+        // RendererPlain at zoom 1: the colour as a float, / SMOOTH_FACTOR,
+        // truncated, its low byte; exact without the division below 2^24
+        const bool small = (((uint32_t)rgb[0] + (1u << 24)) | ((uint32_t)rgb[1] + (1u << 24)) |
+                            ((uint32_t)rgb[2] + (1u << 24))) < (1u << 25);
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            uint8_t px;
+            if (p.frame_smooth <= 1 && small) {
+                px = (uint8_t)rgb[ch];
+            } else {
+                float v = (float)rgb[ch];
+                if (p.frame_smooth > 0) v = __fdiv_rn(v, (float)p.frame_smooth);
+                px = (uint8_t)(int)v;
+            }
+            p.frame[3 * i + ch] = px;
+        }
+    }
+}
+
+cudaError_t xk_gravity_step(const uint64_t *src, uint64_t *dst, int32_t *col, const xk_desc &d,
+                            cudaStream_t s, uint8_t *frame, int frame_smooth)
+{
+    GravParams p;
+    p.W = (int32_t)d.size[0];
+    p.H = (int32_t)d.size[1];
+    p.border = d.border_value;
+    p.color_kind = d.color_kind;
+    p.fade_in = d.fade_in;
+    p.fade_out = d.fade_out;
+    p.smooth = d.smooth;
+    p.frame = frame;
+    p.frame_smooth = frame_smooth;
+    dim3 block(XK_GC_TX, XK_GC_TY);
+    dim3 grid((p.W + XK_GC_TX - 1) / XK_GC_TX, (p.H + XK_GC_TY - 1) / XK_GC_TY);
+    return d.torus ? xk_launch_pdl(xk_k_gravity<true>, grid, block, 0, s, src, dst, col, p)
+                   : xk_launch_pdl(xk_k_gravity<false>, grid, block, 0, s, src, dst, col, p);
+}

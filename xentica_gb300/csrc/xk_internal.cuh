@@ -275,6 +275,9 @@ cudaError_t xk_lifecolor_step(const uint32_t *src, uint32_t *dst, int32_t *col, 
 // launch, in place (1 when the zoom-1 frame of a 2-D lattice is written)
 cudaError_t xk_noise_step(uint16_t *cells, int32_t *col, const xk_desc &d, int64_t n, int generations,
                           cudaStream_t s, uint8_t *frame = nullptr, int frame_smooth = 0);
+// one GraviCowboys generation, cells ping-pong (gravity.cu)
+cudaError_t xk_gravity_step(const uint64_t *src, uint64_t *dst, int32_t *col, const xk_desc &d,
+                            cudaStream_t s, uint8_t *frame, int frame_smooth);
 
 // Programmatic dependent launch for kernels that run once per generation: the
 // launch may begin while the previous kernel in the stream finishes, and the
