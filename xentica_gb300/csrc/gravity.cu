@@ -17,12 +17,14 @@
 // (unsigned)(gravity * 108) twice.  An off-board neighbour of a static border
 // reads as the whole border container (border.py:144-151).
 //
-// One launch per generation: a block loads its 32 x 8 cells with a halo of
-// two into shared memory, runs emit on the tile and a halo of one (what a
-// neighbour sends is a bit of an 8-bit mask, its new energy and the one
-// float every buffer carries), then absorb on the tile.  A cell's state is
-// read and written once per generation; the reference's nine containers per
-// cell never exist.
+// One launch per generation: a block loads the gravities and energies of its
+// 32 x 16 cells with a halo of two into shared memory, runs emit on the tile
+// and a halo of one (what a neighbour sends is a bit of an 8-bit mask, its
+// new energy and the one float every buffer carries), then absorb on the
+// tile, two rows a thread.  A cell's state is read and written once per
+// generation; the reference's nine containers per cell never exist.  The
+// division by 8.008 runs in float arithmetic with an exactness test (the
+// double-precision pipe is narrow on this part).
 #include "xk_internal.cuh"
 
 struct GravParams {
@@ -35,7 +37,8 @@ struct GravParams {
 };
 
 #define XK_GC_TX 32
-#define XK_GC_TY 8
+#define XK_GC_TY 16             // rows of a tile; each of the 8 warps runs two of them
+#define XK_GC_THREADS 256
 
 // the Moore deltas in the reference's order (x, y): (-1,-1) (-1,0) (-1,1)
 // (0,-1) (0,1) (1,-1) (1,0) (1,1); neighbour 7 - k points back along k
@@ -44,57 +47,87 @@ __device__ __forceinline__ int xk_gc_dy(int k) { return (k == 0 || k == 3 || k =
 
 __device__ __forceinline__ float xk_gc_grav(uint64_t c) { return __uint_as_float((uint32_t)(c >> 24)); }
 
-// (float)((double)f / 8.008), correctly rounded: the quotient by Markstein's
-// method (q0 = f * RN(1/8.008), remainder by an exact fma, one corrected
-// product; correctly rounded when the reciprocal is and q0 is within an ulp;
-// checked equal to the division for every finite non-zero float), a zero
-// keeps its sign, non-finite values go through the division itself
-__device__ __forceinline__ float xk_gc_mean(float f)
+// (float)((double)f / 8.008) by the division itself: zeros keep their sign
+__device__ __noinline__ float xk_gc_mean_f64(float f)
 {
-    constexpr double c = 8.008, r = 1.0 / 8.008;
-    const double x = (double)f;
     if (f == 0.0f) return f;
-    if (!isfinite(f)) return __double2float_rn(__ddiv_rn(x, c));
-    const double q0 = __dmul_rn(x, r);
-    const double rem = __fma_rn(-q0, c, x);
-    return __double2float_rn(__fma_rn(rem, r, q0));
+    return __double2float_rn(__ddiv_rn((double)f, 8.008));
 }
 
-// emit of the cell at tile position (y, x): bit k of the mask = the unit sent
-// to neighbour k, new_energy << 8, the buffers' gravity << 32
-__device__ __forceinline__ uint64_t xk_gc_emit(const uint64_t (*S)[XK_GC_TX + 4], int y, int x)
+// (float)((double)f / 8.008) in float arithmetic: the quotient as the
+// unevaluated sum q1 + t (8.008 split as CH + CL, R = RN(1/8.008); the
+// remainder f - q1 * 8.008 by two fmas), relative error below 2^-45; s =
+// RN(q1 + t) and err = q1 + t - s exactly (Fast2Sum).  When q1 + t lies more
+// than 2^-43 |s| from the midpoint between s and its neighbour on err's side,
+// the exact quotient, and its double rounding, round to s; otherwise (and for
+// |f| outside [2^-60, 2^120], zeros and non-finite values) the division
+// itself.  Checked equal to the double division for every finite float.
+__device__ __forceinline__ float xk_gc_mean(float f)
 {
-    const uint64_t c = S[y][x];
-    const uint32_t energy = (uint32_t)c & 4095u;
+    constexpr float CH = 0x1.00418ap+3f, CL = -0x1.916872p-22f, R = 0x1.ff7d1p-4f;
+    const float af = fabsf(f);
+    if (!(af >= 0x1p-60f && af <= 0x1p+120f)) return xk_gc_mean_f64(f);
+    const float q1 = __fmul_rn(f, R);
+    const float e = __fmaf_rn(-q1, CH, f);
+    const float e2 = __fmaf_rn(-q1, CL, e);
+    const float t = __fmul_rn(e2, R);
+    const float s = __fadd_rn(q1, t);
+    const float err = __fsub_rn(t, __fsub_rn(s, q1));
+    const uint32_t sb = __float_as_uint(s), es = sb & 0x7F800000u;
+    float h = __fmul_rn(__uint_as_float(es - (23u << 23)), 0.5f);     // ulp(s) / 2
+    if ((sb & 0x007FFFFFu) == 0 && ((__float_as_uint(err) ^ sb) >> 31)) h = __fmul_rn(h, 0.5f);
+    const float bound = __fmul_rn(__uint_as_float(es), 0x1p-43f);
+    if (fabsf(__fsub_rn(fabsf(err), h)) <= bound) return xk_gc_mean_f64(f);
+    return s;
+}
+
+struct GravTile {
+    float g[XK_GC_TY + 4][XK_GC_TX + 4];        // gravities, halo of two
+    uint32_t e[XK_GC_TY + 4][XK_GC_TX + 4];     // energies
+    float xg[XK_GC_TY + 2][XK_GC_TX + 2];       // emitted: the gravity every buffer carries
+    uint32_t xm[XK_GC_TY + 2][XK_GC_TX + 2];    // emitted: units sent (bit k: to neighbour k) | new_energy << 8
+};
+
+// emit of the cell at tile position (y, x): the units go to the neighbours of
+// the lowest gravity in neighbour order, one each while energy lasts, i.e. to
+// the first min(energy, ties) of them
+__device__ __forceinline__ void xk_gc_emit(GravTile &T, int y, int x, int ey, int ex)
+{
+    const uint32_t energy = T.e[y][x];
     float gk[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) gk[k] = xk_gc_grav(S[y + xk_gc_dy(k)][x + xk_gc_dx(k)]);
+    for (int k = 0; k < 8; ++k) gk[k] = T.g[y + xk_gc_dy(k)][x + xk_gc_dx(k)];
     float m = gk[0];
 #pragma unroll
     for (int k = 1; k < 8; ++k) m = m < gk[k] ? m : gk[k];
     const float lowest = __fadd_rn(0.0f, m);
-    uint32_t sent = 0, mask = 0;
+    uint32_t ties = 0;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const uint32_t unit = (lowest == gk[k]) & (energy - sent > 0u);
-        sent += unit;
-        mask |= unit << k;
+    for (int k = 0; k < 8; ++k) ties |= (uint32_t)(lowest == gk[k]) << k;
+    uint32_t mask = ties;
+    if (energy < (uint32_t)__popc(ties)) {       // energy < 8: only its first set bits
+        uint32_t rest = ties;
+        mask = 0;
+        for (uint32_t j = 0; j < energy; ++j) {
+            const uint32_t low = rest & (0u - rest);
+            mask |= low;
+            rest ^= low;
+        }
     }
-    const float gsend = __fadd_rn(xk_gc_grav(c), (float)energy);
-    return (uint64_t)mask | (uint64_t)((energy - sent) & 4095u) << 8 | (uint64_t)__float_as_uint(gsend) << 32;
+    T.xg[ey][ex] = __fadd_rn(T.g[y][x], (float)energy);
+    T.xm[ey][ex] = mask | (energy - (uint32_t)__popc(mask)) << 8;
 }
 
 template <bool TORUS>
-__global__ void __launch_bounds__(XK_GC_TX * XK_GC_TY)
+__global__ void __launch_bounds__(XK_GC_THREADS)
 xk_k_gravity(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32_t *__restrict__ col,
              GravParams p)
 {
-    __shared__ uint64_t S[XK_GC_TY + 4][XK_GC_TX + 4];   // cells, halo of two
-    __shared__ uint64_t X[XK_GC_TY + 2][XK_GC_TX + 2];   // emitted, halo of one
+    __shared__ GravTile T;
     const int tid = threadIdx.y * XK_GC_TX + threadIdx.x;
     const int x0 = blockIdx.x * XK_GC_TX, y0 = blockIdx.y * XK_GC_TY;
     xk_grid_dep_wait();                 // launched as a dependent of the previous generation
-    for (int e = tid; e < (XK_GC_TY + 4) * (XK_GC_TX + 4); e += XK_GC_TX * XK_GC_TY) {
+    for (int e = tid; e < (XK_GC_TY + 4) * (XK_GC_TX + 4); e += XK_GC_THREADS) {
         const int sy = e / (XK_GC_TX + 4), sx = e % (XK_GC_TX + 4);
         int gx = x0 + sx - 2, gy = y0 + sy - 2;
         uint64_t v;
@@ -105,68 +138,74 @@ xk_k_gravity(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
         } else {
             v = (gx >= 0 && gx < p.W && gy >= 0 && gy < p.H) ? __ldg(src + (int64_t)gy * p.W + gx) : p.border;
         }
-        S[sy][sx] = v;
+        T.g[sy][sx] = xk_gc_grav(v);
+        T.e[sy][sx] = (uint32_t)v & 4095u;
     }
     __syncthreads();
-    for (int e = tid; e < (XK_GC_TY + 2) * (XK_GC_TX + 2); e += XK_GC_TX * XK_GC_TY) {
+    for (int e = tid; e < (XK_GC_TY + 2) * (XK_GC_TX + 2); e += XK_GC_THREADS) {
         const int ey = e / (XK_GC_TX + 2), ex = e % (XK_GC_TX + 2);
-        X[ey][ex] = xk_gc_emit(S, ey + 1, ex + 1);   // off-board positions are never read
+        xk_gc_emit(T, ey + 1, ex + 1, ey, ex);   // off-board positions are never read
     }
     __syncthreads();
-    const int gx = x0 + threadIdx.x, gy = y0 + threadIdx.y;
-    if (gx >= p.W || gy >= p.H) return;
-    const int ty = threadIdx.y + 1, tx = threadIdx.x + 1;
-    uint32_t received = 0;
-    float gk[8];
+    const int gx = x0 + threadIdx.x;
+    if (gx >= p.W) return;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const int dx = xk_gc_dx(k), dy = xk_gc_dy(k);
-        const bool on = TORUS || ((unsigned)(gx + dx) < (unsigned)p.W && (unsigned)(gy + dy) < (unsigned)p.H);
-        if (on) {
-            const uint64_t w = X[ty + dy][tx + dx];
-            received += (uint32_t)(w >> (7 - k)) & 1u;
-            gk[k] = __uint_as_float((uint32_t)(w >> 32));
-        } else {
-            received += (uint32_t)p.border & 4095u;
-            gk[k] = xk_gc_grav(p.border);
+    for (int r = 0; r < XK_GC_TY / 8; ++r) {
+        const int ly = threadIdx.y + 8 * r, gy = y0 + ly;
+        if (gy >= p.H) return;
+        const int ty = ly + 1, tx = threadIdx.x + 1;
+        uint32_t got = 0, received = 0;
+        float gk[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int dx = xk_gc_dx(k), dy = xk_gc_dy(k);
+            const bool on = TORUS || ((unsigned)(gx + dx) < (unsigned)p.W && (unsigned)(gy + dy) < (unsigned)p.H);
+            if (on) {
+                got |= T.xm[ty + dy][tx + dx] & (1u << (7 - k));   // the unit neighbour k sent back along k
+                gk[k] = T.xg[ty + dy][tx + dx];
+            } else {
+                received += (uint32_t)p.border & 4095u;
+                gk[k] = xk_gc_grav(p.border);
+            }
         }
-    }
-    float field = 0.0f;
+        received += (uint32_t)__popc(got);
+        float field = 0.0f;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) field = __fadd_rn(field, gk[k]);
-    const uint32_t newe = (uint32_t)(X[ty][tx] >> 8) & 4095u;
-    const uint32_t energy = (newe + received) & 0xFFFFu;
-    const float g = xk_gc_mean(field);
-    const int64_t i = (int64_t)gy * p.W + gx;
-    dst[i] = (uint64_t)(energy & 4095u) | (uint64_t)newe << 12 | (uint64_t)__float_as_uint(g) << 24;
-    if (p.color_kind == XK_COLOR_NONE) return;
-    const int gg = (int)__float2uint_rz(__fmul_rn(g, 108.0f));
-    int rgb[3] = {(int)energy * 255 * p.smooth, gg * p.smooth, gg * p.smooth};
-#pragma unroll
-    for (int ch = 0; ch < 3; ++ch) {
-        const int old = col[3 * i + ch];
-        const int m = rgb[ch] < old + p.fade_in ? rgb[ch] : old + p.fade_in;
-        rgb[ch] = m > old - p.fade_out ? m : old - p.fade_out;
-    }
-    col[3 * i] = rgb[0];
-    col[3 * i + 1] = rgb[1];
-    col[3 * i + 2] = rgb[2];
-    if (p.frame) {
-        // RendererPlain at zoom 1: the colour as a float, / SMOOTH_FACTOR,
-        // truncated, its low byte; exact without the division below 2^24
-        const bool small = (((uint32_t)rgb[0] + (1u << 24)) | ((uint32_t)rgb[1] + (1u << 24)) |
-                            ((uint32_t)rgb[2] + (1u << 24))) < (1u << 25);
+        for (int k = 0; k < 8; ++k) field = __fadd_rn(field, gk[k]);
+        const uint32_t newe = T.xm[ty][tx] >> 8;
+        const uint32_t energy = (newe + received) & 0xFFFFu;
+        const float g = xk_gc_mean(field);
+        const int64_t i = (int64_t)gy * p.W + gx;
+        dst[i] = (uint64_t)(energy & 4095u) | (uint64_t)newe << 12 | (uint64_t)__float_as_uint(g) << 24;
+        if (p.color_kind == XK_COLOR_NONE) continue;
+        const int gg = (int)__float2uint_rz(__fmul_rn(g, 108.0f));
+        int rgb[3] = {(int)energy * 255 * p.smooth, gg * p.smooth, gg * p.smooth};
 #pragma unroll
         for (int ch = 0; ch < 3; ++ch) {
-            uint8_t px;
-            if (p.frame_smooth <= 1 && small) {
-                px = (uint8_t)rgb[ch];
-            } else {
-                float v = (float)rgb[ch];
-                if (p.frame_smooth > 0) v = __fdiv_rn(v, (float)p.frame_smooth);
-                px = (uint8_t)(int)v;
+            const int old = col[3 * i + ch];
+            const int m = rgb[ch] < old + p.fade_in ? rgb[ch] : old + p.fade_in;
+            rgb[ch] = m > old - p.fade_out ? m : old - p.fade_out;
+        }
+        col[3 * i] = rgb[0];
+        col[3 * i + 1] = rgb[1];
+        col[3 * i + 2] = rgb[2];
+        if (p.frame) {
+            // RendererPlain at zoom 1: the colour as a float, / SMOOTH_FACTOR,
+            // truncated, its low byte; exact without the division below 2^24
+            const bool small = (((uint32_t)rgb[0] + (1u << 24)) | ((uint32_t)rgb[1] + (1u << 24)) |
+                                ((uint32_t)rgb[2] + (1u << 24))) < (1u << 25);
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+                uint8_t px;
+                if (p.frame_smooth <= 1 && small) {
+                    px = (uint8_t)rgb[ch];
+                } else {
+                    float v = (float)rgb[ch];
+                    if (p.frame_smooth > 0) v = __fdiv_rn(v, (float)p.frame_smooth);
+                    px = (uint8_t)(int)v;
+                }
+                p.frame[3 * i + ch] = px;
             }
-            p.frame[3 * i + ch] = px;
         }
     }
 }
@@ -184,7 +223,7 @@ cudaError_t xk_gravity_step(const uint64_t *src, uint64_t *dst, int32_t *col, co
     p.smooth = d.smooth;
     p.frame = frame;
     p.frame_smooth = frame_smooth;
-    dim3 block(XK_GC_TX, XK_GC_TY);
+    dim3 block(XK_GC_TX, XK_GC_THREADS / XK_GC_TX);
     dim3 grid((p.W + XK_GC_TX - 1) / XK_GC_TX, (p.H + XK_GC_TY - 1) / XK_GC_TY);
     return d.torus ? xk_launch_pdl(xk_k_gravity<true>, grid, block, 0, s, src, dst, col, p)
                    : xk_launch_pdl(xk_k_gravity<false>, grid, block, 0, s, src, dst, col, p);
