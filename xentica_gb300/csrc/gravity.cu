@@ -24,7 +24,8 @@
 // tile, two rows a thread.  A cell's state is read and written once per
 // generation; the reference's nine containers per cell never exist.  The
 // division by 8.008 runs in float arithmetic with an exactness test (the
-// double-precision pipe is narrow on this part).
+// double-precision pipe is narrow on this part).  What a cell emits is one
+// 64-bit shared entry, so absorb reads each neighbour's with one load.
 #include "xk_internal.cuh"
 
 struct GravParams {
@@ -84,8 +85,9 @@ __device__ __forceinline__ float xk_gc_mean(float f)
 struct GravTile {
     float g[XK_GC_TY + 4][XK_GC_TX + 4];        // gravities, halo of two
     uint32_t e[XK_GC_TY + 4][XK_GC_TX + 4];     // energies
-    float xg[XK_GC_TY + 2][XK_GC_TX + 2];       // emitted: the gravity every buffer carries
-    uint32_t xm[XK_GC_TY + 2][XK_GC_TX + 2];    // emitted: units sent (bit k: to neighbour k) | new_energy << 8
+    // emitted: .x units sent (bit k: to neighbour k) | new_energy << 8, .y the
+    // bits of the gravity every buffer carries (one 64-bit load in absorb)
+    uint2 x[XK_GC_TY + 2][XK_GC_TX + 2];
 };
 
 // emit of the cell at tile position (y, x): the units go to the neighbours of
@@ -114,8 +116,8 @@ __device__ __forceinline__ void xk_gc_emit(GravTile &T, int y, int x, int ey, in
             rest ^= low;
         }
     }
-    T.xg[ey][ex] = __fadd_rn(T.g[y][x], (float)energy);
-    T.xm[ey][ex] = mask | (energy - (uint32_t)__popc(mask)) << 8;
+    T.x[ey][ex] = make_uint2(mask | (energy - (uint32_t)__popc(mask)) << 8,
+                             __float_as_uint(__fadd_rn(T.g[y][x], (float)energy)));
 }
 
 template <bool TORUS>
@@ -161,8 +163,9 @@ xk_k_gravity(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
             const int dx = xk_gc_dx(k), dy = xk_gc_dy(k);
             const bool on = TORUS || ((unsigned)(gx + dx) < (unsigned)p.W && (unsigned)(gy + dy) < (unsigned)p.H);
             if (on) {
-                got |= T.xm[ty + dy][tx + dx] & (1u << (7 - k));   // the unit neighbour k sent back along k
-                gk[k] = T.xg[ty + dy][tx + dx];
+                const uint2 w = T.x[ty + dy][tx + dx];
+                got |= w.x & (1u << (7 - k));   // the unit neighbour k sent back along k
+                gk[k] = __uint_as_float(w.y);
             } else {
                 received += (uint32_t)p.border & 4095u;
                 gk[k] = xk_gc_grav(p.border);
@@ -172,7 +175,7 @@ xk_k_gravity(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int32
         float field = 0.0f;
 #pragma unroll
         for (int k = 0; k < 8; ++k) field = __fadd_rn(field, gk[k]);
-        const uint32_t newe = T.xm[ty][tx] >> 8;
+        const uint32_t newe = T.x[ty][tx].x >> 8;
         const uint32_t energy = (newe + received) & 0xFFFFu;
         const float g = xk_gc_mean(field);
         const int64_t i = (int64_t)gy * p.W + gx;
