@@ -18,10 +18,10 @@
 // reads as the whole border container (border.py:144-151).
 //
 // One launch per generation: a block loads the gravities and energies of its
-// 32 x 16 cells with a halo of two into shared memory, runs emit on the tile
+// 32 x 32 cells with a halo of two into shared memory, runs emit on the tile
 // and a halo of one (what a neighbour sends is a bit of an 8-bit mask, its
 // new energy and the one float every buffer carries), then absorb on the
-// tile, two rows a thread.  A cell's state is read and written once per
+// tile, four rows a thread.  A cell's state is read and written once per
 // generation; the reference's nine containers per cell never exist.  The
 // division by 8.008 runs in float arithmetic with an exactness test (the
 // double-precision pipe is narrow on this part).  What a cell emits is one
@@ -38,7 +38,7 @@ struct GravParams {
 };
 
 #define XK_GC_TX 32
-#define XK_GC_TY 16             // rows of a tile; each of the 8 warps runs two of them
+#define XK_GC_TY 32             // rows of a tile; each of the 8 warps runs four of them
 #define XK_GC_THREADS 256
 
 // the Moore deltas in the reference's order (x, y): (-1,-1) (-1,0) (-1,1)
