@@ -56,3 +56,31 @@ def test_desc_layout_matches_c(tmp_path):
     assert int(got["__sizeof__"]) == ctypes.sizeof(nat.XkDesc)
     for f in fields:
         assert int(got[f]) == getattr(nat.XkDesc, f).offset, f
+
+
+@pytest.mark.parametrize("family,field,value", [
+    (nat.XK_FAMILY_GRAVITY, "state_bytes", 4),
+    (nat.XK_FAMILY_GRAVITY, "nbr", 4),
+    (nat.XK_FAMILY_GRAVITY, "color_kind", nat.XK_COLOR_PLAIN),
+    (nat.XK_FAMILY_LIFECOLOR, "state_bytes", 8),
+    (nat.XK_FAMILY_LIFECOLOR, "ndim", 3),
+    (nat.XK_FAMILY_NOISE, "state_bytes", 4),
+    (nat.XK_FAMILY_EVOLIFE, "torus", 0),
+    (99, "family", 99),
+])
+def test_fused_families_reject_other_descriptors(lib, family, field, value):
+    """A descriptor a fused family's kernel cannot run is refused with a
+    status (before any device work, so this runs without a GPU)."""
+    from tests.models import GraviCowboys, GraviExperiment
+    d = GraviCowboys(GraviExperiment).gpu.template.descriptor()
+    d.family = family
+    if family == nat.XK_FAMILY_LIFECOLOR:
+        d.state_bytes = 4
+    elif family == nat.XK_FAMILY_NOISE:
+        d.state_bytes = 2
+    setattr(d, field, value)
+    h = ctypes.c_void_p()
+    rc = lib.xk_model_create(ctypes.byref(d), ctypes.byref(h))
+    assert rc in (nat.XK_ERR_ARG, nat.XK_ERR_UNSUPPORTED), rc
+    assert not h.value
+    assert nat.last_error()

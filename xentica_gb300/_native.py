@@ -51,7 +51,7 @@ class XkDesc(ctypes.Structure):
 
 XK_SERVE_LIFE2D, XK_SERVE_LIFE3D_VN, XK_SERVE_MASS3D = 1, 2, 3
 XK_REQ_PENDING, XK_REQ_ACTIVE, XK_REQ_DONE, XK_REQ_CANCELLED, XK_REQ_FAILED = 0, 1, 2, 3, 4
-XK_ERR_ARG, XK_ERR_CUDA, XK_ERR_OOM, XK_ERR_STATE, XK_ERR_TIMEOUT = -1, -2, -3, -5, -6
+XK_ERR_ARG, XK_ERR_CUDA, XK_ERR_OOM, XK_ERR_UNSUPPORTED, XK_ERR_STATE, XK_ERR_TIMEOUT = -1, -2, -3, -4, -5, -6
 
 
 class XkRequest(ctypes.Structure):
